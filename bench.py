@@ -1,0 +1,312 @@
+"""Benchmark of the RI-K exchange step on one GB300.
+
+Workload (synthetic RI-K system, seeded): 40 atoms uniform in a 12 Angstrom
+box, 24 basis and 84 auxiliary functions per atom (n_bf 960, n_aux 3360),
+n_occ 200, block size 24, tau 1e-10.  One step is the reference's exchange
+pipeline: the 3c->2c transform B = X * V^{-1/2} on the compressed
+significant-pair integrals (3c_2c_transform.cpp:44-57) followed by the occ-RI-K
+step K = sum_{P,i} (mu i|P)[(ij|P)+(ji|P)] (occ_ri_k_step.cpp:83-130).
+
+Metric: effective TFLOP/s = dense-equivalent FLOPs of the step
+(2*n_vec2*n_aux^2 + 2*(n_bf^2*n_occ*n_aux + 2*n_bf*n_occ^2*n_aux), the
+counts the reference's drivers print) / step time; higher is better.
+
+`value`: inputs resident in HBM, device-timed with CUDA events on the
+library's stream.  `e2e`: the same step through the C ABI with host buffers
+(pinned), host->device copies and the K read-back inside the timed region.
+`--impl reference` times the reference's CPU algorithm (the C oracle port,
+OpenMP over P partitions, dgemm through OpenBLAS) on the host cores, on a
+bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CFG = dict(n_atoms=40, nbf=24, naux=84, n_occ=200, box=12.0, bs=24, thresh=1e-10, seed=42)
+METRIC = "RI-K step time & eff. TFLOP/s: mixed vs FP64 GPU form at rel err ≤1e-9"
+WORKLOAD = ("RI-K exchange step (3c->2c transform + occ-RI-K), 40 atoms in 12 A box, n_bf 960, n_aux 3360, n_occ 200,"
+            " bs 24, tau 1e-10")
+
+
+def step_flops(n_bf, n_aux, n_occ, n_vec2):
+    f3c = 2.0 * n_vec2 * n_aux * n_aux  # 3c_2c_transform.cpp:52
+    focc = 2.0 * (n_bf * n_bf * n_occ * n_aux + 2.0 * n_bf * n_occ * n_occ * n_aux)  # occ_ri_k_step.cpp:75
+    return f3c, focc
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region"""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu=0):
+        self.gpu = gpu
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm = [float(r[1]) for r in self.rows if len(r) > 8 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 8 and r[2].replace(".", "").isdigit()]
+        reasons = set()
+        for r in self.rows:
+            if len(r) > 8:
+                for name, v in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"),
+                                   r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
+
+
+def make_system():
+    from strassen_gb300 import synth as S
+
+    return S.RikSystem(seed=CFG["seed"], n_atoms=CFG["n_atoms"], nbf=CFG["nbf"], naux=CFG["naux"], n_occ=CFG["n_occ"],
+                       box=CFG["box"])
+
+
+def cpu_sample(sysm, Xr, Bp, V, C):
+    """The reference CPU algorithm (oracle port, OpenMP over P partitions,
+    dgemm through OpenBLAS) on a bounded sample: the 3c->2c transform of the
+    integral rows Xr and the occ-RI-K step on the transformed columns Bp.
+    Returns (dense-equivalent flops, seconds, threads)."""
+    from oracle import oracle as O
+
+    O.enable_fast_gemm(True)
+    bs, thr = CFG["bs"], CFG["thresh"]
+    cores = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    O.transform_3c2c(Xr, V, bs, thr)
+    t1 = time.perf_counter()
+    O.rik_occ_step(Bp, sysm.keys, C, sysm.n_bf, Bp.shape[1], sysm.n_occ, bs, thr, cores)
+    t2 = time.perf_counter()
+    O.enable_fast_gemm(False)
+    n_rows, n_p = Xr.shape[0], Bp.shape[1]
+    f3c = 2.0 * n_rows * sysm.n_aux * sysm.n_aux
+    focc = 2.0 * (sysm.n_bf ** 2 * sysm.n_occ * n_p + 2.0 * sysm.n_bf * sysm.n_occ ** 2 * n_p)
+    return f3c + focc, t2 - t0, cores
+
+
+def occ_sample_input(sysm, V, n_p):
+    """B[:, :n_p] = X V^{-1/2}[:, :n_p] for the occ-RI-K sample (setup, untimed;
+    X generated in P chunks with the bit-identical torch generator)"""
+    import torch
+
+    out = np.zeros((sysm.n_vec2, n_p))
+    for p0 in range(0, sysm.n_aux, 256):
+        p1 = min(sysm.n_aux, p0 + 256)
+        Xc = sysm.ints_3c_torch("cpu", p0, p1).numpy().T
+        out += Xc @ V[p0:p1, :n_p]
+    return np.asfortranarray(out)
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    n_rows, n_p = 48, 48
+    sysm = make_system()
+    V = sysm.v_m12()
+    C = sysm.c_occ()
+    Xr = sysm.ints_3c_rows(0, n_rows)
+    Bp = occ_sample_input(sysm, V, n_p)
+    for _ in range(args.warmup):
+        cpu_sample(sysm, Xr, Bp, V, C)
+    times, flops, cores = [], 0.0, 1
+    for _ in range(args.steps):
+        f, t, cores = cpu_sample(sysm, Xr, Bp, V, C)
+        times.append(t)
+        flops = f
+    t = statistics.median(times)
+    v = flops / t / 1e12
+    sample = f"3c->2c on {n_rows} of {sysm.n_vec2} integral rows + occ-RI-K on {n_p} of {sysm.n_aux} aux functions"
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "TFLOP/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "sample": sample},
+            "cpu_baseline": {"value": v, "unit": "TFLOP/s", "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    import torch
+
+    from strassen_gb300 import api
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    sysm = make_system()
+    n_bf, n_aux, n_occ, n_vec2, bs, thr = sysm.n_bf, sysm.n_aux, sysm.n_occ, sysm.n_vec2, CFG["bs"], CFG["thresh"]
+    form = api.FORM_OZAKI if args.form == "ozaki" else api.FORM_FP64
+    # inputs: generated on the device (bit-identical to the numpy generator)
+    Xt = sysm.ints_3c_torch(dev)  # n_aux x n_vec2 row-major == n_vec2 x n_aux column-major
+    X = Xt.T
+    V = torch.from_numpy(np.ascontiguousarray(sysm.v_m12().T)).to(dev).T
+    C = torch.from_numpy(np.ascontiguousarray(sysm.c_occ().T)).to(dev).T
+    keys = torch.from_numpy(sysm.keys.view(np.int64)).to(dev)
+    B = torch.empty((n_aux, n_vec2), dtype=torch.float64, device=dev).T
+    K = torch.empty((n_occ, n_bf), dtype=torch.float64, device=dev).T
+    stream = torch.cuda.Stream(device=dev)
+    ctx = api.Context(local, stream=stream.cuda_stream)
+
+    def step(form_):
+        api.transform_3c2c(X, V, bs, thr, form=form_, out=B, ctx=ctx)
+        api.rik_occ_step(B, keys, C, n_bf, n_aux, n_occ, bs, thr, n_part=1, form=form_, out=K, ctx=ctx)
+
+    def timed(fn, steps, warmup):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize(dev)
+        if world > 1:
+            torch.distributed.barrier()
+        l0 = ctx.launch_count()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with Clocks(local) as clk:
+            with torch.cuda.stream(stream):
+                e0.record(stream)
+                for _ in range(steps):
+                    fn()
+                e1.record(stream)
+            torch.cuda.synchronize(dev)
+        if world > 1:
+            torch.distributed.barrier()
+        ms = e0.elapsed_time(e1) / steps
+        return ms, (ctx.launch_count() - l0) / steps, clk.summary()
+
+    f3c, focc = step_flops(n_bf, n_aux, n_occ, n_vec2)
+    ms, launches, clocks = timed(lambda: step(form), args.steps, args.warmup)
+    Kc = K.cpu().numpy().copy()
+    if world > 1:
+        t = torch.tensor([ms], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    extra = {}
+    if form != api.FORM_FP64 and not args.skip_fp64:
+        ms64, _, _ = timed(lambda: step(api.FORM_FP64), 1, 1)
+        K64 = K.cpu().numpy()
+        extra = {"fp64_ms_per_step": ms64, "speedup_vs_fp64": ms64 / ms,
+                 "rel_err_vs_fp64": float(np.linalg.norm(Kc - K64) / np.linalg.norm(K64))}
+    # e2e through the C ABI with pinned host buffers
+    Xh = torch.empty((n_aux, n_vec2), dtype=torch.float64, pin_memory=True)
+    Xh.copy_(Xt)
+    Vh = V.T.cpu().pin_memory()
+    Ch = C.T.cpu().pin_memory()
+    kh = keys.cpu().pin_memory()
+    Kh = torch.empty((n_occ, n_bf), dtype=torch.float64, pin_memory=True)
+
+    keys_d = torch.empty_like(keys)
+    C_d = torch.empty((n_occ, n_bf), dtype=torch.float64, device=dev)
+
+    def step_e2e():
+        api.transform_3c2c(Xh.T.numpy(), Vh.T.numpy(), bs, thr, form=form, out=B, ctx=ctx)
+        keys_d.copy_(kh, non_blocking=True)
+        C_d.copy_(Ch, non_blocking=True)
+        api.rik_occ_step(B, keys_d, C_d.T, n_bf, n_aux, n_occ, bs, thr, n_part=1, form=form, out=Kh.T.numpy(),
+                         ctx=ctx)
+
+    e2e_ms, _, _ = timed(step_e2e, max(1, args.steps), 1)
+    h2d = (Xh.numel() + Vh.numel() + Ch.numel() + kh.numel()) * 8
+    d2h = Kh.numel() * 8
+    flops = f3c + focc
+    value = world * flops / (ms * 1e-3) / 1e12
+    peaks = measured_peaks()
+    line = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64" if form == api.FORM_FP64 else "bf16x4-ozaki/f64",
+            "data": "synthetic (seeded RI-K system, generated on device)",
+            "config": {"workload": WORKLOAD + f"; n_vec2 {n_vec2}", "form": args.form,
+                       "l2": "inputs larger than L2 (X is %.1f GB)" % (n_vec2 * n_aux * 8 / 1e9)},
+            "e2e": {"value": world * flops / (e2e_ms * 1e-3) / 1e12, "unit": "TFLOP/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
+            "gpu_launches": int(round(launches)), "clocks": clocks,
+            "flops_split": {"3c2c": f3c, "occ": focc}}
+    line.update(extra)
+    line["roofline"] = roofline_placeholder(peaks, ms, flops, form)
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        Vn = np.asfortranarray(V.T.cpu().numpy().T)
+        Cn = np.asfortranarray(C.T.cpu().numpy().T)
+        Bs = np.asfortranarray(B[:, :48].cpu().numpy())
+        f, t, cores = cpu_sample(sysm, sysm.ints_3c_rows(0, 48), Bs, Vn, Cn)
+        line["cpu_baseline"] = {"value": f / t / 1e12, "unit": "TFLOP/s", "cores": cores, "kind": "port",
+                                "sample": f"3c->2c on 48 of {n_vec2} integral rows + occ-RI-K on 48 of {n_aux} aux "
+                                          "functions (OpenMP over P partitions, dgemm via OpenBLAS)"}
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def roofline_placeholder(peaks, ms, flops, form):
+    return None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--form", default="fp64", choices=["fp64", "ozaki"])
+    ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,175 @@
+/*
+ * bsgpu -- GB300 (sm_103a) block-sparse GEMM, hybrid Strassen-Winograd /
+ * sparse recursion and RI-K exchange step behind a C ABI.
+ *
+ * Every entry point is extern "C", takes plain pointers and sizes, returns a
+ * bsg_status (0 = success) and leaves a message in bsg_last_error() on
+ * failure.  Where the reference asserts or calls exit(1) (matrix.hpp:63-74,
+ * blocksparsematrix.hpp:308-338, strassen.hpp:693-705) these functions
+ * return BSG_ERR_ARG or BSG_ERR_PRECOND instead and launch nothing.
+ *
+ * Arithmetic: the FP64 form performs, for every output element, the same
+ * sequence of IEEE-754 operations as the reference linked against the
+ * deterministic BLAS definition documented in the design doc (fma chains over k in
+ * order, per-block accumulation C = alpha*t + C, 32-lane norm tree), so its
+ * results, block masks and cached norms are bit-identical to that reference.
+ *
+ * Threading: a bsg_ctx owns one CUDA stream; calls on one context are
+ * ordered on that stream.  Host threads may call concurrently only on
+ * distinct contexts (and matrices belonging to them).
+ */
+#ifndef BSGPU_H
+#define BSGPU_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int bsg_status;
+enum {
+    BSG_OK = 0,
+    BSG_ERR_ARG = 1,         /* bad argument or dimension mismatch */
+    BSG_ERR_PRECOND = 2,     /* a precondition the reference asserts on */
+    BSG_ERR_CUDA = 3,        /* CUDA runtime error (message has details) */
+    BSG_ERR_NOMEM = 4,       /* device or host allocation failed */
+    BSG_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up */
+    BSG_ERR_UNSUPPORTED = 6  /* configuration outside what is implemented */
+};
+
+enum { BSG_HOST = 0, BSG_DEVICE = 1 }; /* where a buffer lives */
+
+/* arithmetic form of a product */
+enum {
+    BSG_FORM_FP64 = 0,  /* plain FP64, bit-identical to the reference */
+    BSG_FORM_OZAKI = 1  /* bf16 digit slices on tcgen05, exact fp32 partial sums, fp64 combine */
+};
+
+typedef struct bsg_ctx_s *bsg_ctx;
+typedef struct bsg_pool_s *bsg_pool;
+typedef struct bsg_bsm_s *bsg_bsm;
+
+const char *bsg_last_error(void);
+int bsg_version(void);
+
+/* ---- context (device + stream) ---- */
+bsg_status bsg_ctx_create(int device, void *cuda_stream, bsg_ctx *out);
+bsg_status bsg_ctx_destroy(bsg_ctx ctx);
+bsg_status bsg_ctx_sync(bsg_ctx ctx);
+/* number of kernels this context has launched so far */
+bsg_status bsg_ctx_launch_count(bsg_ctx ctx, uint64_t *out);
+
+/* ---- block pool: BlockMemoryPool<double> (blockallocator.h:8-25,
+ *      blockallocator.hpp:7-56).  Device slabs grow geometrically from 16 MB
+ *      to 1 GB; blocks are handed out from a free list.  A pool is shared by
+ *      every matrix created on it and lives until its last user is gone. ---- */
+bsg_status bsg_pool_create(bsg_ctx ctx, size_t block_elems, bsg_pool *out);
+bsg_status bsg_pool_release(bsg_pool pool);                          /* drop the caller's reference */
+bsg_status bsg_pool_adjust_blocksize(bsg_pool pool, size_t block_elems); /* blockallocator.hpp:51-56 */
+bsg_status bsg_pool_release_all_memory(bsg_pool pool);               /* blockallocator.hpp:58-62 */
+bsg_status bsg_pool_stats(bsg_pool pool, size_t *blocks_total, size_t *blocks_free, size_t *bytes);
+
+/* ---- BlockSparseMatrix<double> (blocksparsematrix.h:19-93) ---- */
+/* BlockSparseMatrix(nr, nc, bsr, bsc, thresh[, pool]) blocksparsematrix.hpp:5-15;
+ * pool may be NULL (a fresh pool of bsr*bsc-element blocks, :15) */
+bsg_status bsg_bsm_create(bsg_ctx ctx, size_t nr, size_t nc, size_t bsr, size_t bsc, double thresh, bsg_pool pool,
+                          bsg_bsm *out);
+bsg_status bsg_bsm_destroy(bsg_bsm m);
+/* dims[0..5] = nr, nc, bsr, bsc, nrb, ncb; *thresh = the per-element threshold */
+bsg_status bsg_bsm_info(bsg_bsm m, size_t dims[6], double *thresh);
+bsg_status bsg_bsm_pool(bsg_bsm m, bsg_pool *out); /* mem_pool_ptr() blocksparsematrix.h:81 */
+/* copy assignment: blocks and cached norms (used as `ijs = ij`, occ_ri_k_step.cpp:112) */
+bsg_status bsg_bsm_assign(bsg_bsm dst, bsg_bsm src);
+/* copy_from_input_array / copy_from_input_matrix blocksparsematrix.hpp:35-69:
+ * column-major nr x nc input; blocks with norm < thresh*bsr*bsc are dropped */
+bsg_status bsg_bsm_copy_from_dense(bsg_bsm m, const double *in, int where);
+bsg_status bsg_bsm_fill(bsg_bsm m, double val);  /* fill_with_values :84-101 */
+bsg_status bsg_bsm_zero(bsg_bsm m);              /* zero :79-82 */
+bsg_status bsg_bsm_scale(bsg_bsm m, double s);   /* scale / operator*= :71-77,250-254 */
+bsg_status bsg_bsm_add(bsg_bsm m, bsg_bsm rhs);  /* operator+= :170-194 */
+bsg_status bsg_bsm_sub(bsg_bsm m, bsg_bsm rhs);  /* operator-= :196-221 */
+bsg_status bsg_bsm_add_transpose(bsg_bsm m, bsg_bsm rhs); /* add_transpose :224-248 */
+bsg_status bsg_bsm_calc_norms(bsg_bsm m);        /* calc_frobenius_norms :139-147 */
+bsg_status bsg_bsm_recompress(bsg_bsm m);        /* recompress :149-156 */
+bsg_status bsg_bsm_frobenius_norm(bsg_bsm m, double *out);       /* frobenius_norm :256-261 */
+bsg_status bsg_bsm_no_of_alloc_blocks(bsg_bsm m, size_t *out);   /* no_of_alloc_blocks :158-162 */
+bsg_status bsg_bsm_calc_alloc_dim(bsg_bsm m, size_t *out);       /* calc_alloc_dim :164-168 */
+/* to_pointer / to_matrix :103-131 (absent blocks read as zero) */
+bsg_status bsg_bsm_to_dense(bsg_bsm m, double *out, int where);
+/* block presence (1/0) and cached norms, block (r,c) at index r + c*nrb */
+bsg_status bsg_bsm_get_mask(bsg_bsm m, uint8_t *mask_host);
+bsg_status bsg_bsm_get_norms(bsg_bsm m, double *norms_host);
+
+/* dot(BSM, BSM, thresh) blocksparsematrix.hpp:263-290 */
+bsg_status bsg_dot(bsg_bsm a, bsg_bsm b, double thresh, double *out);
+
+/* matmult(C, A, tA, B, tB, thresh, alpha, beta) blocksparsematrix.hpp:293-414:
+ * C = alpha*op(A)*op(B) + beta*C over block triples with
+ * ||A_ik||*||B_kj|| >= thresh*bs_i*bs_j*bs_k.  *nsig_out (may be NULL)
+ * receives the number of surviving block products. */
+bsg_status bsg_matmult(bsg_bsm C, bsg_bsm A, int tA, bsg_bsm B, int tB, double thresh, double alpha, double beta,
+                       uint64_t *nsig_out);
+/* the same product in a chosen arithmetic form (BSG_FORM_OZAKI: n_digits
+ * bf16 slices per operand, 2..5; screening stays FP64 so masks are exact) */
+bsg_status bsg_matmult_form(bsg_bsm C, bsg_bsm A, int tA, bsg_bsm B, int tB, double thresh, double alpha,
+                            double beta, int form, int n_digits, uint64_t *nsig_out);
+
+/* ---- hybrid Strassen-Winograd / sparse recursion (strassen.hpp) ---- */
+/* matmult_strassen_dryrun strassen.hpp:511-679: decision-tree bits of levels
+ * 0..L-1 concatenated into tree_host (level l holds ceil(nb/2^(l+1))^3
+ * entries, index si + sj*n + sk*n*n), flops_per_level[0..L] */
+bsg_status bsg_strassen_dryrun(bsg_bsm A, bsg_bsm B, double thresh_per_block, int *n_levels, uint8_t *tree_host,
+                               size_t tree_cap, uint64_t *flops_per_level);
+/* matmult_strassen_sparse strassen.hpp:687-753 (square, no transposes,
+ * alpha = 1, beta ignored: C must be pre-filled, as main.cpp:57 does);
+ * min_size_for_strassen is the reference's global knob (main.cpp:9) */
+bsg_status bsg_matmult_strassen_sparse(bsg_bsm C, bsg_bsm A, int tA, bsg_bsm B, int tB, double thresh,
+                                       double alpha, double beta, size_t min_size_for_strassen);
+bsg_status bsg_matmult_strassen_sparse_form(bsg_bsm C, bsg_bsm A, bsg_bsm B, double thresh,
+                                            size_t min_size_for_strassen, int form, int n_digits);
+
+/* ---- BlockSparse3DTensor<double> = slices of BlockSparseMatrix
+ *      (blocksparse3d_tensor.h:8-43; declared but never defined there) ---- */
+/* C_ij = sum_l sum_k op(A^l)_ik op(B^l)_kj  (blocksparse3d_tensor.h:11-16) */
+bsg_status bsg_tensormult_contract(bsg_bsm C, const bsg_bsm *A, int tA, const bsg_bsm *B, int tB, size_t n_slices,
+                                   double thresh, double alpha, double beta);
+/* C^l_ij = sum_k op(A)_ik op(B^l)_kj  (blocksparse3d_tensor.h:18-24), one launch over all slices */
+bsg_status bsg_tensormult_batched(const bsg_bsm *C, bsg_bsm A, int tA, const bsg_bsm *B, int tB, size_t n_slices,
+                                  double thresh, double alpha, double beta);
+
+/* ---- drivers ---- */
+typedef struct bsg_rik_args {
+    size_t n_bf, n_aux, n_occ, n_vec2; /* occ_ri_k_step.cpp:19-22 */
+    const double *ints;                /* n_vec2 x n_aux column-major, (mn|P)' compressed (:29-30) */
+    const uint64_t *keys;              /* n_vec2 v2m keys, key = row + col*n_bf (:35-36) */
+    const double *c_occ;               /* n_bf x n_occ column-major occupied MOs (:33-34) */
+    int where;                         /* BSG_HOST or BSG_DEVICE for the three inputs */
+    size_t bs;                         /* block size (:26) */
+    double thresh;                     /* per-element screening threshold (:27) */
+    int n_part;                        /* P partitions summed in order (OpenMP team size, :90-122) */
+    int form;                          /* BSG_FORM_FP64 or BSG_FORM_OZAKI */
+    int n_digits;                      /* Ozaki slices per operand (form OZAKI) */
+    size_t p_chunk;                    /* aux functions per batched launch (0 = automatic) */
+} bsg_rik_args;
+
+/* occ-RI-K step (occ_ri_k_step.cpp:83-130): K_{mu j} = sum_{P,i} (mu i|P) [(ij|P)+(ji|P)],
+ * K_out n_bf x n_occ column-major.  stats_out (may be NULL) receives
+ * [surviving block products of the three GEMMs, mui blocks, ij blocks]. */
+bsg_status bsg_rik_occ_step(bsg_ctx ctx, const bsg_rik_args *args, double *K_out, int out_where,
+                            uint64_t stats_out[5]);
+
+/* 3c->2c transform (3c_2c_transform.cpp:44-57): out = X * V^{-1/2} through
+ * matmult on block-sparse copies (input threshold 0, out pre-filled 0). */
+bsg_status bsg_3c2c_transform(bsg_ctx ctx, size_t n_vec2, size_t n_aux, const double *ints_3c,
+                              const double *v_m12, int where, size_t bs, double thresh, int form, int n_digits,
+                              double *out, int out_where);
+
+/* ---- measurement helpers ---- */
+/* device FP64 FMA throughput probe (GFLOP/s) for the roofline denominator */
+bsg_status bsg_probe_fp64_peak(bsg_ctx ctx, double *gflops_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

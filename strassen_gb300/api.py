@@ -1,0 +1,341 @@
+"""Python mirror of the reference's interface over libbsgpu.so.
+
+Names and argument meaning follow the reference's C++ API:
+
+* :class:`BlockMemoryPool`   -- blockallocator.h:8-25
+* :class:`BlockSparseMatrix` -- blocksparsematrix.h:19-93
+* :func:`matmult`            -- blocksparsematrix.h:96-99
+* :func:`dot`                -- blocksparsematrix.h:102
+* :func:`matmult_strassen_sparse`, :func:`matmult_strassen_dryrun` -- strassen.hpp:511,688
+* :func:`tensormult_contract`, :func:`tensormult_batched` -- blocksparse3d_tensor.h:11-24
+* :func:`rik_occ_step`       -- occ_ri_k_step.cpp:83-130
+* :func:`transform_3c2c`     -- 3c_2c_transform.cpp:44-57
+
+Errors the reference turns into assert/exit(1) raise :class:`BsgError`.
+Dense arrays are column-major float64; numpy arrays live on the host, torch
+CUDA tensors on the device.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from ._lib import BSG_DEVICE, BSG_HOST, FORM_FP64, FORM_OZAKI, BsgError, RikArgs, check, lib  # noqa: F401
+
+_DEFAULT_CTX = None
+
+
+def _is_device(a):
+    return hasattr(a, "data_ptr") and getattr(a, "is_cuda", False)
+
+
+def _buf(a, dtype=np.float64):
+    """(pointer, where, keepalive) for a host numpy array or a CUDA tensor."""
+    if a is None:
+        return None, BSG_HOST, None
+    if _is_device(a):
+        return C.c_void_p(a.data_ptr()), BSG_DEVICE, a
+    if hasattr(a, "data_ptr"):  # CPU torch tensor
+        a = a.numpy()
+    arr = np.asfortranarray(a, dtype=dtype)
+    return arr.ctypes.data_as(C.c_void_p), BSG_HOST, arr
+
+
+class Context:
+    """A device plus the CUDA stream every call on it is ordered on."""
+
+    def __init__(self, device=0, stream=None):
+        h = C.c_void_p()
+        check(lib.bsg_ctx_create(device, stream, C.byref(h)))
+        self.h = h
+        self.device = device
+
+    def close(self):
+        if self.h:
+            lib.bsg_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def sync(self):
+        check(lib.bsg_ctx_sync(self.h))
+
+    def launch_count(self):
+        n = C.c_uint64()
+        check(lib.bsg_ctx_launch_count(self.h, C.byref(n)))
+        return n.value
+
+
+def default_context():
+    global _DEFAULT_CTX
+    if _DEFAULT_CTX is None:
+        _DEFAULT_CTX = Context(0)
+    return _DEFAULT_CTX
+
+
+class BlockMemoryPool:
+    """Device block pool shared by the matrices created on it."""
+
+    def __init__(self, block_elems, ctx=None, _handle=None):
+        self.ctx = ctx or default_context()
+        if _handle is not None:
+            self.h = _handle
+        else:
+            h = C.c_void_p()
+            check(lib.bsg_pool_create(self.ctx.h, block_elems, C.byref(h)))
+            self.h = h
+
+    def __del__(self):
+        try:
+            lib.bsg_pool_release(self.h)
+        except Exception:
+            pass
+
+    def adjust_blocksize(self, n):
+        check(lib.bsg_pool_adjust_blocksize(self.h, n))
+
+    def release_all_memory(self):
+        check(lib.bsg_pool_release_all_memory(self.h))
+
+    def stats(self):
+        t, f, b = C.c_size_t(), C.c_size_t(), C.c_size_t()
+        check(lib.bsg_pool_stats(self.h, C.byref(t), C.byref(f), C.byref(b)))
+        return {"blocks_total": t.value, "blocks_free": f.value, "bytes": b.value}
+
+
+class BlockSparseMatrix:
+    """BlockSparseMatrix<double>: a grid of dense blocks in a device pool."""
+
+    def __init__(self, nr, nc, bsr, bsc, thresh, pool=None, ctx=None, dense=None):
+        self.ctx = ctx or (pool.ctx if pool is not None else default_context())
+        h = C.c_void_p()
+        check(lib.bsg_bsm_create(self.ctx.h, nr, nc, bsr, bsc, float(thresh), pool.h if pool else None, C.byref(h)))
+        self.h = h
+        self.nr, self.nc, self.bsr, self.bsc = nr, nc, bsr, bsc
+        self.nrb = -(-nr // bsr) if nr else 0
+        self.ncb = -(-nc // bsc) if nc else 0
+        self.thresh = thresh
+        if dense is not None:
+            self.copy_from_input_matrix(dense)
+
+    @classmethod
+    def from_dense(cls, a, bsr, bsc, thresh, pool=None, ctx=None):
+        """BlockSparseMatrix(const Matrix&, bsr, bsc, thresh) blocksparsematrix.hpp:27-32"""
+        return cls(a.shape[0], a.shape[1], bsr, bsc, thresh, pool=pool, ctx=ctx, dense=a)
+
+    def __del__(self):
+        try:
+            lib.bsg_bsm_destroy(self.h)
+        except Exception:
+            pass
+
+    @property
+    def nblocks(self):
+        return self.nrb * self.ncb
+
+    def mem_pool(self):
+        h = C.c_void_p()
+        check(lib.bsg_bsm_pool(self.h, C.byref(h)))
+        return BlockMemoryPool(0, ctx=self.ctx, _handle=h)
+
+    def assign(self, other):
+        """operator= (occ_ri_k_step.cpp:112)"""
+        check(lib.bsg_bsm_assign(self.h, other.h))
+        return self
+
+    def copy_from_input_matrix(self, a):
+        assert tuple(a.shape) == (self.nr, self.nc), "copy_from_input_matrix: shape mismatch"
+        p, where, keep = _buf(a)
+        check(lib.bsg_bsm_copy_from_dense(self.h, p, where))
+        del keep
+
+    copy_from_input_array = copy_from_input_matrix
+
+    def fill_with_values(self, v):
+        check(lib.bsg_bsm_fill(self.h, float(v)))
+
+    def zero(self):
+        check(lib.bsg_bsm_zero(self.h))
+
+    def scale(self, s):
+        check(lib.bsg_bsm_scale(self.h, float(s)))
+
+    def __imul__(self, s):
+        self.scale(s)
+        return self
+
+    def __iadd__(self, o):
+        check(lib.bsg_bsm_add(self.h, o.h))
+        return self
+
+    def __isub__(self, o):
+        check(lib.bsg_bsm_sub(self.h, o.h))
+        return self
+
+    def add_transpose(self, o):
+        check(lib.bsg_bsm_add_transpose(self.h, o.h))
+
+    def calc_frobenius_norms(self):
+        check(lib.bsg_bsm_calc_norms(self.h))
+
+    def recompress(self):
+        check(lib.bsg_bsm_recompress(self.h))
+
+    def frobenius_norm(self):
+        v = C.c_double()
+        check(lib.bsg_bsm_frobenius_norm(self.h, C.byref(v)))
+        return v.value
+
+    def no_of_alloc_blocks(self):
+        v = C.c_size_t()
+        check(lib.bsg_bsm_no_of_alloc_blocks(self.h, C.byref(v)))
+        return v.value
+
+    def calc_alloc_dim(self):
+        v = C.c_size_t()
+        check(lib.bsg_bsm_calc_alloc_dim(self.h, C.byref(v)))
+        return v.value
+
+    def to_matrix(self, out=None):
+        """to_matrix / to_pointer (absent blocks read as zero)"""
+        if out is None:
+            out = np.zeros((self.nr, self.nc), dtype=np.float64, order="F")
+        p, where, keep = _buf(out)
+        check(lib.bsg_bsm_to_dense(self.h, p, where))
+        if where == BSG_HOST and keep is not out:
+            out[...] = keep
+        return out
+
+    def mask(self):
+        m = np.zeros(self.nblocks, dtype=np.uint8)
+        check(lib.bsg_bsm_get_mask(self.h, m.ctypes.data_as(C.c_void_p)))
+        return m
+
+    def norms(self):
+        n = np.zeros(self.nblocks, dtype=np.float64)
+        check(lib.bsg_bsm_get_norms(self.h, n.ctypes.data_as(C.c_void_p)))
+        return n
+
+
+def matmult(C_, A, tA, B, tB, thresh, alpha=1.0, beta=0.0, form=FORM_FP64, n_digits=4):
+    """matmult(C, A, transA, B, transB, thresh, alpha, beta); returns the
+    number of surviving block products."""
+    n = C.c_uint64()
+    check(lib.bsg_matmult_form(C_.h, A.h, int(bool(tA)), B.h, int(bool(tB)), float(thresh), float(alpha), float(beta),
+                               form, n_digits, C.byref(n)))
+    return n.value
+
+
+def dot(A, B, thresh=0.0):
+    v = C.c_double()
+    check(lib.bsg_dot(A.h, B.h, float(thresh), C.byref(v)))
+    return v.value
+
+
+def matmult_strassen_dryrun(A, B, thresh_per_block):
+    """Decision tree per level (bool arrays, index si + sj*n + sk*n*n) and the
+    flop count per level."""
+    nb = A.nrb
+    sizes = []
+    l = 0
+    while 2 ** l <= 2 * nb + 1 and l < 64:
+        sizes.append((-(-nb // 2 ** (l + 1))) ** 3)
+        l += 1
+    cap = sum(sizes) + 8
+    tree = np.zeros(cap, dtype=np.uint8)
+    flops = np.zeros(70, dtype=np.uint64)
+    nl = C.c_int()
+    check(lib.bsg_strassen_dryrun(A.h, B.h, float(thresh_per_block), C.byref(nl), tree.ctypes.data_as(C.c_void_p),
+                                  cap, flops.ctypes.data_as(C.POINTER(C.c_uint64))))
+    levels, off = [], 0
+    for lv in range(nl.value):
+        n = -(-nb // 2 ** (lv + 1))
+        levels.append(tree[off:off + n ** 3].astype(bool))
+        off += n ** 3
+    return levels, flops[: nl.value + 1].copy()
+
+
+def matmult_strassen_sparse(C_, A, tA, B, tB, thresh, alpha, beta, min_size_for_strassen, form=FORM_FP64,
+                            n_digits=4):
+    if form == FORM_FP64:
+        check(lib.bsg_matmult_strassen_sparse(C_.h, A.h, int(bool(tA)), B.h, int(bool(tB)), float(thresh),
+                                              float(alpha), float(beta), int(min_size_for_strassen)))
+    else:
+        if tA or tB or alpha != 1.0:
+            raise BsgError(2, "matmult_strassen_sparse supports no transposes and alpha = 1")
+        check(lib.bsg_matmult_strassen_sparse_form(C_.h, A.h, B.h, float(thresh), int(min_size_for_strassen), form,
+                                                   n_digits))
+
+
+def _handles(ms):
+    arr = (C.c_void_p * len(ms))(*[m.h.value for m in ms])
+    return arr
+
+
+def tensormult_contract(C_, As, tA, Bs, tB, thresh, alpha=1.0, beta=0.0):
+    """C_ij = sum_l sum_k op(A^l)_ik op(B^l)_kj"""
+    assert len(As) == len(Bs) and len(As) > 0
+    check(lib.bsg_tensormult_contract(C_.h, _handles(As), int(bool(tA)), _handles(Bs), int(bool(tB)), len(As),
+                                      float(thresh), float(alpha), float(beta)))
+
+
+def tensormult_batched(Cs, A, tA, Bs, tB, thresh, alpha=1.0, beta=0.0):
+    """C^l_ij = sum_k op(A)_ik op(B^l)_kj for every slice l"""
+    assert len(Cs) == len(Bs) and len(Bs) > 0
+    check(lib.bsg_tensormult_batched(_handles(Cs), A.h, int(bool(tA)), _handles(Bs), int(bool(tB)), len(Bs),
+                                     float(thresh), float(alpha), float(beta)))
+
+
+def rik_occ_step(ints, keys, c_occ, n_bf, n_aux, n_occ, bs, thresh, n_part=1, form=FORM_FP64, n_digits=4,
+                 p_chunk=0, out=None, ctx=None, stats=False):
+    """K_{mu j} = sum_{P,i} (mu i|P)[(ij|P)+(ji|P)] (occ_ri_k_step.cpp:83-130).
+
+    ints: n_vec2 x n_aux, keys: n_vec2 uint64, c_occ: n_bf x n_occ; numpy
+    (host) or torch CUDA tensors (device, all three alike)."""
+    ctx = ctx or default_context()
+    pi, w1, k1 = _buf(ints)
+    pk, w2, k2 = _buf(keys, np.uint64)
+    pc, w3, k3 = _buf(c_occ)
+    if not (w1 == w2 == w3):
+        raise BsgError(1, "ints, keys and c_occ must all be host or all device arrays")
+    n_vec2 = ints.shape[0]
+    a = RikArgs(n_bf, n_aux, n_occ, n_vec2, pi, pk, pc, w1, bs, float(thresh), n_part, form, n_digits, p_chunk)
+    if out is None:
+        out = np.zeros((n_bf, n_occ), dtype=np.float64, order="F")
+    po, wo, ko = _buf(out)
+    st = (C.c_uint64 * 5)()
+    check(lib.bsg_rik_occ_step(ctx.h, C.byref(a), po, wo, st))
+    if wo == BSG_HOST and ko is not out:
+        out[...] = ko
+    del k1, k2, k3
+    return (out, list(st)) if stats else out
+
+
+def transform_3c2c(ints_3c, v_m12, bs, thresh, form=FORM_FP64, n_digits=4, out=None, ctx=None):
+    """(mu nu|P)' = sum_Q (mu nu|Q)(Q|P)^{-1/2} (3c_2c_transform.cpp:44-57)"""
+    ctx = ctx or default_context()
+    px, w1, k1 = _buf(ints_3c)
+    pv, w2, k2 = _buf(v_m12)
+    if w1 != w2:
+        raise BsgError(1, "inputs must both be host or both device arrays")
+    n_vec2, n_aux = ints_3c.shape
+    if out is None:
+        out = np.zeros((n_vec2, n_aux), dtype=np.float64, order="F")
+    po, wo, ko = _buf(out)
+    check(lib.bsg_3c2c_transform(ctx.h, n_vec2, n_aux, px, pv, w1, bs, float(thresh), form, n_digits, po, wo))
+    if wo == BSG_HOST and ko is not out:
+        out[...] = ko
+    del k1, k2
+    return out
+
+
+def probe_fp64_peak(ctx=None):
+    ctx = ctx or default_context()
+    v = C.c_double()
+    check(lib.bsg_probe_fp64_peak(ctx.h, C.byref(v)))
+    return v.value

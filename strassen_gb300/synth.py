@@ -100,3 +100,117 @@ def block_mask_matrix(seed, stream, n, m, bs, density):
     I = np.arange(n) // bs
     J = np.arange(m) // bs
     return np.asfortranarray(keep[I][:, J] * gauss_matrix(seed, stream, n, m))
+
+
+def _torch_splitmix64(x):
+    """splitmix64 on int64 torch tensors (two's-complement wraparound gives the
+    uint64 bits; logical shifts are emulated by masking)."""
+    import torch
+
+    def srl(v, k):
+        return (v >> k) & ((1 << (64 - k)) - 1)
+
+    gold = int(np.int64(np.uint64(0x9E3779B97F4A7C15).view(np.int64)))
+    m1 = int(np.int64(np.uint64(0xBF58476D1CE4E5B9).view(np.int64)))
+    m2 = int(np.int64(np.uint64(0x94D049BB133111EB).view(np.int64)))
+    z = x + gold
+    z = (z ^ srl(z, 30)) * m1
+    z = (z ^ srl(z, 27)) * m2
+    return z ^ srl(z, 31)
+
+
+def gauss_torch(key, idx):
+    """`gauss` on a torch int64 index tensor (any device); bit-identical to the
+    numpy version."""
+    import torch
+
+    k = int(np.int64(np.uint64(key).view(np.int64)))
+    i4 = idx * 4
+    acc = []
+    for j in range(4):
+        h = _torch_splitmix64((i4 + j) ^ k)
+        u = ((h >> 11) & ((1 << 53) - 1)).to(torch.float64) * (1.0 / 9007199254740992.0)
+        acc.append(u)
+    return (((acc[0] + acc[1]) + (acc[2] + acc[3])) - 2.0) * _SQRT3
+
+
+class RikSystem:
+    """Synthetic RI-K inputs: atoms in a cubic box, `nbf` basis and `naux`
+    auxiliary functions per atom, significant (mu <= nu) pairs kept where
+    exp(-r_ab^2/2) >= sig.  Integrals (mu nu|P) = exp(-(r_ab^2 + r_ap^2)/2) *
+    deviate, the Coulomb metric's inverse square root from a random SPD matrix
+    with a geometric spectrum of the given condition number, and localized
+    occupied orbitals (Gaussian envelope around a centre atom, orthonormalized
+    by QR)."""
+
+    def __init__(self, seed=42, n_atoms=40, nbf=24, naux=84, n_occ=200, box=12.0, sig=1e-10, cond=1e4, width=2.0):
+        self.seed, self.n_atoms, self.nbf, self.naux, self.box = seed, n_atoms, nbf, naux, box
+        self.n_bf, self.n_aux, self.n_occ = n_atoms * nbf, n_atoms * naux, n_occ
+        key = stream_key(seed, 1000)
+        self.pos = uniform(key, np.arange(3 * n_atoms, dtype=np.uint64)).reshape(n_atoms, 3) * box
+        d = self.pos[:, None, :] - self.pos[None, :, :]
+        self.r2 = (d * d).sum(axis=2)
+        self.pair_env = np.exp(-0.5 * self.r2)
+        atom = np.arange(self.n_bf) // nbf
+        mu, nu = np.triu_indices(self.n_bf)  # row-major upper triangle: mu <= nu
+        keep = self.pair_env[atom[mu], atom[nu]] >= sig
+        mu, nu = mu[keep], nu[keep]
+        order = np.lexsort((mu, nu))  # column-major: by nu, then mu
+        self.mu, self.nu = mu[order], nu[order]
+        self.keys = (self.mu + self.nu * self.n_bf).astype(np.uint64)
+        self.n_vec2 = len(self.keys)
+        self.a_of_v = atom[self.mu]
+        self.b_of_v = atom[self.nu]
+        # (a, b, p) envelope table
+        self.env3 = np.exp(-0.5 * (self.r2[:, :, None] + self.r2[:, None, :]))  # [a, b, p] = r_ab^2 + r_ap^2
+        self.ints_key = stream_key(seed, 1001)
+
+    def ints_3c(self, p_lo=0, p_hi=None):
+        """columns P in [p_lo, p_hi) of the compressed (mu nu|P), n_vec2 x nP"""
+        p_hi = self.n_aux if p_hi is None else p_hi
+        P = np.arange(p_lo, p_hi)
+        env = self.env3[self.a_of_v[:, None], self.b_of_v[:, None], (P // self.naux)[None, :]]
+        idx = (np.arange(self.n_vec2, dtype=np.uint64)[:, None] + P.astype(np.uint64)[None, :] * np.uint64(self.n_vec2))
+        return np.asfortranarray(env * gauss(self.ints_key, idx))
+
+    def ints_3c_rows(self, r_lo, r_hi):
+        """rows [r_lo, r_hi) of the compressed (mu nu|P) over every P"""
+        v = np.arange(r_lo, r_hi)
+        P = np.arange(self.n_aux)
+        env = self.env3[self.a_of_v[v][:, None], self.b_of_v[v][:, None], (P // self.naux)[None, :]]
+        idx = v.astype(np.uint64)[:, None] + P.astype(np.uint64)[None, :] * np.uint64(self.n_vec2)
+        return np.asfortranarray(env * gauss(self.ints_key, idx))
+
+    def ints_3c_torch(self, device, p_lo=0, p_hi=None, dtype=None):
+        """the same columns generated on a torch device (bit-identical)"""
+        import torch
+
+        p_hi = self.n_aux if p_hi is None else p_hi
+        env3 = torch.from_numpy(np.ascontiguousarray(self.env3)).to(device)
+        a = torch.from_numpy(self.a_of_v.astype(np.int64)).to(device)
+        b = torch.from_numpy(self.b_of_v.astype(np.int64)).to(device)
+        out = torch.empty((p_hi - p_lo, self.n_vec2), dtype=torch.float64, device=device)  # row P = column of F-order
+        v = torch.arange(self.n_vec2, dtype=torch.int64, device=device)
+        for P in range(p_lo, p_hi):
+            e = env3[a, b, P // self.naux]
+            out[P - p_lo] = e * gauss_torch(self.ints_key, v + P * self.n_vec2)
+        return out  # out.T is the column-major n_vec2 x nP matrix
+
+    def v_m12(self, cond=1e4):
+        """(P|Q)^{-1/2} of a random SPD metric with condition number `cond`"""
+        n = self.n_aux
+        g = gauss_matrix(self.seed, 1002, n, n)
+        q, r = np.linalg.qr(g)
+        q = q * np.sign(np.diag(r))[None, :]
+        lam = np.geomspace(1.0, 1.0 / cond, n)
+        return np.asfortranarray((q * lam ** -0.5) @ q.T)
+
+    def c_occ(self, width=2.0):
+        """localized occupied orbitals: orbital i centred on atom i % n_atoms"""
+        atom = np.arange(self.n_bf) // self.nbf
+        centre = np.arange(self.n_occ) % self.n_atoms
+        env = np.exp(-0.5 * self.r2[atom[:, None], centre[None, :]] / width ** 2)
+        c = env * gauss_matrix(self.seed, 1003, self.n_bf, self.n_occ)
+        q, r = np.linalg.qr(c)
+        q = q * np.sign(np.diag(r))[None, :]
+        return np.asfortranarray(q)
