@@ -159,6 +159,22 @@ typedef struct bsg_rik_args {
 bsg_status bsg_rik_occ_step(bsg_ctx ctx, const bsg_rik_args *args, double *K_out, int out_where,
                             uint64_t stats_out[5]);
 
+/* The occ-RI-K step above without any device allocation (no counterpart in
+ * the reference, which runs on the host).  For callers that cannot allocate
+ * device memory: code under a framework whose caching allocator owns the
+ * device heap, processes with a fixed memory budget, and latency-critical
+ * streams that cannot absorb cudaFree's implicit synchronization.  Inputs
+ * (args->where must be BSG_DEVICE) and K_dev (n_bf x n_occ, column-major) are
+ * the caller's device buffers; FP64 form only.  All intermediates live in a
+ * 32 MiB file-scope device array that every GPU loading the library keeps
+ * until exit; problems whose per-aux-function workspace exceeds it are
+ * rejected with BSG_ERR_ARG.  The first call on a device looks up that
+ * array's address (make it before any stream capture); calls share the array,
+ * so calls that overlap on the GPU race -- serialize them.  Results equal
+ * bsg_rik_occ_step's bit for bit. */
+bsg_status bsg_rik_occ_step_noalloc(const bsg_rik_args *args, double *K_dev, void *cuda_stream,
+                                    uint64_t stats_out[5]);
+
 /* 3c->2c transform (3c_2c_transform.cpp:44-57): out = X * V^{-1/2} through
  * matmult on block-sparse copies (input threshold 0, out pre-filled 0). */
 bsg_status bsg_3c2c_transform(bsg_ctx ctx, size_t n_vec2, size_t n_aux, const double *ints_3c,

@@ -460,3 +460,175 @@ extern "C" bsg_status bsg_3c2c_transform(bsg_ctx ctx, size_t n_vec2, size_t n_au
         cleanup();
     });
 }
+
+// ---------------------------------------------------------------------------
+// Allocation-free RI-K step.
+//
+// For callers that must not allocate device memory themselves: code running
+// under a framework whose caching allocator owns the whole device heap (a
+// cudaMalloc/cudaFree behind its back fragments that heap, and cudaFree
+// synchronizes the device), services with a fixed per-process memory budget,
+// and code on latency-critical streams where an allocation's implicit
+// synchronization is not acceptable.  All intermediates live in one
+// file-scope device array of kRikScratchBytes; every GPU that loads this
+// library keeps that array until the process exits.  The first call on a
+// device looks up the array's device address (cudaGetSymbolAddress) with
+// that device current; make that first call before any stream capture.
+// Every call reuses the same array, so calls that overlap on the GPU (other
+// streams, other host threads) race on it: serialize them.
+// ---------------------------------------------------------------------------
+
+namespace bsg {
+
+constexpr size_t kRikScratchBytes = 32ull << 20;  // 32 MiB
+static __device__ __align__(256) unsigned char g_rik_scratch[kRikScratchBytes];
+
+constexpr int kMaxDevices = 64;
+static std::mutex g_rik_scratch_mu;
+static void *g_rik_scratch_addr[kMaxDevices] = {};
+
+// device address of g_rik_scratch on the current device (looked up once)
+static void *rik_scratch_address() {
+    int dev = 0;
+    BSG_CUDA(cudaGetDevice(&dev));
+    BSG_REQUIRE(dev >= 0 && dev < kMaxDevices, BSG_ERR_UNSUPPORTED, "device index out of range");
+    std::lock_guard<std::mutex> lk(g_rik_scratch_mu);
+    if (!g_rik_scratch_addr[dev]) {
+        void *p = nullptr;
+        BSG_CUDA(cudaGetSymbolAddress(&p, g_rik_scratch));
+        BSG_REQUIRE(p != nullptr, BSG_ERR_CUDA, "cudaGetSymbolAddress returned NULL for the RI-K scratch array");
+        g_rik_scratch_addr[dev] = p;
+    }
+    return g_rik_scratch_addr[dev];
+}
+
+// per-partition P range inside a chunk (libgomp static schedule), on device
+__global__ void k_part_table(uint32_t *plo, uint32_t *phi, int T, size_t n_aux, size_t P0, size_t np) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= T) return;
+    const size_t q = n_aux / (size_t)T, r = n_aux % (size_t)T, tt = (size_t)t;
+    const size_t lo_all = tt * q + (tt < r ? tt : r), hi_all = lo_all + q + (tt < r ? 1 : 0);
+    const size_t lo = lo_all > P0 ? lo_all : P0, hi = hi_all < P0 + np ? hi_all : P0 + np;
+    plo[t] = lo < hi ? (uint32_t)(lo - P0) : 0;
+    phi[t] = lo < hi ? (uint32_t)(hi - P0) : 0;
+}
+
+struct ScratchLayout {
+    size_t off = 0;
+    size_t take(size_t bytes) {
+        const size_t o = off;
+        off += (bytes + 255) & ~size_t(255);
+        return o;
+    }
+};
+
+}  // namespace bsg
+
+extern "C" bsg_status bsg_rik_occ_step_noalloc(const bsg_rik_args *a, double *K_dev, void *cuda_stream,
+                                               uint64_t stats_out[5]) {
+    return guard([&] {
+        BSG_REQUIRE(a && K_dev, BSG_ERR_ARG, "NULL argument");
+        BSG_REQUIRE(a->where == BSG_DEVICE, BSG_ERR_ARG, "the allocation-free RI-K step takes device inputs only");
+        BSG_REQUIRE(a->form == BSG_FORM_FP64, BSG_ERR_UNSUPPORTED, "the allocation-free RI-K step is FP64 only");
+        BSG_REQUIRE(a->bs > 0 && a->n_part >= 1 && a->n_bf > 0 && a->n_occ > 0, BSG_ERR_ARG, "bad dimensions");
+        BSG_REQUIRE(a->n_vec2 == 0 || (a->ints && a->keys), BSG_ERR_ARG, "integrals or keys missing");
+        BSG_REQUIRE(a->c_occ, BSG_ERR_ARG, "occupied coefficients missing");
+        BSG_REQUIRE((size_t)a->bs * a->bs <= (size_t)kREPT * 256, BSG_ERR_UNSUPPORTED, "bs <= 64 required");
+        cudaStream_t s = (cudaStream_t)cuda_stream;
+        const size_t n_bf = a->n_bf, n_occ = a->n_occ, bs = a->bs, n_aux = a->n_aux, n_vec2 = a->n_vec2;
+        const size_t nb = ceil_div(n_bf, bs), nob = ceil_div(n_occ, bs);
+        const int T = a->n_part;
+        // fixed part, then as many aux functions per chunk as fit
+        ScratchLayout fixed;
+        const size_t oK = fixed.take((size_t)T * n_bf * n_occ * 8), oCn = fixed.take(nb * nob * 8),
+                     oLo = fixed.take((size_t)T * 4), oHi = fixed.take((size_t)T * 4), oCnt = fixed.take(5 * 8),
+                     oBad = fixed.take(8);
+        auto per_chunk = [&](size_t pc) {
+            ScratchLayout l;
+            l.off = fixed.off;
+            l.take(pc * n_bf * n_bf * 8);
+            l.take(pc * nb * nb * 8);
+            l.take(pc * nb * nb);
+            l.take(pc * n_bf * n_occ * 8);
+            l.take(pc * nb * nob * 8);
+            l.take(pc * nb * nob);
+            l.take(pc * n_occ * n_occ * 8);
+            l.take(pc * nob * nob);
+            l.take(pc * n_occ * n_occ * 8);
+            l.take(pc * nob * nob * 8);
+            l.take(pc * nob * nob);
+            return l.off;
+        };
+        BSG_REQUIRE(per_chunk(1) <= kRikScratchBytes, BSG_ERR_ARG,
+                    "RI-K problem too large for the 32 MiB allocation-free scratch (needs " +
+                        std::to_string(per_chunk(1)) + " bytes for one aux function)");
+        size_t pc = a->p_chunk ? a->p_chunk : n_aux;
+        pc = std::max<size_t>(1, std::min(pc, std::max<size_t>(1, n_aux)));
+        while (pc > 1 && per_chunk(pc) > kRikScratchBytes) pc = std::max<size_t>(1, pc / 2);
+        unsigned char *base = static_cast<unsigned char *>(rik_scratch_address());
+        ScratchLayout l;
+        l.off = fixed.off;
+        double *dU = (double *)(base + l.take(pc * n_bf * n_bf * 8));
+        double *dun = (double *)(base + l.take(pc * nb * nb * 8));
+        uint8_t *duf = base + l.take(pc * nb * nb);
+        double *dmui = (double *)(base + l.take(pc * n_bf * n_occ * 8));
+        double *dmn = (double *)(base + l.take(pc * nb * nob * 8));
+        uint8_t *dmf = base + l.take(pc * nb * nob);
+        double *dij = (double *)(base + l.take(pc * n_occ * n_occ * 8));
+        uint8_t *dijf = base + l.take(pc * nob * nob);
+        double *dijs = (double *)(base + l.take(pc * n_occ * n_occ * 8));
+        double *dsn = (double *)(base + l.take(pc * nob * nob * 8));
+        uint8_t *dsf = base + l.take(pc * nob * nob);
+        double *dK = (double *)(base + oK);
+        double *dcn = (double *)(base + oCn);
+        uint32_t *dplo = (uint32_t *)(base + oLo), *dphi = (uint32_t *)(base + oHi);
+        auto *cnt = (unsigned long long *)(base + oCnt);
+        int *bad = (int *)(base + oBad);
+        // the array keeps the previous call's contents: clear what accumulates
+        BSG_CUDA(cudaMemsetAsync(dK, 0, (size_t)T * n_bf * n_occ * 8, s));
+        BSG_CUDA(cudaMemsetAsync(cnt, 0, 5 * 8, s));
+        BSG_CUDA(cudaMemsetAsync(bad, 0, 4, s));
+        if (n_vec2) {
+            k_check_keys<<<(unsigned)ceil_div(n_vec2, 256), 256, 0, s>>>(a->keys, n_vec2, (uint64_t)(n_bf * n_bf), bad);
+            int h = 0;
+            BSG_CUDA(cudaMemcpyAsync(&h, bad, 4, cudaMemcpyDeviceToHost, s));
+            BSG_CUDA(cudaStreamSynchronize(s));
+            BSG_REQUIRE(!h, BSG_ERR_ARG, "v2m key outside the N_bf x N_bf matrix");
+        }
+        const int wpb = 8;
+        k_cnorms<<<(unsigned)ceil_div(nb * nob, wpb), wpb * 32, 0, s>>>(a->c_occ, n_bf, n_occ, bs, nb, nob, dcn);
+        const double tpb_u = 1e-20 * (double)(bs * bs);
+        const double tpb = a->thresh * (double)(bs * bs * bs);
+        for (size_t P0 = 0; P0 < n_aux; P0 += pc) {
+            const size_t np = std::min(pc, n_aux - P0);
+            BSG_CUDA(cudaMemsetAsync(dU, 0, np * n_bf * n_bf * 8, s));
+            if (n_vec2) {
+                dim3 g((unsigned)ceil_div(n_vec2, 256), (unsigned)np);
+                k_scatter<<<g, 256, 0, s>>>(a->ints, a->keys, n_vec2, P0, n_bf * n_bf, dU);
+            }
+            k_unorms<<<(unsigned)ceil_div(np * nb * nb, wpb), wpb * 32, 0, s>>>(dU, n_bf, bs, nb, np, tpb_u, dun, duf);
+            k_mui<<<(unsigned)(np * nb * nob), threads_for((int)bs, (int)bs), 0, s>>>(
+                dU, dun, duf, a->c_occ, dcn, n_bf, n_occ, bs, nb, nob, tpb, dmui, dmn, dmf, cnt + 0);
+            k_ij<<<(unsigned)(np * nob * nob), threads_for((int)bs, (int)bs), 0, s>>>(
+                a->c_occ, dcn, dmui, dmn, dmf, n_bf, n_occ, bs, nb, nob, tpb, dij, dijf, cnt + 1);
+            k_ijs<<<(unsigned)(np * nob * nob), 128, 0, s>>>(dij, dijf, n_occ, bs, nob, dijs, dsn, dsf);
+            k_part_table<<<(unsigned)ceil_div((size_t)T, 128), 128, 0, s>>>(dplo, dphi, T, n_aux, P0, np);
+            k_kupd<<<(unsigned)((size_t)T * nb * nob), threads_for((int)bs, (int)bs), 0, s>>>(
+                dmui, dmn, dmf, dijs, dsn, dsf, n_bf, n_occ, bs, nb, nob, tpb, dplo, dphi, dK, cnt + 2);
+            cudaError_t e = cudaGetLastError();
+            if (e != cudaSuccess) throw Error{BSG_ERR_CUDA, std::string("rik (no-alloc) chunk: ") + cudaGetErrorString(e)};
+        }
+        if (n_aux)
+            k_kreduce<<<(unsigned)ceil_div(n_bf * n_occ, 256), 256, 0, s>>>(dK, n_bf * n_occ, T, K_dev);
+        else
+            BSG_CUDA(cudaMemsetAsync(K_dev, 0, n_bf * n_occ * 8, s));
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) throw Error{BSG_ERR_CUDA, std::string("rik (no-alloc) reduce: ") + cudaGetErrorString(e)};
+        if (stats_out) {
+            unsigned long long h[5];
+            BSG_CUDA(cudaMemcpyAsync(h, cnt, 5 * 8, cudaMemcpyDeviceToHost, s));
+            BSG_CUDA(cudaStreamSynchronize(s));
+            for (int i = 0; i < 5; ++i) stats_out[i] = h[i];
+        }
+    });
+}
