@@ -73,11 +73,7 @@ void launch_gemm64(bsg_ctx ctx, const GemmItem *d_items, size_t n_items, const G
     }
 }
 
-struct Geom {
-    int tA, tB;
-    size_t nib, njb, nkb, ibs, jbs, kbs, ni, nj, nk;
-    double tpb;
-};
+using Geom = ScreenGeom;
 
 __device__ __forceinline__ bool survives(const SliceOps &s, const Geom &g, size_t ib, size_t jb, size_t kb,
                                          size_t *ai_out, size_t *bi_out) {
@@ -212,6 +208,7 @@ uint64_t screened_product(bsg_ctx ctx, const std::vector<bsg_bsm> &Cs, const std
     std::vector<GemmItem> items;
     int max_r = 0, max_c = 0;
     std::vector<bool> touched(Cs.size(), false);
+    std::vector<uint32_t> item_ib, item_jb;
     for (size_t x = 0; x < n_out; ++x) {
         off[x] = (uint32_t)total;
         if (!cnt[x]) continue;
@@ -232,11 +229,19 @@ uint64_t screened_product(bsg_ctx ctx, const std::vector<bsg_bsm> &Cs, const std
         max_r = std::max(max_r, it.rows);
         max_c = std::max(max_c, it.cols);
         items.push_back(it);
+        item_ib.push_back((uint32_t)ib);
+        item_jb.push_back((uint32_t)jb);
         total += cnt[x];
     }
     for (size_t c = 0; c < Cs.size(); ++c)
         if (touched[c]) Cs[c]->upload_table();
     if (!total) return 0;
+    if (form == BSG_FORM_OZAKI) {
+        BSG_REQUIRE(As.size() == 1 && Cs.size() == 1, BSG_ERR_UNSUPPORTED, "Ozaki form: single products only");
+        ozaki_screened(ctx, C0, A0, B0, g, items, item_ib, item_jb, alpha, n_digits, s);
+        BSG_CUDA(cudaStreamSynchronize(s));
+        return total;
+    }
     DevBuf doff(n_out * 4, s), dpairs(total * sizeof(GemmPair), s), ditems(items.size() * sizeof(GemmItem), s);
     BSG_CUDA(cudaMemcpyAsync(doff.p, off.data(), n_out * 4, cudaMemcpyHostToDevice, s));
     BSG_CUDA(cudaMemcpyAsync(ditems.p, items.data(), items.size() * sizeof(GemmItem), cudaMemcpyHostToDevice, s));
@@ -244,12 +249,7 @@ uint64_t screened_product(bsg_ctx ctx, const std::vector<bsg_bsm> &Cs, const std
                                                            n_c, doff.as<uint32_t>(), dpairs.as<GemmPair>());
     ctx->note_launch();
     ctx->check_launch("pair fill");
-    if (form == BSG_FORM_FP64) {
-        launch_gemm64(ctx, ditems.as<GemmItem>(), items.size(), dpairs.as<GemmPair>(), tA, tB, alpha, max_r, max_c, s);
-    } else {
-        ozaki_grouped_gemm(ctx, items, ditems.as<GemmItem>(), dpairs.as<GemmPair>(), total, tA, tB, alpha, max_r,
-                           max_c, g.kbs, n_digits, s);
-    }
+    launch_gemm64(ctx, ditems.as<GemmItem>(), items.size(), dpairs.as<GemmPair>(), tA, tB, alpha, max_r, max_c, s);
     BSG_CUDA(cudaStreamSynchronize(s));
     return total;
 }

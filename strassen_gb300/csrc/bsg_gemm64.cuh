@@ -28,6 +28,13 @@ struct GemmPair {
 void launch_gemm64(bsg_ctx ctx, const GemmItem *d_items, size_t n_items, const GemmPair *d_pairs, int tA, int tB,
                    double alpha, int max_rows, int max_cols, cudaStream_t s);
 
+// geometry of a screened product op(A) (ni x nk) * op(B) (nk x nj)
+struct ScreenGeom {
+    int tA, tB;
+    size_t nib, njb, nkb, ibs, jbs, kbs, ni, nj, nk;
+    double tpb;
+};
+
 // Screened block-triple enumeration for matmult and the 3-index tensor
 // products.  A "slice" is one (A, B) operand pair; an output matrix sums the
 // slices in [lo, hi) (contract) or exactly one slice (batched).

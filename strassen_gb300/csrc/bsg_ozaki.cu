@@ -1,18 +1,508 @@
-// Ozaki-style split-precision block products on tcgen05 tensor cores.
+// Ozaki-scheme split-precision block products on tcgen05 tensor cores
+// (see bsg_ozaki.cuh for the arithmetic).
+//
+// k_ozgemm: persistent, one CTA per SM, 6 warps.
+//   warp 0     producer: per step, bulk-copies the digit images of up to R
+//              A blocks (one per row slot; a zero image where the screen
+//              drops the pair) and of the shared B block into a stage of the
+//              shared-memory ring (cp.async.bulk, mbarrier transaction count).
+//   warp 1     MMA issuer (one thread): per k16 step and A digit i, one
+//              tcgen05.mma D_i x [E_1..E_{nd+1-i}] into TMEM region i; a chain
+//              of <= 512 k is committed to the epilogue.
+//   warps 2-5  epilogue: drain the TMEM regions of a chain (tcgen05.ld),
+//              convert to FP64 and accumulate; at the end of a tile scale by
+//              2^(e_row + f_col - 14) and write the FP64 output blocks.
+// Every mbarrier wait is bounded (2 s); a timeout raises a flag that ends
+// all roles and is returned as BSG_ERR_TIMEOUT.
+#include <algorithm>
+#include <mutex>
+
 #include "bsg_ozaki.cuh"
+#include "bsg_rik.cuh"
+#include "bsg_tc.cuh"
 
 namespace bsg {
+
+using bf16 = __nv_bfloat16;
+
+static __device__ __align__(128) bf16 g_oz_zero[8 * 1024];  // 16 KB of zeros (largest A plane image 8 KB)
+
+static void *oz_zero_image() {
+    static std::mutex mu;
+    static void *addr[64] = {};
+    int dev = 0;
+    BSG_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(mu);
+    if (!addr[dev]) BSG_CUDA(cudaGetSymbolAddress(&addr[dev], g_oz_zero));
+    return addr[dev];
+}
+
+static int round_up(int x, int m) { return (x + m - 1) / m * m; }
+
+OzShape oz_shape(int bs_rows, int bs_k, int bs_cols, int nd) {
+    OzShape s;
+    s.nd = nd;
+    s.mp = round_up(bs_rows, 8);
+    s.kp = round_up(bs_k, 16);
+    s.np = round_up(bs_cols, 16);
+    s.R = std::min(kOzMaxSlots, 128 / s.mp);
+    s.F = std::max(1, 512 / s.kp);
+    return s;
+}
+
+static uint32_t oz_stage_bytes(const OzShape &sh) {
+    return (uint32_t)sh.nd * 128u * sh.kp * 2u + (uint32_t)sh.nd * sh.np * sh.kp * 2u;
+}
+constexpr uint32_t kOzSmemBudget = 200u * 1024u;
+
+int oz_default_digits(int requested, int bs_rows, int bs_k, int bs_cols) {
+    if (requested) {
+        const OzShape sh = oz_shape(bs_rows, bs_k, bs_cols, requested);
+        BSG_REQUIRE(requested >= 2 && requested <= kOzMaxDigits, BSG_ERR_ARG, "Ozaki form: 2..8 digits");
+        BSG_REQUIRE(kOzSmemBudget / oz_stage_bytes(sh) >= 2, BSG_ERR_UNSUPPORTED,
+                    "Ozaki form: this digit count does not fit shared memory for the block size");
+        return requested;
+    }
+    // 5 digits (~1e-11 relative per product) where two pipeline stages fit, else 4
+    const OzShape s5 = oz_shape(bs_rows, bs_k, bs_cols, 5);
+    return kOzSmemBudget / oz_stage_bytes(s5) >= 2 ? 5 : 4;
+}
+
+struct OzKParams {
+    int mp, kp, R, nd, S, F;
+    uint32_t tmem_cols;
+    uint32_t tx_bytes;
+    const bf16 *zero;
+    double alpha;
+};
+
+template <int NP>
+__global__ void __launch_bounds__(192, 1)
+    k_ozgemm(const OzTile *__restrict__ tiles, uint32_t n_tiles, const OzStep *__restrict__ steps,
+             const bf16 *__restrict__ a_img, const bf16 *__restrict__ b_img, OzKParams P, int *__restrict__ err) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t a_plane = 128u * P.kp * 2u;  // bytes of one A digit plane in a stage
+    const uint32_t a_stage = P.nd * a_plane;
+    const uint32_t b_stage = (uint32_t)P.nd * NP * P.kp * 2u;
+    const uint32_t stage_bytes = a_stage + b_stage;
+    const uint32_t slot_bytes = (uint32_t)P.mp * P.kp * 2u;
+    const size_t a_plane_elems = (size_t)P.mp * P.kp, b_img_elems = (size_t)P.nd * NP * P.kp;
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + (size_t)P.S * stage_bytes);
+    uint64_t *empty = full + P.S;
+    uint64_t *tfull = empty + P.S;
+    uint64_t *tempty = tfull + 1;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(tempty + 1);
+    volatile int *abort = reinterpret_cast<volatile int *>(tmem_slot + 1);
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < P.S; ++s) {
+            tc::mbar_init(&full[s], 1);
+            tc::mbar_init(&empty[s], 1);
+        }
+        tc::mbar_init(tfull, 1);
+        tc::mbar_init(tempty, 4);
+        *abort = 0;
+        tc::fence_barrier_init();
+    }
+    // rows past the last slot are never copied: keep them zero
+    for (uint32_t i = threadIdx.x; i < (uint32_t)P.S * stage_bytes / 16u; i += blockDim.x)
+        reinterpret_cast<uint4 *>(smem)[i] = make_uint4(0, 0, 0, 0);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    if (warp == 1) {
+        tc::tmem_alloc(tmem_slot, P.tmem_cols);
+        tc::tmem_relinquish();
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        // ---------------- producer ----------------
+        uint32_t it = 0;
+        for (uint32_t t = blockIdx.x; t < n_tiles && !*abort; t += gridDim.x) {
+            const uint32_t s0 = tiles[t].s0, ns = tiles[t].ns;
+            for (uint32_t k = 0; k < ns; ++k, ++it) {
+                const uint32_t stage = it % P.S, ph = (it / P.S) & 1u;
+                if (!tc::mbar_wait(&empty[stage], ph ^ 1u, abort)) break;
+                const OzStep st = steps[s0 + k];
+                uint8_t *sA = smem + (size_t)stage * stage_bytes;
+                uint8_t *sB = sA + a_stage;
+                if (lane == 0) tc::mbar_arrive_expect_tx(&full[stage], P.tx_bytes);
+                __syncwarp();
+                if (lane < P.R) {
+                    const uint32_t ai = st.a[lane];
+                    for (int i = 0; i < P.nd; ++i) {
+                        const bf16 *src = (ai == kOzNone) ? P.zero : a_img + ((size_t)ai * P.nd + i) * a_plane_elems;
+                        tc::bulk_g2s(sA + i * a_plane + lane * slot_bytes, src, slot_bytes, &full[stage]);
+                    }
+                }
+                if (lane == 31) tc::bulk_g2s(sB, b_img + (size_t)st.b * b_img_elems, b_stage, &full[stage]);
+            }
+        }
+        // let the copies in flight land before the CTA can exit
+        if (lane == 0) {
+            const uint32_t first = it > (uint32_t)P.S ? it - P.S : 0;
+            for (uint32_t j = first; j < it; ++j) tc::mbar_wait(&full[j % P.S], (j / P.S) & 1u, abort);
+        }
+        __syncwarp();
+    } else if (warp == 1) {
+        // ---------------- MMA issuer ----------------
+        if (lane == 0) {
+            uint32_t it = 0, ch = 0;
+            const uint32_t sbo = (uint32_t)P.kp * 16u;  // bytes between 8-row core-matrix groups
+            bool ok = true;
+            for (uint32_t t = blockIdx.x; t < n_tiles && ok; t += gridDim.x) {
+                const uint32_t ns = tiles[t].ns;
+                const uint32_t nch = (ns + P.F - 1) / P.F;
+                for (uint32_t c = 0; c < nch && ok; ++c, ++ch) {
+                    if (!tc::mbar_wait(tempty, (ch & 1u) ^ 1u, abort)) {
+                        ok = false;
+                        break;
+                    }
+                    tc::tc_fence_after();
+                    const uint32_t kend = min(ns, (c + 1) * (uint32_t)P.F);
+                    for (uint32_t k = c * P.F; k < kend; ++k, ++it) {
+                        const uint32_t stage = it % P.S, ph = (it / P.S) & 1u;
+                        if (!tc::mbar_wait(&full[stage], ph, abort)) {
+                            ok = false;
+                            break;
+                        }
+                        tc::tc_fence_after();
+                        const uint32_t aA = tc::smem_u32(smem + (size_t)stage * stage_bytes);
+                        const uint32_t aB = aA + a_stage;
+                        constexpr int kMaxPlanes = 256 / NP;  // B planes one MMA can take (N <= 256)
+                        for (int q = 0; q < P.kp / 16; ++q) {
+                            for (int i = 0; i < P.nd; ++i) {
+                                const uint64_t ad = tc::smem_desc(aA + i * a_plane + q * 256u, 128u, sbo);
+                                // first MMA into every TMEM region of a chain overwrites it
+                                const uint32_t acc = (k == c * P.F && q == 0 && i == 0) ? 0u : 1u;
+                                for (int j0 = 0; j0 < P.nd - i; j0 += kMaxPlanes) {
+                                    const int j1 = min(P.nd - i, j0 + kMaxPlanes);
+                                    const uint64_t bd =
+                                        tc::smem_desc(aB + (uint32_t)j0 * NP * P.kp * 2u + q * 256u, 128u, sbo);
+                                    const uint32_t id = tc::idesc_bf16_f32(128u, (uint32_t)(j1 - j0) * NP);
+                                    tc::mma_bf16(tmem + (uint32_t)((i + j0) * NP), ad, bd, id, acc);
+                                }
+                            }
+                        }
+                        tc::mma_commit(&empty[stage]);
+                    }
+                    if (!ok) break;
+                    tc::mma_commit(tfull);
+                }
+            }
+        }
+        __syncwarp();
+    } else {
+        // ---------------- epilogue ----------------
+        const int q = warp & 3;
+        const int m = q * 32 + lane;
+        const uint32_t lane_addr = tmem + ((uint32_t)(q * 32) << 16);
+        uint32_t ch = 0;
+        bool ok = true;
+        for (uint32_t t = blockIdx.x; t < n_tiles && ok; t += gridDim.x) {
+            const OzTile &T = tiles[t];
+            const uint32_t ns = T.ns;
+            const uint32_t nch = (ns + P.F - 1) / P.F;
+            double acc[NP];
+#pragma unroll
+            for (int c = 0; c < NP; ++c) acc[c] = 0.0;
+            for (uint32_t c = 0; c < nch; ++c, ++ch) {
+                if (!tc::mbar_wait(tfull, ch & 1u, abort)) {
+                    ok = false;
+                    break;
+                }
+                tc::tc_fence_after();
+                // regions in order of weight: sum = R_0 + R_1 + ... in FP64
+#pragma unroll
+                for (int c0 = 0; c0 < NP; c0 += 16) {
+                    double sum[16];
+                    float v[16];
+                    tc::tmem_ld16(lane_addr + (uint32_t)c0, v);
+                    tc::tmem_wait_ld();
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) sum[j] = (double)v[j];
+                    for (int w = 1; w < P.nd; ++w) {
+                        tc::tmem_ld16(lane_addr + (uint32_t)(w * NP + c0), v);
+                        tc::tmem_wait_ld();
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) sum[j] += (double)v[j];
+                    }
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) acc[c0 + j] += sum[j];
+                }
+                tc::tc_fence_before();
+                __syncwarp();
+                if (lane == 0) tc::mbar_arrive(tempty);
+            }
+            if (!ok) break;
+            const int s = m / P.mp, r = m % P.mp;
+            if (s < P.R && T.c[s] != nullptr && r < T.rows[s]) {
+                const double rs = ldexp(1.0, T.rexp[s][r] - 14);
+                double *cp = T.c[s];
+                const int ldc = T.ldc[s];
+                const bool fresh = (T.fresh_mask >> s) & 1u;
+#pragma unroll
+                for (int c = 0; c < NP; ++c) {
+                    if (c < T.cols) {
+                        const double out = P.alpha * (acc[c] * (rs * ldexp(1.0, T.cexp[c])));
+                        double *dst = cp + r + (size_t)c * ldc;
+                        *dst = fresh ? out : *dst + out;
+                    }
+                }
+                if (fresh && r == 0 && T.cnorm[s]) *T.cnorm[s] = 0.0;
+            }
+        }
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    if (warp == 1) tc::tmem_dealloc(tmem, P.tmem_cols);
+    if (threadIdx.x == 0 && *abort) atomicExch(err, 1);
+}
+
+template <int NP>
+static void launch_oz(bsg_ctx ctx, const OzShape &sh, const OzTile *tiles, size_t n_tiles, const OzStep *steps,
+                      const bf16 *a_img, const bf16 *b_img, double alpha, int *err, cudaStream_t s) {
+    OzKParams P;
+    P.mp = sh.mp;
+    P.kp = sh.kp;
+    P.R = sh.R;
+    P.nd = sh.nd;
+    P.F = sh.F;
+    P.alpha = alpha;
+    P.zero = static_cast<const bf16 *>(oz_zero_image());
+    const uint32_t stage_bytes = oz_stage_bytes(sh);
+    P.S = (int)std::min<uint32_t>(4, kOzSmemBudget / stage_bytes);
+    BSG_REQUIRE(P.S >= 2, BSG_ERR_UNSUPPORTED, "Ozaki tile does not fit shared memory");
+    uint32_t cols = 32;
+    while (cols < (uint32_t)sh.nd * NP) cols <<= 1;
+    P.tmem_cols = cols;
+    P.tx_bytes = (uint32_t)sh.R * sh.nd * sh.mp * sh.kp * 2u + (uint32_t)sh.nd * NP * sh.kp * 2u;
+    const size_t smem = (size_t)P.S * stage_bytes + (2 * P.S + 2) * 8 + 16;
+    BSG_CUDA(cudaFuncSetAttribute(k_ozgemm<NP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const unsigned grid = (unsigned)std::min<size_t>(n_tiles, (size_t)ctx->sm_count);
+    k_ozgemm<NP><<<grid, 192, smem, s>>>(tiles, (uint32_t)n_tiles, steps, a_img, b_img, P, err);
+    ctx->note_launch();
+    ctx->check_launch("ozaki gemm");
+}
+
+void oz_run(bsg_ctx ctx, const OzShape &sh, const OzTile *d_tiles, size_t n_tiles, const OzStep *d_steps,
+            const bf16 *a_img, const bf16 *b_img, double alpha, cudaStream_t s) {
+    if (!n_tiles) return;
+    BSG_REQUIRE(sh.nd >= 2 && sh.nd <= kOzMaxDigits && sh.nd * sh.np <= 512, BSG_ERR_UNSUPPORTED,
+                "Ozaki form: 2..8 digits, digits x padded block columns <= 512");
+    DevBuf err(4, s);
+    BSG_CUDA(cudaMemsetAsync(err.p, 0, 4, s));
+    switch (sh.np) {
+        case 16: launch_oz<16>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err.as<int>(), s); break;
+        case 32: launch_oz<32>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err.as<int>(), s); break;
+        case 48: launch_oz<48>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err.as<int>(), s); break;
+        case 64: launch_oz<64>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err.as<int>(), s); break;
+        default: throw Error{BSG_ERR_UNSUPPORTED, "Ozaki form supports block sizes up to 64"};
+    }
+    int h = 0;
+    BSG_CUDA(cudaMemcpyAsync(&h, err.p, 4, cudaMemcpyDeviceToHost, s));
+    BSG_CUDA(cudaStreamSynchronize(s));
+    BSG_REQUIRE(!h, BSG_ERR_TIMEOUT, "Ozaki GEMM: a pipeline wait timed out");
+}
+
+// ---------------------------------------------------------------------------
+// operand splitting for BlockSparseMatrix operands
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ int ext_of(size_t blk, size_t bs, size_t n) {
+    return (int)(((blk + 1) * bs <= n) ? bs : n - blk * bs);
+}
+
+// exponent of the largest |op(A)(r, :)| of each row of op(A), block row ib
+__global__ void k_rowexp_opA(double *const *__restrict__ tab, size_t a_nrb, int tA, ScreenGeom g, int *__restrict__ rexp) {
+    const size_t ib = blockIdx.x;
+    const int r = threadIdx.x;
+    if (r >= (int)g.ibs) return;
+    const int rows = ext_of(ib, g.ibs, g.ni);
+    double mx = 0.0;
+    if (r < rows) {
+        for (size_t kb = 0; kb < g.nkb; ++kb) {
+            const double *blk = tA ? tab[kb + ib * a_nrb] : tab[ib + kb * a_nrb];
+            if (!blk) continue;
+            const int k = ext_of(kb, g.kbs, g.nk);
+            const int ld = tA ? k : rows;
+            for (int l = 0; l < k; ++l) mx = fmax(mx, fabs(tA ? blk[l + (size_t)r * ld] : blk[r + (size_t)l * ld]));
+        }
+    }
+    rexp[ib * g.ibs + r] = oz_exp_of(mx);
+}
+
+// exponent of the largest |op(B)(:, c)| of each column of op(B), block column jb
+__global__ void k_colexp_opB(double *const *__restrict__ tab, size_t b_nrb, int tB, ScreenGeom g, int *__restrict__ cexp) {
+    const size_t jb = blockIdx.x;
+    const int c = threadIdx.x;
+    if (c >= (int)g.jbs) return;
+    const int cols = ext_of(jb, g.jbs, g.nj);
+    double mx = 0.0;
+    if (c < cols) {
+        for (size_t kb = 0; kb < g.nkb; ++kb) {
+            const double *blk = tB ? tab[jb + kb * b_nrb] : tab[kb + jb * b_nrb];
+            if (!blk) continue;
+            const int k = ext_of(kb, g.kbs, g.nk);
+            const int ld = tB ? cols : k;
+            for (int l = 0; l < k; ++l) mx = fmax(mx, fabs(tB ? blk[c + (size_t)l * ld] : blk[l + (size_t)c * ld]));
+        }
+    }
+    cexp[jb * g.jbs + c] = oz_exp_of(mx);
+}
+
+// digit image of op(A) block (ib, kb) stored at table index b (rows x k,
+// padded to mp x kp)
+__global__ void k_img_opA(double *const *__restrict__ tab, size_t a_nrb, int tA, ScreenGeom g,
+                          const int *__restrict__ rexp, int mp, int kp, int nd, bf16 *__restrict__ img) {
+    const size_t b = blockIdx.x;
+    const double *blk = tab[b];
+    if (!blk) return;
+    const size_t sr = b % a_nrb, sc = b / a_nrb;
+    const size_t ib = tA ? sc : sr, kb = tA ? sr : sc;
+    const int rows = ext_of(ib, g.ibs, g.ni), k = ext_of(kb, g.kbs, g.nk);
+    const int ld = tA ? k : rows;
+    const size_t plane = (size_t)mp * kp;
+    bf16 *dst = img + b * nd * plane;
+    for (int e = threadIdx.x; e < mp * kp; e += blockDim.x) {
+        const int r = e % mp, l = e / mp;
+        double x = 0.0;
+        if (r < rows && l < k) {
+            const double v = tA ? blk[l + (size_t)r * ld] : blk[r + (size_t)l * ld];
+            x = scalbn(v, -rexp[ib * g.ibs + r]);
+        }
+        oz_digits(x, nd, dst, plane, (size_t)oz_img_off(r, l, kp));
+    }
+}
+
+// digit image of op(B) block (kb, jb) stored at table index b, as np rows
+// (output columns) x kp
+__global__ void k_img_opB(double *const *__restrict__ tab, size_t b_nrb, int tB, ScreenGeom g,
+                          const int *__restrict__ cexp, int np, int kp, int nd, bf16 *__restrict__ img) {
+    const size_t b = blockIdx.x;
+    const double *blk = tab[b];
+    if (!blk) return;
+    const size_t sr = b % b_nrb, sc = b / b_nrb;
+    const size_t kb = tB ? sc : sr, jb = tB ? sr : sc;
+    const int cols = ext_of(jb, g.jbs, g.nj), k = ext_of(kb, g.kbs, g.nk);
+    const int ld = tB ? cols : k;
+    const size_t plane = (size_t)np * kp;
+    bf16 *dst = img + b * nd * plane;
+    for (int e = threadIdx.x; e < np * kp; e += blockDim.x) {
+        const int n = e % np, l = e / np;
+        double x = 0.0;
+        if (n < cols && l < k) {
+            const double v = tB ? blk[n + (size_t)l * ld] : blk[l + (size_t)n * ld];
+            x = scalbn(v, -cexp[jb * g.jbs + n]);
+        }
+        oz_digits(x, nd, dst, plane, (size_t)oz_img_off(n, l, kp));
+    }
+}
+
+// steps of every tile: k blocks where the B block exists and at least one
+// slot's (A, B) pair survives the screen (the FP64 form's predicate)
+__global__ void k_oz_steps(OzTile *__restrict__ tiles, size_t n_tiles, const uint32_t *__restrict__ tile_ib,
+                           const uint32_t *__restrict__ tile_jb, double *const *__restrict__ A,
+                           const double *__restrict__ An, size_t a_nrb, double *const *__restrict__ B,
+                           const double *__restrict__ Bn, size_t b_nrb, ScreenGeom g, int R, OzStep *__restrict__ steps) {
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_tiles) return;
+    const uint32_t jb = tile_jb[t];
+    uint32_t n = 0;
+    OzStep *out = steps + tiles[t].s0;
+    for (size_t kb = 0; kb < g.nkb; ++kb) {
+        const size_t bi = g.tB ? jb + kb * b_nrb : kb + jb * b_nrb;
+        if (!B[bi]) continue;
+        OzStep st;
+        st.b = (uint32_t)bi;
+        bool any = false;
+        for (int s = 0; s < kOzMaxSlots; ++s) {
+            st.a[s] = kOzNone;
+            if (s >= R) continue;
+            const uint32_t ib = tile_ib[t * kOzMaxSlots + s];
+            if (ib == kOzNone) continue;
+            const size_t ai = g.tA ? kb + ib * a_nrb : ib + kb * a_nrb;
+            if (!A[ai]) continue;
+            if (!(__dmul_rn(An[ai], Bn[bi]) >= g.tpb)) continue;
+            st.a[s] = (uint32_t)ai;
+            any = true;
+        }
+        if (any) out[n++] = st;
+    }
+    tiles[t].ns = n;
+}
+
+void ozaki_screened(bsg_ctx ctx, bsg_bsm C, bsg_bsm A, bsg_bsm B, const ScreenGeom &g, const std::vector<GemmItem> &items,
+                    const std::vector<uint32_t> &item_ib, const std::vector<uint32_t> &item_jb, double alpha,
+                    int n_digits, cudaStream_t s) {
+    if (items.empty()) return;
+    BSG_REQUIRE(g.ibs <= 64 && g.jbs <= 64 && g.kbs <= 64, BSG_ERR_UNSUPPORTED, "Ozaki form supports blocks up to 64");
+    const int nd = oz_default_digits(n_digits, (int)g.ibs, (int)g.kbs, (int)g.jbs);
+    const OzShape sh = oz_shape((int)g.ibs, (int)g.kbs, (int)g.jbs, nd);
+    // exponents and digit images
+    DevBuf rexp(g.nib * g.ibs * 4, s), cexp(g.njb * g.jbs * 4, s);
+    k_rowexp_opA<<<(unsigned)g.nib, (unsigned)std::max<size_t>(32, round_up((int)g.ibs, 32)), 0, s>>>(
+        A->dptr, A->nrb, g.tA, g, rexp.as<int>());
+    k_colexp_opB<<<(unsigned)g.njb, (unsigned)std::max<size_t>(32, round_up((int)g.jbs, 32)), 0, s>>>(
+        B->dptr, B->nrb, g.tB, g, cexp.as<int>());
+    ctx->note_launch(2);
+    const size_t a_plane = (size_t)sh.mp * sh.kp, b_plane = (size_t)sh.np * sh.kp;
+    DevBuf aimg(A->nblocks() * nd * a_plane * 2, s), bimg(B->nblocks() * nd * b_plane * 2, s);
+    k_img_opA<<<(unsigned)A->nblocks(), 256, 0, s>>>(A->dptr, A->nrb, g.tA, g, rexp.as<int>(), sh.mp, sh.kp, nd,
+                                                    aimg.as<bf16>());
+    k_img_opB<<<(unsigned)B->nblocks(), 256, 0, s>>>(B->dptr, B->nrb, g.tB, g, cexp.as<int>(), sh.np, sh.kp, nd,
+                                                    bimg.as<bf16>());
+    ctx->note_launch(2);
+    ctx->check_launch("ozaki split");
+    // tiles: up to R consecutive output blocks of one block column
+    std::vector<OzTile> tiles;
+    std::vector<uint32_t> tib, tjb;
+    size_t i = 0;
+    while (i < items.size()) {
+        OzTile T;
+        std::memset(&T, 0, sizeof(T));
+        const uint32_t jb = item_jb[i];
+        T.cexp = cexp.as<int>() + jb * g.jbs;
+        T.cols = items[i].cols;
+        size_t base = tib.size();
+        tib.resize(base + kOzMaxSlots, kOzNone);
+        int sl = 0;
+        while (i < items.size() && item_jb[i] == jb && sl < sh.R) {
+            T.c[sl] = items[i].c;
+            T.cnorm[sl] = items[i].c_norm;
+            T.rows[sl] = items[i].rows;
+            T.ldc[sl] = items[i].rows;
+            T.rexp[sl] = rexp.as<int>() + item_ib[i] * g.ibs;
+            if (items[i].fresh) T.fresh_mask |= 1u << sl;
+            tib[base + sl] = item_ib[i];
+            ++sl;
+            ++i;
+        }
+        T.s0 = (uint32_t)(tiles.size() * g.nkb);
+        T.ns = 0;
+        tiles.push_back(T);
+        tjb.push_back(jb);
+    }
+    BSG_REQUIRE(tiles.size() * g.nkb < 0xffffffffull, BSG_ERR_UNSUPPORTED, "too many Ozaki steps in one call");
+    DevBuf dt(tiles.size() * sizeof(OzTile), s), dib(tib.size() * 4, s), djb(tjb.size() * 4, s),
+        dst(tiles.size() * g.nkb * sizeof(OzStep), s);
+    BSG_CUDA(cudaMemcpyAsync(dt.p, tiles.data(), tiles.size() * sizeof(OzTile), cudaMemcpyHostToDevice, s));
+    BSG_CUDA(cudaMemcpyAsync(dib.p, tib.data(), tib.size() * 4, cudaMemcpyHostToDevice, s));
+    BSG_CUDA(cudaMemcpyAsync(djb.p, tjb.data(), tjb.size() * 4, cudaMemcpyHostToDevice, s));
+    k_oz_steps<<<(unsigned)ceil_div(tiles.size(), 128), 128, 0, s>>>(
+        dt.as<OzTile>(), tiles.size(), dib.as<uint32_t>(), djb.as<uint32_t>(), A->dptr, A->dnorm, A->nrb, B->dptr,
+        B->dnorm, B->nrb, g, sh.R, dst.as<OzStep>());
+    ctx->note_launch();
+    ctx->check_launch("ozaki steps");
+    oz_run(ctx, sh, dt.as<OzTile>(), tiles.size(), dst.as<OzStep>(), aimg.as<bf16>(), bimg.as<bf16>(), alpha, s);
+}
 
 void ozaki_grouped_gemm(bsg_ctx, const std::vector<GemmItem> &, const GemmItem *, const GemmPair *, uint64_t, int, int,
                         double, int, int, size_t, int, cudaStream_t) {
-    throw Error{BSG_ERR_UNSUPPORTED, "Ozaki form not available"};
+    throw Error{BSG_ERR_UNSUPPORTED, "Ozaki form of grouped item/pair products not available"};
 }
 
-}  // namespace bsg
-
-#include "bsg_rik.cuh"
-namespace bsg {
-void rik_ozaki(bsg_ctx, const RikDev &, double *, uint64_t *) {
-    throw Error{BSG_ERR_UNSUPPORTED, "Ozaki RI-K form not available"};
-}
 }  // namespace bsg

@@ -16,6 +16,16 @@ struct RikDev {
 };
 
 void rik_fp64(bsg_ctx ctx, const RikDev &d, double *K_dev, uint64_t stats[5]);
+
+// stage kernels shared by the FP64 and Ozaki pipelines (bsg_rik.cu)
+__global__ void k_scatter(const double *__restrict__ ints, const uint64_t *__restrict__ keys, size_t n_vec2,
+                          size_t P0, size_t u_stride, double *__restrict__ U);
+__global__ void k_unorms(const double *__restrict__ U, size_t n_bf, size_t bs, size_t nb, size_t n_p, double tpb,
+                         double *__restrict__ norm, uint8_t *__restrict__ flag);
+__global__ void k_ijs(const double *__restrict__ ij, const uint8_t *__restrict__ ijflag, size_t n_occ, size_t bs,
+                      size_t nob, double *__restrict__ ijs, double *__restrict__ snorm, uint8_t *__restrict__ sflag);
+__global__ void k_cnorms(const double *__restrict__ C, size_t n_bf, size_t n_occ, size_t bs, size_t nb, size_t nob,
+                         double *__restrict__ cnorm);
 void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, uint64_t stats[5]);
 
 }  // namespace bsg

@@ -1,0 +1,513 @@
+// occ-RI-K exchange step, Ozaki form: the three block products of every P run
+// on tcgen05 tensor cores as bf16 digit slices with exact fp32 chains; the
+// screening (block norms, masks, surviving pairs), the transpose-add and the
+// K accumulation stay FP64.
+//
+// Per chunk of aux functions P:
+//   scatter + U block norms / flags        (FP64 kernels shared with bsg_rik.cu)
+//   mui_P = U_P C        tiles (P, j, 5 block rows a), steps over b
+//   mui norms            FP64, from the computed mui blocks
+//   ij_P  = C^T mui_P    tiles (P, jb, 5 block rows ib), steps over a
+//   ijs_P = ij + ij^T    FP64 (shared kernel)
+//   K    += mui_P ijs_P  tiles (P sub-range, jb, 5 block rows a), steps over
+//                        (P, ib); per-tile partial blocks summed in order
+// Operand scales: U rows per (P, mu); C columns per i (also the rows of C^T);
+// mui columns per (P, j) for the ij product; mui rows and ijs columns per
+// (P sub-range, mu / j) for the K product.  Every tile has one scale set, so
+// its steps chain exactly (<= 512 k per chain).
+#include <algorithm>
+
+#include "bsg_ozaki.cuh"
+#include "bsg_rik.cuh"
+
+namespace bsg {
+
+using bf16 = __nv_bfloat16;
+
+__device__ __forceinline__ int ext_r(size_t blk, size_t bs, size_t n) {
+    return (int)(((blk + 1) * bs <= n) ? bs : n - blk * bs);
+}
+
+// image of one block: A role (rows r, k l -> src[r + l*ld]) or B role (rows
+// n = output columns, k l -> src[l + n*ld]); exps indexed by image row
+__device__ __forceinline__ void block_image(const double *src, size_t ld, bool b_role, int rows, int k,
+                                            const int *exps, int mpad, int kp, int nd, bf16 *dst) {
+    const size_t plane = (size_t)mpad * kp;
+    for (int e = threadIdx.x; e < mpad * kp; e += blockDim.x) {
+        const int r = e % mpad, l = e / mpad;
+        double x = 0.0;
+        if (r < rows && l < k) {
+            const double v = b_role ? src[l + (size_t)r * ld] : src[r + (size_t)l * ld];
+            x = scalbn(v, -exps[r]);
+        }
+        oz_digits(x, nd, dst, plane, (size_t)oz_img_off(r, l, kp));
+    }
+}
+
+// ---- scale exponents ----
+
+// U_p rows over present blocks; grid (p, a), one thread per row
+__global__ void k_rexp_U(const double *__restrict__ U, const uint8_t *__restrict__ uflag, size_t n_bf, size_t bs,
+                         size_t nb, int *__restrict__ rexp) {
+    const size_t p = blockIdx.x / nb, a = blockIdx.x % nb;
+    const int r = threadIdx.x, rows = ext_r(a, bs, n_bf);
+    if (r >= rows) return;
+    const double *Up = U + p * n_bf * n_bf;
+    double mx = 0.0;
+    for (size_t b = 0; b < nb; ++b) {
+        if (!uflag[p * nb * nb + a + b * nb]) continue;
+        const int k = ext_r(b, bs, n_bf);
+        for (int l = 0; l < k; ++l) mx = fmax(mx, fabs(Up[a * bs + r + (b * bs + l) * n_bf]));
+    }
+    rexp[p * n_bf + a * bs + r] = oz_exp_of(mx);
+}
+
+// columns of C over every row; grid jb
+__global__ void k_cexp_C(const double *__restrict__ C, size_t n_bf, size_t n_occ, size_t bs, int *__restrict__ cexp) {
+    const size_t jb = blockIdx.x;
+    const int c = threadIdx.x;
+    if (c >= ext_r(jb, bs, n_occ)) return;
+    double mx = 0.0;
+    for (size_t mu = 0; mu < n_bf; ++mu) mx = fmax(mx, fabs(C[mu + (jb * bs + c) * n_bf]));
+    cexp[jb * bs + c] = oz_exp_of(mx);
+}
+
+// columns of mui_p over present blocks; grid (p, jb)
+__global__ void k_cexp_mui(const double *__restrict__ mui, const uint8_t *__restrict__ mflag, size_t n_bf,
+                           size_t n_occ, size_t bs, size_t nb, size_t nob, int *__restrict__ cexp) {
+    const size_t p = blockIdx.x / nob, jb = blockIdx.x % nob;
+    const int c = threadIdx.x;
+    if (c >= ext_r(jb, bs, n_occ)) return;
+    const double *M = mui + p * n_bf * n_occ;
+    double mx = 0.0;
+    for (size_t a = 0; a < nb; ++a) {
+        if (!mflag[p * nb * nob + a + jb * nb]) continue;
+        const int rows = ext_r(a, bs, n_bf);
+        for (int r = 0; r < rows; ++r) mx = fmax(mx, fabs(M[a * bs + r + (jb * bs + c) * n_bf]));
+    }
+    cexp[p * n_occ + jb * bs + c] = oz_exp_of(mx);
+}
+
+// rows of mui over (p in sub-range, i); grid (sub, a)
+__global__ void k_rexp_mui_sub(const double *__restrict__ mui, const uint8_t *__restrict__ mflag, size_t n_bf,
+                               size_t n_occ, size_t bs, size_t nb, size_t nob, size_t np, size_t Q,
+                               int *__restrict__ rexp) {
+    const size_t sub = blockIdx.x / nb, a = blockIdx.x % nb;
+    const int r = threadIdx.x;
+    if (r >= ext_r(a, bs, n_bf)) return;
+    double mx = 0.0;
+    const size_t p1 = min(np, (sub + 1) * Q);
+    for (size_t p = sub * Q; p < p1; ++p)
+        for (size_t ib = 0; ib < nob; ++ib) {
+            if (!mflag[p * nb * nob + a + ib * nb]) continue;
+            const double *M = mui + p * n_bf * n_occ;
+            const int k = ext_r(ib, bs, n_occ);
+            for (int l = 0; l < k; ++l) mx = fmax(mx, fabs(M[a * bs + r + (ib * bs + l) * n_bf]));
+        }
+    rexp[sub * n_bf + a * bs + r] = oz_exp_of(mx);
+}
+
+// columns of ijs over (p in sub-range, i); grid (sub, jb)
+__global__ void k_cexp_ijs_sub(const double *__restrict__ ijs, const uint8_t *__restrict__ sflag, size_t n_occ,
+                               size_t bs, size_t nob, size_t np, size_t Q, int *__restrict__ cexp) {
+    const size_t sub = blockIdx.x / nob, jb = blockIdx.x % nob;
+    const int c = threadIdx.x;
+    if (c >= ext_r(jb, bs, n_occ)) return;
+    double mx = 0.0;
+    const size_t p1 = min(np, (sub + 1) * Q);
+    for (size_t p = sub * Q; p < p1; ++p)
+        for (size_t ib = 0; ib < nob; ++ib) {
+            if (!sflag[p * nob * nob + ib + jb * nob]) continue;
+            const double *S = ijs + p * n_occ * n_occ;
+            const int k = ext_r(ib, bs, n_occ);
+            for (int l = 0; l < k; ++l) mx = fmax(mx, fabs(S[ib * bs + l + (jb * bs + c) * n_occ]));
+        }
+    cexp[sub * n_occ + jb * bs + c] = oz_exp_of(mx);
+}
+
+// ---- digit images ----
+
+struct OzDims {
+    size_t n_bf, n_occ, bs, nb, nob;
+    int mp, kp, np, nd, R;
+};
+
+// U_p blocks (A role); grid (p, a, b), image index p*nb*nb + a + b*nb
+__global__ void k_img_U(const double *__restrict__ U, const uint8_t *__restrict__ uflag, const int *__restrict__ rexp,
+                        OzDims D, bf16 *__restrict__ img) {
+    const size_t x = blockIdx.x;
+    if (!uflag[x]) return;
+    const size_t p = x / (D.nb * D.nb), a = x % D.nb, b = (x / D.nb) % D.nb;
+    block_image(U + p * D.n_bf * D.n_bf + a * D.bs + b * D.bs * D.n_bf, D.n_bf, false, ext_r(a, D.bs, D.n_bf),
+                ext_r(b, D.bs, D.n_bf), rexp + p * D.n_bf + a * D.bs, D.mp, D.kp, D.nd,
+                img + x * D.nd * (size_t)D.mp * D.kp);
+}
+
+// C blocks (b, j) in the B role of mui = U C; index b + j*nb
+__global__ void k_img_C_B(const double *__restrict__ C, const int *__restrict__ cexp, OzDims D, bf16 *__restrict__ img) {
+    const size_t x = blockIdx.x, b = x % D.nb, j = x / D.nb;
+    block_image(C + b * D.bs + j * D.bs * D.n_bf, D.n_bf, true, ext_r(j, D.bs, D.n_occ), ext_r(b, D.bs, D.n_bf),
+                cexp + j * D.bs, D.np, D.kp, D.nd, img + x * D.nd * (size_t)D.np * D.kp);
+}
+
+// C^T blocks (ib, a) in the A role of ij = C^T mui; index ib + a*nob
+__global__ void k_img_Ct_A(const double *__restrict__ C, const int *__restrict__ cexp, OzDims D, bf16 *__restrict__ img) {
+    const size_t x = blockIdx.x, ib = x % D.nob, a = x / D.nob;
+    block_image(C + a * D.bs + ib * D.bs * D.n_bf, D.n_bf, true, ext_r(ib, D.bs, D.n_occ), ext_r(a, D.bs, D.n_bf),
+                cexp + ib * D.bs, D.mp, D.kp, D.nd, img + x * D.nd * (size_t)D.mp * D.kp);
+}
+
+// mui_p blocks (a, jb) in the B role of ij; index p*nb*nob + a + jb*nb
+__global__ void k_img_mui_B(const double *__restrict__ mui, const uint8_t *__restrict__ mflag,
+                            const int *__restrict__ cexp, OzDims D, bf16 *__restrict__ img) {
+    const size_t x = blockIdx.x;
+    if (!mflag[x]) return;
+    const size_t p = x / (D.nb * D.nob), a = x % D.nb, jb = (x / D.nb) % D.nob;
+    block_image(mui + p * D.n_bf * D.n_occ + a * D.bs + jb * D.bs * D.n_bf, D.n_bf, true, ext_r(jb, D.bs, D.n_occ),
+                ext_r(a, D.bs, D.n_bf), cexp + p * D.n_occ + jb * D.bs, D.np, D.kp, D.nd,
+                img + x * D.nd * (size_t)D.np * D.kp);
+}
+
+// mui_p blocks (a, ib) in the A role of K += mui ijs; index p*nb*nob + a + ib*nb
+__global__ void k_img_mui_A(const double *__restrict__ mui, const uint8_t *__restrict__ mflag,
+                            const int *__restrict__ rexp, size_t Q, OzDims D, bf16 *__restrict__ img) {
+    const size_t x = blockIdx.x;
+    if (!mflag[x]) return;
+    const size_t p = x / (D.nb * D.nob), a = x % D.nb, ib = (x / D.nb) % D.nob;
+    block_image(mui + p * D.n_bf * D.n_occ + a * D.bs + ib * D.bs * D.n_bf, D.n_bf, false, ext_r(a, D.bs, D.n_bf),
+                ext_r(ib, D.bs, D.n_occ), rexp + (p / Q) * D.n_bf + a * D.bs, D.mp, D.kp, D.nd,
+                img + x * D.nd * (size_t)D.mp * D.kp);
+}
+
+// ijs_p blocks (ib, jb) in the B role of the K product; index p*nob*nob + ib + jb*nob
+__global__ void k_img_ijs_B(const double *__restrict__ ijs, const uint8_t *__restrict__ sflag,
+                            const int *__restrict__ cexp, size_t Q, OzDims D, bf16 *__restrict__ img) {
+    const size_t x = blockIdx.x;
+    if (!sflag[x]) return;
+    const size_t p = x / (D.nob * D.nob), ib = x % D.nob, jb = (x / D.nob) % D.nob;
+    block_image(ijs + p * D.n_occ * D.n_occ + ib * D.bs + jb * D.bs * D.n_occ, D.n_occ, true, ext_r(jb, D.bs, D.n_occ),
+                ext_r(ib, D.bs, D.n_occ), cexp + (p / Q) * D.n_occ + jb * D.bs, D.np, D.kp, D.nd,
+                img + x * D.nd * (size_t)D.np * D.kp);
+}
+
+// ---- tiles and steps (one thread per tile) ----
+
+__device__ __forceinline__ void tile_clear(OzTile &T) {
+    for (int s = 0; s < kOzMaxSlots; ++s) {
+        T.c[s] = nullptr;
+        T.cnorm[s] = nullptr;
+        T.rexp[s] = nullptr;
+        T.rows[s] = 0;
+        T.ldc[s] = 0;
+    }
+    T.fresh_mask = 0xFFu;
+}
+
+// mui tiles: t = (p, j, group g of R block rows a)
+__global__ void k_tiles_mui(const uint8_t *__restrict__ uflag, const double *__restrict__ unorm,
+                            const double *__restrict__ cnorm, const int *__restrict__ rexp_U,
+                            const int *__restrict__ cexp_C, double *__restrict__ mui, OzDims D, size_t n_tiles,
+                            double tpb, OzTile *__restrict__ tiles, OzStep *__restrict__ steps,
+                            uint8_t *__restrict__ mflag, unsigned long long *__restrict__ nsig) {
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_tiles) return;
+    const size_t ng = (D.nb + D.R - 1) / D.R;
+    const size_t g = t % ng, j = (t / ng) % D.nob, p = t / (ng * D.nob);
+    OzTile T;
+    tile_clear(T);
+    int cnt[kOzMaxSlots] = {0};
+    for (int s = 0; s < D.R; ++s) {
+        const size_t a = g * D.R + s;
+        if (a >= D.nb) break;
+        T.c[s] = mui + p * D.n_bf * D.n_occ + a * D.bs + j * D.bs * D.n_bf;
+        T.ldc[s] = (int)D.n_bf;
+        T.rows[s] = ext_r(a, D.bs, D.n_bf);
+        T.rexp[s] = rexp_U + p * D.n_bf + a * D.bs;
+    }
+    T.cols = ext_r(j, D.bs, D.n_occ);
+    T.cexp = cexp_C + j * D.bs;
+    T.s0 = (uint32_t)(t * D.nb);
+    uint32_t n = 0;
+    for (size_t b = 0; b < D.nb; ++b) {
+        OzStep st;
+        st.b = (uint32_t)(b + j * D.nb);
+        bool any = false;
+        for (int s = 0; s < kOzMaxSlots; ++s) {
+            st.a[s] = kOzNone;
+            if (s >= D.R || !T.c[s]) continue;
+            const size_t a = g * D.R + s, ub = p * D.nb * D.nb + a + b * D.nb;
+            if (!uflag[ub]) continue;
+            if (!(__dmul_rn(unorm[ub], cnorm[b + j * D.nb]) >= tpb)) continue;
+            st.a[s] = (uint32_t)ub;
+            ++cnt[s];
+            any = true;
+        }
+        if (any) steps[T.s0 + n++] = st;
+    }
+    T.ns = n;
+    tiles[t] = T;
+    unsigned long long tot = 0;
+    for (int s = 0; s < D.R; ++s) {
+        const size_t a = g * D.R + s;
+        if (a >= D.nb) break;
+        mflag[p * D.nb * D.nob + a + j * D.nb] = cnt[s] > 0;
+        tot += cnt[s];
+    }
+    if (tot) atomicAdd(nsig, tot);
+}
+
+// ij tiles: t = (p, jb, group of R block rows ib)
+__global__ void k_tiles_ij(const uint8_t *__restrict__ mflag, const double *__restrict__ mnorm,
+                           const double *__restrict__ cnorm, const int *__restrict__ cexp_C,
+                           const int *__restrict__ cexp_mui, double *__restrict__ ij, OzDims D, size_t n_tiles,
+                           double tpb, OzTile *__restrict__ tiles, OzStep *__restrict__ steps,
+                           uint8_t *__restrict__ ijflag, unsigned long long *__restrict__ nsig) {
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_tiles) return;
+    const size_t ng = (D.nob + D.R - 1) / D.R;
+    const size_t g = t % ng, jb = (t / ng) % D.nob, p = t / (ng * D.nob);
+    OzTile T;
+    tile_clear(T);
+    int cnt[kOzMaxSlots] = {0};
+    for (int s = 0; s < D.R; ++s) {
+        const size_t ib = g * D.R + s;
+        if (ib >= D.nob) break;
+        T.c[s] = ij + p * D.n_occ * D.n_occ + ib * D.bs + jb * D.bs * D.n_occ;
+        T.ldc[s] = (int)D.n_occ;
+        T.rows[s] = ext_r(ib, D.bs, D.n_occ);
+        T.rexp[s] = cexp_C + ib * D.bs;
+    }
+    T.cols = ext_r(jb, D.bs, D.n_occ);
+    T.cexp = cexp_mui + p * D.n_occ + jb * D.bs;
+    T.s0 = (uint32_t)(t * D.nb);
+    uint32_t n = 0;
+    for (size_t a = 0; a < D.nb; ++a) {
+        const size_t mb = p * D.nb * D.nob + a + jb * D.nb;
+        if (!mflag[mb]) continue;
+        OzStep st;
+        st.b = (uint32_t)mb;
+        bool any = false;
+        for (int s = 0; s < kOzMaxSlots; ++s) {
+            st.a[s] = kOzNone;
+            if (s >= D.R || !T.c[s]) continue;
+            const size_t ib = g * D.R + s;
+            if (!(__dmul_rn(cnorm[a + ib * D.nb], mnorm[mb]) >= tpb)) continue;
+            st.a[s] = (uint32_t)(ib + a * D.nob);
+            ++cnt[s];
+            any = true;
+        }
+        if (any) steps[T.s0 + n++] = st;
+    }
+    T.ns = n;
+    tiles[t] = T;
+    unsigned long long tot = 0;
+    for (int s = 0; s < D.R; ++s) {
+        const size_t ib = g * D.R + s;
+        if (ib >= D.nob) break;
+        ijflag[p * D.nob * D.nob + ib + jb * D.nob] = cnt[s] > 0;
+        tot += cnt[s];
+    }
+    if (tot) atomicAdd(nsig, tot);
+}
+
+// K tiles: t = (sub-range, jb, group of R block rows a), steps over (p, ib)
+__global__ void k_tiles_K(const uint8_t *__restrict__ mflag, const double *__restrict__ mnorm,
+                          const uint8_t *__restrict__ sflag, const double *__restrict__ snorm,
+                          const int *__restrict__ rexp_sub, const int *__restrict__ cexp_sub, double *__restrict__ Kpart,
+                          OzDims D, size_t np, size_t Q, size_t n_tiles, double tpb, OzTile *__restrict__ tiles,
+                          OzStep *__restrict__ steps, unsigned long long *__restrict__ nsig) {
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_tiles) return;
+    const size_t ng = (D.nb + D.R - 1) / D.R;
+    const size_t g = t % ng, jb = (t / ng) % D.nob, sub = t / (ng * D.nob);
+    OzTile T;
+    tile_clear(T);
+    const size_t bs2 = D.bs * D.bs;
+    for (int s = 0; s < D.R; ++s) {
+        const size_t a = g * D.R + s;
+        if (a >= D.nb) break;
+        T.c[s] = Kpart + ((sub * D.nob + jb) * D.nb + a) * bs2;
+        T.rows[s] = ext_r(a, D.bs, D.n_bf);
+        T.ldc[s] = T.rows[s];
+        T.rexp[s] = rexp_sub + sub * D.n_bf + a * D.bs;
+    }
+    T.cols = ext_r(jb, D.bs, D.n_occ);
+    T.cexp = cexp_sub + sub * D.n_occ + jb * D.bs;
+    T.s0 = (uint32_t)(t * Q * D.nob);
+    uint32_t n = 0;
+    unsigned long long tot = 0;
+    const size_t p1 = min(np, (sub + 1) * Q);
+    for (size_t p = sub * Q; p < p1; ++p)
+        for (size_t ib = 0; ib < D.nob; ++ib) {
+            const size_t sb = p * D.nob * D.nob + ib + jb * D.nob;
+            if (!sflag[sb]) continue;
+            OzStep st;
+            st.b = (uint32_t)sb;
+            bool any = false;
+            for (int s = 0; s < kOzMaxSlots; ++s) {
+                st.a[s] = kOzNone;
+                if (s >= D.R || !T.c[s]) continue;
+                const size_t a = g * D.R + s, mb = p * D.nb * D.nob + a + ib * D.nb;
+                if (!mflag[mb]) continue;
+                if (!(__dmul_rn(mnorm[mb], snorm[sb]) >= tpb)) continue;
+                st.a[s] = (uint32_t)mb;
+                ++tot;
+                any = true;
+            }
+            if (any) steps[T.s0 + n++] = st;
+        }
+    T.ns = n;
+    tiles[t] = T;
+    if (tot) atomicAdd(nsig, tot);
+}
+
+// K(a, jb) += sum over sub-ranges (in order) of the tiles' partial blocks
+__global__ void k_K_reduce(const double *__restrict__ Kpart, size_t n_sub, OzDims D, double *__restrict__ K) {
+    const size_t blk = blockIdx.x;  // (jb, a)
+    const size_t a = blk % D.nb, jb = blk / D.nb;
+    const int rows = ext_r(a, D.bs, D.n_bf), cols = ext_r(jb, D.bs, D.n_occ);
+    const size_t bs2 = D.bs * D.bs;
+    for (int e = threadIdx.x; e < rows * cols; e += blockDim.x) {
+        const int r = e % rows, c = e / rows;
+        double acc = K[a * D.bs + r + (jb * D.bs + c) * D.n_bf];
+        for (size_t sub = 0; sub < n_sub; ++sub) acc += Kpart[((sub * D.nob + jb) * D.nb + a) * bs2 + e];
+        K[a * D.bs + r + (jb * D.bs + c) * D.n_bf] = acc;
+    }
+}
+
+// FP64 block norms of mui (warp per present block)
+__global__ void k_mui_norms(const double *__restrict__ mui, const uint8_t *__restrict__ mflag, size_t n_bf,
+                            size_t n_occ, size_t bs, size_t nb, size_t nob, size_t n, double *__restrict__ mnorm) {
+    const size_t x = (size_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    if (x >= n || !mflag[x]) return;
+    const size_t p = x / (nb * nob), a = x % nb, j = (x / nb) % nob;
+    const double est = warp_block_norm(mui + p * n_bf * n_occ + a * bs + j * bs * n_bf, ext_r(a, bs, n_bf),
+                                       ext_r(j, bs, n_occ), n_bf);
+    if ((threadIdx.x & 31) == 0) mnorm[x] = est;
+}
+
+void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, uint64_t stats[5]) {
+    cudaStream_t s = ctx->stream;
+    const size_t n_bf = d.n_bf, n_occ = d.n_occ, bs = d.bs, n_aux = d.n_aux;
+    BSG_REQUIRE(bs <= 64, BSG_ERR_UNSUPPORTED, "RI-K Ozaki form supports bs <= 64");
+    const int nd = oz_default_digits(d.n_digits, (int)bs, (int)bs, (int)bs);
+    const OzShape sh = oz_shape((int)bs, (int)bs, (int)bs, nd);
+    OzDims D;
+    D.n_bf = n_bf;
+    D.n_occ = n_occ;
+    D.bs = bs;
+    D.nb = ceil_div(n_bf, bs);
+    D.nob = ceil_div(n_occ, bs);
+    D.mp = sh.mp;
+    D.kp = sh.kp;
+    D.np = sh.np;
+    D.nd = nd;
+    D.R = sh.R;
+    const size_t nb = D.nb, nob = D.nob;
+    const size_t a_img = (size_t)nd * sh.mp * sh.kp, b_img = (size_t)nd * sh.np * sh.kp;  // elements per image
+    // bytes per aux function of every per-chunk buffer
+    const size_t per_p = n_bf * n_bf * 8 + nb * nb * 9 + nb * nb * a_img * 2 + n_bf * n_occ * 8 + nb * nob * 9 +
+                         nb * nob * (a_img + b_img) * 2 + 3 * n_occ * n_occ * 8 + 3 * nob * nob * 9 +
+                         nob * nob * b_img * 2;
+    size_t pc = d.p_chunk ? d.p_chunk : std::max<size_t>(1, (size_t)(8ull << 30) / per_p);
+    pc = std::max<size_t>(1, std::min(pc, n_aux));
+    const size_t Q = 8;  // aux functions per K-product tile
+    const size_t n_sub_max = ceil_div(pc, Q);
+
+    DevBuf dU(pc * n_bf * n_bf * 8, s), dun(pc * nb * nb * 8, s), duf(pc * nb * nb, s);
+    DevBuf dmui(pc * n_bf * n_occ * 8, s), dmn(pc * nb * nob * 8, s), dmf(pc * nb * nob, s);
+    DevBuf dij(pc * n_occ * n_occ * 8, s), dijf(pc * nob * nob, s);
+    DevBuf dijs(pc * n_occ * n_occ * 8, s), dsn(pc * nob * nob * 8, s), dsf(pc * nob * nob, s);
+    DevBuf dcn(nb * nob * 8, s), dcexpC(nob * bs * 4, s), dimgCB(nb * nob * b_img * 2, s),
+        dimgCtA(nob * nb * a_img * 2, s);
+    DevBuf drexpU(pc * n_bf * 4, s), dimgU(pc * nb * nb * a_img * 2, s);
+    DevBuf dcexpM(pc * n_occ * 4, s), dimgMB(pc * nb * nob * b_img * 2, s);
+    DevBuf drexpMs(n_sub_max * n_bf * 4, s), dcexpSs(n_sub_max * n_occ * 4, s);
+    DevBuf dimgMA(pc * nb * nob * a_img * 2, s), dimgSB(pc * nob * nob * b_img * 2, s);
+    DevBuf dKp(n_sub_max * nob * nb * bs * bs * 8, s), dcnt(5 * 8, s);
+    const size_t ng_a = ceil_div(nb, (size_t)D.R), ng_i = ceil_div(nob, (size_t)D.R);
+    const size_t tiles_mui = pc * nob * ng_a, tiles_ij = pc * nob * ng_i, tiles_K = n_sub_max * nob * ng_a;
+    DevBuf dtm(tiles_mui * sizeof(OzTile), s), dsm(tiles_mui * nb * sizeof(OzStep), s);
+    DevBuf dti(tiles_ij * sizeof(OzTile), s), dsi(tiles_ij * nb * sizeof(OzStep), s);
+    DevBuf dtk(tiles_K * sizeof(OzTile), s), dsk(tiles_K * Q * nob * sizeof(OzStep), s);
+    BSG_CUDA(cudaMemsetAsync(K_dev, 0, n_bf * n_occ * 8, s));
+    BSG_CUDA(cudaMemsetAsync(dcnt.p, 0, 5 * 8, s));
+    auto *cnt = dcnt.as<unsigned long long>();
+    const unsigned tb = (unsigned)std::max<size_t>(32, ((bs + 31) / 32) * 32);
+
+    // call-constant operands: C norms, C column exponents, C images in both roles
+    const int wpb = 8;
+    k_cnorms<<<(unsigned)ceil_div(nb * nob, wpb), wpb * 32, 0, s>>>(d.c_occ, n_bf, n_occ, bs, nb, nob, dcn.as<double>());
+    k_cexp_C<<<(unsigned)nob, tb, 0, s>>>(d.c_occ, n_bf, n_occ, bs, dcexpC.as<int>());
+    k_img_C_B<<<(unsigned)(nb * nob), 256, 0, s>>>(d.c_occ, dcexpC.as<int>(), D, dimgCB.as<bf16>());
+    k_img_Ct_A<<<(unsigned)(nob * nb), 256, 0, s>>>(d.c_occ, dcexpC.as<int>(), D, dimgCtA.as<bf16>());
+    ctx->note_launch(4);
+    const double tpb_u = 1e-20 * (double)(bs * bs);
+    const double tpb = d.thresh * (double)(bs * bs * bs);
+    for (size_t P0 = 0; P0 < n_aux; P0 += pc) {
+        const size_t np = std::min(pc, n_aux - P0), n_sub = ceil_div(np, Q);
+        BSG_CUDA(cudaMemsetAsync(dU.p, 0, np * n_bf * n_bf * 8, s));
+        if (d.n_vec2) {
+            dim3 g((unsigned)ceil_div(d.n_vec2, 256), (unsigned)np);
+            k_scatter<<<g, 256, 0, s>>>(d.ints, d.keys, d.n_vec2, P0, n_bf * n_bf, dU.as<double>());
+            ctx->note_launch();
+        }
+        k_unorms<<<(unsigned)ceil_div(np * nb * nb, wpb), wpb * 32, 0, s>>>(dU.as<double>(), n_bf, bs, nb, np, tpb_u,
+                                                                            dun.as<double>(), duf.as<uint8_t>());
+        // mui = U C
+        k_rexp_U<<<(unsigned)(np * nb), tb, 0, s>>>(dU.as<double>(), duf.as<uint8_t>(), n_bf, bs, nb, drexpU.as<int>());
+        k_img_U<<<(unsigned)(np * nb * nb), 256, 0, s>>>(dU.as<double>(), duf.as<uint8_t>(), drexpU.as<int>(), D,
+                                                        dimgU.as<bf16>());
+        const size_t tm = np * nob * ng_a;
+        k_tiles_mui<<<(unsigned)ceil_div(tm, 128), 128, 0, s>>>(
+            duf.as<uint8_t>(), dun.as<double>(), dcn.as<double>(), drexpU.as<int>(), dcexpC.as<int>(),
+            dmui.as<double>(), D, tm, tpb, dtm.as<OzTile>(), dsm.as<OzStep>(), dmf.as<uint8_t>(), cnt + 0);
+        ctx->note_launch(4);
+        ctx->check_launch("rik ozaki mui prep");
+        oz_run(ctx, sh, dtm.as<OzTile>(), tm, dsm.as<OzStep>(), dimgU.as<bf16>(), dimgCB.as<bf16>(), 1.0, s);
+        k_mui_norms<<<(unsigned)ceil_div(np * nb * nob, wpb), wpb * 32, 0, s>>>(
+            dmui.as<double>(), dmf.as<uint8_t>(), n_bf, n_occ, bs, nb, nob, np * nb * nob, dmn.as<double>());
+        // ij = C^T mui
+        k_cexp_mui<<<(unsigned)(np * nob), tb, 0, s>>>(dmui.as<double>(), dmf.as<uint8_t>(), n_bf, n_occ, bs, nb, nob,
+                                                       dcexpM.as<int>());
+        k_img_mui_B<<<(unsigned)(np * nb * nob), 256, 0, s>>>(dmui.as<double>(), dmf.as<uint8_t>(), dcexpM.as<int>(), D,
+                                                              dimgMB.as<bf16>());
+        const size_t ti = np * nob * ng_i;
+        k_tiles_ij<<<(unsigned)ceil_div(ti, 128), 128, 0, s>>>(
+            dmf.as<uint8_t>(), dmn.as<double>(), dcn.as<double>(), dcexpC.as<int>(), dcexpM.as<int>(),
+            dij.as<double>(), D, ti, tpb, dti.as<OzTile>(), dsi.as<OzStep>(), dijf.as<uint8_t>(), cnt + 1);
+        ctx->note_launch(4);
+        ctx->check_launch("rik ozaki ij prep");
+        oz_run(ctx, sh, dti.as<OzTile>(), ti, dsi.as<OzStep>(), dimgCtA.as<bf16>(), dimgMB.as<bf16>(), 1.0, s);
+        // ijs = ij + ij^T (FP64, with the reference's norm bookkeeping)
+        k_ijs<<<(unsigned)(np * nob * nob), 128, 0, s>>>(dij.as<double>(), dijf.as<uint8_t>(), n_occ, bs, nob,
+                                                          dijs.as<double>(), dsn.as<double>(), dsf.as<uint8_t>());
+        // K += mui ijs
+        k_rexp_mui_sub<<<(unsigned)(n_sub * nb), tb, 0, s>>>(dmui.as<double>(), dmf.as<uint8_t>(), n_bf, n_occ, bs, nb,
+                                                             nob, np, Q, drexpMs.as<int>());
+        k_cexp_ijs_sub<<<(unsigned)(n_sub * nob), tb, 0, s>>>(dijs.as<double>(), dsf.as<uint8_t>(), n_occ, bs, nob, np,
+                                                              Q, dcexpSs.as<int>());
+        k_img_mui_A<<<(unsigned)(np * nb * nob), 256, 0, s>>>(dmui.as<double>(), dmf.as<uint8_t>(), drexpMs.as<int>(), Q,
+                                                              D, dimgMA.as<bf16>());
+        k_img_ijs_B<<<(unsigned)(np * nob * nob), 256, 0, s>>>(dijs.as<double>(), dsf.as<uint8_t>(), dcexpSs.as<int>(),
+                                                              Q, D, dimgSB.as<bf16>());
+        const size_t tk = n_sub * nob * ng_a;
+        k_tiles_K<<<(unsigned)ceil_div(tk, 128), 128, 0, s>>>(
+            dmf.as<uint8_t>(), dmn.as<double>(), dsf.as<uint8_t>(), dsn.as<double>(), drexpMs.as<int>(),
+            dcexpSs.as<int>(), dKp.as<double>(), D, np, Q, tk, tpb, dtk.as<OzTile>(), dsk.as<OzStep>(), cnt + 2);
+        ctx->note_launch(6);
+        ctx->check_launch("rik ozaki K prep");
+        oz_run(ctx, sh, dtk.as<OzTile>(), tk, dsk.as<OzStep>(), dimgMA.as<bf16>(), dimgSB.as<bf16>(), 1.0, s);
+        k_K_reduce<<<(unsigned)(nb * nob), 256, 0, s>>>(dKp.as<double>(), n_sub, D, K_dev);
+        ctx->note_launch();
+        ctx->check_launch("rik ozaki K reduce");
+    }
+    if (stats) {
+        unsigned long long h[5];
+        BSG_CUDA(cudaMemcpyAsync(h, cnt, 5 * 8, cudaMemcpyDeviceToHost, s));
+        BSG_CUDA(cudaStreamSynchronize(s));
+        for (int i = 0; i < 5; ++i) stats[i] = h[i];
+    }
+}
+
+}  // namespace bsg
