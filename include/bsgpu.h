@@ -59,6 +59,12 @@ bsg_status bsg_ctx_destroy(bsg_ctx ctx);
 bsg_status bsg_ctx_sync(bsg_ctx ctx);
 /* number of kernels this context has launched so far */
 bsg_status bsg_ctx_launch_count(bsg_ctx ctx, uint64_t *out);
+/* Timing of the tensor-core (Ozaki form) GEMM launches with CUDA events on
+ * the context's stream: enable/disable (resets the totals), then read the
+ * launch count, total milliseconds and the unpadded block-product
+ * multiply-adds they performed (FP64-equivalent; x digit products for bf16). */
+bsg_status bsg_ctx_set_timing(bsg_ctx ctx, int on);
+bsg_status bsg_ctx_gemm_timing(bsg_ctx ctx, uint64_t *launches, double *ms, double *useful_macs);
 
 /* ---- block pool: BlockMemoryPool<double> (blockallocator.h:8-25,
  *      blockallocator.hpp:7-56).  Device slabs grow geometrically from 16 MB

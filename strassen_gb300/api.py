@@ -70,6 +70,16 @@ class Context:
         check(lib.bsg_ctx_launch_count(self.h, C.byref(n)))
         return n.value
 
+    def set_timing(self, on=True):
+        """CUDA-event timing of the tensor-core GEMM launches (resets totals)"""
+        check(lib.bsg_ctx_set_timing(self.h, int(bool(on))))
+
+    def gemm_timing(self):
+        """(launches, milliseconds, unpadded FP64-equivalent multiply-adds)"""
+        n, ms, macs = C.c_uint64(), C.c_double(), C.c_double()
+        check(lib.bsg_ctx_gemm_timing(self.h, C.byref(n), C.byref(ms), C.byref(macs)))
+        return n.value, ms.value, macs.value
+
 
 def default_context():
     global _DEFAULT_CTX

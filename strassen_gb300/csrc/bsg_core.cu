@@ -103,6 +103,25 @@ extern "C" bsg_status bsg_ctx_launch_count(bsg_ctx ctx, uint64_t *out) {
     });
 }
 
+extern "C" bsg_status bsg_ctx_set_timing(bsg_ctx ctx, int on) {
+    return guard([&] {
+        BSG_REQUIRE(ctx, BSG_ERR_ARG, "ctx is NULL");
+        ctx->timing = on != 0;
+        ctx->oz_ms = 0.0;
+        ctx->oz_launches = 0;
+        ctx->oz_useful_macs = 0.0;
+    });
+}
+
+extern "C" bsg_status bsg_ctx_gemm_timing(bsg_ctx ctx, uint64_t *launches, double *ms, double *useful_macs) {
+    return guard([&] {
+        BSG_REQUIRE(ctx, BSG_ERR_ARG, "ctx is NULL");
+        if (launches) *launches = ctx->oz_launches;
+        if (ms) *ms = ctx->oz_ms;
+        if (useful_macs) *useful_macs = ctx->oz_useful_macs;
+    });
+}
+
 // ---------------------------------------------------------------------------
 // Block pool (blockallocator.hpp:7-62)
 // ---------------------------------------------------------------------------

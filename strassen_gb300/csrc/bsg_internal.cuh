@@ -88,6 +88,11 @@ struct bsg_ctx_s {
     bool own_stream = false;
     int sm_count = 0;
     uint64_t launches = 0;
+    // timing of the tensor-core GEMM launches (CUDA events on `stream`)
+    bool timing = false;
+    double oz_ms = 0.0;
+    uint64_t oz_launches = 0;
+    double oz_useful_macs = 0.0;  // unpadded block-product multiply-adds (FP64-equivalent)
     void note_launch(uint64_t n = 1) { launches += n; }
     void check_launch(const char *what);
 };

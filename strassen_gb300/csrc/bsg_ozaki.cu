@@ -289,12 +289,18 @@ static void launch_oz(bsg_ctx ctx, const OzShape &sh, const OzTile *tiles, size_
 }
 
 void oz_run(bsg_ctx ctx, const OzShape &sh, const OzTile *d_tiles, size_t n_tiles, const OzStep *d_steps,
-            const bf16 *a_img, const bf16 *b_img, double alpha, cudaStream_t s) {
+            const bf16 *a_img, const bf16 *b_img, double alpha, cudaStream_t s, const unsigned long long *d_macs) {
     if (!n_tiles) return;
     BSG_REQUIRE(sh.nd >= 2 && sh.nd <= kOzMaxDigits && sh.nd * sh.np <= 512, BSG_ERR_UNSUPPORTED,
                 "Ozaki form: 2..8 digits, digits x padded block columns <= 512");
     DevBuf err(4, s);
     BSG_CUDA(cudaMemsetAsync(err.p, 0, 4, s));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (ctx->timing) {
+        BSG_CUDA(cudaEventCreate(&e0));
+        BSG_CUDA(cudaEventCreate(&e1));
+        BSG_CUDA(cudaEventRecord(e0, s));
+    }
     switch (sh.np) {
         case 16: launch_oz<16>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err.as<int>(), s); break;
         case 32: launch_oz<32>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err.as<int>(), s); break;
@@ -302,9 +308,21 @@ void oz_run(bsg_ctx ctx, const OzShape &sh, const OzTile *d_tiles, size_t n_tile
         case 64: launch_oz<64>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err.as<int>(), s); break;
         default: throw Error{BSG_ERR_UNSUPPORTED, "Ozaki form supports block sizes up to 64"};
     }
+    if (ctx->timing) BSG_CUDA(cudaEventRecord(e1, s));
     int h = 0;
+    unsigned long long macs = 0;
     BSG_CUDA(cudaMemcpyAsync(&h, err.p, 4, cudaMemcpyDeviceToHost, s));
+    if (ctx->timing && d_macs) BSG_CUDA(cudaMemcpyAsync(&macs, d_macs, 8, cudaMemcpyDeviceToHost, s));
     BSG_CUDA(cudaStreamSynchronize(s));
+    if (ctx->timing) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        ctx->oz_ms += ms;
+        ctx->oz_launches += 1;
+        ctx->oz_useful_macs += (double)macs;
+    }
     BSG_REQUIRE(!h, BSG_ERR_TIMEOUT, "Ozaki GEMM: a pipeline wait timed out");
 }
 
@@ -407,11 +425,14 @@ __global__ void k_img_opB(double *const *__restrict__ tab, size_t b_nrb, int tB,
 __global__ void k_oz_steps(OzTile *__restrict__ tiles, size_t n_tiles, const uint32_t *__restrict__ tile_ib,
                            const uint32_t *__restrict__ tile_jb, double *const *__restrict__ A,
                            const double *__restrict__ An, size_t a_nrb, double *const *__restrict__ B,
-                           const double *__restrict__ Bn, size_t b_nrb, ScreenGeom g, int R, OzStep *__restrict__ steps) {
+                           const double *__restrict__ Bn, size_t b_nrb, ScreenGeom g, int R, OzStep *__restrict__ steps,
+                           unsigned long long *__restrict__ macs) {
     const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n_tiles) return;
     const uint32_t jb = tile_jb[t];
     uint32_t n = 0;
+    unsigned long long m = 0;
+    const unsigned long long cols = ext_of(jb, g.jbs, g.nj);
     OzStep *out = steps + tiles[t].s0;
     for (size_t kb = 0; kb < g.nkb; ++kb) {
         const size_t bi = g.tB ? jb + kb * b_nrb : kb + jb * b_nrb;
@@ -428,11 +449,13 @@ __global__ void k_oz_steps(OzTile *__restrict__ tiles, size_t n_tiles, const uin
             if (!A[ai]) continue;
             if (!(__dmul_rn(An[ai], Bn[bi]) >= g.tpb)) continue;
             st.a[s] = (uint32_t)ai;
+            m += (unsigned long long)ext_of(ib, g.ibs, g.ni) * cols * ext_of(kb, g.kbs, g.nk);
             any = true;
         }
         if (any) out[n++] = st;
     }
     tiles[t].ns = n;
+    if (m) atomicAdd(macs, m);
 }
 
 void ozaki_screened(bsg_ctx ctx, bsg_bsm C, bsg_bsm A, bsg_bsm B, const ScreenGeom &g, const std::vector<GemmItem> &items,
@@ -488,16 +511,18 @@ void ozaki_screened(bsg_ctx ctx, bsg_bsm C, bsg_bsm A, bsg_bsm B, const ScreenGe
     }
     BSG_REQUIRE(tiles.size() * g.nkb < 0xffffffffull, BSG_ERR_UNSUPPORTED, "too many Ozaki steps in one call");
     DevBuf dt(tiles.size() * sizeof(OzTile), s), dib(tib.size() * 4, s), djb(tjb.size() * 4, s),
-        dst(tiles.size() * g.nkb * sizeof(OzStep), s);
+        dst(tiles.size() * g.nkb * sizeof(OzStep), s), dmacs(8, s);
+    BSG_CUDA(cudaMemsetAsync(dmacs.p, 0, 8, s));
     BSG_CUDA(cudaMemcpyAsync(dt.p, tiles.data(), tiles.size() * sizeof(OzTile), cudaMemcpyHostToDevice, s));
     BSG_CUDA(cudaMemcpyAsync(dib.p, tib.data(), tib.size() * 4, cudaMemcpyHostToDevice, s));
     BSG_CUDA(cudaMemcpyAsync(djb.p, tjb.data(), tjb.size() * 4, cudaMemcpyHostToDevice, s));
     k_oz_steps<<<(unsigned)ceil_div(tiles.size(), 128), 128, 0, s>>>(
         dt.as<OzTile>(), tiles.size(), dib.as<uint32_t>(), djb.as<uint32_t>(), A->dptr, A->dnorm, A->nrb, B->dptr,
-        B->dnorm, B->nrb, g, sh.R, dst.as<OzStep>());
+        B->dnorm, B->nrb, g, sh.R, dst.as<OzStep>(), dmacs.as<unsigned long long>());
     ctx->note_launch();
     ctx->check_launch("ozaki steps");
-    oz_run(ctx, sh, dt.as<OzTile>(), tiles.size(), dst.as<OzStep>(), aimg.as<bf16>(), bimg.as<bf16>(), alpha, s);
+    oz_run(ctx, sh, dt.as<OzTile>(), tiles.size(), dst.as<OzStep>(), aimg.as<bf16>(), bimg.as<bf16>(), alpha, s,
+           dmacs.as<unsigned long long>());
 }
 
 void ozaki_grouped_gemm(bsg_ctx, const std::vector<GemmItem> &, const GemmItem *, const GemmPair *, uint64_t, int, int,

@@ -56,8 +56,11 @@ struct OzStep {
 
 // Runs the tiles: C_slot = alpha * sum_steps A_slot,step * B_step (+ C_slot
 // unless fresh).  a_img / b_img hold nd planes per image in the UMMA layout.
+// d_macs (may be null): device counter of the unpadded multiply-adds the
+// tiles perform, read for the context's GEMM timing
 void oz_run(bsg_ctx ctx, const OzShape &sh, const OzTile *d_tiles, size_t n_tiles, const OzStep *d_steps,
-            const __nv_bfloat16 *a_img, const __nv_bfloat16 *b_img, double alpha, cudaStream_t s);
+            const __nv_bfloat16 *a_img, const __nv_bfloat16 *b_img, double alpha, cudaStream_t s,
+            const unsigned long long *d_macs = nullptr);
 
 // Ozaki form of one screened product (single slice): same screening and C
 // block bookkeeping as the FP64 form; items come from screened_product.

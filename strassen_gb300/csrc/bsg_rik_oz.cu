@@ -208,11 +208,13 @@ __global__ void k_tiles_mui(const uint8_t *__restrict__ uflag, const double *__r
                             const double *__restrict__ cnorm, const int *__restrict__ rexp_U,
                             const int *__restrict__ cexp_C, double *__restrict__ mui, OzDims D, size_t n_tiles,
                             double tpb, OzTile *__restrict__ tiles, OzStep *__restrict__ steps,
-                            uint8_t *__restrict__ mflag, unsigned long long *__restrict__ nsig) {
+                            uint8_t *__restrict__ mflag, unsigned long long *__restrict__ nsig,
+                            unsigned long long *__restrict__ macs) {
     const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n_tiles) return;
     const size_t ng = (D.nb + D.R - 1) / D.R;
     const size_t g = t % ng, j = (t / ng) % D.nob, p = t / (ng * D.nob);
+    unsigned long long m = 0;
     OzTile T;
     tile_clear(T);
     int cnt[kOzMaxSlots] = {0};
@@ -239,6 +241,7 @@ __global__ void k_tiles_mui(const uint8_t *__restrict__ uflag, const double *__r
             if (!uflag[ub]) continue;
             if (!(__dmul_rn(unorm[ub], cnorm[b + j * D.nb]) >= tpb)) continue;
             st.a[s] = (uint32_t)ub;
+            m += (unsigned long long)T.rows[s] * ext_r(j, D.bs, D.n_occ) * ext_r(b, D.bs, D.n_bf);
             ++cnt[s];
             any = true;
         }
@@ -254,6 +257,7 @@ __global__ void k_tiles_mui(const uint8_t *__restrict__ uflag, const double *__r
         tot += cnt[s];
     }
     if (tot) atomicAdd(nsig, tot);
+    if (m) atomicAdd(macs, m);
 }
 
 // ij tiles: t = (p, jb, group of R block rows ib)
@@ -261,11 +265,13 @@ __global__ void k_tiles_ij(const uint8_t *__restrict__ mflag, const double *__re
                            const double *__restrict__ cnorm, const int *__restrict__ cexp_C,
                            const int *__restrict__ cexp_mui, double *__restrict__ ij, OzDims D, size_t n_tiles,
                            double tpb, OzTile *__restrict__ tiles, OzStep *__restrict__ steps,
-                           uint8_t *__restrict__ ijflag, unsigned long long *__restrict__ nsig) {
+                           uint8_t *__restrict__ ijflag, unsigned long long *__restrict__ nsig,
+                           unsigned long long *__restrict__ macs) {
     const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n_tiles) return;
     const size_t ng = (D.nob + D.R - 1) / D.R;
     const size_t g = t % ng, jb = (t / ng) % D.nob, p = t / (ng * D.nob);
+    unsigned long long m = 0;
     OzTile T;
     tile_clear(T);
     int cnt[kOzMaxSlots] = {0};
@@ -293,6 +299,7 @@ __global__ void k_tiles_ij(const uint8_t *__restrict__ mflag, const double *__re
             const size_t ib = g * D.R + s;
             if (!(__dmul_rn(cnorm[a + ib * D.nb], mnorm[mb]) >= tpb)) continue;
             st.a[s] = (uint32_t)(ib + a * D.nob);
+            m += (unsigned long long)T.rows[s] * ext_r(jb, D.bs, D.n_occ) * ext_r(a, D.bs, D.n_bf);
             ++cnt[s];
             any = true;
         }
@@ -308,6 +315,7 @@ __global__ void k_tiles_ij(const uint8_t *__restrict__ mflag, const double *__re
         tot += cnt[s];
     }
     if (tot) atomicAdd(nsig, tot);
+    if (m) atomicAdd(macs, m);
 }
 
 // K tiles: t = (sub-range, jb, group of R block rows a), steps over (p, ib)
@@ -315,11 +323,13 @@ __global__ void k_tiles_K(const uint8_t *__restrict__ mflag, const double *__res
                           const uint8_t *__restrict__ sflag, const double *__restrict__ snorm,
                           const int *__restrict__ rexp_sub, const int *__restrict__ cexp_sub, double *__restrict__ Kpart,
                           OzDims D, size_t np, size_t Q, size_t n_tiles, double tpb, OzTile *__restrict__ tiles,
-                          OzStep *__restrict__ steps, unsigned long long *__restrict__ nsig) {
+                          OzStep *__restrict__ steps, unsigned long long *__restrict__ nsig,
+                          unsigned long long *__restrict__ macs) {
     const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n_tiles) return;
     const size_t ng = (D.nb + D.R - 1) / D.R;
     const size_t g = t % ng, jb = (t / ng) % D.nob, sub = t / (ng * D.nob);
+    unsigned long long m = 0;
     OzTile T;
     tile_clear(T);
     const size_t bs2 = D.bs * D.bs;
@@ -351,6 +361,7 @@ __global__ void k_tiles_K(const uint8_t *__restrict__ mflag, const double *__res
                 if (!mflag[mb]) continue;
                 if (!(__dmul_rn(mnorm[mb], snorm[sb]) >= tpb)) continue;
                 st.a[s] = (uint32_t)mb;
+                m += (unsigned long long)T.rows[s] * T.cols * ext_r(ib, D.bs, D.n_occ);
                 ++tot;
                 any = true;
             }
@@ -359,6 +370,7 @@ __global__ void k_tiles_K(const uint8_t *__restrict__ mflag, const double *__res
     T.ns = n;
     tiles[t] = T;
     if (tot) atomicAdd(nsig, tot);
+    if (m) atomicAdd(macs, m);
 }
 
 // K(a, jb) += sum over sub-ranges (in order) of the tiles' partial blocks
@@ -424,7 +436,7 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, uint64_t stats[5]) {
     DevBuf dcexpM(pc * n_occ * 4, s), dimgMB(pc * nb * nob * b_img * 2, s);
     DevBuf drexpMs(n_sub_max * n_bf * 4, s), dcexpSs(n_sub_max * n_occ * 4, s);
     DevBuf dimgMA(pc * nb * nob * a_img * 2, s), dimgSB(pc * nob * nob * b_img * 2, s);
-    DevBuf dKp(n_sub_max * nob * nb * bs * bs * 8, s), dcnt(5 * 8, s);
+    DevBuf dKp(n_sub_max * nob * nb * bs * bs * 8, s), dcnt(5 * 8, s), dmacs(3 * 8, s);
     const size_t ng_a = ceil_div(nb, (size_t)D.R), ng_i = ceil_div(nob, (size_t)D.R);
     const size_t tiles_mui = pc * nob * ng_a, tiles_ij = pc * nob * ng_i, tiles_K = n_sub_max * nob * ng_a;
     DevBuf dtm(tiles_mui * sizeof(OzTile), s), dsm(tiles_mui * nb * sizeof(OzStep), s);
@@ -433,6 +445,7 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, uint64_t stats[5]) {
     BSG_CUDA(cudaMemsetAsync(K_dev, 0, n_bf * n_occ * 8, s));
     BSG_CUDA(cudaMemsetAsync(dcnt.p, 0, 5 * 8, s));
     auto *cnt = dcnt.as<unsigned long long>();
+    auto *macs = dmacs.as<unsigned long long>();
     const unsigned tb = (unsigned)std::max<size_t>(32, ((bs + 31) / 32) * 32);
 
     // call-constant operands: C norms, C column exponents, C images in both roles
@@ -446,6 +459,7 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, uint64_t stats[5]) {
     const double tpb = d.thresh * (double)(bs * bs * bs);
     for (size_t P0 = 0; P0 < n_aux; P0 += pc) {
         const size_t np = std::min(pc, n_aux - P0), n_sub = ceil_div(np, Q);
+        BSG_CUDA(cudaMemsetAsync(macs, 0, 3 * 8, s));
         BSG_CUDA(cudaMemsetAsync(dU.p, 0, np * n_bf * n_bf * 8, s));
         if (d.n_vec2) {
             dim3 g((unsigned)ceil_div(d.n_vec2, 256), (unsigned)np);
@@ -461,10 +475,10 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, uint64_t stats[5]) {
         const size_t tm = np * nob * ng_a;
         k_tiles_mui<<<(unsigned)ceil_div(tm, 128), 128, 0, s>>>(
             duf.as<uint8_t>(), dun.as<double>(), dcn.as<double>(), drexpU.as<int>(), dcexpC.as<int>(),
-            dmui.as<double>(), D, tm, tpb, dtm.as<OzTile>(), dsm.as<OzStep>(), dmf.as<uint8_t>(), cnt + 0);
+            dmui.as<double>(), D, tm, tpb, dtm.as<OzTile>(), dsm.as<OzStep>(), dmf.as<uint8_t>(), cnt + 0, macs + 0);
         ctx->note_launch(4);
         ctx->check_launch("rik ozaki mui prep");
-        oz_run(ctx, sh, dtm.as<OzTile>(), tm, dsm.as<OzStep>(), dimgU.as<bf16>(), dimgCB.as<bf16>(), 1.0, s);
+        oz_run(ctx, sh, dtm.as<OzTile>(), tm, dsm.as<OzStep>(), dimgU.as<bf16>(), dimgCB.as<bf16>(), 1.0, s, macs + 0);
         k_mui_norms<<<(unsigned)ceil_div(np * nb * nob, wpb), wpb * 32, 0, s>>>(
             dmui.as<double>(), dmf.as<uint8_t>(), n_bf, n_occ, bs, nb, nob, np * nb * nob, dmn.as<double>());
         // ij = C^T mui
@@ -475,10 +489,10 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, uint64_t stats[5]) {
         const size_t ti = np * nob * ng_i;
         k_tiles_ij<<<(unsigned)ceil_div(ti, 128), 128, 0, s>>>(
             dmf.as<uint8_t>(), dmn.as<double>(), dcn.as<double>(), dcexpC.as<int>(), dcexpM.as<int>(),
-            dij.as<double>(), D, ti, tpb, dti.as<OzTile>(), dsi.as<OzStep>(), dijf.as<uint8_t>(), cnt + 1);
+            dij.as<double>(), D, ti, tpb, dti.as<OzTile>(), dsi.as<OzStep>(), dijf.as<uint8_t>(), cnt + 1, macs + 1);
         ctx->note_launch(4);
         ctx->check_launch("rik ozaki ij prep");
-        oz_run(ctx, sh, dti.as<OzTile>(), ti, dsi.as<OzStep>(), dimgCtA.as<bf16>(), dimgMB.as<bf16>(), 1.0, s);
+        oz_run(ctx, sh, dti.as<OzTile>(), ti, dsi.as<OzStep>(), dimgCtA.as<bf16>(), dimgMB.as<bf16>(), 1.0, s, macs + 1);
         // ijs = ij + ij^T (FP64, with the reference's norm bookkeeping)
         k_ijs<<<(unsigned)(np * nob * nob), 128, 0, s>>>(dij.as<double>(), dijf.as<uint8_t>(), n_occ, bs, nob,
                                                           dijs.as<double>(), dsn.as<double>(), dsf.as<uint8_t>());
@@ -494,10 +508,11 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, uint64_t stats[5]) {
         const size_t tk = n_sub * nob * ng_a;
         k_tiles_K<<<(unsigned)ceil_div(tk, 128), 128, 0, s>>>(
             dmf.as<uint8_t>(), dmn.as<double>(), dsf.as<uint8_t>(), dsn.as<double>(), drexpMs.as<int>(),
-            dcexpSs.as<int>(), dKp.as<double>(), D, np, Q, tk, tpb, dtk.as<OzTile>(), dsk.as<OzStep>(), cnt + 2);
+            dcexpSs.as<int>(), dKp.as<double>(), D, np, Q, tk, tpb, dtk.as<OzTile>(), dsk.as<OzStep>(), cnt + 2,
+            macs + 2);
         ctx->note_launch(6);
         ctx->check_launch("rik ozaki K prep");
-        oz_run(ctx, sh, dtk.as<OzTile>(), tk, dsk.as<OzStep>(), dimgMA.as<bf16>(), dimgSB.as<bf16>(), 1.0, s);
+        oz_run(ctx, sh, dtk.as<OzTile>(), tk, dsk.as<OzStep>(), dimgMA.as<bf16>(), dimgSB.as<bf16>(), 1.0, s, macs + 2);
         k_K_reduce<<<(unsigned)(nb * nob), 256, 0, s>>>(dKp.as<double>(), n_sub, D, K_dev);
         ctx->note_launch();
         ctx->check_launch("rik ozaki K reduce");
