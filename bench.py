@@ -46,6 +46,10 @@ def step_flops(n_bf, n_aux, n_occ, n_vec2):
     return f3c, focc
 
 
+def flops_total(n_bf, n_aux, n_occ, n_vec2):
+    return sum(step_flops(n_bf, n_aux, n_occ, n_vec2))
+
+
 class Clocks:
     """nvidia-smi samples during the timed region"""
 
@@ -102,11 +106,16 @@ def measured_peaks():
         return {}
 
 
-def make_system():
+def make_system(n_atoms=None):
+    """the benchmark system; a smaller one (same density of atoms per volume)
+    when n_atoms is given, for profiler captures"""
     from strassen_gb300 import synth as S
 
-    return S.RikSystem(seed=CFG["seed"], n_atoms=CFG["n_atoms"], nbf=CFG["nbf"], naux=CFG["naux"], n_occ=CFG["n_occ"],
-                       box=CFG["box"])
+    if not n_atoms or n_atoms == CFG["n_atoms"]:
+        return S.RikSystem(seed=CFG["seed"], n_atoms=CFG["n_atoms"], nbf=CFG["nbf"], naux=CFG["naux"],
+                           n_occ=CFG["n_occ"], box=CFG["box"])
+    box = CFG["box"] * (n_atoms / CFG["n_atoms"]) ** (1.0 / 3.0)
+    return S.RikSystem(seed=CFG["seed"], n_atoms=n_atoms, nbf=CFG["nbf"], naux=CFG["naux"], n_occ=5 * n_atoms, box=box)
 
 
 def cpu_sample(sysm, Xr, Bp, V, C):
@@ -187,7 +196,7 @@ def run_ours(args):
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    sysm = make_system()
+    sysm = make_system(args.atoms)
     n_bf, n_aux, n_occ, n_vec2, bs, thr = sysm.n_bf, sysm.n_aux, sysm.n_occ, sysm.n_vec2, CFG["bs"], CFG["thresh"]
     form = api.FORM_OZAKI if args.form == "ozaki" else api.FORM_FP64
     d3, docc = args.digits_3c2c, args.digits_occ
@@ -254,6 +263,11 @@ def run_ours(args):
         extra = {"fp64_ms_per_step": ms64, "speedup_vs_fp64": ms64 / ms,
                  "rel_err_vs_fp64": float(np.linalg.norm(Kc - K64) / np.linalg.norm(K64)),
                  "rel_err_bound": 1e-9}
+    if args.no_e2e:
+        print(json.dumps({"metric": METRIC, "value": flops_total(n_bf, n_aux, n_occ, n_vec2) / (ms * 1e-3) / 1e12,
+                          "unit": "TFLOP/s", "ms_per_step": ms, "note": "profiling run (no e2e / baselines)",
+                          "n_vec2": n_vec2, "gemm": gemm}))
+        return
     # e2e through the C ABI with pinned host buffers
     Xh = torch.empty((n_aux, n_vec2), dtype=torch.float64, pin_memory=True)
     Xh.copy_(Xt)
@@ -331,6 +345,8 @@ def main():
     ap.add_argument("--digits-occ", type=int, default=5)
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="profiling runs: timed device step only")
+    ap.add_argument("--atoms", type=int, default=0, help="smaller system for profiler captures")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -1,0 +1,206 @@
+// 3c->2c transform (3c_2c_transform.cpp:44-57), Ozaki form, on dense device
+// operands: out = X * V^{-1/2} over the block triples that survive
+// ||X_ik|| ||V_kj|| >= thresh*bs^3, written straight into the dense output.
+//
+// The reference builds block-sparse copies of both inputs at threshold 0
+// (every block kept), pre-fills the output with zeros and accumulates; this
+// path computes the same block norms (the deterministic 32-lane order), the
+// same screen, and writes each output block as the sum of its surviving
+// products (blocks without any are written as zeros) -- no block pool, no
+// host loops over blocks.  Tiles (R block rows x 1 block column) are ordered
+// in Gr x Gc row-group x column super-tiles so that the digit images of
+// concurrently running tiles stay resident in L2.
+#include <algorithm>
+
+#include "bsg_ozaki.cuh"
+
+namespace bsg {
+
+using bf16 = __nv_bfloat16;
+
+__device__ __forceinline__ int ext3(size_t blk, size_t bs, size_t n) {
+    return (int)(((blk + 1) * bs <= n) ? bs : n - blk * bs);
+}
+
+// one warp per block of a dense column-major matrix: deterministic norm
+__global__ void k_dense_norms(const double *__restrict__ M, size_t ld, size_t nr, size_t nc, size_t bs, size_t nrb,
+                              size_t nblk, double *__restrict__ norm) {
+    const size_t b = (size_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    if (b >= nblk) return;
+    const size_t rb = b % nrb, cb = b / nrb;
+    const double est = warp_block_norm(M + rb * bs + cb * bs * ld, ext3(rb, bs, nr), ext3(cb, bs, nc), ld);
+    if ((threadIdx.x & 31) == 0) norm[b] = est;
+}
+
+// exponent of every row of X (over all columns); one thread per row
+__global__ void k_rowexp_dense(const double *__restrict__ X, size_t nr, size_t nc, int *__restrict__ rexp) {
+    const size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nr) return;
+    long long mx = 0;
+    for (size_t c = 0; c < nc; ++c) {
+        const long long b = oz_absbits(X[r + c * nr]);
+        mx = b > mx ? b : mx;
+    }
+    rexp[r] = oz_exp_of_bits(mx);
+}
+
+// exponent of every column of V (over all rows); one block per column
+__global__ void k_colexp_dense(const double *__restrict__ V, size_t nr, int *__restrict__ cexp) {
+    const size_t c = blockIdx.x;
+    long long mx = 0;
+    for (size_t r = threadIdx.x; r < nr; r += blockDim.x) {
+        const long long b = oz_absbits(V[r + c * nr]);
+        mx = b > mx ? b : mx;
+    }
+    for (int o = 16; o >= 1; o >>= 1) {
+        const long long other = __shfl_down_sync(0xffffffffu, mx, o);
+        mx = other > mx ? other : mx;
+    }
+    __shared__ long long wmax[32];
+    if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        long long m = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = wmax[w] > m ? wmax[w] : m;
+        cexp[c] = oz_exp_of_bits(m);
+    }
+}
+
+struct Dense3c {
+    size_t n_vec2, n_aux, bs, nib, nkb, njb;
+    int mp, kp, np, nd, R;
+};
+
+// A images of X blocks (ib, kb), index ib + kb*nib
+__global__ void k_img_X(const double *__restrict__ X, const int *__restrict__ rexp, Dense3c D, bf16 *__restrict__ img) {
+    const size_t x = blockIdx.x, ib = x % D.nib, kb = x / D.nib;
+    oz_block_image(X + ib * D.bs + kb * D.bs * D.n_vec2, D.n_vec2, false, ext3(ib, D.bs, D.n_vec2),
+                   ext3(kb, D.bs, D.n_aux), rexp + ib * D.bs, D.mp, D.kp, D.nd, img + x * D.nd * (size_t)D.mp * D.kp);
+}
+
+// B images of V blocks (kb, jb), index kb + jb*nkb
+__global__ void k_img_V(const double *__restrict__ V, const int *__restrict__ cexp, Dense3c D, bf16 *__restrict__ img) {
+    const size_t x = blockIdx.x, kb = x % D.nkb, jb = x / D.nkb;
+    oz_block_image(V + kb * D.bs + jb * D.bs * D.n_aux, D.n_aux, true, ext3(jb, D.bs, D.n_aux), ext3(kb, D.bs, D.n_aux),
+                   cexp + jb * D.bs, D.np, D.kp, D.nd, img + x * D.nd * (size_t)D.np * D.kp);
+}
+
+// tiles and their steps; tile t covers block rows rg*R.. and block column jb
+// from the super-tile order table
+__global__ void k_tiles_3c(const uint32_t *__restrict__ order, size_t n_tiles, const double *__restrict__ xn,
+                           const double *__restrict__ vn, const int *__restrict__ rexp, const int *__restrict__ cexp,
+                           double *__restrict__ out, Dense3c D, double tpb, OzTile *__restrict__ tiles,
+                           OzStep *__restrict__ steps, unsigned long long *__restrict__ nsig,
+                           unsigned long long *__restrict__ macs) {
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_tiles) return;
+    const size_t rg = order[2 * t], jb = order[2 * t + 1];
+    OzTile T;
+    for (int s = 0; s < kOzMaxSlots; ++s) {
+        T.c[s] = nullptr;
+        T.cnorm[s] = nullptr;
+        T.rexp[s] = nullptr;
+        T.rows[s] = 0;
+        T.ldc[s] = 0;
+    }
+    const int cols = ext3(jb, D.bs, D.n_aux);
+    for (int s = 0; s < D.R; ++s) {
+        const size_t ib = rg * D.R + s;
+        if (ib >= D.nib) break;
+        T.c[s] = out + ib * D.bs + jb * D.bs * D.n_vec2;
+        T.ldc[s] = (int)D.n_vec2;
+        T.rows[s] = ext3(ib, D.bs, D.n_vec2);
+        T.rexp[s] = rexp + ib * D.bs;
+    }
+    T.cols = cols;
+    T.cexp = cexp + jb * D.bs;
+    T.fresh_mask = 0xFFu;  // out = 0 + sum of the surviving products
+    T.s0 = (uint32_t)(t * D.nkb);
+    uint32_t n = 0;
+    unsigned long long cnt = 0, m = 0;
+    for (size_t kb = 0; kb < D.nkb; ++kb) {
+        OzStep st;
+        st.b = (uint32_t)(kb + jb * D.nkb);
+        bool any = false;
+        const double v = vn[kb + jb * D.nkb];
+        for (int s = 0; s < kOzMaxSlots; ++s) {
+            st.a[s] = kOzNone;
+            if (s >= D.R || !T.c[s]) continue;
+            const size_t ib = rg * D.R + s;
+            if (!(__dmul_rn(xn[ib + kb * D.nib], v) >= tpb)) continue;
+            st.a[s] = (uint32_t)(ib + kb * D.nib);
+            ++cnt;
+            m += (unsigned long long)T.rows[s] * cols * ext3(kb, D.bs, D.n_aux);
+            any = true;
+        }
+        if (any) steps[T.s0 + n++] = st;
+    }
+    T.ns = n;
+    tiles[t] = T;
+    if (cnt) atomicAdd(nsig, cnt);
+    if (m) atomicAdd(macs, m);
+}
+
+void transform_3c2c_ozaki(bsg_ctx ctx, size_t n_vec2, size_t n_aux, const double *X, const double *V, size_t bs,
+                          double thresh, int n_digits, double *out, uint64_t *nsig_out) {
+    cudaStream_t s = ctx->stream;
+    BSG_REQUIRE(bs <= 64, BSG_ERR_UNSUPPORTED, "Ozaki form supports blocks up to 64");
+    const int nd = oz_default_digits(n_digits, (int)bs, (int)bs, (int)bs);
+    const OzShape sh = oz_shape((int)bs, (int)bs, (int)bs, nd);
+    Dense3c D;
+    D.n_vec2 = n_vec2;
+    D.n_aux = n_aux;
+    D.bs = bs;
+    D.nib = ceil_div(n_vec2, bs);
+    D.nkb = D.njb = ceil_div(n_aux, bs);
+    D.mp = sh.mp;
+    D.kp = sh.kp;
+    D.np = sh.np;
+    D.nd = nd;
+    D.R = sh.R;
+    if (!n_vec2 || !n_aux) return;
+    const size_t a_img = (size_t)nd * sh.mp * sh.kp, b_img = (size_t)nd * sh.np * sh.kp;
+    DevBuf xn(D.nib * D.nkb * 8, s), vn(D.nkb * D.njb * 8, s), rexp(n_vec2 * 4, s), cexp(n_aux * 4, s);
+    DevBuf ai(D.nib * D.nkb * a_img * 2, s), bi(D.nkb * D.njb * b_img * 2, s), cnt(16, s);
+    BSG_CUDA(cudaMemsetAsync(cnt.p, 0, 16, s));
+    const int wpb = 8;
+    k_dense_norms<<<(unsigned)ceil_div(D.nib * D.nkb, wpb), wpb * 32, 0, s>>>(X, n_vec2, n_vec2, n_aux, bs, D.nib,
+                                                                              D.nib * D.nkb, xn.as<double>());
+    k_dense_norms<<<(unsigned)ceil_div(D.nkb * D.njb, wpb), wpb * 32, 0, s>>>(V, n_aux, n_aux, n_aux, bs, D.nkb,
+                                                                              D.nkb * D.njb, vn.as<double>());
+    k_rowexp_dense<<<(unsigned)ceil_div(n_vec2, 256), 256, 0, s>>>(X, n_vec2, n_aux, rexp.as<int>());
+    k_colexp_dense<<<(unsigned)n_aux, 256, 0, s>>>(V, n_aux, cexp.as<int>());
+    k_img_X<<<(unsigned)(D.nib * D.nkb), 128, 0, s>>>(X, rexp.as<int>(), D, ai.as<bf16>());
+    k_img_V<<<(unsigned)(D.nkb * D.njb), 128, 0, s>>>(V, cexp.as<int>(), D, bi.as<bf16>());
+    ctx->note_launch(6);
+    ctx->check_launch("3c2c ozaki prep");
+    // super-tile order: Gr row groups x Gc block columns per super-tile
+    const size_t n_rg = ceil_div(D.nib, (size_t)D.R), n_tiles = n_rg * D.njb;
+    const size_t Gr = 8, Gc = std::max<size_t>(1, std::min<size_t>(D.njb, 2 * (size_t)ctx->sm_count / Gr));
+    std::vector<uint32_t> order;
+    order.reserve(2 * n_tiles);
+    for (size_t r0 = 0; r0 < n_rg; r0 += Gr)
+        for (size_t c0 = 0; c0 < D.njb; c0 += Gc)
+            for (size_t rg = r0; rg < std::min(n_rg, r0 + Gr); ++rg)
+                for (size_t jb = c0; jb < std::min(D.njb, c0 + Gc); ++jb) {
+                    order.push_back((uint32_t)rg);
+                    order.push_back((uint32_t)jb);
+                }
+    BSG_REQUIRE(n_tiles * D.nkb < 0xffffffffull, BSG_ERR_UNSUPPORTED, "too many Ozaki steps in one call");
+    DevBuf dord(order.size() * 4, s), dt(n_tiles * sizeof(OzTile), s), dst(n_tiles * D.nkb * sizeof(OzStep), s);
+    BSG_CUDA(cudaMemcpyAsync(dord.p, order.data(), order.size() * 4, cudaMemcpyHostToDevice, s));
+    const double tpb = thresh * (double)(bs * bs * bs);
+    auto *c = cnt.as<unsigned long long>();
+    k_tiles_3c<<<(unsigned)ceil_div(n_tiles, 128), 128, 0, s>>>(dord.as<uint32_t>(), n_tiles, xn.as<double>(),
+                                                                vn.as<double>(), rexp.as<int>(), cexp.as<int>(), out, D,
+                                                                tpb, dt.as<OzTile>(), dst.as<OzStep>(), c, c + 1);
+    ctx->note_launch();
+    ctx->check_launch("3c2c ozaki tiles");
+    oz_run(ctx, sh, dt.as<OzTile>(), n_tiles, dst.as<OzStep>(), ai.as<bf16>(), bi.as<bf16>(), 1.0, s, c + 1);
+    if (nsig_out) {
+        BSG_CUDA(cudaMemcpyAsync(nsig_out, c, 8, cudaMemcpyDeviceToHost, s));
+        BSG_CUDA(cudaStreamSynchronize(s));
+    }
+}
+
+}  // namespace bsg

@@ -9,12 +9,17 @@
 //   warp 1     MMA issuer (one thread): per k16 step and A digit i, one
 //              tcgen05.mma D_i x [E_1..E_{nd+1-i}] into TMEM region i; a chain
 //              of <= 512 k is committed to the epilogue.
-//   warps 2-5  epilogue: drain the TMEM regions of a chain (tcgen05.ld),
-//              convert to FP64 and accumulate; at the end of a tile scale by
-//              2^(e_row + f_col - 14) and write the FP64 output blocks.
+//   warps 2-9  epilogue, two groups of four (one TMEM lane quadrant per
+//              warp, half of the columns per group): per chain, the exact
+//              regions R0 (integers), R1 (multiples of 2^-8) and R2
+//              (multiples of 2^-16) are added as integers into an int64
+//              accumulator, the lower-weight regions in FP32; FP64 is used once per tile to combine, scale by
+//              2^(e_row + f_col - 14) and write the output blocks (GB300's
+//              FP64 rate is far below its integer / FP32 rates).
 // Every mbarrier wait is bounded (2 s); a timeout raises a flag that ends
 // all roles and is returned as BSG_ERR_TIMEOUT.
 #include <algorithm>
+#include <tuple>
 #include <mutex>
 
 #include "bsg_ozaki.cuh"
@@ -76,8 +81,10 @@ struct OzKParams {
     double alpha;
 };
 
+constexpr int kOzThreads = 320;  // producer, MMA issuer, 8 epilogue warps
+
 template <int NP>
-__global__ void __launch_bounds__(192, 1)
+__global__ void __launch_bounds__(kOzThreads, 1)
     k_ozgemm(const OzTile *__restrict__ tiles, uint32_t n_tiles, const OzStep *__restrict__ steps,
              const bf16 *__restrict__ a_img, const bf16 *__restrict__ b_img, OzKParams P, int *__restrict__ err) {
     extern __shared__ __align__(1024) uint8_t smem[];
@@ -88,7 +95,8 @@ __global__ void __launch_bounds__(192, 1)
     const uint32_t stage_bytes = a_stage + b_stage;
     const uint32_t slot_bytes = (uint32_t)P.mp * P.kp * 2u;
     const size_t a_plane_elems = (size_t)P.mp * P.kp, b_img_elems = (size_t)P.nd * NP * P.kp;
-    uint64_t *full = reinterpret_cast<uint64_t *>(smem + (size_t)P.S * stage_bytes);
+    OzStep *sstep = reinterpret_cast<OzStep *>(smem + (size_t)P.S * stage_bytes);  // 32 prefetched steps
+    uint64_t *full = reinterpret_cast<uint64_t *>(sstep + 32);
     uint64_t *empty = full + P.S;
     uint64_t *tfull = empty + P.S;
     uint64_t *tempty = tfull + 1;
@@ -101,7 +109,7 @@ __global__ void __launch_bounds__(192, 1)
             tc::mbar_init(&empty[s], 1);
         }
         tc::mbar_init(tfull, 1);
-        tc::mbar_init(tempty, 4);
+        tc::mbar_init(tempty, 8);
         *abort = 0;
         tc::fence_barrier_init();
     }
@@ -124,9 +132,18 @@ __global__ void __launch_bounds__(192, 1)
         for (uint32_t t = blockIdx.x; t < n_tiles && !*abort; t += gridDim.x) {
             const uint32_t s0 = tiles[t].s0, ns = tiles[t].ns;
             for (uint32_t k = 0; k < ns; ++k, ++it) {
+                if ((k & 31u) == 0) {
+                    // the warp loads the next 32 step descriptors at once
+                    __syncwarp();
+                    if (k + lane < ns) sstep[lane] = steps[s0 + k + lane];
+                    __syncwarp();
+                }
                 const uint32_t stage = it % P.S, ph = (it / P.S) & 1u;
-                if (!tc::mbar_wait(&empty[stage], ph ^ 1u, abort)) break;
-                const OzStep st = steps[s0 + k];
+                // one lane waits, the warp follows its verdict (keeps the warp converged)
+                int okw = 1;
+                if (lane == 0) okw = tc::mbar_wait(&empty[stage], ph ^ 1u, abort) ? 1 : 0;
+                if (!__shfl_sync(0xffffffffu, okw, 0)) break;
+                const OzStep st = sstep[k & 31u];
                 uint8_t *sA = smem + (size_t)stage * stage_bytes;
                 uint8_t *sB = sA + a_stage;
                 if (lane == 0) tc::mbar_arrive_expect_tx(&full[stage], P.tx_bytes);
@@ -197,7 +214,10 @@ __global__ void __launch_bounds__(192, 1)
         __syncwarp();
     } else {
         // ---------------- epilogue ----------------
+        constexpr int NPH = NP / 2;  // columns per epilogue group
         const int q = warp & 3;
+        const int grp = (warp - 2) >> 2;
+        const int cbase = grp * NPH;
         const int m = q * 32 + lane;
         const uint32_t lane_addr = tmem + ((uint32_t)(q * 32) << 16);
         uint32_t ch = 0;
@@ -206,32 +226,43 @@ __global__ void __launch_bounds__(192, 1)
             const OzTile &T = tiles[t];
             const uint32_t ns = T.ns;
             const uint32_t nch = (ns + P.F - 1) / P.F;
-            double acc[NP];
+            long long hi[NPH];  // R0 + R1 + R2 in units of 2^-16
+            float lo[NPH];      // R3 + R4 + ...
 #pragma unroll
-            for (int c = 0; c < NP; ++c) acc[c] = 0.0;
+            for (int c = 0; c < NPH; ++c) {
+                hi[c] = 0;
+                lo[c] = 0.f;
+            }
             for (uint32_t c = 0; c < nch; ++c, ++ch) {
                 if (!tc::mbar_wait(tfull, ch & 1u, abort)) {
                     ok = false;
                     break;
                 }
                 tc::tc_fence_after();
-                // regions in order of weight: sum = R_0 + R_1 + ... in FP64
 #pragma unroll
-                for (int c0 = 0; c0 < NP; c0 += 16) {
-                    double sum[16];
-                    float v[16];
-                    tc::tmem_ld16(lane_addr + (uint32_t)c0, v);
+                for (int c0 = 0; c0 < NPH; c0 += 8) {
+                    float v0[8], v1[8], v2[8];
+                    tc::tmem_ld8(lane_addr + (uint32_t)(cbase + c0), v0);
+                    tc::tmem_ld8(lane_addr + (uint32_t)(NP + cbase + c0), v1);
+                    if (P.nd > 2) tc::tmem_ld8(lane_addr + (uint32_t)(2 * NP + cbase + c0), v2);
                     tc::tmem_wait_ld();
+                    // R0 is an integer < 2^24 and R1 a multiple of 2^-8 below 2^16: both
+                    // exact in the FP32 accumulator.  R2 is a multiple of 2^-16 and exact
+                    // while its partial sums stay below 2^8 (else rounded once here).
 #pragma unroll
-                    for (int j = 0; j < 16; ++j) sum[j] = (double)v[j];
-                    for (int w = 1; w < P.nd; ++w) {
-                        tc::tmem_ld16(lane_addr + (uint32_t)(w * NP + c0), v);
+                    for (int j = 0; j < 8; ++j) {
+                        long long h = ((long long)__float2int_rn(v0[j]) << 16) +
+                                      ((long long)__float2int_rn(v1[j] * 256.f) << 8);
+                        if (P.nd > 2) h += (long long)__float2int_rn(v2[j] * 65536.f);
+                        hi[c0 + j] += h;
+                    }
+                    for (int w = 3; w < P.nd; ++w) {
+                        float v[8];
+                        tc::tmem_ld8(lane_addr + (uint32_t)(w * NP + cbase + c0), v);
                         tc::tmem_wait_ld();
 #pragma unroll
-                        for (int j = 0; j < 16; ++j) sum[j] += (double)v[j];
+                        for (int j = 0; j < 8; ++j) lo[c0 + j] += v[j];
                     }
-#pragma unroll
-                    for (int j = 0; j < 16; ++j) acc[c0 + j] += sum[j];
                 }
                 tc::tc_fence_before();
                 __syncwarp();
@@ -245,14 +276,16 @@ __global__ void __launch_bounds__(192, 1)
                 const int ldc = T.ldc[s];
                 const bool fresh = (T.fresh_mask >> s) & 1u;
 #pragma unroll
-                for (int c = 0; c < NP; ++c) {
+                for (int j = 0; j < NPH; ++j) {
+                    const int c = cbase + j;
                     if (c < T.cols) {
-                        const double out = P.alpha * (acc[c] * (rs * ldexp(1.0, T.cexp[c])));
+                        const double tot = (double)hi[j] * (1.0 / 65536.0) + (double)lo[j];
+                        const double out = P.alpha * (tot * (rs * ldexp(1.0, T.cexp[c])));
                         double *dst = cp + r + (size_t)c * ldc;
                         *dst = fresh ? out : *dst + out;
                     }
                 }
-                if (fresh && r == 0 && T.cnorm[s]) *T.cnorm[s] = 0.0;
+                if (fresh && r == 0 && grp == 0 && T.cnorm[s]) *T.cnorm[s] = 0.0;
             }
         }
     }
@@ -280,10 +313,10 @@ static void launch_oz(bsg_ctx ctx, const OzShape &sh, const OzTile *tiles, size_
     while (cols < (uint32_t)sh.nd * NP) cols <<= 1;
     P.tmem_cols = cols;
     P.tx_bytes = (uint32_t)sh.R * sh.nd * sh.mp * sh.kp * 2u + (uint32_t)sh.nd * NP * sh.kp * 2u;
-    const size_t smem = (size_t)P.S * stage_bytes + (2 * P.S + 2) * 8 + 16;
+    const size_t smem = (size_t)P.S * stage_bytes + 32 * sizeof(OzStep) + (2 * P.S + 2) * 8 + 16;
     BSG_CUDA(cudaFuncSetAttribute(k_ozgemm<NP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const unsigned grid = (unsigned)std::min<size_t>(n_tiles, (size_t)ctx->sm_count);
-    k_ozgemm<NP><<<grid, 192, smem, s>>>(tiles, (uint32_t)n_tiles, steps, a_img, b_img, P, err);
+    k_ozgemm<NP><<<grid, kOzThreads, smem, s>>>(tiles, (uint32_t)n_tiles, steps, a_img, b_img, P, err);
     ctx->note_launch();
     ctx->check_launch("ozaki gemm");
 }
@@ -340,17 +373,20 @@ __global__ void k_rowexp_opA(double *const *__restrict__ tab, size_t a_nrb, int 
     const int r = threadIdx.x;
     if (r >= (int)g.ibs) return;
     const int rows = ext_of(ib, g.ibs, g.ni);
-    double mx = 0.0;
+    long long mx = 0;
     if (r < rows) {
         for (size_t kb = 0; kb < g.nkb; ++kb) {
             const double *blk = tA ? tab[kb + ib * a_nrb] : tab[ib + kb * a_nrb];
             if (!blk) continue;
             const int k = ext_of(kb, g.kbs, g.nk);
             const int ld = tA ? k : rows;
-            for (int l = 0; l < k; ++l) mx = fmax(mx, fabs(tA ? blk[l + (size_t)r * ld] : blk[r + (size_t)l * ld]));
+            for (int l = 0; l < k; ++l) {
+                const long long b = oz_absbits(tA ? blk[l + (size_t)r * ld] : blk[r + (size_t)l * ld]);
+                mx = b > mx ? b : mx;
+            }
         }
     }
-    rexp[ib * g.ibs + r] = oz_exp_of(mx);
+    rexp[ib * g.ibs + r] = oz_exp_of_bits(mx);
 }
 
 // exponent of the largest |op(B)(:, c)| of each column of op(B), block column jb
@@ -359,17 +395,20 @@ __global__ void k_colexp_opB(double *const *__restrict__ tab, size_t b_nrb, int 
     const int c = threadIdx.x;
     if (c >= (int)g.jbs) return;
     const int cols = ext_of(jb, g.jbs, g.nj);
-    double mx = 0.0;
+    long long mx = 0;
     if (c < cols) {
         for (size_t kb = 0; kb < g.nkb; ++kb) {
             const double *blk = tB ? tab[jb + kb * b_nrb] : tab[kb + jb * b_nrb];
             if (!blk) continue;
             const int k = ext_of(kb, g.kbs, g.nk);
             const int ld = tB ? cols : k;
-            for (int l = 0; l < k; ++l) mx = fmax(mx, fabs(tB ? blk[c + (size_t)l * ld] : blk[l + (size_t)c * ld]));
+            for (int l = 0; l < k; ++l) {
+                const long long b = oz_absbits(tB ? blk[c + (size_t)l * ld] : blk[l + (size_t)c * ld]);
+                mx = b > mx ? b : mx;
+            }
         }
     }
-    cexp[jb * g.jbs + c] = oz_exp_of(mx);
+    cexp[jb * g.jbs + c] = oz_exp_of_bits(mx);
 }
 
 // digit image of op(A) block (ib, kb) stored at table index b (rows x k,
@@ -382,18 +421,9 @@ __global__ void k_img_opA(double *const *__restrict__ tab, size_t a_nrb, int tA,
     const size_t sr = b % a_nrb, sc = b / a_nrb;
     const size_t ib = tA ? sc : sr, kb = tA ? sr : sc;
     const int rows = ext_of(ib, g.ibs, g.ni), k = ext_of(kb, g.kbs, g.nk);
-    const int ld = tA ? k : rows;
-    const size_t plane = (size_t)mp * kp;
-    bf16 *dst = img + b * nd * plane;
-    for (int e = threadIdx.x; e < mp * kp; e += blockDim.x) {
-        const int r = e % mp, l = e / mp;
-        double x = 0.0;
-        if (r < rows && l < k) {
-            const double v = tA ? blk[l + (size_t)r * ld] : blk[r + (size_t)l * ld];
-            x = scalbn(v, -rexp[ib * g.ibs + r]);
-        }
-        oz_digits(x, nd, dst, plane, (size_t)oz_img_off(r, l, kp));
-    }
+    // op(A)(r, l): stored block column-major (rows x k, or k x rows when transposed)
+    oz_block_image(blk, tA ? k : rows, tA != 0, rows, k, rexp + ib * g.ibs, mp, kp, nd,
+                   img + b * nd * (size_t)mp * kp);
 }
 
 // digit image of op(B) block (kb, jb) stored at table index b, as np rows
@@ -406,18 +436,9 @@ __global__ void k_img_opB(double *const *__restrict__ tab, size_t b_nrb, int tB,
     const size_t sr = b % b_nrb, sc = b / b_nrb;
     const size_t kb = tB ? sc : sr, jb = tB ? sr : sc;
     const int cols = ext_of(jb, g.jbs, g.nj), k = ext_of(kb, g.kbs, g.nk);
-    const int ld = tB ? cols : k;
-    const size_t plane = (size_t)np * kp;
-    bf16 *dst = img + b * nd * plane;
-    for (int e = threadIdx.x; e < np * kp; e += blockDim.x) {
-        const int n = e % np, l = e / np;
-        double x = 0.0;
-        if (n < cols && l < k) {
-            const double v = tB ? blk[n + (size_t)l * ld] : blk[l + (size_t)n * ld];
-            x = scalbn(v, -cexp[jb * g.jbs + n]);
-        }
-        oz_digits(x, nd, dst, plane, (size_t)oz_img_off(n, l, kp));
-    }
+    // image row n, k l = op(B)(l, n): stored (k x cols) -> src[l + n*k]; transposed (cols x k) -> src[n + l*cols]
+    oz_block_image(blk, tB ? cols : k, tB == 0, cols, k, cexp + jb * g.jbs, np, kp, nd,
+                   img + b * nd * (size_t)np * kp);
 }
 
 // steps of every tile: k blocks where the B block exists and at least one
@@ -508,6 +529,30 @@ void ozaki_screened(bsg_ctx ctx, bsg_bsm C, bsg_bsm A, bsg_bsm B, const ScreenGe
         T.ns = 0;
         tiles.push_back(T);
         tjb.push_back(jb);
+    }
+    // super-tile order (Gr row groups x Gc block columns) keeps the digit
+    // images of concurrently running tiles in L2
+    {
+        const size_t Gr = 8, Gc = std::max<size_t>(1, 2 * (size_t)ctx->sm_count / Gr);
+        std::vector<size_t> idx(tiles.size());
+        for (size_t t = 0; t < idx.size(); ++t) idx[t] = t;
+        auto key = [&](size_t t) {
+            const size_t rg = tib[t * kOzMaxSlots] / (size_t)sh.R, jb = tjb[t];
+            return std::make_tuple(rg / Gr, jb / Gc, rg % Gr, jb % Gc, rg, t);
+        };
+        std::sort(idx.begin(), idx.end(), [&](size_t a, size_t b) { return key(a) < key(b); });
+        std::vector<OzTile> t2(tiles.size());
+        std::vector<uint32_t> ib2(tib.size()), jb2(tjb.size());
+        for (size_t n = 0; n < idx.size(); ++n) {
+            t2[n] = tiles[idx[n]];
+            t2[n].s0 = (uint32_t)(n * g.nkb);
+            std::copy(tib.begin() + idx[n] * kOzMaxSlots, tib.begin() + (idx[n] + 1) * kOzMaxSlots,
+                      ib2.begin() + n * kOzMaxSlots);
+            jb2[n] = tjb[idx[n]];
+        }
+        tiles.swap(t2);
+        tib.swap(ib2);
+        tjb.swap(jb2);
     }
     BSG_REQUIRE(tiles.size() * g.nkb < 0xffffffffull, BSG_ERR_UNSUPPORTED, "too many Ozaki steps in one call");
     DevBuf dt(tiles.size() * sizeof(OzTile), s), dib(tib.size() * 4, s), djb(tjb.size() * 4, s),

@@ -73,8 +73,22 @@ void ozaki_grouped_gemm(bsg_ctx ctx, const std::vector<GemmItem> &items, const G
                         const GemmPair *d_pairs, uint64_t n_pairs, int tA, int tB, double alpha, int max_r, int max_c,
                         size_t kbs, int n_digits, cudaStream_t s);
 
-// device helpers shared with the RI-K pipeline
-__device__ __forceinline__ int oz_exp_of(double mx) { return mx > 0.0 ? ilogb(mx) + 1 : 0; }
+// ---- device helpers shared with the RI-K pipeline ----
+
+// |x| as an ordered integer (non-negative doubles compare like their bits)
+__device__ __forceinline__ long long oz_absbits(double x) {
+    return __double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFll;
+}
+
+// scale exponent e of a row/column whose largest |x| has bit pattern mb:
+// max < 2^e, i.e. the frexp exponent (0 for an all-zero row)
+__device__ __forceinline__ int oz_exp_of_bits(long long mb) {
+    if (mb == 0) return 0;
+    const int E = (int)((mb >> 52) & 0x7FF);
+    if (E) return E - 1022;
+    return ilogb(__longlong_as_double(mb)) + 1;  // subnormal
+}
+__device__ __forceinline__ int oz_exp_of(double mx) { return oz_exp_of_bits(oz_absbits(mx)); }
 
 // element offset of (row r, k l) inside one digit plane of an image with kp
 // columns: core matrices of 8x8, row groups outer, k groups inner
@@ -82,17 +96,75 @@ __device__ __forceinline__ int oz_img_off(int r, int l, int kp) {
     return (((r >> 3) * (kp >> 3) + (l >> 3)) << 6) + ((r & 7) << 3) + (l & 7);
 }
 
-// writes the nd digit planes of x (already scaled by 2^-e) at offset off
-__device__ __forceinline__ void oz_digits(double x, int nd, __nv_bfloat16 *img, size_t plane_elems, size_t off) {
-    double y = x * 128.0;
-    double scale = 1.0;
+// Fixed-point split of v with row/column exponent e into nd balanced base-256
+// digits, integer arithmetic only: N = round(v 2^(7 + 8(nd-1) - e)) (ties to
+// even), then d_{nd-1}, ..., d_1 from the low end and d_0 = the rest
+// (|d_i| <= 128).  Digit i is stored as d_i 2^(-8i).
+__device__ __forceinline__ void oz_split(double v, int e, int nd, int (&d)[kOzMaxDigits]) {
+    const long long bits = __double_as_longlong(v);
+    const int E = (int)((bits >> 52) & 0x7FF);
+    long long M = (bits & 0xFFFFFFFFFFFFFll) | (E ? (1ll << 52) : 0ll);
+    const int Eb = E ? E : 1;
+    const int K = 7 + 8 * (nd - 1);
+    const int sh = Eb - 1075 + K - e;  // N = M * 2^sh
+    long long N;
+    if (M == 0) {
+        N = 0;
+    } else if (sh >= 0) {
+        N = M << sh;
+    } else {
+        const int s = -sh;
+        if (s > 54) {
+            N = 0;
+        } else {
+            const long long q = M >> s, rem = M & ((1ll << s) - 1), half = 1ll << (s - 1);
+            N = q + ((rem > half || (rem == half && (q & 1))) ? 1 : 0);
+        }
+    }
+    if (bits < 0) N = -N;
 #pragma unroll
-    for (int i = 0; i < kOzMaxDigits; ++i) {
+    for (int i = kOzMaxDigits - 1; i >= 1; --i) {
         if (i < nd) {
-            const double d = rint(y);
-            img[i * plane_elems + off] = __float2bfloat16_rn((float)(d * scale));
-            y = (y - d) * 256.0;
-            scale *= 1.0 / 256.0;
+            const long long di = ((N + 128) & 255) - 128;
+            d[i] = (int)di;
+            N = (N - di) >> 8;
+        } else {
+            d[i] = 0;
+        }
+    }
+    d[0] = (int)N;
+}
+
+// Digit image of one block, 8 consecutive k per thread and one 16-byte store
+// per digit plane.  A role: image row r = block row, value src[r + l*ld];
+// B role: image row r = output column, value src[l + r*ld].  exps[r] is the
+// scale exponent of image row r; rows >= `rows` and k >= `k` are zero.
+__device__ __forceinline__ void oz_block_image(const double *__restrict__ src, size_t ld, bool b_role, int rows,
+                                               int k, const int *__restrict__ exps, int mpad, int kp, int nd,
+                                               __nv_bfloat16 *__restrict__ dst) {
+    const size_t plane = (size_t)mpad * kp;
+    const int hk = kp >> 3;
+    for (int idx = threadIdx.x; idx < mpad * hk; idx += blockDim.x) {
+        const int r = idx % mpad, h = idx / mpad;
+        const int e = r < rows ? exps[r] : 0;
+        int dig[8][kOzMaxDigits];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int l = h * 8 + j;
+            double v = 0.0;
+            if (r < rows && l < k) v = b_role ? src[l + (size_t)r * ld] : src[r + (size_t)l * ld];
+            oz_split(v, e, nd, dig[j]);
+        }
+        const size_t off = (size_t)oz_img_off(r, h * 8, kp);
+#pragma unroll
+        for (int i = 0; i < kOzMaxDigits; ++i) {
+            if (i < nd) {
+                const float sc = __int_as_float((127 - 8 * i) << 23);  // 2^(-8i)
+                __align__(16) __nv_bfloat16 w[8];
+#pragma unroll
+                for (int j = 0; j < 8; ++j) w[j] = __float2bfloat16_rn((float)dig[j][i] * sc);
+                *reinterpret_cast<uint4 *>(dst + i * plane + off) = *reinterpret_cast<const uint4 *>(w);
+            }
         }
     }
 }

@@ -433,6 +433,31 @@ extern "C" bsg_status bsg_3c2c_transform(bsg_ctx ctx, size_t n_vec2, size_t n_au
     return guard([&] {
         BSG_REQUIRE(ctx && ints_3c && v_m12 && out, BSG_ERR_ARG, "NULL argument");
         BSG_REQUIRE(bs > 0, BSG_ERR_ARG, "block size must be positive");
+        if (form == BSG_FORM_OZAKI) {
+            // dense device path: same norms and screen as the block-sparse
+            // path below, products on tensor cores, output written directly
+            cudaStream_t s = ctx->stream;
+            DevBuf dx, dv, dout;
+            const double *x = ints_3c, *v = v_m12;
+            double *o = out;
+            if (where == BSG_HOST) {
+                dx = DevBuf(n_vec2 * n_aux * 8, s);
+                dv = DevBuf(n_aux * n_aux * 8, s);
+                BSG_CUDA(cudaMemcpyAsync(dx.p, ints_3c, n_vec2 * n_aux * 8, cudaMemcpyHostToDevice, s));
+                BSG_CUDA(cudaMemcpyAsync(dv.p, v_m12, n_aux * n_aux * 8, cudaMemcpyHostToDevice, s));
+                x = dx.as<double>();
+                v = dv.as<double>();
+            }
+            if (out_where == BSG_HOST) {
+                dout = DevBuf(n_vec2 * n_aux * 8, s);
+                o = dout.as<double>();
+            }
+            transform_3c2c_ozaki(ctx, n_vec2, n_aux, x, v, bs, thresh, n_digits, o, nullptr);
+            if (out_where == BSG_HOST)
+                BSG_CUDA(cudaMemcpyAsync(out, o, n_vec2 * n_aux * 8, cudaMemcpyDeviceToHost, s));
+            BSG_CUDA(cudaStreamSynchronize(s));
+            return;
+        }
         bsg_bsm X = nullptr, V = nullptr, O = nullptr;
         auto cleanup = [&] {
             bsg_bsm_destroy(X);

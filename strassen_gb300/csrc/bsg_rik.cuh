@@ -27,5 +27,8 @@ __global__ void k_ijs(const double *__restrict__ ij, const uint8_t *__restrict__
 __global__ void k_cnorms(const double *__restrict__ C, size_t n_bf, size_t n_occ, size_t bs, size_t nb, size_t nob,
                          double *__restrict__ cnorm);
 void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, uint64_t stats[5]);
+// dense device 3c->2c in the Ozaki form (bsg_3c2c_oz.cu)
+void transform_3c2c_ozaki(bsg_ctx ctx, size_t n_vec2, size_t n_aux, const double *X, const double *V, size_t bs,
+                          double thresh, int n_digits, double *out, uint64_t *nsig_out);
 
 }  // namespace bsg

@@ -28,22 +28,6 @@ __device__ __forceinline__ int ext_r(size_t blk, size_t bs, size_t n) {
     return (int)(((blk + 1) * bs <= n) ? bs : n - blk * bs);
 }
 
-// image of one block: A role (rows r, k l -> src[r + l*ld]) or B role (rows
-// n = output columns, k l -> src[l + n*ld]); exps indexed by image row
-__device__ __forceinline__ void block_image(const double *src, size_t ld, bool b_role, int rows, int k,
-                                            const int *exps, int mpad, int kp, int nd, bf16 *dst) {
-    const size_t plane = (size_t)mpad * kp;
-    for (int e = threadIdx.x; e < mpad * kp; e += blockDim.x) {
-        const int r = e % mpad, l = e / mpad;
-        double x = 0.0;
-        if (r < rows && l < k) {
-            const double v = b_role ? src[l + (size_t)r * ld] : src[r + (size_t)l * ld];
-            x = scalbn(v, -exps[r]);
-        }
-        oz_digits(x, nd, dst, plane, (size_t)oz_img_off(r, l, kp));
-    }
-}
-
 // ---- scale exponents ----
 
 // U_p rows over present blocks; grid (p, a), one thread per row
@@ -53,13 +37,13 @@ __global__ void k_rexp_U(const double *__restrict__ U, const uint8_t *__restrict
     const int r = threadIdx.x, rows = ext_r(a, bs, n_bf);
     if (r >= rows) return;
     const double *Up = U + p * n_bf * n_bf;
-    double mx = 0.0;
+    long long mx = 0;
     for (size_t b = 0; b < nb; ++b) {
         if (!uflag[p * nb * nb + a + b * nb]) continue;
         const int k = ext_r(b, bs, n_bf);
-        for (int l = 0; l < k; ++l) mx = fmax(mx, fabs(Up[a * bs + r + (b * bs + l) * n_bf]));
+        for (int l = 0; l < k; ++l) { const long long bb_ = oz_absbits(Up[a * bs + r + (b * bs + l) * n_bf]); mx = bb_ > mx ? bb_ : mx; }
     }
-    rexp[p * n_bf + a * bs + r] = oz_exp_of(mx);
+    rexp[p * n_bf + a * bs + r] = oz_exp_of_bits(mx);
 }
 
 // columns of C over every row; grid jb
@@ -67,9 +51,9 @@ __global__ void k_cexp_C(const double *__restrict__ C, size_t n_bf, size_t n_occ
     const size_t jb = blockIdx.x;
     const int c = threadIdx.x;
     if (c >= ext_r(jb, bs, n_occ)) return;
-    double mx = 0.0;
-    for (size_t mu = 0; mu < n_bf; ++mu) mx = fmax(mx, fabs(C[mu + (jb * bs + c) * n_bf]));
-    cexp[jb * bs + c] = oz_exp_of(mx);
+    long long mx = 0;
+    for (size_t mu = 0; mu < n_bf; ++mu) { const long long bb_ = oz_absbits(C[mu + (jb * bs + c) * n_bf]); mx = bb_ > mx ? bb_ : mx; }
+    cexp[jb * bs + c] = oz_exp_of_bits(mx);
 }
 
 // columns of mui_p over present blocks; grid (p, jb)
@@ -79,13 +63,13 @@ __global__ void k_cexp_mui(const double *__restrict__ mui, const uint8_t *__rest
     const int c = threadIdx.x;
     if (c >= ext_r(jb, bs, n_occ)) return;
     const double *M = mui + p * n_bf * n_occ;
-    double mx = 0.0;
+    long long mx = 0;
     for (size_t a = 0; a < nb; ++a) {
         if (!mflag[p * nb * nob + a + jb * nb]) continue;
         const int rows = ext_r(a, bs, n_bf);
-        for (int r = 0; r < rows; ++r) mx = fmax(mx, fabs(M[a * bs + r + (jb * bs + c) * n_bf]));
+        for (int r = 0; r < rows; ++r) { const long long bb_ = oz_absbits(M[a * bs + r + (jb * bs + c) * n_bf]); mx = bb_ > mx ? bb_ : mx; }
     }
-    cexp[p * n_occ + jb * bs + c] = oz_exp_of(mx);
+    cexp[p * n_occ + jb * bs + c] = oz_exp_of_bits(mx);
 }
 
 // rows of mui over (p in sub-range, i); grid (sub, a)
@@ -95,16 +79,16 @@ __global__ void k_rexp_mui_sub(const double *__restrict__ mui, const uint8_t *__
     const size_t sub = blockIdx.x / nb, a = blockIdx.x % nb;
     const int r = threadIdx.x;
     if (r >= ext_r(a, bs, n_bf)) return;
-    double mx = 0.0;
+    long long mx = 0;
     const size_t p1 = min(np, (sub + 1) * Q);
     for (size_t p = sub * Q; p < p1; ++p)
         for (size_t ib = 0; ib < nob; ++ib) {
             if (!mflag[p * nb * nob + a + ib * nb]) continue;
             const double *M = mui + p * n_bf * n_occ;
             const int k = ext_r(ib, bs, n_occ);
-            for (int l = 0; l < k; ++l) mx = fmax(mx, fabs(M[a * bs + r + (ib * bs + l) * n_bf]));
+            for (int l = 0; l < k; ++l) { const long long bb_ = oz_absbits(M[a * bs + r + (ib * bs + l) * n_bf]); mx = bb_ > mx ? bb_ : mx; }
         }
-    rexp[sub * n_bf + a * bs + r] = oz_exp_of(mx);
+    rexp[sub * n_bf + a * bs + r] = oz_exp_of_bits(mx);
 }
 
 // columns of ijs over (p in sub-range, i); grid (sub, jb)
@@ -113,16 +97,16 @@ __global__ void k_cexp_ijs_sub(const double *__restrict__ ijs, const uint8_t *__
     const size_t sub = blockIdx.x / nob, jb = blockIdx.x % nob;
     const int c = threadIdx.x;
     if (c >= ext_r(jb, bs, n_occ)) return;
-    double mx = 0.0;
+    long long mx = 0;
     const size_t p1 = min(np, (sub + 1) * Q);
     for (size_t p = sub * Q; p < p1; ++p)
         for (size_t ib = 0; ib < nob; ++ib) {
             if (!sflag[p * nob * nob + ib + jb * nob]) continue;
             const double *S = ijs + p * n_occ * n_occ;
             const int k = ext_r(ib, bs, n_occ);
-            for (int l = 0; l < k; ++l) mx = fmax(mx, fabs(S[ib * bs + l + (jb * bs + c) * n_occ]));
+            for (int l = 0; l < k; ++l) { const long long bb_ = oz_absbits(S[ib * bs + l + (jb * bs + c) * n_occ]); mx = bb_ > mx ? bb_ : mx; }
         }
-    cexp[sub * n_occ + jb * bs + c] = oz_exp_of(mx);
+    cexp[sub * n_occ + jb * bs + c] = oz_exp_of_bits(mx);
 }
 
 // ---- digit images ----
@@ -138,7 +122,7 @@ __global__ void k_img_U(const double *__restrict__ U, const uint8_t *__restrict_
     const size_t x = blockIdx.x;
     if (!uflag[x]) return;
     const size_t p = x / (D.nb * D.nb), a = x % D.nb, b = (x / D.nb) % D.nb;
-    block_image(U + p * D.n_bf * D.n_bf + a * D.bs + b * D.bs * D.n_bf, D.n_bf, false, ext_r(a, D.bs, D.n_bf),
+    oz_block_image(U + p * D.n_bf * D.n_bf + a * D.bs + b * D.bs * D.n_bf, D.n_bf, false, ext_r(a, D.bs, D.n_bf),
                 ext_r(b, D.bs, D.n_bf), rexp + p * D.n_bf + a * D.bs, D.mp, D.kp, D.nd,
                 img + x * D.nd * (size_t)D.mp * D.kp);
 }
@@ -146,14 +130,14 @@ __global__ void k_img_U(const double *__restrict__ U, const uint8_t *__restrict_
 // C blocks (b, j) in the B role of mui = U C; index b + j*nb
 __global__ void k_img_C_B(const double *__restrict__ C, const int *__restrict__ cexp, OzDims D, bf16 *__restrict__ img) {
     const size_t x = blockIdx.x, b = x % D.nb, j = x / D.nb;
-    block_image(C + b * D.bs + j * D.bs * D.n_bf, D.n_bf, true, ext_r(j, D.bs, D.n_occ), ext_r(b, D.bs, D.n_bf),
+    oz_block_image(C + b * D.bs + j * D.bs * D.n_bf, D.n_bf, true, ext_r(j, D.bs, D.n_occ), ext_r(b, D.bs, D.n_bf),
                 cexp + j * D.bs, D.np, D.kp, D.nd, img + x * D.nd * (size_t)D.np * D.kp);
 }
 
 // C^T blocks (ib, a) in the A role of ij = C^T mui; index ib + a*nob
 __global__ void k_img_Ct_A(const double *__restrict__ C, const int *__restrict__ cexp, OzDims D, bf16 *__restrict__ img) {
     const size_t x = blockIdx.x, ib = x % D.nob, a = x / D.nob;
-    block_image(C + a * D.bs + ib * D.bs * D.n_bf, D.n_bf, true, ext_r(ib, D.bs, D.n_occ), ext_r(a, D.bs, D.n_bf),
+    oz_block_image(C + a * D.bs + ib * D.bs * D.n_bf, D.n_bf, true, ext_r(ib, D.bs, D.n_occ), ext_r(a, D.bs, D.n_bf),
                 cexp + ib * D.bs, D.mp, D.kp, D.nd, img + x * D.nd * (size_t)D.mp * D.kp);
 }
 
@@ -163,7 +147,7 @@ __global__ void k_img_mui_B(const double *__restrict__ mui, const uint8_t *__res
     const size_t x = blockIdx.x;
     if (!mflag[x]) return;
     const size_t p = x / (D.nb * D.nob), a = x % D.nb, jb = (x / D.nb) % D.nob;
-    block_image(mui + p * D.n_bf * D.n_occ + a * D.bs + jb * D.bs * D.n_bf, D.n_bf, true, ext_r(jb, D.bs, D.n_occ),
+    oz_block_image(mui + p * D.n_bf * D.n_occ + a * D.bs + jb * D.bs * D.n_bf, D.n_bf, true, ext_r(jb, D.bs, D.n_occ),
                 ext_r(a, D.bs, D.n_bf), cexp + p * D.n_occ + jb * D.bs, D.np, D.kp, D.nd,
                 img + x * D.nd * (size_t)D.np * D.kp);
 }
@@ -174,7 +158,7 @@ __global__ void k_img_mui_A(const double *__restrict__ mui, const uint8_t *__res
     const size_t x = blockIdx.x;
     if (!mflag[x]) return;
     const size_t p = x / (D.nb * D.nob), a = x % D.nb, ib = (x / D.nb) % D.nob;
-    block_image(mui + p * D.n_bf * D.n_occ + a * D.bs + ib * D.bs * D.n_bf, D.n_bf, false, ext_r(a, D.bs, D.n_bf),
+    oz_block_image(mui + p * D.n_bf * D.n_occ + a * D.bs + ib * D.bs * D.n_bf, D.n_bf, false, ext_r(a, D.bs, D.n_bf),
                 ext_r(ib, D.bs, D.n_occ), rexp + (p / Q) * D.n_bf + a * D.bs, D.mp, D.kp, D.nd,
                 img + x * D.nd * (size_t)D.mp * D.kp);
 }
@@ -185,7 +169,7 @@ __global__ void k_img_ijs_B(const double *__restrict__ ijs, const uint8_t *__res
     const size_t x = blockIdx.x;
     if (!sflag[x]) return;
     const size_t p = x / (D.nob * D.nob), ib = x % D.nob, jb = (x / D.nob) % D.nob;
-    block_image(ijs + p * D.n_occ * D.n_occ + ib * D.bs + jb * D.bs * D.n_occ, D.n_occ, true, ext_r(jb, D.bs, D.n_occ),
+    oz_block_image(ijs + p * D.n_occ * D.n_occ + ib * D.bs + jb * D.bs * D.n_occ, D.n_occ, true, ext_r(jb, D.bs, D.n_occ),
                 ext_r(ib, D.bs, D.n_occ), cexp + (p / Q) * D.n_occ + jb * D.bs, D.np, D.kp, D.nd,
                 img + x * D.nd * (size_t)D.np * D.kp);
 }
