@@ -215,11 +215,13 @@ def run_ours(args):
         api.transform_3c2c(X, V, bs, thr, form=form_, n_digits=d3, out=B, ctx=ctx)
         if stats is not None:
             stats["3c2c"] = ctx.gemm_timing()
+            stats["3c2c_stalls"] = ctx.gemm_stalls()
             ctx.set_timing(True)
         _, st = api.rik_occ_step(B, keys, C, n_bf, n_aux, n_occ, bs, thr, n_part=1, form=form_, n_digits=docc, out=K,
                                  ctx=ctx, stats=True)
         if stats is not None:
             stats["occ"] = ctx.gemm_timing()
+            stats["occ_stalls"] = ctx.gemm_stalls()
             stats["nsig"] = st[:3]
 
     def timed(fn, steps, warmup):

@@ -65,6 +65,13 @@ bsg_status bsg_ctx_launch_count(bsg_ctx ctx, uint64_t *out);
  * multiply-adds they performed (FP64-equivalent; x digit products for bf16). */
 bsg_status bsg_ctx_set_timing(bsg_ctx ctx, int on);
 bsg_status bsg_ctx_gemm_timing(bsg_ctx ctx, uint64_t *launches, double *ms, double *useful_macs);
+/* Pipeline stall breakdown of the same launches (SM clock cycles summed over
+ * CTAs; collected only while timing is on): [0] MMA issuer waiting for
+ * operand stages, [1] MMA issuer waiting for a drained accumulator, [2] MMA
+ * issuer lifetime, [3] producer waiting for a free stage, [4] epilogue
+ * waiting for a finished chain, [5] epilogue draining TMEM, [6] epilogue
+ * writing output blocks, [7] operand stages consumed. */
+bsg_status bsg_ctx_gemm_stalls(bsg_ctx ctx, uint64_t out[8]);
 
 /* ---- block pool: BlockMemoryPool<double> (blockallocator.h:8-25,
  *      blockallocator.hpp:7-56).  Device slabs grow geometrically from 16 MB

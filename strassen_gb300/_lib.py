@@ -55,6 +55,7 @@ _sig("bsg_ctx_sync", [c_vp])
 _sig("bsg_ctx_launch_count", [c_vp, c_u64p])
 _sig("bsg_ctx_set_timing", [c_vp, c_int])
 _sig("bsg_ctx_gemm_timing", [c_vp, c_u64p, C.POINTER(c_dbl), C.POINTER(c_dbl)])
+_sig("bsg_ctx_gemm_stalls", [c_vp, c_u64p])
 _sig("bsg_rik_occ_step_noalloc", [C.POINTER(RikArgs), c_vp, c_vp, c_u64p])
 _sig("bsg_pool_create", [c_vp, c_size, C.POINTER(c_vp)])
 _sig("bsg_pool_release", [c_vp])

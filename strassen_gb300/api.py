@@ -80,6 +80,15 @@ class Context:
         check(lib.bsg_ctx_gemm_timing(self.h, C.byref(n), C.byref(ms), C.byref(macs)))
         return n.value, ms.value, macs.value
 
+    STALL_KEYS = ("mma_wait_operands", "mma_wait_accumulator", "mma_total", "producer_wait_stage",
+                  "epilogue_wait_chain", "epilogue_drain", "epilogue_store", "steps")
+
+    def gemm_stalls(self):
+        """stall breakdown of the timed tensor-core GEMM launches (SM cycles summed over CTAs)"""
+        out = (C.c_uint64 * 8)()
+        check(lib.bsg_ctx_gemm_stalls(self.h, out))
+        return dict(zip(self.STALL_KEYS, list(out)))
+
 
 def default_context():
     global _DEFAULT_CTX

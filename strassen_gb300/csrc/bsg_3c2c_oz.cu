@@ -7,9 +7,7 @@
 // path computes the same block norms (the deterministic 32-lane order), the
 // same screen, and writes each output block as the sum of its surviving
 // products (blocks without any are written as zeros) -- no block pool, no
-// host loops over blocks.  Tiles (R block rows x 1 block column) are ordered
-// in Gr x Gc row-group x column super-tiles so that the digit images of
-// concurrently running tiles stay resident in L2.
+// host loops over blocks.
 #include <algorithm>
 
 #include "bsg_ozaki.cuh"
@@ -71,30 +69,39 @@ struct Dense3c {
     int mp, kp, np, nd, R;
 };
 
-// A images of X blocks (ib, kb), index ib + kb*nib
+// The tile is transposed with respect to the output: its slots (the MMA's M
+// side) are R output block columns jb, fed by V^T blocks, and its columns
+// (the N side) one output block row ib, fed by the X block of each k step.
+// V^{-1/2} has no block locality, so whether a triple survives the screen is
+// decided by ||X_ib,kb|| for all R slots alike and a step's slots are nearly
+// always all live; with block rows as slots a step would carry the
+// insignificant X blocks of its other rows as zero images.
+
+// N-side images of X blocks (ib, kb): image row = output row, index ib + kb*nib
 __global__ void k_img_X(const double *__restrict__ X, const int *__restrict__ rexp, Dense3c D, bf16 *__restrict__ img) {
     const size_t x = blockIdx.x, ib = x % D.nib, kb = x / D.nib;
     oz_block_image(X + ib * D.bs + kb * D.bs * D.n_vec2, D.n_vec2, false, ext3(ib, D.bs, D.n_vec2),
-                   ext3(kb, D.bs, D.n_aux), rexp + ib * D.bs, D.mp, D.kp, D.nd, img + x * D.nd * (size_t)D.mp * D.kp);
+                   ext3(kb, D.bs, D.n_aux), rexp + ib * D.bs, D.np, D.kp, D.nd, img + x * D.nd * (size_t)D.np * D.kp, false);
 }
 
-// B images of V blocks (kb, jb), index kb + jb*nkb
+// M-side images of V^T blocks (jb, kb): image row = output column, index
+// jb + kb*njb (a tile's slots are consecutive images)
 __global__ void k_img_V(const double *__restrict__ V, const int *__restrict__ cexp, Dense3c D, bf16 *__restrict__ img) {
-    const size_t x = blockIdx.x, kb = x % D.nkb, jb = x / D.nkb;
+    const size_t x = blockIdx.x, jb = x % D.njb, kb = x / D.njb;
     oz_block_image(V + kb * D.bs + jb * D.bs * D.n_aux, D.n_aux, true, ext3(jb, D.bs, D.n_aux), ext3(kb, D.bs, D.n_aux),
-                   cexp + jb * D.bs, D.np, D.kp, D.nd, img + x * D.nd * (size_t)D.np * D.kp);
+                   cexp + jb * D.bs, D.mp, D.kp, D.nd, img + x * D.nd * (size_t)D.mp * D.kp, true);
 }
 
-// tiles and their steps; tile t covers block rows rg*R.. and block column jb
-// from the super-tile order table
-__global__ void k_tiles_3c(const uint32_t *__restrict__ order, size_t n_tiles, const double *__restrict__ xn,
-                           const double *__restrict__ vn, const int *__restrict__ rexp, const int *__restrict__ cexp,
-                           double *__restrict__ out, Dense3c D, double tpb, OzTile *__restrict__ tiles,
-                           OzStep *__restrict__ steps, unsigned long long *__restrict__ nsig,
-                           unsigned long long *__restrict__ macs) {
+// tiles and their steps; tile t covers output block row ib and block columns
+// jg*R .. jg*R+R-1, ib-major so that the tiles sharing an X block row run
+// together and read its images from L2
+__global__ void k_tiles_3c(size_t n_tiles, size_t n_jg, const double *__restrict__ xn, const double *__restrict__ vn,
+                           const int *__restrict__ rexp, const int *__restrict__ cexp, double *__restrict__ out,
+                           Dense3c D, double tpb, OzTile *__restrict__ tiles, OzStep *__restrict__ steps,
+                           unsigned long long *__restrict__ nsig, unsigned long long *__restrict__ macs) {
     const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n_tiles) return;
-    const size_t rg = order[2 * t], jb = order[2 * t + 1];
+    const size_t ib = t / n_jg, jg = t % n_jg;
     OzTile T;
     for (int s = 0; s < kOzMaxSlots; ++s) {
         T.c[s] = nullptr;
@@ -103,34 +110,35 @@ __global__ void k_tiles_3c(const uint32_t *__restrict__ order, size_t n_tiles, c
         T.rows[s] = 0;
         T.ldc[s] = 0;
     }
-    const int cols = ext3(jb, D.bs, D.n_aux);
+    const int rows = ext3(ib, D.bs, D.n_vec2);
     for (int s = 0; s < D.R; ++s) {
-        const size_t ib = rg * D.R + s;
-        if (ib >= D.nib) break;
+        const size_t jb = jg * D.R + s;
+        if (jb >= D.njb) break;
         T.c[s] = out + ib * D.bs + jb * D.bs * D.n_vec2;
         T.ldc[s] = (int)D.n_vec2;
-        T.rows[s] = ext3(ib, D.bs, D.n_vec2);
-        T.rexp[s] = rexp + ib * D.bs;
+        T.rows[s] = ext3(jb, D.bs, D.n_aux);  // slot rows are output columns
+        T.rexp[s] = cexp + jb * D.bs;
     }
-    T.cols = cols;
-    T.cexp = cexp + jb * D.bs;
+    T.cols = rows;  // tile columns are output rows
+    T.cexp = rexp + ib * D.bs;
+    T.trans = 1;
     T.fresh_mask = 0xFFu;  // out = 0 + sum of the surviving products
     T.s0 = (uint32_t)(t * D.nkb);
     uint32_t n = 0;
     unsigned long long cnt = 0, m = 0;
     for (size_t kb = 0; kb < D.nkb; ++kb) {
         OzStep st;
-        st.b = (uint32_t)(kb + jb * D.nkb);
+        st.b = (uint32_t)(ib + kb * D.nib);
         bool any = false;
-        const double v = vn[kb + jb * D.nkb];
+        const double x = xn[ib + kb * D.nib];
         for (int s = 0; s < kOzMaxSlots; ++s) {
             st.a[s] = kOzNone;
             if (s >= D.R || !T.c[s]) continue;
-            const size_t ib = rg * D.R + s;
-            if (!(__dmul_rn(xn[ib + kb * D.nib], v) >= tpb)) continue;
-            st.a[s] = (uint32_t)(ib + kb * D.nib);
+            const size_t jb = jg * D.R + s;
+            if (!(__dmul_rn(x, vn[kb + jb * D.nkb]) >= tpb)) continue;
+            st.a[s] = (uint32_t)(jb + kb * D.njb);
             ++cnt;
-            m += (unsigned long long)T.rows[s] * cols * ext3(kb, D.bs, D.n_aux);
+            m += (unsigned long long)rows * T.rows[s] * ext3(kb, D.bs, D.n_aux);
             any = true;
         }
         if (any) steps[T.s0 + n++] = st;
@@ -161,7 +169,7 @@ void transform_3c2c_ozaki(bsg_ctx ctx, size_t n_vec2, size_t n_aux, const double
     if (!n_vec2 || !n_aux) return;
     const size_t a_img = (size_t)nd * sh.mp * sh.kp, b_img = (size_t)nd * sh.np * sh.kp;
     DevBuf xn(D.nib * D.nkb * 8, s), vn(D.nkb * D.njb * 8, s), rexp(n_vec2 * 4, s), cexp(n_aux * 4, s);
-    DevBuf ai(D.nib * D.nkb * a_img * 2, s), bi(D.nkb * D.njb * b_img * 2, s), cnt(16, s);
+    DevBuf ai(D.nkb * D.njb * a_img * 2, s), bi(D.nib * D.nkb * b_img * 2, s), cnt(16, s);
     BSG_CUDA(cudaMemsetAsync(cnt.p, 0, 16, s));
     const int wpb = 8;
     k_dense_norms<<<(unsigned)ceil_div(D.nib * D.nkb, wpb), wpb * 32, 0, s>>>(X, n_vec2, n_vec2, n_aux, bs, D.nib,
@@ -170,33 +178,22 @@ void transform_3c2c_ozaki(bsg_ctx ctx, size_t n_vec2, size_t n_aux, const double
                                                                               D.nkb * D.njb, vn.as<double>());
     k_rowexp_dense<<<(unsigned)ceil_div(n_vec2, 256), 256, 0, s>>>(X, n_vec2, n_aux, rexp.as<int>());
     k_colexp_dense<<<(unsigned)n_aux, 256, 0, s>>>(V, n_aux, cexp.as<int>());
-    k_img_X<<<(unsigned)(D.nib * D.nkb), 128, 0, s>>>(X, rexp.as<int>(), D, ai.as<bf16>());
-    k_img_V<<<(unsigned)(D.nkb * D.njb), 128, 0, s>>>(V, cexp.as<int>(), D, bi.as<bf16>());
+    k_img_X<<<(unsigned)(D.nib * D.nkb), 128, 0, s>>>(X, rexp.as<int>(), D, bi.as<bf16>());
+    k_img_V<<<(unsigned)(D.nkb * D.njb), 128, 0, s>>>(V, cexp.as<int>(), D, ai.as<bf16>());
     ctx->note_launch(6);
     ctx->check_launch("3c2c ozaki prep");
-    // super-tile order: Gr row groups x Gc block columns per super-tile
-    const size_t n_rg = ceil_div(D.nib, (size_t)D.R), n_tiles = n_rg * D.njb;
-    const size_t Gr = 8, Gc = std::max<size_t>(1, std::min<size_t>(D.njb, 2 * (size_t)ctx->sm_count / Gr));
-    std::vector<uint32_t> order;
-    order.reserve(2 * n_tiles);
-    for (size_t r0 = 0; r0 < n_rg; r0 += Gr)
-        for (size_t c0 = 0; c0 < D.njb; c0 += Gc)
-            for (size_t rg = r0; rg < std::min(n_rg, r0 + Gr); ++rg)
-                for (size_t jb = c0; jb < std::min(D.njb, c0 + Gc); ++jb) {
-                    order.push_back((uint32_t)rg);
-                    order.push_back((uint32_t)jb);
-                }
+    const size_t n_jg = ceil_div(D.njb, (size_t)D.R), n_tiles = D.nib * n_jg;
     BSG_REQUIRE(n_tiles * D.nkb < 0xffffffffull, BSG_ERR_UNSUPPORTED, "too many Ozaki steps in one call");
-    DevBuf dord(order.size() * 4, s), dt(n_tiles * sizeof(OzTile), s), dst(n_tiles * D.nkb * sizeof(OzStep), s);
-    BSG_CUDA(cudaMemcpyAsync(dord.p, order.data(), order.size() * 4, cudaMemcpyHostToDevice, s));
+    DevBuf dt(n_tiles * sizeof(OzTile), s), dst(n_tiles * D.nkb * sizeof(OzStep), s);
     const double tpb = thresh * (double)(bs * bs * bs);
     auto *c = cnt.as<unsigned long long>();
-    k_tiles_3c<<<(unsigned)ceil_div(n_tiles, 128), 128, 0, s>>>(dord.as<uint32_t>(), n_tiles, xn.as<double>(),
-                                                                vn.as<double>(), rexp.as<int>(), cexp.as<int>(), out, D,
-                                                                tpb, dt.as<OzTile>(), dst.as<OzStep>(), c, c + 1);
+    k_tiles_3c<<<(unsigned)ceil_div(n_tiles, 128), 128, 0, s>>>(n_tiles, n_jg, xn.as<double>(), vn.as<double>(),
+                                                                rexp.as<int>(), cexp.as<int>(), out, D, tpb,
+                                                                dt.as<OzTile>(), dst.as<OzStep>(), c, c + 1);
     ctx->note_launch();
     ctx->check_launch("3c2c ozaki tiles");
     oz_run(ctx, sh, dt.as<OzTile>(), n_tiles, dst.as<OzStep>(), ai.as<bf16>(), bi.as<bf16>(), 1.0, s, c + 1);
+    ctx->gemm_check();
     if (nsig_out) {
         BSG_CUDA(cudaMemcpyAsync(nsig_out, c, 8, cudaMemcpyDeviceToHost, s));
         BSG_CUDA(cudaStreamSynchronize(s));

@@ -46,6 +46,7 @@ void ctx_release(bsg_ctx c) {
     if (!c) return;
     if (c->refs.fetch_sub(1) == 1) {
         cudaStreamSynchronize(c->stream);
+        if (c->d_gemm_err) cudaFree(c->d_gemm_err);
         if (c->own_stream) cudaStreamDestroy(c->stream);
         delete c;
     }
@@ -61,6 +62,24 @@ extern "C" int bsg_version(void) { return 10000; }
 void bsg_ctx_s::check_launch(const char *what) {
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) throw Error{BSG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e)};
+}
+
+int *bsg_ctx_s::gemm_err_flag() {
+    if (!d_gemm_err) BSG_CUDA(cudaMalloc(&d_gemm_err, sizeof(int)));
+    if (!gemm_err_pending) {
+        BSG_CUDA(cudaMemsetAsync(d_gemm_err, 0, sizeof(int), stream));
+        gemm_err_pending = true;
+    }
+    return d_gemm_err;
+}
+
+void bsg_ctx_s::gemm_check() {
+    if (!gemm_err_pending) return;
+    int h = 0;
+    BSG_CUDA(cudaMemcpyAsync(&h, d_gemm_err, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    BSG_CUDA(cudaStreamSynchronize(stream));
+    gemm_err_pending = false;
+    BSG_REQUIRE(!h, BSG_ERR_TIMEOUT, "Ozaki GEMM: a pipeline wait timed out");
 }
 
 extern "C" bsg_status bsg_ctx_create(int device, void *cuda_stream, bsg_ctx *out) {
@@ -79,6 +98,14 @@ extern "C" bsg_status bsg_ctx_create(int device, void *cuda_stream, bsg_ctx *out
             c->own_stream = true;
         }
         BSG_CUDA(cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device));
+        // keep freed stream-ordered allocations cached in this process (the
+        // default pool would hand them back at every synchronization and map
+        // them again on the next call); this process's own runtime state only
+        cudaMemPool_t mp;
+        if (cudaDeviceGetDefaultMemPool(&mp, device) == cudaSuccess) {
+            uint64_t keep = 64ull << 30;
+            cudaMemPoolSetAttribute(mp, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
         *out = c;
     });
 }
@@ -110,6 +137,7 @@ extern "C" bsg_status bsg_ctx_set_timing(bsg_ctx ctx, int on) {
         ctx->oz_ms = 0.0;
         ctx->oz_launches = 0;
         ctx->oz_useful_macs = 0.0;
+        for (auto &v : ctx->oz_stall) v = 0;
     });
 }
 
@@ -119,6 +147,13 @@ extern "C" bsg_status bsg_ctx_gemm_timing(bsg_ctx ctx, uint64_t *launches, doubl
         if (launches) *launches = ctx->oz_launches;
         if (ms) *ms = ctx->oz_ms;
         if (useful_macs) *useful_macs = ctx->oz_useful_macs;
+    });
+}
+
+extern "C" bsg_status bsg_ctx_gemm_stalls(bsg_ctx ctx, uint64_t out[8]) {
+    return guard([&] {
+        BSG_REQUIRE(ctx && out, BSG_ERR_ARG, "NULL argument");
+        for (int i = 0; i < 8; ++i) out[i] = ctx->oz_stall[i];
     });
 }
 

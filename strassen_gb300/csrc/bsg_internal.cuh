@@ -93,8 +93,15 @@ struct bsg_ctx_s {
     double oz_ms = 0.0;
     uint64_t oz_launches = 0;
     double oz_useful_macs = 0.0;  // unpadded block-product multiply-adds (FP64-equivalent)
+    uint64_t oz_stall[8] = {};    // pipeline stall counters of the GEMM kernel (SM cycles over CTAs)
+    // timeout flag of the tensor-core GEMM launches: set on the device, read
+    // once per public call (gemm_check) instead of after every launch
+    int *d_gemm_err = nullptr;
+    bool gemm_err_pending = false;
     void note_launch(uint64_t n = 1) { launches += n; }
     void check_launch(const char *what);
+    int *gemm_err_flag();  // the device flag, cleared before the first launch of a call
+    void gemm_check();     // synchronizes if launches are pending; throws BSG_ERR_TIMEOUT if one timed out
 };
 
 // BlockMemoryPool<double> on the device (blockallocator.h:8-25).

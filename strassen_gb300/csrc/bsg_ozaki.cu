@@ -30,7 +30,8 @@ namespace bsg {
 
 using bf16 = __nv_bfloat16;
 
-static __device__ __align__(128) bf16 g_oz_zero[8 * 1024];  // 16 KB of zeros (largest A plane image 8 KB)
+// zeros for masked slots: the largest A stage (8 digits x 128 rows x 64 k)
+static __device__ __align__(128) bf16 g_oz_zero[8 * 128 * 64];
 
 static void *oz_zero_image() {
     static std::mutex mu;
@@ -49,14 +50,18 @@ OzShape oz_shape(int bs_rows, int bs_k, int bs_cols, int nd) {
     s.nd = nd;
     s.mp = round_up(bs_rows, 8);
     s.kp = round_up(bs_k, 16);
-    s.np = round_up(bs_cols, 16);
+    s.np = round_up(bs_cols, 8);
     s.R = std::min(kOzMaxSlots, 128 / s.mp);
     s.F = std::max(1, 512 / s.kp);
     return s;
 }
 
+// B rows of a stage: the nd stacked digit planes, rounded up to the MMA's
+// N granularity of 16 (an MMA over an odd number of 8-row planes reads 8
+// zero rows past the stack)
+static uint32_t oz_b_rows(int nd, int np) { return (uint32_t)round_up(nd * np, 16); }
 static uint32_t oz_stage_bytes(const OzShape &sh) {
-    return (uint32_t)sh.nd * 128u * sh.kp * 2u + (uint32_t)sh.nd * sh.np * sh.kp * 2u;
+    return (uint32_t)sh.nd * 128u * sh.kp * 2u + oz_b_rows(sh.nd, sh.np) * sh.kp * 2u;
 }
 constexpr uint32_t kOzSmemBudget = 200u * 1024u;
 
@@ -75,10 +80,25 @@ int oz_default_digits(int requested, int bs_rows, int bs_k, int bs_cols) {
 
 struct OzKParams {
     int mp, kp, R, nd, S, F;
-    uint32_t tmem_cols;
+    int nbuf;            // TMEM accumulator sets (2: the MMA fills one while the epilogue drains the other)
+    uint32_t tmem_cols;  // columns of one accumulator set
     uint32_t tx_bytes;
     const bf16 *zero;
     double alpha;
+    unsigned long long *prof;  // optional stall counters (kOzProf entries), null when not timing
+};
+
+// stall counters (SM clock cycles summed over CTAs), read through bsg_ctx_gemm_stalls
+enum OzProf {
+    kProfMmaWaitFull,    // MMA issuer waiting for operand stages
+    kProfMmaWaitTmem,    // MMA issuer waiting for a drained accumulator set
+    kProfMmaTotal,       // MMA issuer lifetime
+    kProfProdWaitEmpty,  // producer waiting for a free stage
+    kProfEpiWaitFull,    // epilogue waiting for a finished chain
+    kProfEpiDrain,       // epilogue reading TMEM and accumulating
+    kProfEpiStore,       // epilogue scaling and writing output blocks
+    kProfSteps,          // operand stages consumed by the MMA issuer
+    kOzProf
 };
 
 constexpr int kOzThreads = 320;  // producer, MMA issuer, 8 epilogue warps
@@ -89,27 +109,30 @@ __global__ void __launch_bounds__(kOzThreads, 1)
              const bf16 *__restrict__ a_img, const bf16 *__restrict__ b_img, OzKParams P, int *__restrict__ err) {
     extern __shared__ __align__(1024) uint8_t smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t a_plane = 128u * P.kp * 2u;  // bytes of one A digit plane in a stage
-    const uint32_t a_stage = P.nd * a_plane;
-    const uint32_t b_stage = (uint32_t)P.nd * NP * P.kp * 2u;
+    const uint32_t a_stage = (uint32_t)P.nd * 128u * P.kp * 2u;  // A: 128 rows x nd digits (M-side layout)
+    const uint32_t b_copy = (uint32_t)P.nd * NP * P.kp * 2u;           // bytes of one B digit stack
+    const uint32_t b_stage = (uint32_t)((P.nd * NP + 15) & ~15) * P.kp * 2u;  // stage room (N rounded to 16)
     const uint32_t stage_bytes = a_stage + b_stage;
-    const uint32_t slot_bytes = (uint32_t)P.mp * P.kp * 2u;
-    const size_t a_plane_elems = (size_t)P.mp * P.kp, b_img_elems = (size_t)P.nd * NP * P.kp;
+    const uint32_t slot_bytes = (uint32_t)P.nd * P.mp * P.kp * 2u;  // one slot's full digit image
+    const size_t slot_elems = (size_t)P.nd * P.mp * P.kp, b_img_elems = (size_t)P.nd * NP * P.kp;
     OzStep *sstep = reinterpret_cast<OzStep *>(smem + (size_t)P.S * stage_bytes);  // 32 prefetched steps
     uint64_t *full = reinterpret_cast<uint64_t *>(sstep + 32);
     uint64_t *empty = full + P.S;
-    uint64_t *tfull = empty + P.S;
-    uint64_t *tempty = tfull + 1;
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(tempty + 1);
+    uint64_t *tfull = empty + P.S;  // [2]
+    uint64_t *tempty = tfull + 2;   // [2]
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(tempty + 2);
     volatile int *abort = reinterpret_cast<volatile int *>(tmem_slot + 1);
+    const bool prof = P.prof != nullptr;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < P.S; ++s) {
             tc::mbar_init(&full[s], 1);
             tc::mbar_init(&empty[s], 1);
         }
-        tc::mbar_init(tfull, 1);
-        tc::mbar_init(tempty, 8);
+        for (int b = 0; b < 2; ++b) {
+            tc::mbar_init(&tfull[b], 1);
+            tc::mbar_init(&tempty[b], 8);
+        }
         *abort = 0;
         tc::fence_barrier_init();
     }
@@ -118,7 +141,7 @@ __global__ void __launch_bounds__(kOzThreads, 1)
         reinterpret_cast<uint4 *>(smem)[i] = make_uint4(0, 0, 0, 0);
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     if (warp == 1) {
-        tc::tmem_alloc(tmem_slot, P.tmem_cols);
+        tc::tmem_alloc(tmem_slot, P.tmem_cols * P.nbuf);
         tc::tmem_relinquish();
     }
     tc::tc_fence_before();
@@ -129,6 +152,8 @@ __global__ void __launch_bounds__(kOzThreads, 1)
     if (warp == 0) {
         // ---------------- producer ----------------
         uint32_t it = 0;
+        unsigned long long w_empty = 0;
+        uint32_t stage = 0, ph = 0;  // ring position of step `it`
         for (uint32_t t = blockIdx.x; t < n_tiles && !*abort; t += gridDim.x) {
             const uint32_t s0 = tiles[t].s0, ns = tiles[t].ns;
             for (uint32_t k = 0; k < ns; ++k, ++it) {
@@ -138,88 +163,144 @@ __global__ void __launch_bounds__(kOzThreads, 1)
                     if (k + lane < ns) sstep[lane] = steps[s0 + k + lane];
                     __syncwarp();
                 }
-                const uint32_t stage = it % P.S, ph = (it / P.S) & 1u;
                 // one lane waits, the warp follows its verdict (keeps the warp converged)
                 int okw = 1;
-                if (lane == 0) okw = tc::mbar_wait(&empty[stage], ph ^ 1u, abort) ? 1 : 0;
+                if (lane == 0) {
+                    const long long c0 = prof ? clock64() : 0;
+                    okw = tc::mbar_wait_sleep(&empty[stage], ph ^ 1u, abort) ? 1 : 0;
+                    if (prof) w_empty += clock64() - c0;
+                }
                 if (!__shfl_sync(0xffffffffu, okw, 0)) break;
                 const OzStep st = sstep[k & 31u];
                 uint8_t *sA = smem + (size_t)stage * stage_bytes;
                 uint8_t *sB = sA + a_stage;
                 if (lane == 0) tc::mbar_arrive_expect_tx(&full[stage], P.tx_bytes);
                 __syncwarp();
-                if (lane < P.R) {
-                    const uint32_t ai = st.a[lane];
-                    for (int i = 0; i < P.nd; ++i) {
-                        const bf16 *src = (ai == kOzNone) ? P.zero : a_img + ((size_t)ai * P.nd + i) * a_plane_elems;
-                        tc::bulk_g2s(sA + i * a_plane + lane * slot_bytes, src, slot_bytes, &full[stage]);
-                    }
+                // slots whose images are consecutive in a_img (or all zero) go
+                // in one copy: a fully live step is one A copy and one B copy
+                const uint32_t ai = lane < P.R ? st.a[lane] : kOzNone;
+                const uint32_t prev = __shfl_up_sync(0xffffffffu, ai, 1);
+                const bool live = ai != kOzNone;
+                const bool joins = lane > 0 && (live ? (prev != kOzNone && prev + 1u == ai) : prev == kOzNone);
+                const uint32_t starts = __ballot_sync(0xffffffffu, lane < P.R && !joins) | (1u << P.R);
+                if (lane < P.R && !joins) {
+                    const int len = __ffs(starts & ~((2u << lane) - 1u)) - 1 - lane;
+                    const bf16 *src = live ? a_img + (size_t)ai * slot_elems : P.zero;
+                    tc::bulk_g2s(sA + lane * slot_bytes, src, (uint32_t)len * slot_bytes, &full[stage]);
                 }
-                if (lane == 31) tc::bulk_g2s(sB, b_img + (size_t)st.b * b_img_elems, b_stage, &full[stage]);
+                if (lane == 31) tc::bulk_g2s(sB, b_img + (size_t)st.b * b_img_elems, b_copy, &full[stage]);
+                if (++stage == (uint32_t)P.S) {
+                    stage = 0;
+                    ph ^= 1u;
+                }
             }
         }
         // let the copies in flight land before the CTA can exit
         if (lane == 0) {
             const uint32_t first = it > (uint32_t)P.S ? it - P.S : 0;
             for (uint32_t j = first; j < it; ++j) tc::mbar_wait(&full[j % P.S], (j / P.S) & 1u, abort);
+            if (prof) atomicAdd(&P.prof[kProfProdWaitEmpty], w_empty);
         }
         __syncwarp();
     } else if (warp == 1) {
         // ---------------- MMA issuer ----------------
         if (lane == 0) {
-            uint32_t it = 0, ch = 0;
-            const uint32_t sbo = (uint32_t)P.kp * 16u;  // bytes between 8-row core-matrix groups
+            const long long t_start = prof ? clock64() : 0;
+            unsigned long long w_full = 0, w_tmem = 0;
+            uint32_t it = 0, ch = 0, stage = 0, ph = 0;
+            // MMA plan of one k16 slice, computed once: per A digit i, D_i x
+            // [E_j0 .. E_j1) stacked along N (N <= 256, rounded up to 16: the
+            // extra 8 columns land past the last region) into TMEM region i + j0.
+            // Entry: x = TMEM column | (i == 0) << 16, y / z = A / B descriptor
+            // address offsets (16-byte units), w = instruction descriptor.
+            // 8-row groups: nd*kp*16 bytes apart on the M side (digits interleaved), kp*16 on the N side
+            const uint64_t a_desc0 = tc::smem_desc(tc::smem_u32(smem), 128u, (uint32_t)P.nd * P.kp * 16u);
+            const uint64_t b_desc0 = tc::smem_desc(tc::smem_u32(smem + a_stage), 128u, (uint32_t)P.kp * 16u);
+            constexpr int kMaxPlanes = 256 / NP;  // B planes one MMA can take
+            constexpr int kMaxPlan = kOzMaxDigits * ((kOzMaxDigits + kMaxPlanes - 1) / kMaxPlanes);
+            uint32_t pd[kMaxPlan], pa[kMaxPlan], pb[kMaxPlan], pi[kMaxPlan];  // kept in registers (unrolled)
+            int n_plan = 0;
+#pragma unroll
+            for (int e = 0; e < kMaxPlan; ++e) pd[e] = pa[e] = pb[e] = pi[e] = 0;
+            for (int i = 0; i < P.nd; ++i)
+                for (int j0 = 0; j0 < P.nd - i; j0 += kMaxPlanes) {
+                    const int j1 = min(P.nd - i, j0 + kMaxPlanes);
+#pragma unroll
+                    for (int e = 0; e < kMaxPlan; ++e)
+                        if (e == n_plan) {
+                            pd[e] = (uint32_t)((i + j0) * NP) | (i == 0 ? 1u << 16 : 0u);
+                            pa[e] = ((uint32_t)i * P.kp * 16u) >> 4;
+                            pb[e] = ((uint32_t)j0 * NP * P.kp * 2u) >> 4;
+                            pi[e] = tc::idesc_bf16_f32(128u, (uint32_t)(((j1 - j0) * NP + 15) & ~15));
+                        }
+                    ++n_plan;
+                }
+            const uint32_t nq = (uint32_t)P.kp / 16u;
             bool ok = true;
             for (uint32_t t = blockIdx.x; t < n_tiles && ok; t += gridDim.x) {
                 const uint32_t ns = tiles[t].ns;
                 const uint32_t nch = (ns + P.F - 1) / P.F;
                 for (uint32_t c = 0; c < nch && ok; ++c, ++ch) {
-                    if (!tc::mbar_wait(tempty, (ch & 1u) ^ 1u, abort)) {
+                    const uint32_t buf = P.nbuf == 2 ? (ch & 1u) : 0u, use = P.nbuf == 2 ? ch >> 1 : ch;
+                    long long c0 = prof ? clock64() : 0;
+                    if (!tc::mbar_wait(&tempty[buf], (use & 1u) ^ 1u, abort)) {
                         ok = false;
                         break;
                     }
+                    if (prof) w_tmem += clock64() - c0;
                     tc::tc_fence_after();
+                    const uint32_t dbase = tmem + buf * P.tmem_cols;
                     const uint32_t kend = min(ns, (c + 1) * (uint32_t)P.F);
                     for (uint32_t k = c * P.F; k < kend; ++k, ++it) {
-                        const uint32_t stage = it % P.S, ph = (it / P.S) & 1u;
+                        c0 = prof ? clock64() : 0;
                         if (!tc::mbar_wait(&full[stage], ph, abort)) {
                             ok = false;
                             break;
                         }
+                        if (prof) w_full += clock64() - c0;
                         tc::tc_fence_after();
-                        const uint32_t aA = tc::smem_u32(smem + (size_t)stage * stage_bytes);
-                        const uint32_t aB = aA + a_stage;
-                        constexpr int kMaxPlanes = 256 / NP;  // B planes one MMA can take (N <= 256)
-                        for (int q = 0; q < P.kp / 16; ++q) {
-                            for (int i = 0; i < P.nd; ++i) {
-                                const uint64_t ad = tc::smem_desc(aA + i * a_plane + q * 256u, 128u, sbo);
-                                // first MMA into every TMEM region of a chain overwrites it
-                                const uint32_t acc = (k == c * P.F && q == 0 && i == 0) ? 0u : 1u;
-                                for (int j0 = 0; j0 < P.nd - i; j0 += kMaxPlanes) {
-                                    const int j1 = min(P.nd - i, j0 + kMaxPlanes);
-                                    const uint64_t bd =
-                                        tc::smem_desc(aB + (uint32_t)j0 * NP * P.kp * 2u + q * 256u, 128u, sbo);
-                                    const uint32_t id = tc::idesc_bf16_f32(128u, (uint32_t)(j1 - j0) * NP);
-                                    tc::mma_bf16(tmem + (uint32_t)((i + j0) * NP), ad, bd, id, acc);
-                                }
-                            }
+                        const uint64_t a0 = a_desc0 + stage * (stage_bytes >> 4);
+                        const uint64_t b0 = b_desc0 + stage * (stage_bytes >> 4);
+                        // the first MMA of a chain (digit 0, which spans every TMEM
+                        // region) overwrites the accumulator
+                        uint32_t first = (k == c * P.F) ? 1u : 0u;
+                        for (uint32_t q = 0; q < nq; ++q) {
+                            const uint64_t aq = a0 + q * 16u, bq = b0 + q * 16u;
+#pragma unroll
+                            for (int e = 0; e < kMaxPlan; ++e)
+                                if (e < n_plan)
+                                    tc::mma_bf16(dbase + (pd[e] & 0xFFFFu), aq + pa[e], bq + pb[e], pi[e],
+                                                 (first & (pd[e] >> 16)) ? 0u : 1u);
+                            first = 0;
                         }
                         tc::mma_commit(&empty[stage]);
+                        if (++stage == (uint32_t)P.S) {
+                            stage = 0;
+                            ph ^= 1u;
+                        }
                     }
                     if (!ok) break;
-                    tc::mma_commit(tfull);
+                    tc::mma_commit(&tfull[buf]);
                 }
+            }
+            if (prof) {
+                atomicAdd(&P.prof[kProfMmaWaitFull], w_full);
+                atomicAdd(&P.prof[kProfMmaWaitTmem], w_tmem);
+                atomicAdd(&P.prof[kProfMmaTotal], (unsigned long long)(clock64() - t_start));
+                atomicAdd(&P.prof[kProfSteps], (unsigned long long)it);
             }
         }
         __syncwarp();
     } else {
         // ---------------- epilogue ----------------
-        constexpr int NPH = NP / 2;  // columns per epilogue group
+        constexpr int NPH = NP / 2;                   // columns per epilogue group
+        constexpr int CH = (NPH % 8 == 0) ? 8 : 4;  // TMEM columns per load
         const int q = warp & 3;
         const int grp = (warp - 2) >> 2;
         const int cbase = grp * NPH;
         const int m = q * 32 + lane;
-        const uint32_t lane_addr = tmem + ((uint32_t)(q * 32) << 16);
+        const uint32_t lane_off = (uint32_t)(q * 32) << 16;
+        unsigned long long w_full = 0, t_drain = 0, t_store = 0;
         uint32_t ch = 0;
         bool ok = true;
         for (uint32_t t = blockIdx.x; t < n_tiles && ok; t += gridDim.x) {
@@ -234,70 +315,92 @@ __global__ void __launch_bounds__(kOzThreads, 1)
                 lo[c] = 0.f;
             }
             for (uint32_t c = 0; c < nch; ++c, ++ch) {
-                if (!tc::mbar_wait(tfull, ch & 1u, abort)) {
+                const uint32_t buf = P.nbuf == 2 ? (ch & 1u) : 0u, use = P.nbuf == 2 ? ch >> 1 : ch;
+                long long c0 = prof ? clock64() : 0;
+                if (!tc::mbar_wait_sleep(&tfull[buf], use & 1u, abort)) {
                     ok = false;
                     break;
                 }
                 tc::tc_fence_after();
+                long long c1 = prof ? clock64() : 0;
+                if (prof) w_full += c1 - c0;
+                const uint32_t lane_addr = tmem + buf * P.tmem_cols + lane_off;
 #pragma unroll
-                for (int c0 = 0; c0 < NPH; c0 += 8) {
-                    float v0[8], v1[8], v2[8];
-                    tc::tmem_ld8(lane_addr + (uint32_t)(cbase + c0), v0);
-                    tc::tmem_ld8(lane_addr + (uint32_t)(NP + cbase + c0), v1);
-                    if (P.nd > 2) tc::tmem_ld8(lane_addr + (uint32_t)(2 * NP + cbase + c0), v2);
+                for (int c0 = 0; c0 < NPH; c0 += CH) {
+                    float v0[CH], v1[CH], v2[CH];
+                    tc::tmem_ldn<CH>(lane_addr + (uint32_t)(cbase + c0), v0);
+                    tc::tmem_ldn<CH>(lane_addr + (uint32_t)(NP + cbase + c0), v1);
+                    if (P.nd > 2) tc::tmem_ldn<CH>(lane_addr + (uint32_t)(2 * NP + cbase + c0), v2);
                     tc::tmem_wait_ld();
                     // R0 is an integer < 2^24 and R1 a multiple of 2^-8 below 2^16: both
                     // exact in the FP32 accumulator.  R2 is a multiple of 2^-16 and exact
                     // while its partial sums stay below 2^8 (else rounded once here).
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) {
+                    for (int j = 0; j < CH; ++j) {
                         long long h = ((long long)__float2int_rn(v0[j]) << 16) +
                                       ((long long)__float2int_rn(v1[j] * 256.f) << 8);
                         if (P.nd > 2) h += (long long)__float2int_rn(v2[j] * 65536.f);
                         hi[c0 + j] += h;
                     }
                     for (int w = 3; w < P.nd; ++w) {
-                        float v[8];
-                        tc::tmem_ld8(lane_addr + (uint32_t)(w * NP + cbase + c0), v);
+                        float v[CH];
+                        tc::tmem_ldn<CH>(lane_addr + (uint32_t)(w * NP + cbase + c0), v);
                         tc::tmem_wait_ld();
 #pragma unroll
-                        for (int j = 0; j < 8; ++j) lo[c0 + j] += v[j];
+                        for (int j = 0; j < CH; ++j) lo[c0 + j] += v[j];
                     }
                 }
                 tc::tc_fence_before();
                 __syncwarp();
-                if (lane == 0) tc::mbar_arrive(tempty);
+                if (lane == 0) tc::mbar_arrive(&tempty[buf]);
+                if (prof) t_drain += clock64() - c1;
             }
             if (!ok) break;
+            const long long c2 = prof ? clock64() : 0;
             const int s = m / P.mp, r = m % P.mp;
             if (s < P.R && T.c[s] != nullptr && r < T.rows[s]) {
-                const double rs = ldexp(1.0, T.rexp[s][r] - 14);
+                // value = alpha * (hi 2^-16 + lo) 2^(e_row + f_col - 14), formed as
+                // (hi + lo 2^16) 2^(e_row + f_col - 30): the same rounding (scaling
+                // by powers of two is exact), the power of two built from its bits
+                const int er = T.rexp[s][r] - 30;
                 double *cp = T.c[s];
                 const int ldc = T.ldc[s];
                 const bool fresh = (T.fresh_mask >> s) & 1u;
+                const bool unit = P.alpha == 1.0;
 #pragma unroll
                 for (int j = 0; j < NPH; ++j) {
                     const int c = cbase + j;
                     if (c < T.cols) {
-                        const double tot = (double)hi[j] * (1.0 / 65536.0) + (double)lo[j];
-                        const double out = P.alpha * (tot * (rs * ldexp(1.0, T.cexp[c])));
-                        double *dst = cp + r + (size_t)c * ldc;
-                        *dst = fresh ? out : *dst + out;
+                        const double tot = __dadd_rn((double)hi[j], (double)(lo[j] * 65536.f));
+                        const int e = er + T.cexp[c];
+                        const double sc = (e >= -1022 && e <= 1023) ? __longlong_as_double((long long)(e + 1023) << 52)
+                                                                    : ldexp(1.0, e);
+                        double out = __dmul_rn(tot, sc);
+                        if (!unit) out = __dmul_rn(P.alpha, out);
+                        double *dst = T.trans ? cp + c + (size_t)r * ldc : cp + r + (size_t)c * ldc;
+                        *dst = fresh ? out : __dadd_rn(*dst, out);
                     }
                 }
                 if (fresh && r == 0 && grp == 0 && T.cnorm[s]) *T.cnorm[s] = 0.0;
             }
+            if (prof) t_store += clock64() - c2;
+        }
+        if (prof && lane == 0) {
+            atomicAdd(&P.prof[kProfEpiWaitFull], w_full);
+            atomicAdd(&P.prof[kProfEpiDrain], t_drain);
+            atomicAdd(&P.prof[kProfEpiStore], t_store);
         }
     }
     tc::tc_fence_before();
     __syncthreads();
-    if (warp == 1) tc::tmem_dealloc(tmem, P.tmem_cols);
+    if (warp == 1) tc::tmem_dealloc(tmem, P.tmem_cols * P.nbuf);
     if (threadIdx.x == 0 && *abort) atomicExch(err, 1);
 }
 
 template <int NP>
 static void launch_oz(bsg_ctx ctx, const OzShape &sh, const OzTile *tiles, size_t n_tiles, const OzStep *steps,
-                      const bf16 *a_img, const bf16 *b_img, double alpha, int *err, cudaStream_t s) {
+                      const bf16 *a_img, const bf16 *b_img, double alpha, int *err, unsigned long long *prof,
+                      cudaStream_t s) {
     OzKParams P;
     P.mp = sh.mp;
     P.kp = sh.kp;
@@ -305,15 +408,18 @@ static void launch_oz(bsg_ctx ctx, const OzShape &sh, const OzTile *tiles, size_
     P.nd = sh.nd;
     P.F = sh.F;
     P.alpha = alpha;
+    P.prof = prof;
     P.zero = static_cast<const bf16 *>(oz_zero_image());
     const uint32_t stage_bytes = oz_stage_bytes(sh);
     P.S = (int)std::min<uint32_t>(4, kOzSmemBudget / stage_bytes);
     BSG_REQUIRE(P.S >= 2, BSG_ERR_UNSUPPORTED, "Ozaki tile does not fit shared memory");
-    uint32_t cols = 32;
-    while (cols < (uint32_t)sh.nd * NP) cols <<= 1;
+    uint32_t cols = 32;  // regions plus the <= 8 overrun columns of a rounded-up N
+    while (cols < (uint32_t)sh.nd * NP + 8u) cols <<= 1;
     P.tmem_cols = cols;
+    P.nbuf = cols <= 256 ? 2 : 1;
     P.tx_bytes = (uint32_t)sh.R * sh.nd * sh.mp * sh.kp * 2u + (uint32_t)sh.nd * NP * sh.kp * 2u;
-    const size_t smem = (size_t)P.S * stage_bytes + 32 * sizeof(OzStep) + (2 * P.S + 2) * 8 + 16;
+    BSG_REQUIRE(cols <= 512, BSG_ERR_UNSUPPORTED, "Ozaki form: digits x padded block columns exceed TMEM");
+    const size_t smem = (size_t)P.S * stage_bytes + 32 * sizeof(OzStep) + (2 * P.S + 4) * 8 + 16;
     BSG_CUDA(cudaFuncSetAttribute(k_ozgemm<NP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const unsigned grid = (unsigned)std::min<size_t>(n_tiles, (size_t)ctx->sm_count);
     k_ozgemm<NP><<<grid, kOzThreads, smem, s>>>(tiles, (uint32_t)n_tiles, steps, a_img, b_img, P, err);
@@ -324,39 +430,57 @@ static void launch_oz(bsg_ctx ctx, const OzShape &sh, const OzTile *tiles, size_
 void oz_run(bsg_ctx ctx, const OzShape &sh, const OzTile *d_tiles, size_t n_tiles, const OzStep *d_steps,
             const bf16 *a_img, const bf16 *b_img, double alpha, cudaStream_t s, const unsigned long long *d_macs) {
     if (!n_tiles) return;
-    BSG_REQUIRE(sh.nd >= 2 && sh.nd <= kOzMaxDigits && sh.nd * sh.np <= 512, BSG_ERR_UNSUPPORTED,
-                "Ozaki form: 2..8 digits, digits x padded block columns <= 512");
-    DevBuf err(4, s);
-    BSG_CUDA(cudaMemsetAsync(err.p, 0, 4, s));
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
-    if (ctx->timing) {
-        BSG_CUDA(cudaEventCreate(&e0));
-        BSG_CUDA(cudaEventCreate(&e1));
-        BSG_CUDA(cudaEventRecord(e0, s));
+    BSG_REQUIRE(sh.nd >= 2 && sh.nd <= kOzMaxDigits && sh.nd * sh.np + 8 <= 512, BSG_ERR_UNSUPPORTED,
+                "Ozaki form: 2..8 digits, digits x padded block columns < 512");
+    int *err = ctx->gemm_err_flag();
+    if (!ctx->timing) {
+        // no synchronization: the flag is read once at the end of the public call
+        switch (sh.np) {
+            case 8: launch_oz<8>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, nullptr, s); break;
+            case 16: launch_oz<16>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, nullptr, s); break;
+            case 24: launch_oz<24>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, nullptr, s); break;
+            case 32: launch_oz<32>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, nullptr, s); break;
+            case 40: launch_oz<40>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, nullptr, s); break;
+            case 48: launch_oz<48>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, nullptr, s); break;
+            case 56: launch_oz<56>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, nullptr, s); break;
+            case 64: launch_oz<64>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, nullptr, s); break;
+            default: throw Error{BSG_ERR_UNSUPPORTED, "Ozaki form supports block sizes up to 64"};
+        }
+        return;
     }
+    // timing mode: CUDA events around the launch, stall counters, read back at once
+    DevBuf profbuf(8 * kOzProf, s);
+    BSG_CUDA(cudaMemsetAsync(profbuf.p, 0, 8 * kOzProf, s));
+    auto *prof = profbuf.as<unsigned long long>();
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    BSG_CUDA(cudaEventCreate(&e0));
+    BSG_CUDA(cudaEventCreate(&e1));
+    BSG_CUDA(cudaEventRecord(e0, s));
     switch (sh.np) {
-        case 16: launch_oz<16>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err.as<int>(), s); break;
-        case 32: launch_oz<32>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err.as<int>(), s); break;
-        case 48: launch_oz<48>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err.as<int>(), s); break;
-        case 64: launch_oz<64>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err.as<int>(), s); break;
+        case 8: launch_oz<8>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, prof, s); break;
+        case 16: launch_oz<16>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, prof, s); break;
+        case 24: launch_oz<24>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, prof, s); break;
+        case 32: launch_oz<32>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, prof, s); break;
+        case 40: launch_oz<40>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, prof, s); break;
+        case 48: launch_oz<48>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, prof, s); break;
+        case 56: launch_oz<56>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, prof, s); break;
+        case 64: launch_oz<64>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, prof, s); break;
         default: throw Error{BSG_ERR_UNSUPPORTED, "Ozaki form supports block sizes up to 64"};
     }
-    if (ctx->timing) BSG_CUDA(cudaEventRecord(e1, s));
-    int h = 0;
-    unsigned long long macs = 0;
-    BSG_CUDA(cudaMemcpyAsync(&h, err.p, 4, cudaMemcpyDeviceToHost, s));
-    if (ctx->timing && d_macs) BSG_CUDA(cudaMemcpyAsync(&macs, d_macs, 8, cudaMemcpyDeviceToHost, s));
+    BSG_CUDA(cudaEventRecord(e1, s));
+    unsigned long long macs = 0, st[kOzProf] = {};
+    if (d_macs) BSG_CUDA(cudaMemcpyAsync(&macs, d_macs, 8, cudaMemcpyDeviceToHost, s));
+    BSG_CUDA(cudaMemcpyAsync(st, prof, sizeof(st), cudaMemcpyDeviceToHost, s));
     BSG_CUDA(cudaStreamSynchronize(s));
-    if (ctx->timing) {
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, e0, e1);
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
-        ctx->oz_ms += ms;
-        ctx->oz_launches += 1;
-        ctx->oz_useful_macs += (double)macs;
-    }
-    BSG_REQUIRE(!h, BSG_ERR_TIMEOUT, "Ozaki GEMM: a pipeline wait timed out");
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ctx->oz_ms += ms;
+    ctx->oz_launches += 1;
+    ctx->oz_useful_macs += (double)macs;
+    for (int i = 0; i < kOzProf && i < 8; ++i) ctx->oz_stall[i] += st[i];
+    ctx->gemm_check();
 }
 
 // ---------------------------------------------------------------------------
@@ -423,7 +547,7 @@ __global__ void k_img_opA(double *const *__restrict__ tab, size_t a_nrb, int tA,
     const int rows = ext_of(ib, g.ibs, g.ni), k = ext_of(kb, g.kbs, g.nk);
     // op(A)(r, l): stored block column-major (rows x k, or k x rows when transposed)
     oz_block_image(blk, tA ? k : rows, tA != 0, rows, k, rexp + ib * g.ibs, mp, kp, nd,
-                   img + b * nd * (size_t)mp * kp);
+                   img + b * nd * (size_t)mp * kp, true);
 }
 
 // digit image of op(B) block (kb, jb) stored at table index b, as np rows
@@ -438,7 +562,7 @@ __global__ void k_img_opB(double *const *__restrict__ tab, size_t b_nrb, int tB,
     const int cols = ext_of(jb, g.jbs, g.nj), k = ext_of(kb, g.kbs, g.nk);
     // image row n, k l = op(B)(l, n): stored (k x cols) -> src[l + n*k]; transposed (cols x k) -> src[n + l*cols]
     oz_block_image(blk, tB ? cols : k, tB == 0, cols, k, cexp + jb * g.jbs, np, kp, nd,
-                   img + b * nd * (size_t)np * kp);
+                   img + b * nd * (size_t)np * kp, false);
 }
 
 // steps of every tile: k blocks where the B block exists and at least one
@@ -568,6 +692,7 @@ void ozaki_screened(bsg_ctx ctx, bsg_bsm C, bsg_bsm A, bsg_bsm B, const ScreenGe
     ctx->check_launch("ozaki steps");
     oz_run(ctx, sh, dt.as<OzTile>(), tiles.size(), dst.as<OzStep>(), aimg.as<bf16>(), bimg.as<bf16>(), alpha, s,
            dmacs.as<unsigned long long>());
+    ctx->gemm_check();
 }
 
 void ozaki_grouped_gemm(bsg_ctx, const std::vector<GemmItem> &, const GemmItem *, const GemmPair *, uint64_t, int, int,

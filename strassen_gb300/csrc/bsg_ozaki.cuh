@@ -26,9 +26,9 @@ constexpr uint32_t kOzNone = 0xFFFFFFFFu;
 
 // Padded tile geometry for one block size.
 struct OzShape {
-    int mp;  // rows per slot (block rows rounded up to 16; 24 and 48 kept)
+    int mp;  // rows per slot (block rows rounded up to 8)
     int kp;  // k per step (block k rounded up to 16)
-    int np;  // output columns (block cols rounded up to 16)
+    int np;  // output columns (block cols rounded up to 8)
     int R;   // slots per 128-row tile
     int nd;  // digits per operand
     int F;   // steps per exact chain (512 / kp)
@@ -45,6 +45,7 @@ struct OzTile {
     int rows[kOzMaxSlots];
     int ldc[kOzMaxSlots];          // leading dimension of each output block
     int cols;
+    int trans;                     // 1: slot rows are output columns, tile columns output rows
     uint32_t fresh_mask;           // slot s overwrites C (bit set) or adds to it
     uint32_t s0, ns;               // step range
 };
@@ -90,10 +91,21 @@ __device__ __forceinline__ int oz_exp_of_bits(long long mb) {
 }
 __device__ __forceinline__ int oz_exp_of(double mx) { return oz_exp_of_bits(oz_absbits(mx)); }
 
-// element offset of (row r, k l) inside one digit plane of an image with kp
-// columns: core matrices of 8x8, row groups outer, k groups inner
-__device__ __forceinline__ int oz_img_off(int r, int l, int kp) {
-    return (((r >> 3) * (kp >> 3) + (l >> 3)) << 6) + ((r & 7) << 3) + (l & 7);
+// Digit-image layouts (UMMA K-major canonical form without swizzle: core
+// matrices of 8 rows x 16 bytes, the kp/8 core matrices of an 8-row group
+// adjacent along k).
+//  N side (B operand): digit planes one after another, each mpad rows
+//    (8-row groups kp*8 elements apart) -- a block's planes stack along N.
+//  M side (A operand): digits interleaved per 8-row group (group g holds
+//    digit 0..nd-1 of its 8 rows, kp*8 elements each), so that a block's full
+//    image is one contiguous run and consecutive blocks of a tile's slots
+//    are one contiguous run too; digit i is then addressed at offset
+//    i*kp*8 with an 8-row-group stride of nd*kp*8.
+__device__ __forceinline__ size_t oz_rg_stride(bool m_side, int nd, int kp) {
+    return m_side ? (size_t)nd * kp * 8 : (size_t)kp * 8;
+}
+__device__ __forceinline__ size_t oz_plane_stride(bool m_side, int mpad, int kp) {
+    return m_side ? (size_t)kp * 8 : (size_t)mpad * kp;
 }
 
 // Fixed-point split of v with row/column exponent e into nd balanced base-256
@@ -136,13 +148,14 @@ __device__ __forceinline__ void oz_split(double v, int e, int nd, int (&d)[kOzMa
 }
 
 // Digit image of one block, 8 consecutive k per thread and one 16-byte store
-// per digit plane.  A role: image row r = block row, value src[r + l*ld];
-// B role: image row r = output column, value src[l + r*ld].  exps[r] is the
-// scale exponent of image row r; rows >= `rows` and k >= `k` are zero.
+// per digit plane.  b_role false: image row r = block row, value
+// src[r + l*ld]; true: image row r = output column, value src[l + r*ld].
+// exps[r] is the scale exponent of image row r; rows >= `rows` and k >= `k`
+// are zero.  m_side selects the layout (M side of the MMA, or N side).
 __device__ __forceinline__ void oz_block_image(const double *__restrict__ src, size_t ld, bool b_role, int rows,
                                                int k, const int *__restrict__ exps, int mpad, int kp, int nd,
-                                               __nv_bfloat16 *__restrict__ dst) {
-    const size_t plane = (size_t)mpad * kp;
+                                               __nv_bfloat16 *__restrict__ dst, bool m_side) {
+    const size_t plane = oz_plane_stride(m_side, mpad, kp), rgs = oz_rg_stride(m_side, nd, kp);
     const int hk = kp >> 3;
     for (int idx = threadIdx.x; idx < mpad * hk; idx += blockDim.x) {
         const int r = idx % mpad, h = idx / mpad;
@@ -155,7 +168,7 @@ __device__ __forceinline__ void oz_block_image(const double *__restrict__ src, s
             if (r < rows && l < k) v = b_role ? src[l + (size_t)r * ld] : src[r + (size_t)l * ld];
             oz_split(v, e, nd, dig[j]);
         }
-        const size_t off = (size_t)oz_img_off(r, h * 8, kp);
+        const size_t off = (size_t)(r >> 3) * rgs + (size_t)h * 64 + (size_t)(r & 7) * 8;
 #pragma unroll
         for (int i = 0; i < kOzMaxDigits; ++i) {
             if (i < nd) {

@@ -124,21 +124,21 @@ __global__ void k_img_U(const double *__restrict__ U, const uint8_t *__restrict_
     const size_t p = x / (D.nb * D.nb), a = x % D.nb, b = (x / D.nb) % D.nb;
     oz_block_image(U + p * D.n_bf * D.n_bf + a * D.bs + b * D.bs * D.n_bf, D.n_bf, false, ext_r(a, D.bs, D.n_bf),
                 ext_r(b, D.bs, D.n_bf), rexp + p * D.n_bf + a * D.bs, D.mp, D.kp, D.nd,
-                img + x * D.nd * (size_t)D.mp * D.kp);
+                img + x * D.nd * (size_t)D.mp * D.kp, true);
 }
 
 // C blocks (b, j) in the B role of mui = U C; index b + j*nb
 __global__ void k_img_C_B(const double *__restrict__ C, const int *__restrict__ cexp, OzDims D, bf16 *__restrict__ img) {
     const size_t x = blockIdx.x, b = x % D.nb, j = x / D.nb;
     oz_block_image(C + b * D.bs + j * D.bs * D.n_bf, D.n_bf, true, ext_r(j, D.bs, D.n_occ), ext_r(b, D.bs, D.n_bf),
-                cexp + j * D.bs, D.np, D.kp, D.nd, img + x * D.nd * (size_t)D.np * D.kp);
+                cexp + j * D.bs, D.np, D.kp, D.nd, img + x * D.nd * (size_t)D.np * D.kp, false);
 }
 
 // C^T blocks (ib, a) in the A role of ij = C^T mui; index ib + a*nob
 __global__ void k_img_Ct_A(const double *__restrict__ C, const int *__restrict__ cexp, OzDims D, bf16 *__restrict__ img) {
     const size_t x = blockIdx.x, ib = x % D.nob, a = x / D.nob;
     oz_block_image(C + a * D.bs + ib * D.bs * D.n_bf, D.n_bf, true, ext_r(ib, D.bs, D.n_occ), ext_r(a, D.bs, D.n_bf),
-                cexp + ib * D.bs, D.mp, D.kp, D.nd, img + x * D.nd * (size_t)D.mp * D.kp);
+                cexp + ib * D.bs, D.mp, D.kp, D.nd, img + x * D.nd * (size_t)D.mp * D.kp, true);
 }
 
 // mui_p blocks (a, jb) in the B role of ij; index p*nb*nob + a + jb*nb
@@ -149,7 +149,7 @@ __global__ void k_img_mui_B(const double *__restrict__ mui, const uint8_t *__res
     const size_t p = x / (D.nb * D.nob), a = x % D.nb, jb = (x / D.nb) % D.nob;
     oz_block_image(mui + p * D.n_bf * D.n_occ + a * D.bs + jb * D.bs * D.n_bf, D.n_bf, true, ext_r(jb, D.bs, D.n_occ),
                 ext_r(a, D.bs, D.n_bf), cexp + p * D.n_occ + jb * D.bs, D.np, D.kp, D.nd,
-                img + x * D.nd * (size_t)D.np * D.kp);
+                img + x * D.nd * (size_t)D.np * D.kp, false);
 }
 
 // mui_p blocks (a, ib) in the A role of K += mui ijs; index p*nb*nob + a + ib*nb
@@ -160,7 +160,7 @@ __global__ void k_img_mui_A(const double *__restrict__ mui, const uint8_t *__res
     const size_t p = x / (D.nb * D.nob), a = x % D.nb, ib = (x / D.nb) % D.nob;
     oz_block_image(mui + p * D.n_bf * D.n_occ + a * D.bs + ib * D.bs * D.n_bf, D.n_bf, false, ext_r(a, D.bs, D.n_bf),
                 ext_r(ib, D.bs, D.n_occ), rexp + (p / Q) * D.n_bf + a * D.bs, D.mp, D.kp, D.nd,
-                img + x * D.nd * (size_t)D.mp * D.kp);
+                img + x * D.nd * (size_t)D.mp * D.kp, true);
 }
 
 // ijs_p blocks (ib, jb) in the B role of the K product; index p*nob*nob + ib + jb*nob
@@ -171,7 +171,7 @@ __global__ void k_img_ijs_B(const double *__restrict__ ijs, const uint8_t *__res
     const size_t p = x / (D.nob * D.nob), ib = x % D.nob, jb = (x / D.nob) % D.nob;
     oz_block_image(ijs + p * D.n_occ * D.n_occ + ib * D.bs + jb * D.bs * D.n_occ, D.n_occ, true, ext_r(jb, D.bs, D.n_occ),
                 ext_r(ib, D.bs, D.n_occ), cexp + (p / Q) * D.n_occ + jb * D.bs, D.np, D.kp, D.nd,
-                img + x * D.nd * (size_t)D.np * D.kp);
+                img + x * D.nd * (size_t)D.np * D.kp, false);
 }
 
 // ---- tiles and steps (one thread per tile) ----
@@ -211,6 +211,7 @@ __global__ void k_tiles_mui(const uint8_t *__restrict__ uflag, const double *__r
         T.rexp[s] = rexp_U + p * D.n_bf + a * D.bs;
     }
     T.cols = ext_r(j, D.bs, D.n_occ);
+    T.trans = 0;
     T.cexp = cexp_C + j * D.bs;
     T.s0 = (uint32_t)(t * D.nb);
     uint32_t n = 0;
@@ -268,6 +269,7 @@ __global__ void k_tiles_ij(const uint8_t *__restrict__ mflag, const double *__re
         T.rexp[s] = cexp_C + ib * D.bs;
     }
     T.cols = ext_r(jb, D.bs, D.n_occ);
+    T.trans = 0;
     T.cexp = cexp_mui + p * D.n_occ + jb * D.bs;
     T.s0 = (uint32_t)(t * D.nb);
     uint32_t n = 0;
@@ -326,6 +328,7 @@ __global__ void k_tiles_K(const uint8_t *__restrict__ mflag, const double *__res
         T.rexp[s] = rexp_sub + sub * D.n_bf + a * D.bs;
     }
     T.cols = ext_r(jb, D.bs, D.n_occ);
+    T.trans = 0;
     T.cexp = cexp_sub + sub * D.n_occ + jb * D.bs;
     T.s0 = (uint32_t)(t * Q * D.nob);
     uint32_t n = 0;
@@ -501,6 +504,7 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, uint64_t stats[5]) {
         ctx->note_launch();
         ctx->check_launch("rik ozaki K reduce");
     }
+    ctx->gemm_check();
     if (stats) {
         unsigned long long h[5];
         BSG_CUDA(cudaMemcpyAsync(h, cnt, 5 * 8, cudaMemcpyDeviceToHost, s));

@@ -59,6 +59,24 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volati
     return true;
 }
 
+// The same with a sleep between polls, for roles whose wait is not on the
+// critical path (keeps their issue slots free for the MMA-issuing warp).
+__device__ __forceinline__ bool mbar_wait_sleep(uint64_t *bar, uint32_t parity, volatile int *abort) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = globaltimer();
+    uint32_t ns = 32;
+    while (!mbar_try_wait(bar, parity)) {
+        if (*abort) return false;
+        if (globaltimer() - t0 > kWaitNs) {
+            *abort = 1;
+            return false;
+        }
+        __nanosleep(ns);
+        ns = ns < 256 ? ns * 2 : ns;
+    }
+    return true;
+}
+
 // global -> shared bulk copy (16-byte aligned, size a multiple of 16),
 // completing `bytes` of transaction count on the mbarrier
 __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
@@ -142,6 +160,22 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
                  : "memory");
 #pragma unroll
     for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+// 4 consecutive 32-bit columns of this thread's TMEM lane
+__device__ __forceinline__ void tmem_ld4(uint32_t taddr, float (&v)[4]) {
+    uint32_t r[4];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(taddr)
+                 : "memory");
+#pragma unroll
+    for (int i = 0; i < 4; ++i) v[i] = __uint_as_float(r[i]);
+}
+template <int N>
+__device__ __forceinline__ void tmem_ldn(uint32_t taddr, float (&v)[N]) {
+    static_assert(N == 4 || N == 8, "4 or 8 columns");
+    if constexpr (N == 8) tmem_ld8(taddr, v);
+    else tmem_ld4(taddr, v);
 }
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
