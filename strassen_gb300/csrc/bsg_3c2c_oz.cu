@@ -79,7 +79,9 @@ struct Dense3c {
 
 // N-side images of X blocks (ib, kb): image row = output row, index ib + kb*nib
 __global__ void k_img_X(const double *__restrict__ X, const int *__restrict__ rexp, Dense3c D, bf16 *__restrict__ img) {
-    const size_t x = blockIdx.x, ib = x % D.nib, kb = x / D.nib;
+    const size_t x = oz_warp_id();
+    if (x >= D.nib * D.nkb) return;
+    const size_t ib = x % D.nib, kb = x / D.nib;
     oz_block_image(X + ib * D.bs + kb * D.bs * D.n_vec2, D.n_vec2, false, ext3(ib, D.bs, D.n_vec2),
                    ext3(kb, D.bs, D.n_aux), rexp + ib * D.bs, D.np, D.kp, D.nd, img + x * D.nd * (size_t)D.np * D.kp, false);
 }
@@ -87,7 +89,9 @@ __global__ void k_img_X(const double *__restrict__ X, const int *__restrict__ re
 // M-side images of V^T blocks (jb, kb): image row = output column, index
 // jb + kb*njb (a tile's slots are consecutive images)
 __global__ void k_img_V(const double *__restrict__ V, const int *__restrict__ cexp, Dense3c D, bf16 *__restrict__ img) {
-    const size_t x = blockIdx.x, jb = x % D.njb, kb = x / D.njb;
+    const size_t x = oz_warp_id();
+    if (x >= D.nkb * D.njb) return;
+    const size_t jb = x % D.njb, kb = x / D.njb;
     oz_block_image(V + kb * D.bs + jb * D.bs * D.n_aux, D.n_aux, true, ext3(jb, D.bs, D.n_aux), ext3(kb, D.bs, D.n_aux),
                    cexp + jb * D.bs, D.mp, D.kp, D.nd, img + x * D.nd * (size_t)D.mp * D.kp, true);
 }
@@ -178,8 +182,8 @@ void transform_3c2c_ozaki(bsg_ctx ctx, size_t n_vec2, size_t n_aux, const double
                                                                               D.nkb * D.njb, vn.as<double>());
     k_rowexp_dense<<<(unsigned)ceil_div(n_vec2, 256), 256, 0, s>>>(X, n_vec2, n_aux, rexp.as<int>());
     k_colexp_dense<<<(unsigned)n_aux, 256, 0, s>>>(V, n_aux, cexp.as<int>());
-    k_img_X<<<(unsigned)(D.nib * D.nkb), 128, 0, s>>>(X, rexp.as<int>(), D, bi.as<bf16>());
-    k_img_V<<<(unsigned)(D.nkb * D.njb), 128, 0, s>>>(V, cexp.as<int>(), D, ai.as<bf16>());
+    k_img_X<<<oz_img_grid(D.nib * D.nkb), 32 * kOzImgWarps, 0, s>>>(X, rexp.as<int>(), D, bi.as<bf16>());
+    k_img_V<<<oz_img_grid(D.nkb * D.njb), 32 * kOzImgWarps, 0, s>>>(V, cexp.as<int>(), D, ai.as<bf16>());
     ctx->note_launch(6);
     ctx->check_launch("3c2c ozaki prep");
     const size_t n_jg = ceil_div(D.njb, (size_t)D.R), n_tiles = D.nib * n_jg;

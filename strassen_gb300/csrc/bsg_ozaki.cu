@@ -538,8 +538,9 @@ __global__ void k_colexp_opB(double *const *__restrict__ tab, size_t b_nrb, int 
 // digit image of op(A) block (ib, kb) stored at table index b (rows x k,
 // padded to mp x kp)
 __global__ void k_img_opA(double *const *__restrict__ tab, size_t a_nrb, int tA, ScreenGeom g,
-                          const int *__restrict__ rexp, int mp, int kp, int nd, bf16 *__restrict__ img) {
-    const size_t b = blockIdx.x;
+                          const int *__restrict__ rexp, int mp, int kp, int nd, bf16 *__restrict__ img, size_t n) {
+    const size_t b = oz_warp_id();
+    if (b >= n) return;
     const double *blk = tab[b];
     if (!blk) return;
     const size_t sr = b % a_nrb, sc = b / a_nrb;
@@ -553,8 +554,9 @@ __global__ void k_img_opA(double *const *__restrict__ tab, size_t a_nrb, int tA,
 // digit image of op(B) block (kb, jb) stored at table index b, as np rows
 // (output columns) x kp
 __global__ void k_img_opB(double *const *__restrict__ tab, size_t b_nrb, int tB, ScreenGeom g,
-                          const int *__restrict__ cexp, int np, int kp, int nd, bf16 *__restrict__ img) {
-    const size_t b = blockIdx.x;
+                          const int *__restrict__ cexp, int np, int kp, int nd, bf16 *__restrict__ img, size_t n) {
+    const size_t b = oz_warp_id();
+    if (b >= n) return;
     const double *blk = tab[b];
     if (!blk) return;
     const size_t sr = b % b_nrb, sc = b / b_nrb;
@@ -619,10 +621,10 @@ void ozaki_screened(bsg_ctx ctx, bsg_bsm C, bsg_bsm A, bsg_bsm B, const ScreenGe
     ctx->note_launch(2);
     const size_t a_plane = (size_t)sh.mp * sh.kp, b_plane = (size_t)sh.np * sh.kp;
     DevBuf aimg(A->nblocks() * nd * a_plane * 2, s), bimg(B->nblocks() * nd * b_plane * 2, s);
-    k_img_opA<<<(unsigned)A->nblocks(), 256, 0, s>>>(A->dptr, A->nrb, g.tA, g, rexp.as<int>(), sh.mp, sh.kp, nd,
-                                                    aimg.as<bf16>());
-    k_img_opB<<<(unsigned)B->nblocks(), 256, 0, s>>>(B->dptr, B->nrb, g.tB, g, cexp.as<int>(), sh.np, sh.kp, nd,
-                                                    bimg.as<bf16>());
+    k_img_opA<<<oz_img_grid(A->nblocks()), 32 * kOzImgWarps, 0, s>>>(A->dptr, A->nrb, g.tA, g, rexp.as<int>(), sh.mp,
+                                                                     sh.kp, nd, aimg.as<bf16>(), A->nblocks());
+    k_img_opB<<<oz_img_grid(B->nblocks()), 32 * kOzImgWarps, 0, s>>>(B->dptr, B->nrb, g.tB, g, cexp.as<int>(), sh.np,
+                                                                     sh.kp, nd, bimg.as<bf16>(), B->nblocks());
     ctx->note_launch(2);
     ctx->check_launch("ozaki split");
     // tiles: up to R consecutive output blocks of one block column

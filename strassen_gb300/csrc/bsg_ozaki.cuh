@@ -2,17 +2,19 @@
 //
 // Every FP64 operand row of A (column of B) is scaled by a power of two 2^e
 // (max |x| < 2^e) and split into nd bf16 "digits":
-//   x * 2^(7-e) = D1 + D2 + D3 + D4,  D1 = d1, D2 = d2 2^-8, D3 = d3 2^-16, ...
-// with integers |d| <= 128 (7 + 8 + 8 + 8 bits).  A digit product D_i E_j is
-// then an integer multiple of 2^-8(i+j-2) bounded by 2^14 2^-8(i+j-2), so a
-// fp32 tensor-core accumulation of the weight-2 products (D1 E1) is exact up
-// to K = 1024 and of the weight-3 products (D1 E2 + D2 E1) up to K = 512;
-// lower weights carry < 2^-16 of the result and round harmlessly.  Products
-// of equal weight share one TMEM region; one MMA per A digit covers all its
-// partners at once: D_i x [E_1 .. E_{nd+1-i}] stacked along N.  Chains of at
-// most 512 k are flushed to FP64 registers, scaled by 2^(e_r + f_c - 14) and
-// summed.  With nd = 4 the representation error is below 2^-31 of each
-// row/column maximum.
+//   x * 2^(7-e) = D0 + D1 + D2 + ...,  D0 = d0, D1 = d1 2^-8, D2 = d2 2^-16, ...
+// with integers |d| <= 128 (7 + 8 + 8 + ... bits).  A digit product D_i E_j
+// is then an integer multiple of 2^-8(i+j) bounded by 2^14 2^-8(i+j), so a
+// fp32 tensor-core accumulation of the weight-0 products (D0 E0) is exact up
+// to K = 1024 and of the weight-1 products (D0 E1 + D1 E0) up to K = 512;
+// weight 2 is exact while its partial sums stay below 2^8, and lower weights
+// carry < 2^-24 of the result.  Products of equal weight share one TMEM
+// region; one MMA per A digit covers all its partners at once: D_i x
+// [E_0 .. E_{nd-1-i}] stacked along N.  Chains of at most 512 k are drained
+// into an int64 (weights 0-2) and an FP32 (lower weights) accumulator and
+// combined in FP64 once per tile, scaled by 2^(e_r + f_c - 14).  With nd
+// digits the representation error is below 2^-(8 nd - 1) of each row/column
+// maximum.
 #pragma once
 #include <cuda_bf16.h>
 
@@ -108,17 +110,13 @@ __device__ __forceinline__ size_t oz_plane_stride(bool m_side, int mpad, int kp)
     return m_side ? (size_t)kp * 8 : (size_t)mpad * kp;
 }
 
-// Fixed-point split of v with row/column exponent e into nd balanced base-256
-// digits, integer arithmetic only: N = round(v 2^(7 + 8(nd-1) - e)) (ties to
-// even), then d_{nd-1}, ..., d_1 from the low end and d_0 = the rest
-// (|d_i| <= 128).  Digit i is stored as d_i 2^(-8i).
-__device__ __forceinline__ void oz_split(double v, int e, int nd, int (&d)[kOzMaxDigits]) {
+// Fixed-point value of v with row/column exponent e, integer arithmetic only:
+// N = round(v 2^(K - e)) with ties to even (|N| <= 2^K).
+__device__ __forceinline__ long long oz_fixed(double v, int e, int K) {
     const long long bits = __double_as_longlong(v);
     const int E = (int)((bits >> 52) & 0x7FF);
-    long long M = (bits & 0xFFFFFFFFFFFFFll) | (E ? (1ll << 52) : 0ll);
-    const int Eb = E ? E : 1;
-    const int K = 7 + 8 * (nd - 1);
-    const int sh = Eb - 1075 + K - e;  // N = M * 2^sh
+    const long long M = (bits & 0xFFFFFFFFFFFFFll) | (E ? (1ll << 52) : 0ll);
+    const int sh = (E ? E : 1) - 1075 + K - e;  // N = M * 2^sh
     long long N;
     if (M == 0) {
         N = 0;
@@ -133,53 +131,97 @@ __device__ __forceinline__ void oz_split(double v, int e, int nd, int (&d)[kOzMa
             N = q + ((rem > half || (rem == half && (q & 1))) ? 1 : 0);
         }
     }
-    if (bits < 0) N = -N;
-#pragma unroll
-    for (int i = kOzMaxDigits - 1; i >= 1; --i) {
-        if (i < nd) {
-            const long long di = ((N + 128) & 255) - 128;
-            d[i] = (int)di;
-            N = (N - di) >> 8;
-        } else {
-            d[i] = 0;
-        }
-    }
-    d[0] = (int)N;
+    return bits < 0 ? -N : N;
 }
 
-// Digit image of one block, 8 consecutive k per thread and one 16-byte store
-// per digit plane.  b_role false: image row r = block row, value
-// src[r + l*ld]; true: image row r = output column, value src[l + r*ld].
-// exps[r] is the scale exponent of image row r; rows >= `rows` and k >= `k`
-// are zero.  m_side selects the layout (M side of the MMA, or N side).
-__device__ __forceinline__ void oz_block_image(const double *__restrict__ src, size_t ld, bool b_role, int rows,
-                                               int k, const int *__restrict__ exps, int mpad, int kp, int nd,
-                                               __nv_bfloat16 *__restrict__ dst, bool m_side) {
+// Split into nd balanced base-256 digits: N = d_0 256^(nd-1) + ... + d_{nd-1}
+// with d_1.. in [-128, 127] and d_0 in [-128, 128], K = 7 + 8(nd-1).  Adding
+// 128 to each of the nd-1 low bytes (the constant 0x80..80) makes them plain
+// bytes of T = N + C (d_i = byte - 128) and leaves d_0 = T >> 8(nd-1).
+struct OzDigits {
+    long long T;
+    int lowb;  // 8 (nd - 1)
+    __device__ __forceinline__ OzDigits(double v, int e, int nd) {
+        lowb = 8 * (nd - 1);
+        const long long C = nd > 1 ? (long long)(0x8080808080808080ull >> (64 - lowb)) : 0;
+        T = oz_fixed(v, e, 7 + lowb) + C;
+        neg = v < 0;
+    }
+    bool neg;
+    __device__ __forceinline__ int digit(int i) const {
+        if (i == 0) {
+            const int d0 = (int)(T >> lowb);
+            return (d0 < 0 && !neg) ? d0 + 256 : d0;  // nd = 8: N = +2^63 wraps
+        }
+        return (int)((T >> (lowb - 8 * i)) & 255) - 128;
+    }
+};
+
+// bf16 bits of d 2^(-8i) for an integer |d| <= 128 (exact; built from the
+// float bits of d with the exponent lowered by 8i)
+__device__ __forceinline__ uint32_t oz_digit_bf16(int d, int i) {
+    if (!d) return 0u;
+    return (__float_as_uint((float)d) - ((uint32_t)(8 * i) << 23)) >> 16;
+}
+
+// Digit image of one block from a value source get(r, l) (image row r, k l),
+// 8 consecutive k per item and one 16-byte store per digit plane; items are
+// spread over threads tid, tid + nthr, ...  exps[r] is the scale exponent of
+// image row r; rows >= `rows` and k >= `k` are zero.  m_side selects the
+// layout (M side of the MMA, or N side).
+template <class Get>
+__device__ __forceinline__ void oz_block_image_g(const Get &get, int rows, int k, const int *__restrict__ exps, int mpad,
+                                                 int kp, int nd, __nv_bfloat16 *__restrict__ dst, bool m_side, int tid,
+                                                 int nthr) {
     const size_t plane = oz_plane_stride(m_side, mpad, kp), rgs = oz_rg_stride(m_side, nd, kp);
     const int hk = kp >> 3;
-    for (int idx = threadIdx.x; idx < mpad * hk; idx += blockDim.x) {
+    for (int idx = tid; idx < mpad * hk; idx += nthr) {
         const int r = idx % mpad, h = idx / mpad;
-        const int e = r < rows ? exps[r] : 0;
-        int dig[8][kOzMaxDigits];
+        const size_t off = (size_t)(r >> 3) * rgs + (size_t)h * 64 + (size_t)(r & 7) * 8;
+        if (r >= rows || h * 8 >= k) {  // padding: all digits zero
+            for (int i = 0; i < nd; ++i) *reinterpret_cast<uint4 *>(dst + i * plane + off) = make_uint4(0, 0, 0, 0);
+            continue;
+        }
+        const int e = exps[r];
+        uint32_t w[kOzMaxDigits][4];
+#pragma unroll
+        for (int i = 0; i < kOzMaxDigits; ++i) w[i][0] = w[i][1] = w[i][2] = w[i][3] = 0u;
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
             const int l = h * 8 + j;
-            double v = 0.0;
-            if (r < rows && l < k) v = b_role ? src[l + (size_t)r * ld] : src[r + (size_t)l * ld];
-            oz_split(v, e, nd, dig[j]);
-        }
-        const size_t off = (size_t)(r >> 3) * rgs + (size_t)h * 64 + (size_t)(r & 7) * 8;
+            const OzDigits D(l < k ? get(r, l) : 0.0, e, nd);
 #pragma unroll
-        for (int i = 0; i < kOzMaxDigits; ++i) {
-            if (i < nd) {
-                const float sc = __int_as_float((127 - 8 * i) << 23);  // 2^(-8i)
-                __align__(16) __nv_bfloat16 w[8];
-#pragma unroll
-                for (int j = 0; j < 8; ++j) w[j] = __float2bfloat16_rn((float)dig[j][i] * sc);
-                *reinterpret_cast<uint4 *>(dst + i * plane + off) = *reinterpret_cast<const uint4 *>(w);
-            }
+            for (int i = 0; i < kOzMaxDigits; ++i)
+                if (i < nd) w[i][j >> 1] |= oz_digit_bf16(D.digit(i), i) << (16 * (j & 1));
         }
+#pragma unroll
+        for (int i = 0; i < kOzMaxDigits; ++i)
+            if (i < nd)
+                *reinterpret_cast<uint4 *>(dst + i * plane + off) = make_uint4(w[i][0], w[i][1], w[i][2], w[i][3]);
     }
 }
+
+// value source of a column-major block: b_role false: src[r + l*ld] (image
+// row = block row); true: src[l + r*ld] (image row = block column)
+struct OzDenseGet {
+    const double *src;
+    size_t ld;
+    bool b_role;
+    __device__ __forceinline__ double operator()(int r, int l) const {
+        return b_role ? src[l + (size_t)r * ld] : src[r + (size_t)l * ld];
+    }
+};
+
+// Digit image of one column-major block, built by one warp.
+__device__ __forceinline__ void oz_block_image(const double *__restrict__ src, size_t ld, bool b_role, int rows,
+                                               int k, const int *__restrict__ exps, int mpad, int kp, int nd,
+                                               __nv_bfloat16 *__restrict__ dst, bool m_side) {
+    oz_block_image_g(OzDenseGet{src, ld, b_role}, rows, k, exps, mpad, kp, nd, dst, m_side, threadIdx.x & 31, 32);
+}
+
+// one warp per item: global warp index and a guard for launches of 8 warps per CTA
+constexpr int kOzImgWarps = 8;
+__device__ __forceinline__ size_t oz_warp_id() { return (size_t)blockIdx.x * kOzImgWarps + (threadIdx.x >> 5); }
+inline unsigned oz_img_grid(size_t n) { return (unsigned)((n + kOzImgWarps - 1) / kOzImgWarps); }
 
 }  // namespace bsg

@@ -30,18 +30,94 @@ __device__ __forceinline__ int ext_r(size_t blk, size_t bs, size_t n) {
 
 // ---- scale exponents ----
 
-// U_p rows over present blocks; grid (p, a), one thread per row
-__global__ void k_rexp_U(const double *__restrict__ U, const uint8_t *__restrict__ uflag, size_t n_bf, size_t bs,
-                         size_t nb, int *__restrict__ rexp) {
+// ---- U_p straight from the compressed integrals ----
+// The reference rebuilds a dense n_bf x n_bf U_P for every aux function from
+// the significant-pair storage (decompress_integrals, occ_ri_k_step.cpp:
+// 133-146) and then blocks and screens it (:102-104).  Here the dense U is
+// never formed: an inverse key map gives, for every (mu, nu), the index v of
+// its compressed entry (or none), and the block norms, row exponents and
+// digit images gather U_P(mu, nu) = ints[v, P] from column P.
+
+// inv[key] = the last v carrying that key (the reference's sequential scatter
+// keeps the last write), -1 where no entry exists; occ[a + b*nb] = 1 for the
+// blocks of U that hold any entry (the others are zero for every P)
+__global__ void k_key_inverse(const uint64_t *__restrict__ keys, size_t n_vec2, size_t n_bf, size_t bs, size_t nb,
+                              int *__restrict__ inv, uint8_t *__restrict__ occ) {
+    const size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n_vec2) return;
+    const uint64_t key = keys[v];
+    atomicMax(&inv[key], (int)v);
+    occ[(key % n_bf) / bs + (key / n_bf) / bs * nb] = 1;
+}
+
+// U_P(r0 + r, c0 + l) from column P of the compressed integrals
+struct UGet {
+    const int *inv;
+    const double *col;
+    size_t n_bf, r0, c0;
+    __device__ __forceinline__ double operator()(int r, int l) const {
+        const int v = inv[(r0 + r) + (c0 + l) * n_bf];
+        return v >= 0 ? col[v] : 0.0;
+    }
+};
+
+// block norms and keep flags of U_p, one warp per (p, a, b); the elements are
+// visited in the order of the dense block norm (lane-strided column-major),
+// so the result is bit-identical to it
+__global__ void k_unorms_c(const double *__restrict__ ints, const int *__restrict__ inv, const uint8_t *__restrict__ occ,
+                           size_t n_vec2, size_t P0, size_t n_bf, size_t bs, size_t nb, size_t n_p, double tpb,
+                           double *__restrict__ norm, uint8_t *__restrict__ flag) {
+    const size_t x = oz_warp_id();
+    if (x >= n_p * nb * nb) return;
+    const size_t p = x / (nb * nb), rr = x % (nb * nb), a = rr % nb, b = rr / nb;
+    if (!occ[rr]) {  // no entry: the dense block is zero, its norm 0 (< tpb)
+        if ((threadIdx.x & 31) == 0) {
+            norm[x] = 0.0;
+            flag[x] = !(0.0 < tpb);
+        }
+        return;
+    }
+    const int rs = ext_r(a, bs, n_bf), cs = ext_r(b, bs, n_bf);
+    const UGet get{inv, ints + (P0 + p) * n_vec2, n_bf, a * bs, b * bs};
+    const int lane = threadIdx.x & 31, n = rs * cs;
+    double acc = 0.0;
+    for (int i0 = lane; i0 < n; i0 += 32 * 8) {
+        double v[8];  // eight independent gathers in flight, then the chain in the same order
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int i = i0 + 32 * u;
+            v[u] = i < n ? get(i % rs, i / rs) : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+            if (i0 + 32 * u < n) acc = fma(v[u], v[u], acc);
+    }
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) acc = __dadd_rn(acc, __shfl_down_sync(0xffffffffu, acc, o));
+    if (lane == 0) {
+        const double est = sqrt(acc);
+        norm[x] = est;
+        flag[x] = !(est < tpb);
+    }
+}
+
+// U_p row exponents over present blocks; grid (p, a), one thread per row
+__global__ void k_rexp_U_c(const double *__restrict__ ints, const int *__restrict__ inv, size_t n_vec2, size_t P0,
+                           const uint8_t *__restrict__ uflag, size_t n_bf, size_t bs, size_t nb, int *__restrict__ rexp) {
     const size_t p = blockIdx.x / nb, a = blockIdx.x % nb;
     const int r = threadIdx.x, rows = ext_r(a, bs, n_bf);
     if (r >= rows) return;
-    const double *Up = U + p * n_bf * n_bf;
+    const double *col = ints + (P0 + p) * n_vec2;
     long long mx = 0;
     for (size_t b = 0; b < nb; ++b) {
         if (!uflag[p * nb * nb + a + b * nb]) continue;
         const int k = ext_r(b, bs, n_bf);
-        for (int l = 0; l < k; ++l) { const long long bb_ = oz_absbits(Up[a * bs + r + (b * bs + l) * n_bf]); mx = bb_ > mx ? bb_ : mx; }
+        for (int l = 0; l < k; ++l) {
+            const int v = inv[a * bs + r + (b * bs + l) * n_bf];
+            if (v < 0) continue;
+            const long long bb_ = oz_absbits(col[v]);
+            mx = bb_ > mx ? bb_ : mx;
+        }
     }
     rexp[p * n_bf + a * bs + r] = oz_exp_of_bits(mx);
 }
@@ -116,36 +192,42 @@ struct OzDims {
     int mp, kp, np, nd, R;
 };
 
-// U_p blocks (A role); grid (p, a, b), image index p*nb*nb + a + b*nb
-__global__ void k_img_U(const double *__restrict__ U, const uint8_t *__restrict__ uflag, const int *__restrict__ rexp,
-                        OzDims D, bf16 *__restrict__ img) {
-    const size_t x = blockIdx.x;
-    if (!uflag[x]) return;
+// U_p blocks (M side), gathered from the compressed integrals; one warp per
+// (p, a, b), image index p*nb*nb + a + b*nb
+__global__ void k_img_U(const double *__restrict__ ints, const int *__restrict__ inv, size_t n_vec2, size_t P0,
+                        const uint8_t *__restrict__ uflag, const int *__restrict__ rexp, OzDims D, size_t n,
+                        bf16 *__restrict__ img) {
+    const size_t x = oz_warp_id();
+    if (x >= n || !uflag[x]) return;
     const size_t p = x / (D.nb * D.nb), a = x % D.nb, b = (x / D.nb) % D.nb;
-    oz_block_image(U + p * D.n_bf * D.n_bf + a * D.bs + b * D.bs * D.n_bf, D.n_bf, false, ext_r(a, D.bs, D.n_bf),
-                ext_r(b, D.bs, D.n_bf), rexp + p * D.n_bf + a * D.bs, D.mp, D.kp, D.nd,
-                img + x * D.nd * (size_t)D.mp * D.kp, true);
+    const UGet get{inv, ints + (P0 + p) * n_vec2, D.n_bf, a * D.bs, b * D.bs};
+    oz_block_image_g(get, ext_r(a, D.bs, D.n_bf), ext_r(b, D.bs, D.n_bf), rexp + p * D.n_bf + a * D.bs, D.mp, D.kp,
+                     D.nd, img + x * D.nd * (size_t)D.mp * D.kp, true, threadIdx.x & 31, 32);
 }
 
 // C blocks (b, j) in the B role of mui = U C; index b + j*nb
 __global__ void k_img_C_B(const double *__restrict__ C, const int *__restrict__ cexp, OzDims D, bf16 *__restrict__ img) {
-    const size_t x = blockIdx.x, b = x % D.nb, j = x / D.nb;
+    const size_t x = oz_warp_id();
+    if (x >= D.nb * D.nob) return;
+    const size_t b = x % D.nb, j = x / D.nb;
     oz_block_image(C + b * D.bs + j * D.bs * D.n_bf, D.n_bf, true, ext_r(j, D.bs, D.n_occ), ext_r(b, D.bs, D.n_bf),
                 cexp + j * D.bs, D.np, D.kp, D.nd, img + x * D.nd * (size_t)D.np * D.kp, false);
 }
 
 // C^T blocks (ib, a) in the A role of ij = C^T mui; index ib + a*nob
 __global__ void k_img_Ct_A(const double *__restrict__ C, const int *__restrict__ cexp, OzDims D, bf16 *__restrict__ img) {
-    const size_t x = blockIdx.x, ib = x % D.nob, a = x / D.nob;
+    const size_t x = oz_warp_id();
+    if (x >= D.nob * D.nb) return;
+    const size_t ib = x % D.nob, a = x / D.nob;
     oz_block_image(C + a * D.bs + ib * D.bs * D.n_bf, D.n_bf, true, ext_r(ib, D.bs, D.n_occ), ext_r(a, D.bs, D.n_bf),
                 cexp + ib * D.bs, D.mp, D.kp, D.nd, img + x * D.nd * (size_t)D.mp * D.kp, true);
 }
 
 // mui_p blocks (a, jb) in the B role of ij; index p*nb*nob + a + jb*nb
 __global__ void k_img_mui_B(const double *__restrict__ mui, const uint8_t *__restrict__ mflag,
-                            const int *__restrict__ cexp, OzDims D, bf16 *__restrict__ img) {
-    const size_t x = blockIdx.x;
-    if (!mflag[x]) return;
+                            const int *__restrict__ cexp, OzDims D, size_t n, bf16 *__restrict__ img) {
+    const size_t x = oz_warp_id();
+    if (x >= n || !mflag[x]) return;
     const size_t p = x / (D.nb * D.nob), a = x % D.nb, jb = (x / D.nb) % D.nob;
     oz_block_image(mui + p * D.n_bf * D.n_occ + a * D.bs + jb * D.bs * D.n_bf, D.n_bf, true, ext_r(jb, D.bs, D.n_occ),
                 ext_r(a, D.bs, D.n_bf), cexp + p * D.n_occ + jb * D.bs, D.np, D.kp, D.nd,
@@ -154,9 +236,9 @@ __global__ void k_img_mui_B(const double *__restrict__ mui, const uint8_t *__res
 
 // mui_p blocks (a, ib) in the A role of K += mui ijs; index p*nb*nob + a + ib*nb
 __global__ void k_img_mui_A(const double *__restrict__ mui, const uint8_t *__restrict__ mflag,
-                            const int *__restrict__ rexp, size_t Q, OzDims D, bf16 *__restrict__ img) {
-    const size_t x = blockIdx.x;
-    if (!mflag[x]) return;
+                            const int *__restrict__ rexp, size_t Q, OzDims D, size_t n, bf16 *__restrict__ img) {
+    const size_t x = oz_warp_id();
+    if (x >= n || !mflag[x]) return;
     const size_t p = x / (D.nb * D.nob), a = x % D.nb, ib = (x / D.nb) % D.nob;
     oz_block_image(mui + p * D.n_bf * D.n_occ + a * D.bs + ib * D.bs * D.n_bf, D.n_bf, false, ext_r(a, D.bs, D.n_bf),
                 ext_r(ib, D.bs, D.n_occ), rexp + (p / Q) * D.n_bf + a * D.bs, D.mp, D.kp, D.nd,
@@ -165,9 +247,9 @@ __global__ void k_img_mui_A(const double *__restrict__ mui, const uint8_t *__res
 
 // ijs_p blocks (ib, jb) in the B role of the K product; index p*nob*nob + ib + jb*nob
 __global__ void k_img_ijs_B(const double *__restrict__ ijs, const uint8_t *__restrict__ sflag,
-                            const int *__restrict__ cexp, size_t Q, OzDims D, bf16 *__restrict__ img) {
-    const size_t x = blockIdx.x;
-    if (!sflag[x]) return;
+                            const int *__restrict__ cexp, size_t Q, OzDims D, size_t n, bf16 *__restrict__ img) {
+    const size_t x = oz_warp_id();
+    if (x >= n || !sflag[x]) return;
     const size_t p = x / (D.nob * D.nob), ib = x % D.nob, jb = (x / D.nob) % D.nob;
     oz_block_image(ijs + p * D.n_occ * D.n_occ + ib * D.bs + jb * D.bs * D.n_occ, D.n_occ, true, ext_r(jb, D.bs, D.n_occ),
                 ext_r(ib, D.bs, D.n_occ), cexp + (p / Q) * D.n_occ + jb * D.bs, D.np, D.kp, D.nd,
@@ -405,7 +487,7 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, uint64_t stats[5]) {
     const size_t nb = D.nb, nob = D.nob;
     const size_t a_img = (size_t)nd * sh.mp * sh.kp, b_img = (size_t)nd * sh.np * sh.kp;  // elements per image
     // bytes per aux function of every per-chunk buffer
-    const size_t per_p = n_bf * n_bf * 8 + nb * nb * 9 + nb * nb * a_img * 2 + n_bf * n_occ * 8 + nb * nob * 9 +
+    const size_t per_p = nb * nb * 9 + nb * nb * a_img * 2 + n_bf * n_occ * 8 + nb * nob * 9 +
                          nb * nob * (a_img + b_img) * 2 + 3 * n_occ * n_occ * 8 + 3 * nob * nob * 9 +
                          nob * nob * b_img * 2;
     size_t pc = d.p_chunk ? d.p_chunk : std::max<size_t>(1, (size_t)(8ull << 30) / per_p);
@@ -413,7 +495,7 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, uint64_t stats[5]) {
     const size_t Q = 8;  // aux functions per K-product tile
     const size_t n_sub_max = ceil_div(pc, Q);
 
-    DevBuf dU(pc * n_bf * n_bf * 8, s), dun(pc * nb * nb * 8, s), duf(pc * nb * nb, s);
+    DevBuf dinv(n_bf * n_bf * 4, s), docc(nb * nb, s), dun(pc * nb * nb * 8, s), duf(pc * nb * nb, s);
     DevBuf dmui(pc * n_bf * n_occ * 8, s), dmn(pc * nb * nob * 8, s), dmf(pc * nb * nob, s);
     DevBuf dij(pc * n_occ * n_occ * 8, s), dijf(pc * nob * nob, s);
     DevBuf dijs(pc * n_occ * n_occ * 8, s), dsn(pc * nob * nob * 8, s), dsf(pc * nob * nob, s);
@@ -439,26 +521,31 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, uint64_t stats[5]) {
     const int wpb = 8;
     k_cnorms<<<(unsigned)ceil_div(nb * nob, wpb), wpb * 32, 0, s>>>(d.c_occ, n_bf, n_occ, bs, nb, nob, dcn.as<double>());
     k_cexp_C<<<(unsigned)nob, tb, 0, s>>>(d.c_occ, n_bf, n_occ, bs, dcexpC.as<int>());
-    k_img_C_B<<<(unsigned)(nb * nob), 256, 0, s>>>(d.c_occ, dcexpC.as<int>(), D, dimgCB.as<bf16>());
-    k_img_Ct_A<<<(unsigned)(nob * nb), 256, 0, s>>>(d.c_occ, dcexpC.as<int>(), D, dimgCtA.as<bf16>());
-    ctx->note_launch(4);
+    k_img_C_B<<<oz_img_grid(nb * nob), 32 * kOzImgWarps, 0, s>>>(d.c_occ, dcexpC.as<int>(), D, dimgCB.as<bf16>());
+    k_img_Ct_A<<<oz_img_grid(nob * nb), 32 * kOzImgWarps, 0, s>>>(d.c_occ, dcexpC.as<int>(), D, dimgCtA.as<bf16>());
+    // inverse key map of the compressed integrals (replaces the per-P dense rebuild)
+    BSG_CUDA(cudaMemsetAsync(dinv.p, 0xFF, n_bf * n_bf * 4, s));
+    BSG_CUDA(cudaMemsetAsync(docc.p, 0, nb * nb, s));
+    if (d.n_vec2)
+        k_key_inverse<<<(unsigned)ceil_div(d.n_vec2, 256), 256, 0, s>>>(d.keys, d.n_vec2, n_bf, bs, nb, dinv.as<int>(),
+                                                                        docc.as<uint8_t>());
+    ctx->note_launch(5);
     const double tpb_u = 1e-20 * (double)(bs * bs);
     const double tpb = d.thresh * (double)(bs * bs * bs);
     for (size_t P0 = 0; P0 < n_aux; P0 += pc) {
         const size_t np = std::min(pc, n_aux - P0), n_sub = ceil_div(np, Q);
         BSG_CUDA(cudaMemsetAsync(macs, 0, 3 * 8, s));
-        BSG_CUDA(cudaMemsetAsync(dU.p, 0, np * n_bf * n_bf * 8, s));
-        if (d.n_vec2) {
-            dim3 g((unsigned)ceil_div(d.n_vec2, 256), (unsigned)np);
-            k_scatter<<<g, 256, 0, s>>>(d.ints, d.keys, d.n_vec2, P0, n_bf * n_bf, dU.as<double>());
-            ctx->note_launch();
-        }
-        k_unorms<<<(unsigned)ceil_div(np * nb * nb, wpb), wpb * 32, 0, s>>>(dU.as<double>(), n_bf, bs, nb, np, tpb_u,
-                                                                            dun.as<double>(), duf.as<uint8_t>());
+        // U_p block norms, keep flags, row exponents and digit images, all
+        // gathered from the compressed integrals
+        k_unorms_c<<<oz_img_grid(np * nb * nb), 32 * kOzImgWarps, 0, s>>>(
+            d.ints, dinv.as<int>(), docc.as<uint8_t>(), d.n_vec2, P0, n_bf, bs, nb, np, tpb_u, dun.as<double>(),
+            duf.as<uint8_t>());
         // mui = U C
-        k_rexp_U<<<(unsigned)(np * nb), tb, 0, s>>>(dU.as<double>(), duf.as<uint8_t>(), n_bf, bs, nb, drexpU.as<int>());
-        k_img_U<<<(unsigned)(np * nb * nb), 256, 0, s>>>(dU.as<double>(), duf.as<uint8_t>(), drexpU.as<int>(), D,
-                                                        dimgU.as<bf16>());
+        k_rexp_U_c<<<(unsigned)(np * nb), tb, 0, s>>>(d.ints, dinv.as<int>(), d.n_vec2, P0, duf.as<uint8_t>(), n_bf, bs,
+                                                      nb, drexpU.as<int>());
+        k_img_U<<<oz_img_grid(np * nb * nb), 32 * kOzImgWarps, 0, s>>>(d.ints, dinv.as<int>(), d.n_vec2, P0,
+                                                                       duf.as<uint8_t>(), drexpU.as<int>(), D,
+                                                                       np * nb * nb, dimgU.as<bf16>());
         const size_t tm = np * nob * ng_a;
         k_tiles_mui<<<(unsigned)ceil_div(tm, 128), 128, 0, s>>>(
             duf.as<uint8_t>(), dun.as<double>(), dcn.as<double>(), drexpU.as<int>(), dcexpC.as<int>(),
@@ -471,8 +558,8 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, uint64_t stats[5]) {
         // ij = C^T mui
         k_cexp_mui<<<(unsigned)(np * nob), tb, 0, s>>>(dmui.as<double>(), dmf.as<uint8_t>(), n_bf, n_occ, bs, nb, nob,
                                                        dcexpM.as<int>());
-        k_img_mui_B<<<(unsigned)(np * nb * nob), 256, 0, s>>>(dmui.as<double>(), dmf.as<uint8_t>(), dcexpM.as<int>(), D,
-                                                              dimgMB.as<bf16>());
+        k_img_mui_B<<<oz_img_grid(np * nb * nob), 32 * kOzImgWarps, 0, s>>>(
+            dmui.as<double>(), dmf.as<uint8_t>(), dcexpM.as<int>(), D, np * nb * nob, dimgMB.as<bf16>());
         const size_t ti = np * nob * ng_i;
         k_tiles_ij<<<(unsigned)ceil_div(ti, 128), 128, 0, s>>>(
             dmf.as<uint8_t>(), dmn.as<double>(), dcn.as<double>(), dcexpC.as<int>(), dcexpM.as<int>(),
@@ -488,10 +575,10 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, uint64_t stats[5]) {
                                                              nob, np, Q, drexpMs.as<int>());
         k_cexp_ijs_sub<<<(unsigned)(n_sub * nob), tb, 0, s>>>(dijs.as<double>(), dsf.as<uint8_t>(), n_occ, bs, nob, np,
                                                               Q, dcexpSs.as<int>());
-        k_img_mui_A<<<(unsigned)(np * nb * nob), 256, 0, s>>>(dmui.as<double>(), dmf.as<uint8_t>(), drexpMs.as<int>(), Q,
-                                                              D, dimgMA.as<bf16>());
-        k_img_ijs_B<<<(unsigned)(np * nob * nob), 256, 0, s>>>(dijs.as<double>(), dsf.as<uint8_t>(), dcexpSs.as<int>(),
-                                                              Q, D, dimgSB.as<bf16>());
+        k_img_mui_A<<<oz_img_grid(np * nb * nob), 32 * kOzImgWarps, 0, s>>>(
+            dmui.as<double>(), dmf.as<uint8_t>(), drexpMs.as<int>(), Q, D, np * nb * nob, dimgMA.as<bf16>());
+        k_img_ijs_B<<<oz_img_grid(np * nob * nob), 32 * kOzImgWarps, 0, s>>>(
+            dijs.as<double>(), dsf.as<uint8_t>(), dcexpSs.as<int>(), Q, D, np * nob * nob, dimgSB.as<bf16>());
         const size_t tk = n_sub * nob * ng_a;
         k_tiles_K<<<(unsigned)ceil_div(tk, 128), 128, 0, s>>>(
             dmf.as<uint8_t>(), dmn.as<double>(), dsf.as<uint8_t>(), dsn.as<double>(), drexpMs.as<int>(),
