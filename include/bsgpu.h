@@ -49,6 +49,7 @@ enum {
 typedef struct bsg_ctx_s *bsg_ctx;
 typedef struct bsg_pool_s *bsg_pool;
 typedef struct bsg_bsm_s *bsg_bsm;
+typedef struct bsg_sched_s *bsg_sched;
 
 const char *bsg_last_error(void);
 int bsg_version(void);
@@ -141,6 +142,43 @@ bsg_status bsg_matmult_strassen_sparse(bsg_bsm C, bsg_bsm A, int tA, bsg_bsm B, 
                                        double alpha, double beta, size_t min_size_for_strassen);
 bsg_status bsg_matmult_strassen_sparse_form(bsg_bsm C, bsg_bsm A, bsg_bsm B, double thresh,
                                             size_t min_size_for_strassen, int form, int n_digits);
+
+/* ---- learned Strassen scheduling (no counterpart in the reference, whose
+ *      choice is the cost model of matmult_strassen_dryrun,
+ *      strassen.hpp:602-640) ----
+ * Policies for the per-node Strassen-or-sparse choice:
+ *   BSG_SCHED_COST  the reference's cost model (what bsg_matmult_strassen_sparse does)
+ *   BSG_SCHED_NONE  no Strassen node: screened sparse recursion only
+ *   BSG_SCHED_ROOT  Strassen at the root node only (block count a power of two)
+ *   BSG_SCHED_MLP   a trained bsg_sched: Strassen where the network predicts
+ *                   log(t_strassen / t_sparse) < 0 on nodes whose blocks are all
+ *                   present; levels with more than 65536 nodes keep the cost model
+ * A bsg_sched is a 2 x 64 MLP (25 node features: level, flop counts, block
+ * densities, log-norm histograms) trained on the device by the library's own
+ * forward / backward / Adam kernels. */
+enum { BSG_SCHED_COST = 0, BSG_SCHED_NONE = 1, BSG_SCHED_ROOT = 2, BSG_SCHED_MLP = 3 };
+#define BSG_SCHED_FEATURES 25
+bsg_status bsg_sched_create(bsg_ctx ctx, bsg_sched *out);
+bsg_status bsg_sched_destroy(bsg_sched sched);
+bsg_status bsg_sched_param_count(int *out);
+bsg_status bsg_sched_init(bsg_sched sched, uint64_t seed);                 /* He-uniform weights, zero biases */
+bsg_status bsg_sched_set_params(bsg_sched sched, const float *params);     /* host, bsg_sched_param_count floats */
+bsg_status bsg_sched_get_params(bsg_sched sched, float *params);
+/* y[i] = net(x[i]), x host n x BSG_SCHED_FEATURES row-major */
+bsg_status bsg_sched_predict(bsg_sched sched, const float *x, int n, float *y);
+/* mean squared error of net(x) against t and its gradient (host buffers) */
+bsg_status bsg_sched_loss_grad(bsg_sched sched, const float *x, const float *t, int n, float *loss, float *grad);
+/* Adam on the mean squared error, minibatches of a seeded shuffle */
+bsg_status bsg_sched_train(bsg_sched sched, const float *x, const float *t, int n, int epochs, int batch, float lr,
+                           uint64_t seed, float *final_loss);
+/* features and eligibility of the root node of C = A B's decision tree */
+bsg_status bsg_strassen_root_features(bsg_bsm C, bsg_bsm A, bsg_bsm B, double thresh, float *features,
+                                      int *eligible);
+/* matmult_strassen_sparse with a scheduling policy; n_strassen_nodes (may be
+ * NULL) receives the number of Strassen nodes that ran */
+bsg_status bsg_matmult_strassen_sparse_sched(bsg_bsm C, bsg_bsm A, bsg_bsm B, double thresh,
+                                             size_t min_size_for_strassen, int form, int n_digits, int policy,
+                                             bsg_sched sched, uint64_t *n_strassen_nodes);
 
 /* ---- BlockSparse3DTensor<double> = slices of BlockSparseMatrix
  *      (blocksparse3d_tensor.h:8-43; declared but never defined there) ---- */

@@ -93,6 +93,21 @@ _sig("bsg_tensormult_batched", [c_vp, c_vp, c_int, c_vp, c_int, c_size, c_dbl, c
 _sig("bsg_rik_occ_step", [c_vp, C.POINTER(RikArgs), c_vp, c_int, c_u64p])
 _sig("bsg_3c2c_transform", [c_vp, c_size, c_size, c_vp, c_vp, c_int, c_size, c_dbl, c_int, c_int, c_vp, c_int])
 _sig("bsg_probe_fp64_peak", [c_vp, C.POINTER(c_dbl)])
+c_flt = C.c_float
+_sig("bsg_sched_create", [c_vp, C.POINTER(c_vp)])
+_sig("bsg_sched_destroy", [c_vp])
+_sig("bsg_sched_param_count", [C.POINTER(c_int)])
+_sig("bsg_sched_init", [c_vp, C.c_uint64])
+_sig("bsg_sched_set_params", [c_vp, c_vp])
+_sig("bsg_sched_get_params", [c_vp, c_vp])
+_sig("bsg_sched_predict", [c_vp, c_vp, c_int, c_vp])
+_sig("bsg_sched_loss_grad", [c_vp, c_vp, c_vp, c_int, C.POINTER(c_flt), c_vp])
+_sig("bsg_sched_train", [c_vp, c_vp, c_vp, c_int, c_int, c_int, c_flt, C.c_uint64, C.POINTER(c_flt)])
+_sig("bsg_strassen_root_features", [c_vp, c_vp, c_vp, c_dbl, c_vp, C.POINTER(c_int)])
+_sig("bsg_matmult_strassen_sparse_sched", [c_vp, c_vp, c_vp, c_dbl, c_size, c_int, c_int, c_int, c_vp, c_u64p])
+
+SCHED_COST, SCHED_NONE, SCHED_ROOT, SCHED_MLP = 0, 1, 2, 3
+SCHED_FEATURES = 25
 
 
 def check(status):

@@ -22,6 +22,7 @@ import ctypes as C
 import numpy as np
 
 from ._lib import BSG_DEVICE, BSG_HOST, FORM_FP64, FORM_OZAKI, BsgError, RikArgs, check, lib  # noqa: F401
+from ._lib import SCHED_COST, SCHED_FEATURES, SCHED_MLP, SCHED_NONE, SCHED_ROOT  # noqa: F401
 
 _DEFAULT_CTX = None
 
@@ -289,6 +290,82 @@ def matmult_strassen_sparse(C_, A, tA, B, tB, thresh, alpha, beta, min_size_for_
             raise BsgError(2, "matmult_strassen_sparse supports no transposes and alpha = 1")
         check(lib.bsg_matmult_strassen_sparse_form(C_.h, A.h, B.h, float(thresh), int(min_size_for_strassen), form,
                                                    n_digits))
+
+
+class StrassenScheduler:
+    """The learned Strassen-or-sparse node scheduler (a 2 x 64 MLP on the
+    device; forward, backward and Adam are the library's own kernels)."""
+
+    def __init__(self, ctx=None, seed=None):
+        self.ctx = ctx or default_context()
+        h = C.c_void_p()
+        check(lib.bsg_sched_create(self.ctx.h, C.byref(h)))
+        self.h = h
+        n = C.c_int()
+        check(lib.bsg_sched_param_count(C.byref(n)))
+        self.n_params = n.value
+        if seed is not None:
+            check(lib.bsg_sched_init(self.h, int(seed)))
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h and lib is not None:
+            lib.bsg_sched_destroy(h)
+            self.h = None
+
+    @property
+    def params(self):
+        out = np.empty(self.n_params, np.float32)
+        check(lib.bsg_sched_get_params(self.h, out.ctypes.data))
+        return out
+
+    @params.setter
+    def params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        assert p.size == self.n_params
+        check(lib.bsg_sched_set_params(self.h, p.ctypes.data))
+
+    def predict(self, X):
+        X = np.ascontiguousarray(X, np.float32).reshape(-1, SCHED_FEATURES)
+        y = np.empty(len(X), np.float32)
+        check(lib.bsg_sched_predict(self.h, X.ctypes.data, len(X), y.ctypes.data))
+        return y
+
+    def loss_grad(self, X, T):
+        X = np.ascontiguousarray(X, np.float32).reshape(-1, SCHED_FEATURES)
+        T = np.ascontiguousarray(T, np.float32)
+        g = np.empty(self.n_params, np.float32)
+        loss = C.c_float()
+        check(lib.bsg_sched_loss_grad(self.h, X.ctypes.data, T.ctypes.data, len(X), C.byref(loss), g.ctypes.data))
+        return float(loss.value), g
+
+    def train(self, X, T, epochs=200, batch=32, lr=3e-3, seed=7):
+        X = np.ascontiguousarray(X, np.float32).reshape(-1, SCHED_FEATURES)
+        T = np.ascontiguousarray(T, np.float32)
+        loss = C.c_float()
+        check(lib.bsg_sched_train(self.h, X.ctypes.data, T.ctypes.data, len(X), int(epochs), int(batch), float(lr),
+                                  int(seed), C.byref(loss)))
+        return float(loss.value)
+
+
+def strassen_root_features(C_, A, B, thresh):
+    """features of the root node of C = A B's Strassen decision tree and
+    whether it may run Strassen (all blocks present, not an edge node)"""
+    f = np.empty(SCHED_FEATURES, np.float32)
+    ok = C.c_int()
+    check(lib.bsg_strassen_root_features(C_.h, A.h, B.h, float(thresh), f.ctypes.data, C.byref(ok)))
+    return f, bool(ok.value)
+
+
+def matmult_strassen_sparse_sched(C_, A, B, thresh, min_size_for_strassen, policy=SCHED_COST, sched=None,
+                                  form=FORM_FP64, n_digits=4):
+    """matmult_strassen_sparse with a Strassen scheduling policy; returns the
+    number of Strassen nodes that ran"""
+    n = C.c_uint64()
+    check(lib.bsg_matmult_strassen_sparse_sched(C_.h, A.h, B.h, float(thresh), int(min_size_for_strassen), form,
+                                                int(n_digits), int(policy), sched.h if sched is not None else None,
+                                                C.byref(n)))
+    return n.value
 
 
 def _handles(ms):

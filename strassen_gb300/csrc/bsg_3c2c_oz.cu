@@ -97,15 +97,19 @@ __global__ void k_img_V(const double *__restrict__ V, const int *__restrict__ ce
 }
 
 // tiles and their steps; tile t covers output block row ib and block columns
-// jg*R .. jg*R+R-1, ib-major so that the tiles sharing an X block row run
-// together and read its images from L2
-__global__ void k_tiles_3c(size_t n_tiles, size_t n_jg, const double *__restrict__ xn, const double *__restrict__ vn,
-                           const int *__restrict__ rexp, const int *__restrict__ cexp, double *__restrict__ out,
-                           Dense3c D, double tpb, OzTile *__restrict__ tiles, OzStep *__restrict__ steps,
-                           unsigned long long *__restrict__ nsig, unsigned long long *__restrict__ macs) {
+// jg*R .. jg*R+R-1.  Order: column groups of Gj slot groups (their V^T images,
+// Gj*R*nkb of them, stay resident in L2), within a group every block row ib
+// with its Gj tiles together (they share the X images of ib)
+__global__ void k_tiles_3c(size_t n_tiles, size_t n_jg, size_t Gj, const double *__restrict__ xn,
+                           const double *__restrict__ vn, const int *__restrict__ rexp, const int *__restrict__ cexp,
+                           double *__restrict__ out, Dense3c D, double tpb, OzTile *__restrict__ tiles,
+                           OzStep *__restrict__ steps, unsigned long long *__restrict__ nsig,
+                           unsigned long long *__restrict__ macs) {
     const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n_tiles) return;
-    const size_t ib = t / n_jg, jg = t % n_jg;
+    const size_t q = t / (D.nib * Gj), rem = t % (D.nib * Gj);
+    const size_t gsz = min(Gj, n_jg - q * Gj);  // only the last group is smaller
+    const size_t ib = rem / gsz, jg = q * Gj + rem % gsz;
     OzTile T;
     for (int s = 0; s < kOzMaxSlots; ++s) {
         T.c[s] = nullptr;
@@ -191,12 +195,19 @@ void transform_3c2c_ozaki(bsg_ctx ctx, size_t n_vec2, size_t n_aux, const double
     DevBuf dt(n_tiles * sizeof(OzTile), s), dst(n_tiles * D.nkb * sizeof(OzStep), s);
     const double tpb = thresh * (double)(bs * bs * bs);
     auto *c = cnt.as<unsigned long long>();
-    k_tiles_3c<<<(unsigned)ceil_div(n_tiles, 128), 128, 0, s>>>(n_tiles, n_jg, xn.as<double>(), vn.as<double>(),
+    // V^T images of one slot group: R * nkb images; keep about 48 MB of them in L2
+    const size_t grp_bytes = (size_t)D.R * D.nkb * a_img * 2;
+    const size_t Gj = std::max<size_t>(1, std::min<size_t>(n_jg, (48ull << 20) / std::max<size_t>(grp_bytes, 1)));
+    k_tiles_3c<<<(unsigned)ceil_div(n_tiles, 128), 128, 0, s>>>(n_tiles, n_jg, Gj, xn.as<double>(), vn.as<double>(),
                                                                 rexp.as<int>(), cexp.as<int>(), out, D, tpb,
                                                                 dt.as<OzTile>(), dst.as<OzStep>(), c, c + 1);
     ctx->note_launch();
     ctx->check_launch("3c2c ozaki tiles");
-    oz_run(ctx, sh, dt.as<OzTile>(), n_tiles, dst.as<OzStep>(), ai.as<bf16>(), bi.as<bf16>(), 1.0, s, c + 1);
+    // tiles go round-robin (chunk 1): the Gj tiles of one block row run on
+    // neighbouring CTAs at about the same time and share its X images in L2
+    // (a chunk of Gj tiles per CTA puts 152 block rows in flight at once and
+    // measured more DRAM traffic)
+    oz_run(ctx, sh, dt.as<OzTile>(), n_tiles, dst.as<OzStep>(), ai.as<bf16>(), bi.as<bf16>(), 1.0, s, c + 1, 1);
     ctx->gemm_check();
     if (nsig_out) {
         BSG_CUDA(cudaMemcpyAsync(nsig_out, c, 8, cudaMemcpyDeviceToHost, s));

@@ -80,6 +80,7 @@ int oz_default_digits(int requested, int bs_rows, int bs_k, int bs_cols) {
 
 struct OzKParams {
     int mp, kp, R, nd, S, F;
+    uint32_t chunk;      // consecutive tiles per CTA turn
     int nbuf;            // TMEM accumulator sets (2: the MMA fills one while the epilogue drains the other)
     uint32_t tmem_cols;  // columns of one accumulator set
     uint32_t tx_bytes;
@@ -102,6 +103,16 @@ enum OzProf {
 };
 
 constexpr int kOzThreads = 320;  // producer, MMA issuer, 8 epilogue warps
+
+// Tile sequence of a CTA: chunks of `chunk` consecutive tiles, chunk
+// blockIdx.x, then every gridDim.x-th chunk (tiles of one chunk share operand
+// images, which then stay hot in L2 between them).  Every role walks the same
+// sequence.
+__device__ __forceinline__ uint32_t oz_first_tile(uint32_t chunk) { return blockIdx.x * chunk; }
+__device__ __forceinline__ uint32_t oz_next_tile(uint32_t t, uint32_t chunk) {
+    ++t;
+    return (t % chunk) ? t : t + (gridDim.x - 1) * chunk;
+}
 
 template <int NP>
 __global__ void __launch_bounds__(kOzThreads, 1)
@@ -154,7 +165,7 @@ __global__ void __launch_bounds__(kOzThreads, 1)
         uint32_t it = 0;
         unsigned long long w_empty = 0;
         uint32_t stage = 0, ph = 0;  // ring position of step `it`
-        for (uint32_t t = blockIdx.x; t < n_tiles && !*abort; t += gridDim.x) {
+        for (uint32_t t = oz_first_tile(P.chunk); t < n_tiles && !*abort; t = oz_next_tile(t, P.chunk)) {
             const uint32_t s0 = tiles[t].s0, ns = tiles[t].ns;
             for (uint32_t k = 0; k < ns; ++k, ++it) {
                 if ((k & 31u) == 0) {
@@ -237,7 +248,7 @@ __global__ void __launch_bounds__(kOzThreads, 1)
                 }
             const uint32_t nq = (uint32_t)P.kp / 16u;
             bool ok = true;
-            for (uint32_t t = blockIdx.x; t < n_tiles && ok; t += gridDim.x) {
+            for (uint32_t t = oz_first_tile(P.chunk); t < n_tiles && ok; t = oz_next_tile(t, P.chunk)) {
                 const uint32_t ns = tiles[t].ns;
                 const uint32_t nch = (ns + P.F - 1) / P.F;
                 for (uint32_t c = 0; c < nch && ok; ++c, ++ch) {
@@ -303,7 +314,7 @@ __global__ void __launch_bounds__(kOzThreads, 1)
         unsigned long long w_full = 0, t_drain = 0, t_store = 0;
         uint32_t ch = 0;
         bool ok = true;
-        for (uint32_t t = blockIdx.x; t < n_tiles && ok; t += gridDim.x) {
+        for (uint32_t t = oz_first_tile(P.chunk); t < n_tiles && ok; t = oz_next_tile(t, P.chunk)) {
             const OzTile &T = tiles[t];
             const uint32_t ns = T.ns;
             const uint32_t nch = (ns + P.F - 1) / P.F;
@@ -400,8 +411,9 @@ __global__ void __launch_bounds__(kOzThreads, 1)
 template <int NP>
 static void launch_oz(bsg_ctx ctx, const OzShape &sh, const OzTile *tiles, size_t n_tiles, const OzStep *steps,
                       const bf16 *a_img, const bf16 *b_img, double alpha, int *err, unsigned long long *prof,
-                      cudaStream_t s) {
+                      uint32_t chunk, cudaStream_t s) {
     OzKParams P;
+    P.chunk = chunk;
     P.mp = sh.mp;
     P.kp = sh.kp;
     P.R = sh.R;
@@ -421,29 +433,32 @@ static void launch_oz(bsg_ctx ctx, const OzShape &sh, const OzTile *tiles, size_
     BSG_REQUIRE(cols <= 512, BSG_ERR_UNSUPPORTED, "Ozaki form: digits x padded block columns exceed TMEM");
     const size_t smem = (size_t)P.S * stage_bytes + 32 * sizeof(OzStep) + (2 * P.S + 4) * 8 + 16;
     BSG_CUDA(cudaFuncSetAttribute(k_ozgemm<NP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const unsigned grid = (unsigned)std::min<size_t>(n_tiles, (size_t)ctx->sm_count);
+    const unsigned grid = (unsigned)std::min<size_t>(ceil_div(n_tiles, (size_t)chunk), (size_t)ctx->sm_count);
+    BSG_REQUIRE(n_tiles + (size_t)grid * chunk < 0xffffffffull, BSG_ERR_UNSUPPORTED, "too many Ozaki tiles");
     k_ozgemm<NP><<<grid, kOzThreads, smem, s>>>(tiles, (uint32_t)n_tiles, steps, a_img, b_img, P, err);
     ctx->note_launch();
     ctx->check_launch("ozaki gemm");
 }
 
 void oz_run(bsg_ctx ctx, const OzShape &sh, const OzTile *d_tiles, size_t n_tiles, const OzStep *d_steps,
-            const bf16 *a_img, const bf16 *b_img, double alpha, cudaStream_t s, const unsigned long long *d_macs) {
+            const bf16 *a_img, const bf16 *b_img, double alpha, cudaStream_t s, const unsigned long long *d_macs,
+            uint32_t chunk) {
     if (!n_tiles) return;
+    BSG_REQUIRE(chunk >= 1, BSG_ERR_ARG, "tile chunk");
     BSG_REQUIRE(sh.nd >= 2 && sh.nd <= kOzMaxDigits && sh.nd * sh.np + 8 <= 512, BSG_ERR_UNSUPPORTED,
                 "Ozaki form: 2..8 digits, digits x padded block columns < 512");
     int *err = ctx->gemm_err_flag();
     if (!ctx->timing) {
         // no synchronization: the flag is read once at the end of the public call
         switch (sh.np) {
-            case 8: launch_oz<8>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, nullptr, s); break;
-            case 16: launch_oz<16>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, nullptr, s); break;
-            case 24: launch_oz<24>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, nullptr, s); break;
-            case 32: launch_oz<32>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, nullptr, s); break;
-            case 40: launch_oz<40>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, nullptr, s); break;
-            case 48: launch_oz<48>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, nullptr, s); break;
-            case 56: launch_oz<56>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, nullptr, s); break;
-            case 64: launch_oz<64>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, nullptr, s); break;
+            case 8: launch_oz<8>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, nullptr, chunk, s); break;
+            case 16: launch_oz<16>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, nullptr, chunk, s); break;
+            case 24: launch_oz<24>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, nullptr, chunk, s); break;
+            case 32: launch_oz<32>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, nullptr, chunk, s); break;
+            case 40: launch_oz<40>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, nullptr, chunk, s); break;
+            case 48: launch_oz<48>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, nullptr, chunk, s); break;
+            case 56: launch_oz<56>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, nullptr, chunk, s); break;
+            case 64: launch_oz<64>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, nullptr, chunk, s); break;
             default: throw Error{BSG_ERR_UNSUPPORTED, "Ozaki form supports block sizes up to 64"};
         }
         return;
@@ -457,14 +472,14 @@ void oz_run(bsg_ctx ctx, const OzShape &sh, const OzTile *d_tiles, size_t n_tile
     BSG_CUDA(cudaEventCreate(&e1));
     BSG_CUDA(cudaEventRecord(e0, s));
     switch (sh.np) {
-        case 8: launch_oz<8>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, prof, s); break;
-        case 16: launch_oz<16>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, prof, s); break;
-        case 24: launch_oz<24>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, prof, s); break;
-        case 32: launch_oz<32>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, prof, s); break;
-        case 40: launch_oz<40>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, prof, s); break;
-        case 48: launch_oz<48>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, prof, s); break;
-        case 56: launch_oz<56>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, prof, s); break;
-        case 64: launch_oz<64>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, prof, s); break;
+        case 8: launch_oz<8>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, prof, chunk, s); break;
+        case 16: launch_oz<16>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, prof, chunk, s); break;
+        case 24: launch_oz<24>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, prof, chunk, s); break;
+        case 32: launch_oz<32>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, prof, chunk, s); break;
+        case 40: launch_oz<40>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, prof, chunk, s); break;
+        case 48: launch_oz<48>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, prof, chunk, s); break;
+        case 56: launch_oz<56>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, prof, chunk, s); break;
+        case 64: launch_oz<64>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, prof, chunk, s); break;
         default: throw Error{BSG_ERR_UNSUPPORTED, "Ozaki form supports block sizes up to 64"};
     }
     BSG_CUDA(cudaEventRecord(e1, s));
@@ -697,9 +712,129 @@ void ozaki_screened(bsg_ctx ctx, bsg_bsm C, bsg_bsm A, bsg_bsm B, const ScreenGe
     ctx->gemm_check();
 }
 
-void ozaki_grouped_gemm(bsg_ctx, const std::vector<GemmItem> &, const GemmItem *, const GemmPair *, uint64_t, int, int,
-                        double, int, int, size_t, int, cudaStream_t) {
-    throw Error{BSG_ERR_UNSUPPORTED, "Ozaki form of grouped item/pair products not available"};
+// ---------------------------------------------------------------------------
+// dense grid products X += P Q (the Strassen-Winograd leaves,
+// strassen.hpp:311-323): n x n grids of bs x bs blocks, all blocks present
+// ---------------------------------------------------------------------------
+
+// exponent of every row of P (over the whole k range of its product); grid (product, rb)
+__global__ void k_grid_rexp(double *const *__restrict__ P, size_t n, int bs, int *__restrict__ rexp) {
+    const size_t i = blockIdx.x / n, rb = blockIdx.x % n;
+    const int r = threadIdx.x;
+    if (r >= bs) return;
+    long long mx = 0;
+    for (size_t kb = 0; kb < n; ++kb) {
+        const double *blk = P[i * n * n + rb + kb * n];
+        for (int l = 0; l < bs; ++l) {
+            const long long b = oz_absbits(blk[r + (size_t)l * bs]);
+            mx = b > mx ? b : mx;
+        }
+    }
+    rexp[(i * n + rb) * bs + r] = oz_exp_of_bits(mx);
+}
+
+// exponent of every column of Q; grid (product, cb)
+__global__ void k_grid_cexp(double *const *__restrict__ Q, size_t n, int bs, int *__restrict__ cexp) {
+    const size_t i = blockIdx.x / n, cb = blockIdx.x % n;
+    const int c = threadIdx.x;
+    if (c >= bs) return;
+    long long mx = 0;
+    for (size_t kb = 0; kb < n; ++kb) {
+        const double *blk = Q[i * n * n + kb + cb * n];
+        for (int l = 0; l < bs; ++l) {
+            const long long b = oz_absbits(blk[l + (size_t)c * bs]);
+            mx = b > mx ? b : mx;
+        }
+    }
+    cexp[(i * n + cb) * bs + c] = oz_exp_of_bits(mx);
+}
+
+// M-side images of P blocks, index i*n*n + rb + kb*n (a tile's slots are consecutive)
+__global__ void k_grid_img_P(double *const *__restrict__ P, size_t n_blk, size_t n, int bs, const int *__restrict__ rexp,
+                             OzShape sh, bf16 *__restrict__ img) {
+    const size_t x = oz_warp_id();
+    if (x >= n_blk) return;
+    const size_t i = x / (n * n), rb = x % n;
+    oz_block_image(P[x], bs, false, bs, bs, rexp + (i * n + rb) * bs, sh.mp, sh.kp, sh.nd,
+                   img + x * (size_t)sh.nd * sh.mp * sh.kp, true);
+}
+
+// N-side images of Q blocks (image row = output column), index i*n*n + kb + cb*n
+__global__ void k_grid_img_Q(double *const *__restrict__ Q, size_t n_blk, size_t n, int bs, const int *__restrict__ cexp,
+                             OzShape sh, bf16 *__restrict__ img) {
+    const size_t x = oz_warp_id();
+    if (x >= n_blk) return;
+    const size_t i = x / (n * n), cb = (x % (n * n)) / n;
+    oz_block_image(Q[x], bs, true, bs, bs, cexp + (i * n + cb) * bs, sh.np, sh.kp, sh.nd,
+                   img + x * (size_t)sh.nd * sh.np * sh.kp, false);
+}
+
+void ozaki_grid_products(bsg_ctx ctx, size_t n_prod, size_t n, const std::vector<double *> &X,
+                         const std::vector<double *> &P, const std::vector<double *> &Q, int bs, int n_digits,
+                         cudaStream_t s) {
+    if (!n_prod || !n) return;
+    BSG_REQUIRE(bs <= 64, BSG_ERR_UNSUPPORTED, "Ozaki form supports blocks up to 64");
+    const size_t nn = n * n, n_blk = n_prod * nn;
+    BSG_REQUIRE(X.size() == n_blk && P.size() == n_blk && Q.size() == n_blk, BSG_ERR_ARG, "grid tables");
+    const int nd = oz_default_digits(n_digits, bs, bs, bs);
+    const OzShape sh = oz_shape(bs, bs, bs, nd);
+    DevBuf dP(n_blk * 8, s), dQ(n_blk * 8, s), rexp(n_prod * n * bs * 4, s), cexp(n_prod * n * bs * 4, s);
+    DevBuf aimg(n_blk * nd * (size_t)sh.mp * sh.kp * 2, s), bimg(n_blk * nd * (size_t)sh.np * sh.kp * 2, s);
+    BSG_CUDA(cudaMemcpyAsync(dP.p, P.data(), n_blk * 8, cudaMemcpyHostToDevice, s));
+    BSG_CUDA(cudaMemcpyAsync(dQ.p, Q.data(), n_blk * 8, cudaMemcpyHostToDevice, s));
+    const unsigned tb = (unsigned)std::max(32, round_up(bs, 32));
+    k_grid_rexp<<<(unsigned)(n_prod * n), tb, 0, s>>>(dP.as<double *>(), n, bs, rexp.as<int>());
+    k_grid_cexp<<<(unsigned)(n_prod * n), tb, 0, s>>>(dQ.as<double *>(), n, bs, cexp.as<int>());
+    k_grid_img_P<<<oz_img_grid(n_blk), 32 * kOzImgWarps, 0, s>>>(dP.as<double *>(), n_blk, n, bs, rexp.as<int>(), sh,
+                                                                 aimg.as<bf16>());
+    k_grid_img_Q<<<oz_img_grid(n_blk), 32 * kOzImgWarps, 0, s>>>(dQ.as<double *>(), n_blk, n, bs, cexp.as<int>(), sh,
+                                                                 bimg.as<bf16>());
+    ctx->note_launch(4);
+    ctx->check_launch("ozaki grid split");
+    // tiles (product, block column cb, R consecutive block rows), steps over kb
+    const size_t ng = ceil_div(n, (size_t)sh.R);
+    std::vector<OzTile> tiles;
+    std::vector<OzStep> steps;
+    tiles.reserve(n_prod * n * ng);
+    steps.reserve(n_prod * n * ng * n);
+    for (size_t i = 0; i < n_prod; ++i)
+        for (size_t cb = 0; cb < n; ++cb)
+            for (size_t g = 0; g < ng; ++g) {
+                OzTile T;
+                std::memset(&T, 0, sizeof(T));
+                for (int sl = 0; sl < sh.R; ++sl) {
+                    const size_t rb = g * sh.R + sl;
+                    if (rb >= n) break;
+                    T.c[sl] = X[i * nn + rb + cb * n];
+                    T.rows[sl] = bs;
+                    T.ldc[sl] = bs;
+                    T.rexp[sl] = rexp.as<int>() + (i * n + rb) * bs;
+                }
+                T.cols = bs;
+                T.cexp = cexp.as<int>() + (i * n + cb) * bs;
+                T.fresh_mask = 0;  // X += P Q
+                T.s0 = (uint32_t)steps.size();
+                T.ns = (uint32_t)n;
+                for (size_t kb = 0; kb < n; ++kb) {
+                    OzStep st;
+                    st.b = (uint32_t)(i * nn + kb + cb * n);
+                    for (int sl = 0; sl < kOzMaxSlots; ++sl) {
+                        const size_t rb = g * sh.R + sl;
+                        st.a[sl] = (sl < sh.R && rb < n) ? (uint32_t)(i * nn + rb + kb * n) : kOzNone;
+                    }
+                    steps.push_back(st);
+                }
+                tiles.push_back(T);
+            }
+    BSG_REQUIRE(steps.size() < 0xffffffffull && n_blk < 0xffffffffull, BSG_ERR_UNSUPPORTED, "grid products too large");
+    DevBuf dt(tiles.size() * sizeof(OzTile), s), dst(steps.size() * sizeof(OzStep), s), dmacs(8, s);
+    BSG_CUDA(cudaMemcpyAsync(dt.p, tiles.data(), tiles.size() * sizeof(OzTile), cudaMemcpyHostToDevice, s));
+    BSG_CUDA(cudaMemcpyAsync(dst.p, steps.data(), steps.size() * sizeof(OzStep), cudaMemcpyHostToDevice, s));
+    const unsigned long long macs = (unsigned long long)n_prod * n * n * n * bs * bs * bs;
+    BSG_CUDA(cudaMemcpyAsync(dmacs.p, &macs, 8, cudaMemcpyHostToDevice, s));
+    oz_run(ctx, sh, dt.as<OzTile>(), tiles.size(), dst.as<OzStep>(), aimg.as<bf16>(), bimg.as<bf16>(), 1.0, s,
+           dmacs.as<unsigned long long>());
+    ctx->gemm_check();  // also keeps the host tables alive until the copies are done
 }
 
 }  // namespace bsg

@@ -60,10 +60,11 @@ struct OzStep {
 // Runs the tiles: C_slot = alpha * sum_steps A_slot,step * B_step (+ C_slot
 // unless fresh).  a_img / b_img hold nd planes per image in the UMMA layout.
 // d_macs (may be null): device counter of the unpadded multiply-adds the
-// tiles perform, read for the context's GEMM timing
+// tiles perform, read for the context's GEMM timing.  Each persistent CTA
+// takes `chunk` consecutive tiles at a time.
 void oz_run(bsg_ctx ctx, const OzShape &sh, const OzTile *d_tiles, size_t n_tiles, const OzStep *d_steps,
             const __nv_bfloat16 *a_img, const __nv_bfloat16 *b_img, double alpha, cudaStream_t s,
-            const unsigned long long *d_macs = nullptr);
+            const unsigned long long *d_macs = nullptr, uint32_t chunk = 1);
 
 // Ozaki form of one screened product (single slice): same screening and C
 // block bookkeeping as the FP64 form; items come from screened_product.
@@ -71,10 +72,12 @@ void ozaki_screened(bsg_ctx ctx, bsg_bsm C, bsg_bsm A, bsg_bsm B, const ScreenGe
                     const std::vector<uint32_t> &item_ib, const std::vector<uint32_t> &item_jb, double alpha,
                     int n_digits, cudaStream_t s);
 
-// Grouped products given as items and pairs (Strassen leaves).
-void ozaki_grouped_gemm(bsg_ctx ctx, const std::vector<GemmItem> &items, const GemmItem *d_items,
-                        const GemmPair *d_pairs, uint64_t n_pairs, int tA, int tB, double alpha, int max_r, int max_c,
-                        size_t kbs, int n_digits, cudaStream_t s);
+// Dense grid products X_i += P_i Q_i (the Strassen-Winograd leaves): n_prod
+// products of n x n grids of bs x bs blocks; X, P, Q hold the device block
+// pointers of every grid, column-major, product after product.
+void ozaki_grid_products(bsg_ctx ctx, size_t n_prod, size_t n, const std::vector<double *> &X,
+                         const std::vector<double *> &P, const std::vector<double *> &Q, int bs, int n_digits,
+                         cudaStream_t s);
 
 // ---- device helpers shared with the RI-K pipeline ----
 

@@ -21,6 +21,7 @@
 
 #include "bsg_gemm64.cuh"
 #include "bsg_ozaki.cuh"
+#include "bsg_sched.cuh"
 
 namespace bsg {
 
@@ -57,7 +58,8 @@ struct DryLevel {
 __global__ void k_dry_level(const unsigned long long *__restrict__ prev, unsigned long long *__restrict__ next,
                             uint8_t *__restrict__ tree, DryLevel L, size_t nib, size_t njb, size_t nkb, size_t ni,
                             size_t nj, size_t nk, size_t ibs, size_t jbs, size_t kbs,
-                            unsigned long long *__restrict__ total) {
+                            unsigned long long *__restrict__ total, unsigned long long *__restrict__ nf_out,
+                            uint8_t *__restrict__ edge_out) {
     const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     unsigned long long out = 0;
     if (s < L.nsi * L.nsj * L.nsk) {
@@ -75,6 +77,10 @@ __global__ void k_dry_level(const unsigned long long *__restrict__ prev, unsigne
                     nf += prev[(2 * si + a) + (2 * sj + b) * L.pni + (2 * sk + c) * L.pni * L.pnj];
         const bool go = (nf >= L.cost) && !edge;
         tree[si + sj * L.nsi + sk * L.nsi * L.nsj] = go;
+        if (nf_out) {  // the node's cost below it (sparse recursion), for the scheduler's features
+            nf_out[si + sj * L.nsi + sk * L.nsi * L.nsj] = nf;
+            edge_out[si + sj * L.nsi + sk * L.nsi * L.nsj] = edge;
+        }
         out = go ? L.cost : nf;
         next[si + sj * L.nsi + sk * L.nsi * L.nsj] = out;
     }
@@ -86,6 +92,8 @@ struct DryResult {
     int n_levels = 0;
     std::vector<std::vector<uint8_t>> tree;
     std::vector<uint64_t> flops;
+    std::vector<uint64_t> cost;                     // Strassen cost of a node per level
+    std::vector<DevBuf> nf, edge;                   // per level, kept when asked for (scheduler)
 };
 
 static void check_square(bsg_bsm A, bsg_bsm B) {
@@ -97,7 +105,7 @@ static void check_square(bsg_bsm A, bsg_bsm B) {
                 "strassen: only square products are supported (strassen.hpp:547-551)");
 }
 
-static DryResult dryrun(bsg_bsm A, bsg_bsm B, double tpb) {
+static DryResult dryrun(bsg_bsm A, bsg_bsm B, double tpb, bool keep_nodes = false) {
     check_square(A, B);
     bsg_ctx ctx = A->ctx;
     cudaStream_t s = ctx->stream;
@@ -135,9 +143,15 @@ static DryResult dryrun(bsg_bsm A, bsg_bsm B, double tpb) {
         L.pnj = ceil_div(njb, L.psb);
         const size_t n = L.nsi * L.nsj * L.nsk;
         DevBuf next(n * 8, s), tr(n, s);
-        k_dry_level<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(prev.as<unsigned long long>(),
-                                                                next.as<unsigned long long>(), tr.as<uint8_t>(), L,
-                                                                nib, njb, nkb, ni, nj, nk, ibs, jbs, kbs, T + level + 1);
+        R.cost.push_back(L.cost);
+        if (keep_nodes) {
+            R.nf.emplace_back(n * 8, s);
+            R.edge.emplace_back(n, s);
+        }
+        k_dry_level<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(
+            prev.as<unsigned long long>(), next.as<unsigned long long>(), tr.as<uint8_t>(), L, nib, njb, nkb, ni, nj,
+            nk, ibs, jbs, kbs, T + level + 1, keep_nodes ? R.nf.back().as<unsigned long long>() : nullptr,
+            keep_nodes ? R.edge.back().as<uint8_t>() : nullptr);
         ctx->note_launch();
         ctx->check_launch("dryrun level");
         R.tree.emplace_back(n);
@@ -266,6 +280,21 @@ static void run_quads(bsg_ctx ctx, const std::vector<QuadOp> &ops, int op, int b
 // dense 8-product `X(rb,cb) += sum_kb P(rb,kb) Q(kb,cb)` (strassen.hpp:311-323)
 static void leaf_products(bsg_ctx ctx, const std::vector<std::tuple<const Grid *, const Grid *, const Grid *>> &prods,
                           int bs, int form, int n_digits, cudaStream_t s) {
+    if (form != BSG_FORM_FP64) {
+        // mixed form: bf16 digit products on the tensor cores; the Winograd
+        // sums around them stay FP64
+        if (prods.empty()) return;
+        const size_t n = std::get<0>(prods[0])->n;
+        std::vector<double *> X, P, Q;
+        for (auto &t : prods) {
+            BSG_REQUIRE(std::get<0>(t)->n == n, BSG_ERR_PRECOND, "leaf grids of one depth share their side");
+            X.insert(X.end(), std::get<0>(t)->blk.begin(), std::get<0>(t)->blk.end());
+            P.insert(P.end(), std::get<1>(t)->blk.begin(), std::get<1>(t)->blk.end());
+            Q.insert(Q.end(), std::get<2>(t)->blk.begin(), std::get<2>(t)->blk.end());
+        }
+        ozaki_grid_products(ctx, prods.size(), n, X, P, Q, bs, n_digits, s);
+        return;
+    }
     std::vector<GemmItem> items;
     std::vector<GemmPair> pairs;
     for (auto &t : prods) {
@@ -288,11 +317,7 @@ static void leaf_products(bsg_ctx ctx, const std::vector<std::tuple<const Grid *
     DevBuf di(items.size() * sizeof(GemmItem), s), dp(pairs.size() * sizeof(GemmPair), s);
     BSG_CUDA(cudaMemcpyAsync(di.p, items.data(), items.size() * sizeof(GemmItem), cudaMemcpyHostToDevice, s));
     BSG_CUDA(cudaMemcpyAsync(dp.p, pairs.data(), pairs.size() * sizeof(GemmPair), cudaMemcpyHostToDevice, s));
-    if (form == BSG_FORM_FP64)
-        launch_gemm64(ctx, di.as<GemmItem>(), items.size(), dp.as<GemmPair>(), 0, 0, 1.0, bs, bs, s);
-    else
-        ozaki_grouped_gemm(ctx, items, di.as<GemmItem>(), dp.as<GemmPair>(), pairs.size(), 0, 0, 1.0, bs, bs,
-                           (size_t)bs, n_digits, s);
+    launch_gemm64(ctx, di.as<GemmItem>(), items.size(), dp.as<GemmPair>(), 0, 0, 1.0, bs, bs, s);
     BSG_CUDA(cudaStreamSynchronize(s));
 }
 
@@ -494,7 +519,73 @@ __global__ void __launch_bounds__(256) k_apply(double *const *__restrict__ Cp, d
     if (threadIdx.x == 0 && cnt) atomicAdd(nsig, cnt);
 }
 
-static void strassen_sparse(bsg_bsm C, bsg_bsm A, bsg_bsm B, double thresh, size_t min_size, int form, int n_digits) {
+// Features (host copy, kSchedIn floats per node) and eligibility of the nodes
+// of one dry-run level.
+static void level_features(bsg_bsm C, bsg_bsm A, bsg_bsm B, const DryResult &R, int L, std::vector<float> &F,
+                           std::vector<uint8_t> &ok, DevBuf *dF_keep = nullptr) {
+    cudaStream_t s = A->ctx->stream;
+    const size_t sb = (size_t)1 << (L + 1);
+    const size_t nsi = ceil_div(A->nrb, sb), nsj = ceil_div(B->ncb, sb), nsk = ceil_div(A->ncb, sb);
+    const size_t n = nsi * nsj * nsk;
+    DevBuf dF(n * kSchedIn * 4, s), dok(n, s);
+    launch_node_features(A, B, C, L, nsi, nsj, nsk, R.nf[L].as<unsigned long long>(), R.edge[L].as<uint8_t>(),
+                         R.cost[L], dF.as<float>(), dok.as<uint8_t>());
+    F.resize(n * kSchedIn);
+    ok.resize(n);
+    BSG_CUDA(cudaMemcpyAsync(F.data(), dF.p, n * kSchedIn * 4, cudaMemcpyDeviceToHost, s));
+    BSG_CUDA(cudaMemcpyAsync(ok.data(), dok.p, n, cudaMemcpyDeviceToHost, s));
+    BSG_CUDA(cudaStreamSynchronize(s));
+    if (dF_keep) *dF_keep = std::move(dF);
+}
+
+// Replaces the cost model's tree per the scheduling policy (the cost model's
+// own tree is BSG_SCHED_COST and the fallback of BSG_SCHED_MLP on levels with
+// more than kSchedMaxNodes nodes).
+constexpr size_t kSchedMaxNodes = 65536;
+static void apply_policy(bsg_bsm C, bsg_bsm A, bsg_bsm B, DryResult &R, int policy, bsg_sched sched) {
+    const int NL = R.n_levels;
+    if (policy == BSG_SCHED_COST) return;
+    if (policy == BSG_SCHED_NONE) {
+        for (auto &t : R.tree) std::fill(t.begin(), t.end(), 0);
+        return;
+    }
+    if (policy == BSG_SCHED_ROOT) {
+        for (auto &t : R.tree) std::fill(t.begin(), t.end(), 0);
+        if (NL == 0 || R.tree[NL - 1].size() != 1) return;  // no single root node
+        std::vector<float> F;
+        std::vector<uint8_t> ok;
+        level_features(C, A, B, R, NL - 1, F, ok);
+        R.tree[NL - 1][0] = ok[0];
+        return;
+    }
+    BSG_REQUIRE(policy == BSG_SCHED_MLP && sched, BSG_ERR_ARG, "BSG_SCHED_MLP needs a scheduler");
+    BSG_REQUIRE(sched->ctx == A->ctx, BSG_ERR_ARG, "scheduler on another context");
+    // features, forward pass and decisions of every covered level on the
+    // device; one synchronization for all the levels' trees
+    cudaStream_t s = A->ctx->stream;
+    std::vector<DevBuf> keep;
+    std::vector<int> levels;
+    for (int L = 0; L < NL; ++L) {
+        const size_t n = R.tree[L].size();
+        if (n > kSchedMaxNodes || !n) continue;  // cost model
+        const size_t sb = (size_t)1 << (L + 1);
+        DevBuf dF(n * kSchedIn * 4, s), dok(n, s), dY(n * 4, s), dT(n, s);
+        launch_node_features(A, B, C, L, ceil_div(A->nrb, sb), ceil_div(B->ncb, sb), ceil_div(A->ncb, sb),
+                             R.nf[L].as<unsigned long long>(), R.edge[L].as<uint8_t>(), R.cost[L], dF.as<float>(),
+                             dok.as<uint8_t>());
+        sched->predict_dev(dF.as<float>(), (int)n, dY.as<float>());  // predicted log(t_strassen / t_sparse)
+        launch_sched_decide(A->ctx, dok.as<uint8_t>(), dY.as<float>(), n, dT.as<uint8_t>());
+        BSG_CUDA(cudaMemcpyAsync(R.tree[L].data(), dT.p, n, cudaMemcpyDeviceToHost, s));
+        keep.push_back(std::move(dF));
+        keep.push_back(std::move(dok));
+        keep.push_back(std::move(dY));
+        keep.push_back(std::move(dT));
+    }
+    BSG_CUDA(cudaStreamSynchronize(s));
+}
+
+static void strassen_sparse(bsg_bsm C, bsg_bsm A, bsg_bsm B, double thresh, size_t min_size, int form, int n_digits,
+                            int policy = BSG_SCHED_COST, bsg_sched sched = nullptr, uint64_t *n_nodes = nullptr) {
     check_square(A, B);
     BSG_REQUIRE(C && C->ctx == A->ctx, BSG_ERR_ARG, "output on another context");
     BSG_REQUIRE(C->nrb == A->nrb && C->ncb == B->ncb && C->nr == A->nr && C->nc == B->nc, BSG_ERR_ARG,
@@ -506,7 +597,8 @@ static void strassen_sparse(bsg_bsm C, bsg_bsm A, bsg_bsm B, double thresh, size
     const size_t bs = A->bsr, nib = A->nrb;
     BSG_REQUIRE(bs * bs <= 16 * 256, BSG_ERR_UNSUPPORTED, "strassen kernels support bs <= 64");
     const double tpb = thresh * (double)(A->bsr * B->bsc * A->bsc);  // strassen.hpp:710
-    DryResult R = dryrun(A, B, tpb);
+    DryResult R = dryrun(A, B, tpb, policy != BSG_SCHED_COST);
+    apply_policy(C, A, B, R, policy, sched);
     const int NL = R.n_levels;
     // active nodes: tree bit set and no ancestor set
     std::vector<size_t> lvl_n(NL), lvl_off(NL);
@@ -543,6 +635,7 @@ static void strassen_sparse(bsg_bsm C, bsg_bsm A, bsg_bsm B, double thresh, size
                     }
                 }
     }
+    if (n_nodes) *n_nodes = nodes.size();
     // preconditions of the Strassen path: full, present A/B/C blocks
     for (auto &nd : nodes) {
         const size_t sb = (size_t)1 << (nd.L + 1), ib0 = nd.si * sb, jb0 = nd.sj * sb, kb0 = nd.sk * sb;
@@ -661,5 +754,33 @@ extern "C" bsg_status bsg_matmult_strassen_sparse_form(bsg_bsm C, bsg_bsm A, bsg
     return guard([&] {
         BSG_REQUIRE(form == BSG_FORM_FP64 || form == BSG_FORM_OZAKI, BSG_ERR_ARG, "unknown form");
         strassen_sparse(C, A, B, thresh, min_size, form, n_digits);
+    });
+}
+
+extern "C" bsg_status bsg_matmult_strassen_sparse_sched(bsg_bsm C, bsg_bsm A, bsg_bsm B, double thresh, size_t min_size,
+                                                        int form, int n_digits, int policy, bsg_sched sched,
+                                                        uint64_t *n_strassen_nodes) {
+    return guard([&] {
+        BSG_REQUIRE(form == BSG_FORM_FP64 || form == BSG_FORM_OZAKI, BSG_ERR_ARG, "unknown form");
+        BSG_REQUIRE(policy >= BSG_SCHED_COST && policy <= BSG_SCHED_MLP, BSG_ERR_ARG, "unknown policy");
+        strassen_sparse(C, A, B, thresh, min_size, form, n_digits, policy, sched, n_strassen_nodes);
+    });
+}
+
+extern "C" bsg_status bsg_strassen_root_features(bsg_bsm C, bsg_bsm A, bsg_bsm B, double thresh, float *features,
+                                                 int *eligible) {
+    return guard([&] {
+        check_square(A, B);
+        BSG_REQUIRE(C && features && eligible, BSG_ERR_ARG, "NULL argument");
+        BSG_REQUIRE(C->nrb == A->nrb && C->ncb == B->ncb, BSG_ERR_ARG, "output dimensions do not match");
+        const double tpb = thresh * (double)(A->bsr * B->bsc * A->bsc);
+        DryResult R = dryrun(A, B, tpb, true);
+        BSG_REQUIRE(R.n_levels > 0 && R.tree[R.n_levels - 1].size() == 1, BSG_ERR_PRECOND,
+                    "the decision tree has no single root node (block count not a power of two)");
+        std::vector<float> F;
+        std::vector<uint8_t> ok;
+        level_features(C, A, B, R, R.n_levels - 1, F, ok);
+        std::copy(F.begin(), F.begin() + kSchedIn, features);
+        *eligible = ok[0];
     });
 }

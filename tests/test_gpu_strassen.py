@@ -63,3 +63,27 @@ def test_strassen_preconditions(api, ctx):
         api.matmult_strassen_sparse(gC, gA, 1, gB, 0, 0.0, 1.0, 0.0, 64)
     with pytest.raises(api.BsgError):
         api.matmult_strassen_sparse(gC, gA, 0, gB, 0, 0.0, 2.0, 0.0, 64)
+
+
+@pytest.mark.parametrize("n,bs,L,core,thr,ms,nd", [(512, 32, 1.0, 256, 1e-7, 128, 4), (1024, 64, 6.0, 512, 1e-9, 256, 4),
+                                                   (768, 24, 2.0, 384, 1e-8, 96, 5), (2048, 64, 6.0, 2048, 1e-10, 1024, 4)])
+def test_strassen_mixed_form(api, ctx, n, bs, L, core, thr, ms, nd):
+    """Mixed form: Winograd leaves as bf16 digit products on the tensor cores,
+    pre/post sums and the screened sparse part in FP64.  Same decision tree
+    and the same C block structure as the FP64 form; relative Frobenius error
+    within the digit bound."""
+    A = S.decay_matrix(5, 1, n, n, bs, L, core=core)
+    B = S.decay_matrix(5, 2, n, n, bs, L, core=core)
+    gA = api.BlockSparseMatrix.from_dense(A, bs, bs, 0.0, ctx=ctx)
+    gB = api.BlockSparseMatrix.from_dense(B, bs, bs, 0.0, ctx=ctx)
+    C64 = api.BlockSparseMatrix(n, n, bs, bs, 0.0, ctx=ctx)
+    Cmx = api.BlockSparseMatrix(n, n, bs, bs, 0.0, ctx=ctx)
+    C64.fill_with_values(0.0)
+    Cmx.fill_with_values(0.0)
+    api.matmult_strassen_sparse(C64, gA, 0, gB, 0, thr, 1.0, 0.0, ms)
+    api.matmult_strassen_sparse(Cmx, gA, 0, gB, 0, thr, 1.0, 0.0, ms, form=api.FORM_OZAKI, n_digits=nd)
+    assert np.array_equal(C64.mask(), Cmx.mask())
+    r64, rmx = C64.to_matrix(), Cmx.to_matrix()
+    err = np.linalg.norm(rmx - r64) / np.linalg.norm(r64)
+    print("strassen mixed form", n, bs, nd, err)
+    assert err < {4: 1e-7, 5: 1e-9}[nd], err
