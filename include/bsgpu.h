@@ -50,6 +50,7 @@ typedef struct bsg_ctx_s *bsg_ctx;
 typedef struct bsg_pool_s *bsg_pool;
 typedef struct bsg_bsm_s *bsg_bsm;
 typedef struct bsg_sched_s *bsg_sched;
+typedef struct bsg_batch_plan_s *bsg_batch_plan;
 
 const char *bsg_last_error(void);
 int bsg_version(void);
@@ -142,6 +143,32 @@ bsg_status bsg_matmult_strassen_sparse(bsg_bsm C, bsg_bsm A, int tA, bsg_bsm B, 
                                        double alpha, double beta, size_t min_size_for_strassen);
 bsg_status bsg_matmult_strassen_sparse_form(bsg_bsm C, bsg_bsm A, bsg_bsm B, double thresh,
                                             size_t min_size_for_strassen, int form, int n_digits);
+
+/* ---- batched products (BASELINE config 3; no single counterpart in the
+ *      reference, which calls matmult once per product) ----
+ * C_i = alpha A_i B_i + beta C_i for i < n, each with matmult's semantics
+ * (no transposes), any sizes and block sizes.  Mixed form: products are
+ * grouped by block sizes and each group runs as ONE persistent tensor-core
+ * launch; the tile height and pipeline depth per group shape come from an
+ * autotuner (timed on first use, cached in the context).  nsig_total (may be
+ * NULL) receives the surviving block triples of all products. */
+bsg_status bsg_matmult_batched(size_t n, const bsg_bsm *C, const bsg_bsm *A, const bsg_bsm *B, double thresh,
+                               double alpha, double beta, int form, int n_digits, uint64_t *nsig_total);
+/* A batch (mixed form, beta 0) captured as a CUDA graph: creating the plan
+ * screens, allocates the C blocks, tunes and runs the batch once; each run
+ * replays the device work (digit images, step lists, the persistent launches)
+ * from the operands' current values.  Valid while the operands' block
+ * structure and cached norms are those the plan was made with and the C
+ * blocks stay allocated (no zero / recompress / destroy of C in between). */
+bsg_status bsg_batched_plan_create(size_t n, const bsg_bsm *C, const bsg_bsm *A, const bsg_bsm *B, double thresh,
+                                   double alpha, int n_digits, bsg_batch_plan *out);
+bsg_status bsg_batched_plan_run(bsg_batch_plan plan);
+bsg_status bsg_batched_plan_destroy(bsg_batch_plan plan);
+/* autotuner switch (0 off, 1 on, -1 on and forget the cache) and its cache:
+ * entries of 6 ints (block rows, k and cols padded, digits, slots per tile,
+ * stages, 0 = as many as fit) */
+bsg_status bsg_ctx_set_autotune(bsg_ctx ctx, int on);
+bsg_status bsg_ctx_autotune_entries(bsg_ctx ctx, int *entries, int cap, int *n);
 
 /* ---- learned Strassen scheduling (no counterpart in the reference, whose
  *      choice is the cost model of matmult_strassen_dryrun,

@@ -106,6 +106,13 @@ _sig("bsg_sched_train", [c_vp, c_vp, c_vp, c_int, c_int, c_int, c_flt, C.c_uint6
 _sig("bsg_strassen_root_features", [c_vp, c_vp, c_vp, c_dbl, c_vp, C.POINTER(c_int)])
 _sig("bsg_matmult_strassen_sparse_sched", [c_vp, c_vp, c_vp, c_dbl, c_size, c_int, c_int, c_int, c_vp, c_u64p])
 
+_sig("bsg_matmult_batched", [c_size, c_vp, c_vp, c_vp, c_dbl, c_dbl, c_dbl, c_int, c_int, c_u64p])
+_sig("bsg_batched_plan_create", [c_size, c_vp, c_vp, c_vp, c_dbl, c_dbl, c_int, C.POINTER(c_vp)])
+_sig("bsg_batched_plan_run", [c_vp])
+_sig("bsg_batched_plan_destroy", [c_vp])
+_sig("bsg_ctx_set_autotune", [c_vp, c_int])
+_sig("bsg_ctx_autotune_entries", [c_vp, c_vp, c_int, C.POINTER(c_int)])
+
 SCHED_COST, SCHED_NONE, SCHED_ROOT, SCHED_MLP = 0, 1, 2, 3
 SCHED_FEATURES = 25
 

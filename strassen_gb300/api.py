@@ -81,6 +81,19 @@ class Context:
         check(lib.bsg_ctx_gemm_timing(self.h, C.byref(n), C.byref(ms), C.byref(macs)))
         return n.value, ms.value, macs.value
 
+    def set_autotune(self, on=True, forget=False):
+        """switch the tensor-core GEMM's autotuner on or off (forget: drop its cache)"""
+        check(lib.bsg_ctx_set_autotune(self.h, -1 if forget else int(bool(on))))
+
+    def autotune_entries(self):
+        """cached tuning decisions: (mp, kp, np, digits) -> (slots per tile, stages)"""
+        n = C.c_int()
+        check(lib.bsg_ctx_autotune_entries(self.h, None, 0, C.byref(n)))
+        buf = np.zeros(6 * max(n.value, 1), np.int32)
+        check(lib.bsg_ctx_autotune_entries(self.h, buf.ctypes.data, n.value, C.byref(n)))
+        e = buf[:6 * n.value].reshape(-1, 6)
+        return {tuple(int(x) for x in r[:4]): (int(r[4]), int(r[5])) for r in e}
+
     STALL_KEYS = ("mma_wait_operands", "mma_wait_accumulator", "mma_total", "producer_wait_stage",
                   "epilogue_wait_chain", "epilogue_drain", "epilogue_store", "steps")
 
@@ -290,6 +303,38 @@ def matmult_strassen_sparse(C_, A, tA, B, tB, thresh, alpha, beta, min_size_for_
             raise BsgError(2, "matmult_strassen_sparse supports no transposes and alpha = 1")
         check(lib.bsg_matmult_strassen_sparse_form(C_.h, A.h, B.h, float(thresh), int(min_size_for_strassen), form,
                                                    n_digits))
+
+
+def matmult_batched(Cs, As, Bs, thresh, alpha=1.0, beta=0.0, form=FORM_FP64, n_digits=0):
+    """C_i = alpha A_i B_i + beta C_i for every i (matmult semantics, no
+    transposes); the mixed form runs each block-size group as one persistent
+    tensor-core launch.  Returns the surviving block triples of all products."""
+    assert len(Cs) == len(As) == len(Bs)
+    n = C.c_uint64()
+    check(lib.bsg_matmult_batched(len(Cs), _handles(Cs), _handles(As), _handles(Bs), float(thresh), float(alpha),
+                                  float(beta), form, int(n_digits), C.byref(n)))
+    return n.value
+
+
+class BatchPlan:
+    """A mixed-form batch C_i = alpha A_i B_i captured as a CUDA graph (see
+    bsg_batched_plan_create); run() replays it."""
+
+    def __init__(self, Cs, As, Bs, thresh, alpha=1.0, n_digits=0):
+        self._keep = (list(Cs), list(As), list(Bs))
+        h = C.c_void_p()
+        check(lib.bsg_batched_plan_create(len(Cs), _handles(Cs), _handles(As), _handles(Bs), float(thresh),
+                                          float(alpha), int(n_digits), C.byref(h)))
+        self.h = h
+
+    def run(self):
+        check(lib.bsg_batched_plan_run(self.h))
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h and lib is not None:
+            lib.bsg_batched_plan_destroy(h)
+            self.h = None
 
 
 class StrassenScheduler:

@@ -254,6 +254,73 @@ uint64_t screened_product(bsg_ctx ctx, const std::vector<bsg_bsm> &Cs, const std
     return total;
 }
 
+ScreenItems screen_items(bsg_ctx ctx, bsg_bsm C, bsg_bsm A, int tA, bsg_bsm B, int tB, double thresh, double beta) {
+    BSG_REQUIRE(C && A && B, BSG_ERR_ARG, "NULL matrix");
+    BSG_REQUIRE(A->ctx == ctx && B->ctx == ctx && C->ctx == ctx, BSG_ERR_ARG, "operand on another context");
+    ScreenItems R;
+    ScreenGeom &g = R.g;
+    g.tA = tA;
+    g.tB = tB;
+    g.ni = tA ? A->nc : A->nr;
+    g.nj = tB ? B->nr : B->nc;
+    const size_t nk1 = tA ? A->nr : A->nc, nk2 = tB ? B->nc : B->nr;
+    BSG_REQUIRE(nk1 == nk2, BSG_ERR_ARG, "matmult: inner dimensions do not match");
+    g.nk = nk1;
+    g.ibs = tA ? A->bsc : A->bsr;
+    g.jbs = tB ? B->bsr : B->bsc;
+    const size_t kbs1 = tA ? A->bsr : A->bsc, kbs2 = tB ? B->bsc : B->bsr;
+    BSG_REQUIRE(kbs1 == kbs2, BSG_ERR_ARG, "matmult: inner block sizes do not match");
+    g.kbs = kbs1;
+    BSG_REQUIRE(C->bsr == g.ibs && C->bsc == g.jbs && C->nr == g.ni && C->nc == g.nj, BSG_ERR_ARG,
+                "matmult: output dimensions or block sizes do not match");
+    g.nib = ceil_div(g.ni, g.ibs);
+    g.njb = ceil_div(g.nj, g.jbs);
+    g.nkb = ceil_div(g.nk, g.kbs);
+    g.tpb = thresh * (double)(g.ibs * g.jbs * g.kbs);  // blocksparsematrix.hpp:350
+    cudaStream_t s = ctx->stream;
+    if (beta == 0.0) {  // blocksparsematrix.hpp:299-305
+        BSG_REQUIRE(bsg_bsm_zero(C) == BSG_OK, BSG_ERR_CUDA, bsg_last_error());
+    } else if (beta != 1.0) {
+        BSG_REQUIRE(bsg_bsm_scale(C, beta) == BSG_OK, BSG_ERR_CUDA, bsg_last_error());
+    }
+    const size_t n_out = g.nib * g.njb;
+    if (!n_out || !g.nkb) return R;
+    SliceOps h{A->dptr, A->dnorm, A->nrb, B->dptr, B->dnorm, B->nrb};
+    const uint32_t lo = 0, hi = 1;
+    DevBuf dsl(sizeof(SliceOps), s), dlo(4, s), dhi(4, s), dcount(n_out * 4, s);
+    BSG_CUDA(cudaMemcpyAsync(dsl.p, &h, sizeof(SliceOps), cudaMemcpyHostToDevice, s));
+    BSG_CUDA(cudaMemcpyAsync(dlo.p, &lo, 4, cudaMemcpyHostToDevice, s));
+    BSG_CUDA(cudaMemcpyAsync(dhi.p, &hi, 4, cudaMemcpyHostToDevice, s));
+    k_count<<<(unsigned)ceil_div(n_out, 128), 128, 0, s>>>(dsl.as<SliceOps>(), dlo.as<uint32_t>(), dhi.as<uint32_t>(),
+                                                            g, 1, dcount.as<uint32_t>());
+    ctx->note_launch();
+    ctx->check_launch("pair count");
+    std::vector<uint32_t> cnt(n_out);
+    BSG_CUDA(cudaMemcpyAsync(cnt.data(), dcount.p, n_out * 4, cudaMemcpyDeviceToHost, s));
+    BSG_CUDA(cudaStreamSynchronize(s));
+    bool touched = false;
+    for (size_t x = 0; x < n_out; ++x) {
+        if (!cnt[x]) continue;
+        const size_t ib = x % g.nib, jb = x / g.nib, cbk = ib + jb * C->nrb;
+        GemmItem it;
+        it.fresh = C->hptr[cbk] == nullptr;
+        C->ensure_block(cbk);
+        touched = true;
+        it.c = C->hptr[cbk];
+        it.c_norm = C->dnorm + cbk;
+        it.rows = (int)C->rows_of(ib);
+        it.cols = (int)C->cols_of(jb);
+        it.p0 = (uint32_t)R.total;
+        it.p1 = (uint32_t)(R.total + cnt[x]);
+        R.items.push_back(it);
+        R.item_ib.push_back((uint32_t)ib);
+        R.item_jb.push_back((uint32_t)jb);
+        R.total += cnt[x];
+    }
+    if (touched) C->upload_table();
+    return R;
+}
+
 }  // namespace bsg
 
 using namespace bsg;

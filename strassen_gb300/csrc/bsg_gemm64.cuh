@@ -54,4 +54,16 @@ uint64_t screened_product(bsg_ctx ctx, const std::vector<bsg_bsm> &Cs, const std
                           const std::vector<bsg_bsm> &Bs, int tB, const std::vector<std::pair<size_t, size_t>> &ranges,
                           double thresh, double alpha, double beta, int form, int n_digits);
 
+// Screening of one product C = alpha op(A) op(B) + beta C (single slice):
+// geometry, beta handling, surviving-pair counts, the C blocks that become
+// non-empty (allocated; fresh blocks get their first product assigned) and
+// the output items, column-major block order.
+struct ScreenItems {
+    ScreenGeom g;
+    std::vector<GemmItem> items;
+    std::vector<uint32_t> item_ib, item_jb;
+    uint64_t total = 0;  // surviving block triples
+};
+ScreenItems screen_items(bsg_ctx ctx, bsg_bsm C, bsg_bsm A, int tA, bsg_bsm B, int tB, double thresh, double beta);
+
 }  // namespace bsg

@@ -7,6 +7,8 @@
 #include <cstring>
 #include <memory>
 #include <mutex>
+#include <map>
+#include <array>
 #include <string>
 #include <vector>
 
@@ -98,6 +100,10 @@ struct bsg_ctx_s {
     // once per public call (gemm_check) instead of after every launch
     int *d_gemm_err = nullptr;
     bool gemm_err_pending = false;
+    // autotuned tile height (slots) and pipeline stages of the mixed-form
+    // GEMM per (block rows, block k, block cols, digits)
+    bool autotune = true;
+    std::map<std::array<int, 4>, std::array<int, 2>> oz_tune;
     void note_launch(uint64_t n = 1) { launches += n; }
     void check_launch(const char *what);
     int *gemm_err_flag();  // the device flag, cleared before the first launch of a call

@@ -19,6 +19,7 @@
 // Every mbarrier wait is bounded (2 s); a timeout raises a flag that ends
 // all roles and is returned as BSG_ERR_TIMEOUT.
 #include <algorithm>
+#include <atomic>
 #include <tuple>
 #include <mutex>
 
@@ -423,7 +424,7 @@ static void launch_oz(bsg_ctx ctx, const OzShape &sh, const OzTile *tiles, size_
     P.prof = prof;
     P.zero = static_cast<const bf16 *>(oz_zero_image());
     const uint32_t stage_bytes = oz_stage_bytes(sh);
-    P.S = (int)std::min<uint32_t>(4, kOzSmemBudget / stage_bytes);
+    P.S = (int)std::min<uint32_t>(sh.S > 0 ? (uint32_t)sh.S : 4u, kOzSmemBudget / stage_bytes);
     BSG_REQUIRE(P.S >= 2, BSG_ERR_UNSUPPORTED, "Ozaki tile does not fit shared memory");
     uint32_t cols = 32;  // regions plus the <= 8 overrun columns of a rounded-up N
     while (cols < (uint32_t)sh.nd * NP + 8u) cols <<= 1;
@@ -432,7 +433,15 @@ static void launch_oz(bsg_ctx ctx, const OzShape &sh, const OzTile *tiles, size_
     P.tx_bytes = (uint32_t)sh.R * sh.nd * sh.mp * sh.kp * 2u + (uint32_t)sh.nd * NP * sh.kp * 2u;
     BSG_REQUIRE(cols <= 512, BSG_ERR_UNSUPPORTED, "Ozaki form: digits x padded block columns exceed TMEM");
     const size_t smem = (size_t)P.S * stage_bytes + 32 * sizeof(OzStep) + (2 * P.S + 4) * 8 + 16;
-    BSG_CUDA(cudaFuncSetAttribute(k_ozgemm<NP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    {  // raise the shared-memory limit only when needed (never inside a graph capture)
+        static std::atomic<int> set_to[64];
+        int dev = 0;
+        BSG_CUDA(cudaGetDevice(&dev));
+        if (dev < 0 || dev >= 64 || (int)smem > set_to[dev].load()) {
+            BSG_CUDA(cudaFuncSetAttribute(k_ozgemm<NP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            if (dev >= 0 && dev < 64) set_to[dev].store((int)smem);
+        }
+    }
     const unsigned grid = (unsigned)std::min<size_t>(ceil_div(n_tiles, (size_t)chunk), (size_t)ctx->sm_count);
     BSG_REQUIRE(n_tiles + (size_t)grid * chunk < 0xffffffffull, BSG_ERR_UNSUPPORTED, "too many Ozaki tiles");
     k_ozgemm<NP><<<grid, kOzThreads, smem, s>>>(tiles, (uint32_t)n_tiles, steps, a_img, b_img, P, err);
@@ -588,7 +597,7 @@ __global__ void k_oz_steps(OzTile *__restrict__ tiles, size_t n_tiles, const uin
                            const uint32_t *__restrict__ tile_jb, double *const *__restrict__ A,
                            const double *__restrict__ An, size_t a_nrb, double *const *__restrict__ B,
                            const double *__restrict__ Bn, size_t b_nrb, ScreenGeom g, int R, OzStep *__restrict__ steps,
-                           unsigned long long *__restrict__ macs) {
+                           unsigned long long *__restrict__ macs, uint32_t a_base, uint32_t b_base) {
     const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n_tiles) return;
     const uint32_t jb = tile_jb[t];
@@ -600,7 +609,7 @@ __global__ void k_oz_steps(OzTile *__restrict__ tiles, size_t n_tiles, const uin
         const size_t bi = g.tB ? jb + kb * b_nrb : kb + jb * b_nrb;
         if (!B[bi]) continue;
         OzStep st;
-        st.b = (uint32_t)bi;
+        st.b = b_base + (uint32_t)bi;
         bool any = false;
         for (int s = 0; s < kOzMaxSlots; ++s) {
             st.a[s] = kOzNone;
@@ -610,7 +619,7 @@ __global__ void k_oz_steps(OzTile *__restrict__ tiles, size_t n_tiles, const uin
             const size_t ai = g.tA ? kb + ib * a_nrb : ib + kb * a_nrb;
             if (!A[ai]) continue;
             if (!(__dmul_rn(An[ai], Bn[bi]) >= g.tpb)) continue;
-            st.a[s] = (uint32_t)ai;
+            st.a[s] = a_base + (uint32_t)ai;
             m += (unsigned long long)ext_of(ib, g.ibs, g.ni) * cols * ext_of(kb, g.kbs, g.nk);
             any = true;
         }
@@ -620,94 +629,118 @@ __global__ void k_oz_steps(OzTile *__restrict__ tiles, size_t n_tiles, const uin
     if (m) atomicAdd(macs, m);
 }
 
-void ozaki_screened(bsg_ctx ctx, bsg_bsm C, bsg_bsm A, bsg_bsm B, const ScreenGeom &g, const std::vector<GemmItem> &items,
-                    const std::vector<uint32_t> &item_ib, const std::vector<uint32_t> &item_jb, double alpha,
-                    int n_digits, cudaStream_t s) {
-    if (items.empty()) return;
-    BSG_REQUIRE(g.ibs <= 64 && g.jbs <= 64 && g.kbs <= 64, BSG_ERR_UNSUPPORTED, "Ozaki form supports blocks up to 64");
-    const int nd = oz_default_digits(n_digits, (int)g.ibs, (int)g.kbs, (int)g.jbs);
-    const OzShape sh = oz_shape((int)g.ibs, (int)g.kbs, (int)g.jbs, nd);
-    // exponents and digit images
-    DevBuf rexp(g.nib * g.ibs * 4, s), cexp(g.njb * g.jbs * 4, s);
+void oz_operand_images(bsg_ctx ctx, bsg_bsm A, bsg_bsm B, const ScreenGeom &g, const OzShape &sh, int *rexp,
+                       int *cexp, bf16 *aimg, bf16 *bimg) {
+    cudaStream_t s = ctx->stream;
     k_rowexp_opA<<<(unsigned)g.nib, (unsigned)std::max<size_t>(32, round_up((int)g.ibs, 32)), 0, s>>>(
-        A->dptr, A->nrb, g.tA, g, rexp.as<int>());
+        A->dptr, A->nrb, g.tA, g, rexp);
     k_colexp_opB<<<(unsigned)g.njb, (unsigned)std::max<size_t>(32, round_up((int)g.jbs, 32)), 0, s>>>(
-        B->dptr, B->nrb, g.tB, g, cexp.as<int>());
-    ctx->note_launch(2);
-    const size_t a_plane = (size_t)sh.mp * sh.kp, b_plane = (size_t)sh.np * sh.kp;
-    DevBuf aimg(A->nblocks() * nd * a_plane * 2, s), bimg(B->nblocks() * nd * b_plane * 2, s);
-    k_img_opA<<<oz_img_grid(A->nblocks()), 32 * kOzImgWarps, 0, s>>>(A->dptr, A->nrb, g.tA, g, rexp.as<int>(), sh.mp,
-                                                                     sh.kp, nd, aimg.as<bf16>(), A->nblocks());
-    k_img_opB<<<oz_img_grid(B->nblocks()), 32 * kOzImgWarps, 0, s>>>(B->dptr, B->nrb, g.tB, g, cexp.as<int>(), sh.np,
-                                                                     sh.kp, nd, bimg.as<bf16>(), B->nblocks());
-    ctx->note_launch(2);
+        B->dptr, B->nrb, g.tB, g, cexp);
+    k_img_opA<<<oz_img_grid(A->nblocks()), 32 * kOzImgWarps, 0, s>>>(A->dptr, A->nrb, g.tA, g, rexp, sh.mp, sh.kp,
+                                                                     sh.nd, aimg, A->nblocks());
+    k_img_opB<<<oz_img_grid(B->nblocks()), 32 * kOzImgWarps, 0, s>>>(B->dptr, B->nrb, g.tB, g, cexp, sh.np, sh.kp,
+                                                                     sh.nd, bimg, B->nblocks());
+    ctx->note_launch(4);
     ctx->check_launch("ozaki split");
-    // tiles: up to R consecutive output blocks of one block column
+}
+
+void oz_build_tiles(bsg_ctx ctx, const ScreenItems &si, const OzShape &sh, const int *rexp, const int *cexp,
+                    uint32_t step_base, bool all_fresh, double *scratch, OzTilePlan &out) {
+    const ScreenGeom &g = si.g;
+    const auto &items = si.items;
     std::vector<OzTile> tiles;
     std::vector<uint32_t> tib, tjb;
     size_t i = 0;
+    size_t slot_no = 0;
+    const size_t blk_elems = g.ibs * g.jbs;
     while (i < items.size()) {
         OzTile T;
         std::memset(&T, 0, sizeof(T));
-        const uint32_t jb = item_jb[i];
-        T.cexp = cexp.as<int>() + jb * g.jbs;
+        const uint32_t jb = si.item_jb[i];
+        T.cexp = cexp + jb * g.jbs;
         T.cols = items[i].cols;
-        size_t base = tib.size();
+        const size_t base = tib.size();
         tib.resize(base + kOzMaxSlots, kOzNone);
         int sl = 0;
-        while (i < items.size() && item_jb[i] == jb && sl < sh.R) {
-            T.c[sl] = items[i].c;
-            T.cnorm[sl] = items[i].c_norm;
+        while (i < items.size() && si.item_jb[i] == jb && sl < sh.R) {
+            // scratch (autotuning trials): every slot writes its own scratch block
+            T.c[sl] = scratch ? scratch + (slot_no++) * blk_elems : items[i].c;
+            T.cnorm[sl] = scratch ? nullptr : items[i].c_norm;
             T.rows[sl] = items[i].rows;
             T.ldc[sl] = items[i].rows;
-            T.rexp[sl] = rexp.as<int>() + item_ib[i] * g.ibs;
-            if (items[i].fresh) T.fresh_mask |= 1u << sl;
-            tib[base + sl] = item_ib[i];
+            T.rexp[sl] = rexp + si.item_ib[i] * g.ibs;
+            if (items[i].fresh || all_fresh || scratch) T.fresh_mask |= 1u << sl;
+            tib[base + sl] = si.item_ib[i];
             ++sl;
             ++i;
         }
-        T.s0 = (uint32_t)(tiles.size() * g.nkb);
         T.ns = 0;
         tiles.push_back(T);
         tjb.push_back(jb);
     }
     // super-tile order (Gr row groups x Gc block columns) keeps the digit
     // images of concurrently running tiles in L2
-    {
-        const size_t Gr = 8, Gc = std::max<size_t>(1, 2 * (size_t)ctx->sm_count / Gr);
-        std::vector<size_t> idx(tiles.size());
-        for (size_t t = 0; t < idx.size(); ++t) idx[t] = t;
-        auto key = [&](size_t t) {
-            const size_t rg = tib[t * kOzMaxSlots] / (size_t)sh.R, jb = tjb[t];
-            return std::make_tuple(rg / Gr, jb / Gc, rg % Gr, jb % Gc, rg, t);
-        };
-        std::sort(idx.begin(), idx.end(), [&](size_t a, size_t b) { return key(a) < key(b); });
-        std::vector<OzTile> t2(tiles.size());
-        std::vector<uint32_t> ib2(tib.size()), jb2(tjb.size());
-        for (size_t n = 0; n < idx.size(); ++n) {
-            t2[n] = tiles[idx[n]];
-            t2[n].s0 = (uint32_t)(n * g.nkb);
-            std::copy(tib.begin() + idx[n] * kOzMaxSlots, tib.begin() + (idx[n] + 1) * kOzMaxSlots,
-                      ib2.begin() + n * kOzMaxSlots);
-            jb2[n] = tjb[idx[n]];
-        }
-        tiles.swap(t2);
-        tib.swap(ib2);
-        tjb.swap(jb2);
+    const size_t Gr = 8, Gc = std::max<size_t>(1, 2 * (size_t)ctx->sm_count / Gr);
+    std::vector<size_t> idx(tiles.size());
+    for (size_t t = 0; t < idx.size(); ++t) idx[t] = t;
+    auto key = [&](size_t t) {
+        const size_t rg = tib[t * kOzMaxSlots] / (size_t)sh.R, jb = tjb[t];
+        return std::make_tuple(rg / Gr, jb / Gc, rg % Gr, jb % Gc, rg, t);
+    };
+    std::sort(idx.begin(), idx.end(), [&](size_t a, size_t b) { return key(a) < key(b); });
+    const size_t t0 = out.tiles.size();
+    out.tiles.resize(t0 + tiles.size());
+    out.tib.resize((t0 + tiles.size()) * kOzMaxSlots);
+    out.tjb.resize(t0 + tiles.size());
+    for (size_t n = 0; n < idx.size(); ++n) {
+        out.tiles[t0 + n] = tiles[idx[n]];
+        out.tiles[t0 + n].s0 = step_base + (uint32_t)(n * g.nkb);
+        std::copy(tib.begin() + idx[n] * kOzMaxSlots, tib.begin() + (idx[n] + 1) * kOzMaxSlots,
+                  out.tib.begin() + (t0 + n) * kOzMaxSlots);
+        out.tjb[t0 + n] = tjb[idx[n]];
     }
-    BSG_REQUIRE(tiles.size() * g.nkb < 0xffffffffull, BSG_ERR_UNSUPPORTED, "too many Ozaki steps in one call");
-    DevBuf dt(tiles.size() * sizeof(OzTile), s), dib(tib.size() * 4, s), djb(tjb.size() * 4, s),
-        dst(tiles.size() * g.nkb * sizeof(OzStep), s), dmacs(8, s);
-    BSG_CUDA(cudaMemsetAsync(dmacs.p, 0, 8, s));
-    BSG_CUDA(cudaMemcpyAsync(dt.p, tiles.data(), tiles.size() * sizeof(OzTile), cudaMemcpyHostToDevice, s));
-    BSG_CUDA(cudaMemcpyAsync(dib.p, tib.data(), tib.size() * 4, cudaMemcpyHostToDevice, s));
-    BSG_CUDA(cudaMemcpyAsync(djb.p, tjb.data(), tjb.size() * 4, cudaMemcpyHostToDevice, s));
-    k_oz_steps<<<(unsigned)ceil_div(tiles.size(), 128), 128, 0, s>>>(
-        dt.as<OzTile>(), tiles.size(), dib.as<uint32_t>(), djb.as<uint32_t>(), A->dptr, A->dnorm, A->nrb, B->dptr,
-        B->dnorm, B->nrb, g, sh.R, dst.as<OzStep>(), dmacs.as<unsigned long long>());
+}
+
+void oz_launch_steps(bsg_ctx ctx, OzTile *d_tiles, size_t n_tiles, const uint32_t *d_tib, const uint32_t *d_tjb,
+                     bsg_bsm A, bsg_bsm B, const ScreenGeom &g, int R, OzStep *d_steps, unsigned long long *d_macs,
+                     uint32_t a_base, uint32_t b_base) {
+    if (!n_tiles) return;
+    k_oz_steps<<<(unsigned)ceil_div(n_tiles, 128), 128, 0, ctx->stream>>>(d_tiles, n_tiles, d_tib, d_tjb, A->dptr,
+                                                                          A->dnorm, A->nrb, B->dptr, B->dnorm, B->nrb,
+                                                                          g, R, d_steps, d_macs, a_base, b_base);
     ctx->note_launch();
     ctx->check_launch("ozaki steps");
-    oz_run(ctx, sh, dt.as<OzTile>(), tiles.size(), dst.as<OzStep>(), aimg.as<bf16>(), bimg.as<bf16>(), alpha, s,
+}
+
+void ozaki_screened(bsg_ctx ctx, bsg_bsm C, bsg_bsm A, bsg_bsm B, const ScreenGeom &g, const std::vector<GemmItem> &items,
+                    const std::vector<uint32_t> &item_ib, const std::vector<uint32_t> &item_jb, double alpha,
+                    int n_digits, cudaStream_t s) {
+    if (items.empty()) return;
+    (void)C;
+    BSG_REQUIRE(g.ibs <= 64 && g.jbs <= 64 && g.kbs <= 64, BSG_ERR_UNSUPPORTED, "Ozaki form supports blocks up to 64");
+    const int nd = oz_default_digits(n_digits, (int)g.ibs, (int)g.kbs, (int)g.jbs);
+    const OzShape sh = oz_shape((int)g.ibs, (int)g.kbs, (int)g.jbs, nd);
+    DevBuf rexp(g.nib * g.ibs * 4, s), cexp(g.njb * g.jbs * 4, s);
+    DevBuf aimg(A->nblocks() * nd * (size_t)sh.mp * sh.kp * 2, s), bimg(B->nblocks() * nd * (size_t)sh.np * sh.kp * 2, s);
+    oz_operand_images(ctx, A, B, g, sh, rexp.as<int>(), cexp.as<int>(), aimg.as<bf16>(), bimg.as<bf16>());
+    ScreenItems si;
+    si.g = g;
+    si.items = items;
+    si.item_ib = item_ib;
+    si.item_jb = item_jb;
+    OzTilePlan tp;
+    oz_build_tiles(ctx, si, sh, rexp.as<int>(), cexp.as<int>(), 0, false, nullptr, tp);
+    const size_t n_tiles = tp.tiles.size();
+    BSG_REQUIRE(n_tiles * g.nkb < 0xffffffffull, BSG_ERR_UNSUPPORTED, "too many Ozaki steps in one call");
+    DevBuf dt(n_tiles * sizeof(OzTile), s), dib(tp.tib.size() * 4, s), djb(tp.tjb.size() * 4, s),
+        dst(n_tiles * g.nkb * sizeof(OzStep), s), dmacs(8, s);
+    BSG_CUDA(cudaMemsetAsync(dmacs.p, 0, 8, s));
+    BSG_CUDA(cudaMemcpyAsync(dt.p, tp.tiles.data(), n_tiles * sizeof(OzTile), cudaMemcpyHostToDevice, s));
+    BSG_CUDA(cudaMemcpyAsync(dib.p, tp.tib.data(), tp.tib.size() * 4, cudaMemcpyHostToDevice, s));
+    BSG_CUDA(cudaMemcpyAsync(djb.p, tp.tjb.data(), tp.tjb.size() * 4, cudaMemcpyHostToDevice, s));
+    oz_launch_steps(ctx, dt.as<OzTile>(), n_tiles, dib.as<uint32_t>(), djb.as<uint32_t>(), A, B, g, sh.R,
+                    dst.as<OzStep>(), dmacs.as<unsigned long long>(), 0, 0);
+    oz_run(ctx, sh, dt.as<OzTile>(), n_tiles, dst.as<OzStep>(), aimg.as<bf16>(), bimg.as<bf16>(), alpha, s,
            dmacs.as<unsigned long long>());
     ctx->gemm_check();
 }

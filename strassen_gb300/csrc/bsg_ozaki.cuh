@@ -34,6 +34,7 @@ struct OzShape {
     int R;   // slots per 128-row tile
     int nd;  // digits per operand
     int F;   // steps per exact chain (512 / kp)
+    int S = 0;  // pipeline stages (0: as many as fit, at most 4)
 };
 OzShape oz_shape(int bs_rows, int bs_k, int bs_cols, int nd);
 // digits to use: `requested` (validated) or, for 0, 5 where it fits else 4
@@ -65,6 +66,27 @@ struct OzStep {
 void oz_run(bsg_ctx ctx, const OzShape &sh, const OzTile *d_tiles, size_t n_tiles, const OzStep *d_steps,
             const __nv_bfloat16 *a_img, const __nv_bfloat16 *b_img, double alpha, cudaStream_t s,
             const unsigned long long *d_macs = nullptr, uint32_t chunk = 1);
+
+// ---- building blocks of a mixed-form screened product ----
+// row exponents of op(A), column exponents of op(B) and their digit images
+// (one image per stored block, at the block's table index)
+void oz_operand_images(bsg_ctx ctx, bsg_bsm A, bsg_bsm B, const ScreenGeom &g, const OzShape &sh, int *rexp,
+                       int *cexp, __nv_bfloat16 *aimg, __nv_bfloat16 *bimg);
+// host tile lists (tile, slot block rows, block column) appended to a plan
+struct OzTilePlan {
+    std::vector<OzTile> tiles;
+    std::vector<uint32_t> tib, tjb;
+};
+// Tiles of up to sh.R items of one block column, in super-tile order; step
+// ranges start at step_base (nkb per tile).  all_fresh: every item overwrites
+// its block; scratch (may be null): slots write consecutive scratch blocks
+// instead of C (autotuning trials).
+void oz_build_tiles(bsg_ctx ctx, const ScreenItems &si, const OzShape &sh, const int *rexp, const int *cexp,
+                    uint32_t step_base, bool all_fresh, double *scratch, OzTilePlan &out);
+// steps of every tile (the FP64 form's screen), image indices offset by the bases
+void oz_launch_steps(bsg_ctx ctx, OzTile *d_tiles, size_t n_tiles, const uint32_t *d_tib, const uint32_t *d_tjb,
+                     bsg_bsm A, bsg_bsm B, const ScreenGeom &g, int R, OzStep *d_steps, unsigned long long *d_macs,
+                     uint32_t a_base, uint32_t b_base);
 
 // Ozaki form of one screened product (single slice): same screening and C
 // block bookkeeping as the FP64 form; items come from screened_product.
