@@ -515,50 +515,6 @@ __device__ __forceinline__ int ext_of(size_t blk, size_t bs, size_t n) {
     return (int)(((blk + 1) * bs <= n) ? bs : n - blk * bs);
 }
 
-// exponent of the largest |op(A)(r, :)| of each row of op(A), block row ib
-__global__ void k_rowexp_opA(double *const *__restrict__ tab, size_t a_nrb, int tA, ScreenGeom g, int *__restrict__ rexp) {
-    const size_t ib = blockIdx.x;
-    const int r = threadIdx.x;
-    if (r >= (int)g.ibs) return;
-    const int rows = ext_of(ib, g.ibs, g.ni);
-    long long mx = 0;
-    if (r < rows) {
-        for (size_t kb = 0; kb < g.nkb; ++kb) {
-            const double *blk = tA ? tab[kb + ib * a_nrb] : tab[ib + kb * a_nrb];
-            if (!blk) continue;
-            const int k = ext_of(kb, g.kbs, g.nk);
-            const int ld = tA ? k : rows;
-            for (int l = 0; l < k; ++l) {
-                const long long b = oz_absbits(tA ? blk[l + (size_t)r * ld] : blk[r + (size_t)l * ld]);
-                mx = b > mx ? b : mx;
-            }
-        }
-    }
-    rexp[ib * g.ibs + r] = oz_exp_of_bits(mx);
-}
-
-// exponent of the largest |op(B)(:, c)| of each column of op(B), block column jb
-__global__ void k_colexp_opB(double *const *__restrict__ tab, size_t b_nrb, int tB, ScreenGeom g, int *__restrict__ cexp) {
-    const size_t jb = blockIdx.x;
-    const int c = threadIdx.x;
-    if (c >= (int)g.jbs) return;
-    const int cols = ext_of(jb, g.jbs, g.nj);
-    long long mx = 0;
-    if (c < cols) {
-        for (size_t kb = 0; kb < g.nkb; ++kb) {
-            const double *blk = tB ? tab[jb + kb * b_nrb] : tab[kb + jb * b_nrb];
-            if (!blk) continue;
-            const int k = ext_of(kb, g.kbs, g.nk);
-            const int ld = tB ? cols : k;
-            for (int l = 0; l < k; ++l) {
-                const long long b = oz_absbits(tB ? blk[c + (size_t)l * ld] : blk[l + (size_t)c * ld]);
-                mx = b > mx ? b : mx;
-            }
-        }
-    }
-    cexp[jb * g.jbs + c] = oz_exp_of_bits(mx);
-}
-
 // digit image of op(A) block (ib, kb) stored at table index b (rows x k,
 // padded to mp x kp)
 __global__ void k_img_opA(double *const *__restrict__ tab, size_t a_nrb, int tA, ScreenGeom g,
@@ -629,13 +585,66 @@ __global__ void k_oz_steps(OzTile *__restrict__ tiles, size_t n_tiles, const uin
     if (m) atomicAdd(macs, m);
 }
 
+// Row maxima of |op(A)| as bit patterns (non-negative doubles order like
+// their bits), one warp per stored block, atomicMax into rowbits[row]
+__global__ void k_rowmax_opA(double *const *__restrict__ tab, size_t nblk, size_t a_nrb, int tA, ScreenGeom g,
+                             unsigned long long *__restrict__ rowbits) {
+    const size_t b = oz_warp_id();
+    if (b >= nblk) return;
+    const double *blk = tab[b];
+    if (!blk) return;
+    const size_t sr = b % a_nrb, sc = b / a_nrb;
+    const size_t ib = tA ? sc : sr, kb = tA ? sr : sc;
+    const int rows = ext_of(ib, g.ibs, g.ni), k = ext_of(kb, g.kbs, g.nk);
+    const int ld = tA ? k : rows;
+    for (int r = threadIdx.x & 31; r < rows; r += 32) {
+        long long mx = 0;
+        for (int l = 0; l < k; ++l) {
+            const long long v = oz_absbits(tA ? blk[l + (size_t)r * ld] : blk[r + (size_t)l * ld]);
+            mx = v > mx ? v : mx;
+        }
+        if (mx) atomicMax(&rowbits[ib * g.ibs + r], (unsigned long long)mx);
+    }
+}
+
+// column maxima of |op(B)|, one warp per stored block
+__global__ void k_colmax_opB(double *const *__restrict__ tab, size_t nblk, size_t b_nrb, int tB, ScreenGeom g,
+                             unsigned long long *__restrict__ colbits) {
+    const size_t b = oz_warp_id();
+    if (b >= nblk) return;
+    const double *blk = tab[b];
+    if (!blk) return;
+    const size_t sr = b % b_nrb, sc = b / b_nrb;
+    const size_t kb = tB ? sc : sr, jb = tB ? sr : sc;
+    const int cols = ext_of(jb, g.jbs, g.nj), k = ext_of(kb, g.kbs, g.nk);
+    const int ld = tB ? cols : k;
+    for (int c = threadIdx.x & 31; c < cols; c += 32) {
+        long long mx = 0;
+        for (int l = 0; l < k; ++l) {
+            const long long v = oz_absbits(tB ? blk[c + (size_t)l * ld] : blk[l + (size_t)c * ld]);
+            mx = v > mx ? v : mx;
+        }
+        if (mx) atomicMax(&colbits[jb * g.jbs + c], (unsigned long long)mx);
+    }
+}
+
+__global__ void k_bits_to_exp(const unsigned long long *__restrict__ bits, size_t n, int *__restrict__ exps) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) exps[i] = oz_exp_of_bits((long long)bits[i]);
+}
+
 void oz_operand_images(bsg_ctx ctx, bsg_bsm A, bsg_bsm B, const ScreenGeom &g, const OzShape &sh, int *rexp,
                        int *cexp, bf16 *aimg, bf16 *bimg) {
     cudaStream_t s = ctx->stream;
-    k_rowexp_opA<<<(unsigned)g.nib, (unsigned)std::max<size_t>(32, round_up((int)g.ibs, 32)), 0, s>>>(
-        A->dptr, A->nrb, g.tA, g, rexp);
-    k_colexp_opB<<<(unsigned)g.njb, (unsigned)std::max<size_t>(32, round_up((int)g.jbs, 32)), 0, s>>>(
-        B->dptr, B->nrb, g.tB, g, cexp);
+    const size_t nr = g.nib * g.ibs, nc = g.njb * g.jbs;
+    DevBuf bits((nr + nc) * 8, s);
+    auto *rb = bits.as<unsigned long long>(), *cb = rb + nr;
+    BSG_CUDA(cudaMemsetAsync(bits.p, 0, (nr + nc) * 8, s));
+    k_rowmax_opA<<<oz_img_grid(A->nblocks()), 32 * kOzImgWarps, 0, s>>>(A->dptr, A->nblocks(), A->nrb, g.tA, g, rb);
+    k_colmax_opB<<<oz_img_grid(B->nblocks()), 32 * kOzImgWarps, 0, s>>>(B->dptr, B->nblocks(), B->nrb, g.tB, g, cb);
+    if (nr) k_bits_to_exp<<<(unsigned)ceil_div(nr, (size_t)256), 256, 0, s>>>(rb, nr, rexp);
+    if (nc) k_bits_to_exp<<<(unsigned)ceil_div(nc, (size_t)256), 256, 0, s>>>(cb, nc, cexp);
+    ctx->note_launch(2);
     k_img_opA<<<oz_img_grid(A->nblocks()), 32 * kOzImgWarps, 0, s>>>(A->dptr, A->nrb, g.tA, g, rexp, sh.mp, sh.kp,
                                                                      sh.nd, aimg, A->nblocks());
     k_img_opB<<<oz_img_grid(B->nblocks()), 32 * kOzImgWarps, 0, s>>>(B->dptr, B->nrb, g.tB, g, cexp, sh.np, sh.kp,

@@ -101,27 +101,6 @@ __global__ void k_unorms_c(const double *__restrict__ ints, const int *__restric
     }
 }
 
-// U_p row exponents over present blocks; grid (p, a), one thread per row
-__global__ void k_rexp_U_c(const double *__restrict__ ints, const int *__restrict__ inv, size_t n_vec2, size_t P0,
-                           const uint8_t *__restrict__ uflag, size_t n_bf, size_t bs, size_t nb, int *__restrict__ rexp) {
-    const size_t p = blockIdx.x / nb, a = blockIdx.x % nb;
-    const int r = threadIdx.x, rows = ext_r(a, bs, n_bf);
-    if (r >= rows) return;
-    const double *col = ints + (P0 + p) * n_vec2;
-    long long mx = 0;
-    for (size_t b = 0; b < nb; ++b) {
-        if (!uflag[p * nb * nb + a + b * nb]) continue;
-        const int k = ext_r(b, bs, n_bf);
-        for (int l = 0; l < k; ++l) {
-            const int v = inv[a * bs + r + (b * bs + l) * n_bf];
-            if (v < 0) continue;
-            const long long bb_ = oz_absbits(col[v]);
-            mx = bb_ > mx ? bb_ : mx;
-        }
-    }
-    rexp[p * n_bf + a * bs + r] = oz_exp_of_bits(mx);
-}
-
 // columns of C over every row; grid jb
 __global__ void k_cexp_C(const double *__restrict__ C, size_t n_bf, size_t n_occ, size_t bs, int *__restrict__ cexp) {
     const size_t jb = blockIdx.x;
@@ -132,57 +111,89 @@ __global__ void k_cexp_C(const double *__restrict__ C, size_t n_bf, size_t n_occ
     cexp[jb * bs + c] = oz_exp_of_bits(mx);
 }
 
-// columns of mui_p over present blocks; grid (p, jb)
-__global__ void k_cexp_mui(const double *__restrict__ mui, const uint8_t *__restrict__ mflag, size_t n_bf,
-                           size_t n_occ, size_t bs, size_t nb, size_t nob, int *__restrict__ cexp) {
-    const size_t p = blockIdx.x / nob, jb = blockIdx.x % nob;
-    const int c = threadIdx.x;
-    if (c >= ext_r(jb, bs, n_occ)) return;
-    const double *M = mui + p * n_bf * n_occ;
-    long long mx = 0;
-    for (size_t a = 0; a < nb; ++a) {
-        if (!mflag[p * nb * nob + a + jb * nb]) continue;
-        const int rows = ext_r(a, bs, n_bf);
-        for (int r = 0; r < rows; ++r) { const long long bb_ = oz_absbits(M[a * bs + r + (jb * bs + c) * n_bf]); mx = bb_ > mx ? bb_ : mx; }
+// ---- row / column maxima, one warp per present block ----
+// Bit patterns of |x| (non-negative doubles order like their bits) are
+// combined with atomicMax; the exponents follow from the maxima.
+
+__global__ void k_bits_exp(const unsigned long long *__restrict__ bits, size_t n, int *__restrict__ exps) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) exps[i] = oz_exp_of_bits((long long)bits[i]);
+}
+
+// rows of U_p over its present blocks, gathered from the compressed integrals
+__global__ void k_rowmax_U_c(const double *__restrict__ ints, const int *__restrict__ inv, size_t n_vec2, size_t P0,
+                             const uint8_t *__restrict__ uflag, size_t n_bf, size_t bs, size_t nb, size_t n,
+                             unsigned long long *__restrict__ bits) {
+    const size_t x = oz_warp_id();
+    if (x >= n || !uflag[x]) return;
+    const size_t p = x / (nb * nb), a = x % nb, b = (x / nb) % nb;
+    const int rows = ext_r(a, bs, n_bf), k = ext_r(b, bs, n_bf);
+    const double *col = ints + (P0 + p) * n_vec2;
+    for (int r = threadIdx.x & 31; r < rows; r += 32) {
+        long long mx = 0;
+        for (int l = 0; l < k; ++l) {
+            const int v = inv[a * bs + r + (b * bs + l) * n_bf];
+            if (v < 0) continue;
+            const long long bb_ = oz_absbits(col[v]);
+            mx = bb_ > mx ? bb_ : mx;
+        }
+        if (mx) atomicMax(&bits[p * n_bf + a * bs + r], (unsigned long long)mx);
     }
-    cexp[p * n_occ + jb * bs + c] = oz_exp_of_bits(mx);
 }
 
-// rows of mui over (p in sub-range, i); grid (sub, a)
-__global__ void k_rexp_mui_sub(const double *__restrict__ mui, const uint8_t *__restrict__ mflag, size_t n_bf,
-                               size_t n_occ, size_t bs, size_t nb, size_t nob, size_t np, size_t Q,
-                               int *__restrict__ rexp) {
-    const size_t sub = blockIdx.x / nb, a = blockIdx.x % nb;
-    const int r = threadIdx.x;
-    if (r >= ext_r(a, bs, n_bf)) return;
-    long long mx = 0;
-    const size_t p1 = min(np, (sub + 1) * Q);
-    for (size_t p = sub * Q; p < p1; ++p)
-        for (size_t ib = 0; ib < nob; ++ib) {
-            if (!mflag[p * nb * nob + a + ib * nb]) continue;
-            const double *M = mui + p * n_bf * n_occ;
-            const int k = ext_r(ib, bs, n_occ);
-            for (int l = 0; l < k; ++l) { const long long bb_ = oz_absbits(M[a * bs + r + (ib * bs + l) * n_bf]); mx = bb_ > mx ? bb_ : mx; }
+// columns of mui_p (per p) over its present blocks
+__global__ void k_colmax_mui(const double *__restrict__ mui, const uint8_t *__restrict__ mflag, size_t n_bf,
+                             size_t n_occ, size_t bs, size_t nb, size_t nob, size_t n, unsigned long long *__restrict__ bits) {
+    const size_t x = oz_warp_id();
+    if (x >= n || !mflag[x]) return;
+    const size_t p = x / (nb * nob), a = x % nb, jb = (x / nb) % nob;
+    const int rows = ext_r(a, bs, n_bf), cols = ext_r(jb, bs, n_occ);
+    const double *M = mui + p * n_bf * n_occ;
+    for (int c = threadIdx.x & 31; c < cols; c += 32) {
+        long long mx = 0;
+        for (int r = 0; r < rows; ++r) {
+            const long long bb_ = oz_absbits(M[a * bs + r + (jb * bs + c) * n_bf]);
+            mx = bb_ > mx ? bb_ : mx;
         }
-    rexp[sub * n_bf + a * bs + r] = oz_exp_of_bits(mx);
+        if (mx) atomicMax(&bits[p * n_occ + jb * bs + c], (unsigned long long)mx);
+    }
 }
 
-// columns of ijs over (p in sub-range, i); grid (sub, jb)
-__global__ void k_cexp_ijs_sub(const double *__restrict__ ijs, const uint8_t *__restrict__ sflag, size_t n_occ,
-                               size_t bs, size_t nob, size_t np, size_t Q, int *__restrict__ cexp) {
-    const size_t sub = blockIdx.x / nob, jb = blockIdx.x % nob;
-    const int c = threadIdx.x;
-    if (c >= ext_r(jb, bs, n_occ)) return;
-    long long mx = 0;
-    const size_t p1 = min(np, (sub + 1) * Q);
-    for (size_t p = sub * Q; p < p1; ++p)
-        for (size_t ib = 0; ib < nob; ++ib) {
-            if (!sflag[p * nob * nob + ib + jb * nob]) continue;
-            const double *S = ijs + p * n_occ * n_occ;
-            const int k = ext_r(ib, bs, n_occ);
-            for (int l = 0; l < k; ++l) { const long long bb_ = oz_absbits(S[ib * bs + l + (jb * bs + c) * n_occ]); mx = bb_ > mx ? bb_ : mx; }
+// rows of mui over the aux sub-range p / Q
+__global__ void k_rowmax_mui_sub(const double *__restrict__ mui, const uint8_t *__restrict__ mflag, size_t n_bf,
+                                 size_t n_occ, size_t bs, size_t nb, size_t nob, size_t Q, size_t n,
+                                 unsigned long long *__restrict__ bits) {
+    const size_t x = oz_warp_id();
+    if (x >= n || !mflag[x]) return;
+    const size_t p = x / (nb * nob), a = x % nb, ib = (x / nb) % nob;
+    const int rows = ext_r(a, bs, n_bf), k = ext_r(ib, bs, n_occ);
+    const double *M = mui + p * n_bf * n_occ;
+    for (int r = threadIdx.x & 31; r < rows; r += 32) {
+        long long mx = 0;
+        for (int l = 0; l < k; ++l) {
+            const long long bb_ = oz_absbits(M[a * bs + r + (ib * bs + l) * n_bf]);
+            mx = bb_ > mx ? bb_ : mx;
         }
-    cexp[sub * n_occ + jb * bs + c] = oz_exp_of_bits(mx);
+        if (mx) atomicMax(&bits[(p / Q) * n_bf + a * bs + r], (unsigned long long)mx);
+    }
+}
+
+// columns of ijs over the aux sub-range p / Q
+__global__ void k_colmax_ijs_sub(const double *__restrict__ ijs, const uint8_t *__restrict__ sflag, size_t n_occ,
+                                 size_t bs, size_t nob, size_t Q, size_t n, unsigned long long *__restrict__ bits) {
+    const size_t x = oz_warp_id();
+    if (x >= n || !sflag[x]) return;
+    const size_t p = x / (nob * nob), ib = x % nob, jb = (x / nob) % nob;
+    const int k = ext_r(ib, bs, n_occ), cols = ext_r(jb, bs, n_occ);
+    const double *S = ijs + p * n_occ * n_occ;
+    for (int c = threadIdx.x & 31; c < cols; c += 32) {
+        long long mx = 0;
+        for (int l = 0; l < k; ++l) {
+            const long long bb_ = oz_absbits(S[ib * bs + l + (jb * bs + c) * n_occ]);
+            mx = bb_ > mx ? bb_ : mx;
+        }
+        if (mx) atomicMax(&bits[(p / Q) * n_occ + jb * bs + c], (unsigned long long)mx);
+    }
 }
 
 // ---- digit images ----
@@ -504,6 +515,11 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, uint64_t stats[5]) {
     DevBuf drexpU(pc * n_bf * 4, s), dimgU(pc * nb * nb * a_img * 2, s);
     DevBuf dcexpM(pc * n_occ * 4, s), dimgMB(pc * nb * nob * b_img * 2, s);
     DevBuf drexpMs(n_sub_max * n_bf * 4, s), dcexpSs(n_sub_max * n_occ * 4, s);
+    // maxima bit patterns for the four exponent sets of a chunk
+    const size_t nbits = pc * n_bf + pc * n_occ + n_sub_max * n_bf + n_sub_max * n_occ;
+    DevBuf dbits(nbits * 8, s);
+    auto *bitsU = dbits.as<unsigned long long>(), *bitsM = bitsU + pc * n_bf, *bitsMs = bitsM + pc * n_occ,
+         *bitsSs = bitsMs + n_sub_max * n_bf;
     DevBuf dimgMA(pc * nb * nob * a_img * 2, s), dimgSB(pc * nob * nob * b_img * 2, s);
     DevBuf dKp(n_sub_max * nob * nb * bs * bs * 8, s), dcnt(5 * 8, s), dmacs(3 * 8, s);
     const size_t ng_a = ceil_div(nb, (size_t)D.R), ng_i = ceil_div(nob, (size_t)D.R);
@@ -541,8 +557,10 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, uint64_t stats[5]) {
             d.ints, dinv.as<int>(), docc.as<uint8_t>(), d.n_vec2, P0, n_bf, bs, nb, np, tpb_u, dun.as<double>(),
             duf.as<uint8_t>());
         // mui = U C
-        k_rexp_U_c<<<(unsigned)(np * nb), tb, 0, s>>>(d.ints, dinv.as<int>(), d.n_vec2, P0, duf.as<uint8_t>(), n_bf, bs,
-                                                      nb, drexpU.as<int>());
+        BSG_CUDA(cudaMemsetAsync(dbits.p, 0, nbits * 8, s));
+        k_rowmax_U_c<<<oz_img_grid(np * nb * nb), 32 * kOzImgWarps, 0, s>>>(
+            d.ints, dinv.as<int>(), d.n_vec2, P0, duf.as<uint8_t>(), n_bf, bs, nb, np * nb * nb, bitsU);
+        k_bits_exp<<<(unsigned)ceil_div(np * n_bf, (size_t)256), 256, 0, s>>>(bitsU, np * n_bf, drexpU.as<int>());
         k_img_U<<<oz_img_grid(np * nb * nb), 32 * kOzImgWarps, 0, s>>>(d.ints, dinv.as<int>(), d.n_vec2, P0,
                                                                        duf.as<uint8_t>(), drexpU.as<int>(), D,
                                                                        np * nb * nb, dimgU.as<bf16>());
@@ -550,31 +568,36 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, uint64_t stats[5]) {
         k_tiles_mui<<<(unsigned)ceil_div(tm, 128), 128, 0, s>>>(
             duf.as<uint8_t>(), dun.as<double>(), dcn.as<double>(), drexpU.as<int>(), dcexpC.as<int>(),
             dmui.as<double>(), D, tm, tpb, dtm.as<OzTile>(), dsm.as<OzStep>(), dmf.as<uint8_t>(), cnt + 0, macs + 0);
-        ctx->note_launch(4);
+        ctx->note_launch(5);
         ctx->check_launch("rik ozaki mui prep");
         oz_run(ctx, sh, dtm.as<OzTile>(), tm, dsm.as<OzStep>(), dimgU.as<bf16>(), dimgCB.as<bf16>(), 1.0, s, macs + 0);
         k_mui_norms<<<(unsigned)ceil_div(np * nb * nob, wpb), wpb * 32, 0, s>>>(
             dmui.as<double>(), dmf.as<uint8_t>(), n_bf, n_occ, bs, nb, nob, np * nb * nob, dmn.as<double>());
         // ij = C^T mui
-        k_cexp_mui<<<(unsigned)(np * nob), tb, 0, s>>>(dmui.as<double>(), dmf.as<uint8_t>(), n_bf, n_occ, bs, nb, nob,
-                                                       dcexpM.as<int>());
+        k_colmax_mui<<<oz_img_grid(np * nb * nob), 32 * kOzImgWarps, 0, s>>>(
+            dmui.as<double>(), dmf.as<uint8_t>(), n_bf, n_occ, bs, nb, nob, np * nb * nob, bitsM);
+        k_bits_exp<<<(unsigned)ceil_div(np * n_occ, (size_t)256), 256, 0, s>>>(bitsM, np * n_occ, dcexpM.as<int>());
         k_img_mui_B<<<oz_img_grid(np * nb * nob), 32 * kOzImgWarps, 0, s>>>(
             dmui.as<double>(), dmf.as<uint8_t>(), dcexpM.as<int>(), D, np * nb * nob, dimgMB.as<bf16>());
         const size_t ti = np * nob * ng_i;
         k_tiles_ij<<<(unsigned)ceil_div(ti, 128), 128, 0, s>>>(
             dmf.as<uint8_t>(), dmn.as<double>(), dcn.as<double>(), dcexpC.as<int>(), dcexpM.as<int>(),
             dij.as<double>(), D, ti, tpb, dti.as<OzTile>(), dsi.as<OzStep>(), dijf.as<uint8_t>(), cnt + 1, macs + 1);
-        ctx->note_launch(4);
+        ctx->note_launch(5);
         ctx->check_launch("rik ozaki ij prep");
         oz_run(ctx, sh, dti.as<OzTile>(), ti, dsi.as<OzStep>(), dimgCtA.as<bf16>(), dimgMB.as<bf16>(), 1.0, s, macs + 1);
         // ijs = ij + ij^T (FP64, with the reference's norm bookkeeping)
         k_ijs<<<(unsigned)(np * nob * nob), 128, 0, s>>>(dij.as<double>(), dijf.as<uint8_t>(), n_occ, bs, nob,
                                                           dijs.as<double>(), dsn.as<double>(), dsf.as<uint8_t>());
         // K += mui ijs
-        k_rexp_mui_sub<<<(unsigned)(n_sub * nb), tb, 0, s>>>(dmui.as<double>(), dmf.as<uint8_t>(), n_bf, n_occ, bs, nb,
-                                                             nob, np, Q, drexpMs.as<int>());
-        k_cexp_ijs_sub<<<(unsigned)(n_sub * nob), tb, 0, s>>>(dijs.as<double>(), dsf.as<uint8_t>(), n_occ, bs, nob, np,
-                                                              Q, dcexpSs.as<int>());
+        k_rowmax_mui_sub<<<oz_img_grid(np * nb * nob), 32 * kOzImgWarps, 0, s>>>(
+            dmui.as<double>(), dmf.as<uint8_t>(), n_bf, n_occ, bs, nb, nob, Q, np * nb * nob, bitsMs);
+        k_colmax_ijs_sub<<<oz_img_grid(np * nob * nob), 32 * kOzImgWarps, 0, s>>>(
+            dijs.as<double>(), dsf.as<uint8_t>(), n_occ, bs, nob, Q, np * nob * nob, bitsSs);
+        k_bits_exp<<<(unsigned)ceil_div(n_sub * n_bf, (size_t)256), 256, 0, s>>>(bitsMs, n_sub * n_bf,
+                                                                                 drexpMs.as<int>());
+        k_bits_exp<<<(unsigned)ceil_div(n_sub * n_occ, (size_t)256), 256, 0, s>>>(bitsSs, n_sub * n_occ,
+                                                                                  dcexpSs.as<int>());
         k_img_mui_A<<<oz_img_grid(np * nb * nob), 32 * kOzImgWarps, 0, s>>>(
             dmui.as<double>(), dmf.as<uint8_t>(), drexpMs.as<int>(), Q, D, np * nb * nob, dimgMA.as<bf16>());
         k_img_ijs_B<<<oz_img_grid(np * nob * nob), 32 * kOzImgWarps, 0, s>>>(
@@ -584,7 +607,7 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, uint64_t stats[5]) {
             dmf.as<uint8_t>(), dmn.as<double>(), dsf.as<uint8_t>(), dsn.as<double>(), drexpMs.as<int>(),
             dcexpSs.as<int>(), dKp.as<double>(), D, np, Q, tk, tpb, dtk.as<OzTile>(), dsk.as<OzStep>(), cnt + 2,
             macs + 2);
-        ctx->note_launch(6);
+        ctx->note_launch(8);
         ctx->check_launch("rik ozaki K prep");
         oz_run(ctx, sh, dtk.as<OzTile>(), tk, dsk.as<OzStep>(), dimgMA.as<bf16>(), dimgSB.as<bf16>(), 1.0, s, macs + 2);
         k_K_reduce<<<(unsigned)(nb * nob), 256, 0, s>>>(dKp.as<double>(), n_sub, D, K_dev);
