@@ -62,6 +62,35 @@ def build(verbose=False):
     return LIB
 
 
+DRIVERS = os.path.join(HERE, "drivers")
+
+
+def build_drivers(verbose=False):
+    """The reference's three drivers rebuilt against the C++ facade
+    (include/bsgpu.hpp), linked to the in-tree library."""
+    out = os.path.join(DRIVERS, "bin")
+    os.makedirs(out, exist_ok=True)
+    inc = os.path.join(os.path.dirname(HERE), "include")
+    gxx = shutil.which("g++") or "g++"
+    built = []
+    for src in sorted(glob.glob(os.path.join(DRIVERS, "*.cpp"))):
+        exe = os.path.join(out, os.path.splitext(os.path.basename(src))[0])
+        if os.path.exists(exe) and os.path.getmtime(exe) >= max(os.path.getmtime(src), os.path.getmtime(LIB),
+                                                               os.path.getmtime(os.path.join(inc, "bsgpu.hpp"))):
+            built.append(exe)
+            continue
+        cmd = [gxx, "-O2", "-std=c++17", "-I" + inc, src, "-o", exe, "-L" + HERE, "-lbsgpu",
+               "-Wl,-rpath,$ORIGIN/../.."]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"driver build failed for {src}:\n{r.stdout}\n{r.stderr}")
+        built.append(exe)
+    if verbose:
+        print("built", built)
+    return built
+
+
 if __name__ == "__main__":
     build(verbose=True)
+    build_drivers(verbose=True)
     sys.exit(0)
