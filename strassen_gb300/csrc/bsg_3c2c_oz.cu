@@ -67,6 +67,8 @@ __global__ void k_colexp_dense(const double *__restrict__ V, size_t nr, int *__r
 struct Dense3c {
     size_t n_vec2, n_aux, bs, nib, nkb, njb;
     int mp, kp, np, nd, R;
+    int J;        // X block rows per N-side group (np = J * bs rounded to 8)
+    size_t nibp;  // groups of J block rows
 };
 
 // The tile is transposed with respect to the output: its slots (the MMA's M
@@ -77,13 +79,17 @@ struct Dense3c {
 // always all live; with block rows as slots a step would carry the
 // insignificant X blocks of its other rows as zero images.
 
-// N-side images of X blocks (ib, kb): image row = output row, index ib + kb*nib
+// N-side images of X: J consecutive block rows stacked along N, one image
+// per (group ibp, kb), index ibp + kb*nibp; block ib = J*ibp + j fills rows
+// j*bs.. of its group's image (rows of missing blocks are never read)
 __global__ void k_img_X(const double *__restrict__ X, const int *__restrict__ rexp, Dense3c D, bf16 *__restrict__ img) {
     const size_t x = oz_warp_id();
     if (x >= D.nib * D.nkb) return;
-    const size_t ib = x % D.nib, kb = x / D.nib;
-    oz_block_image(X + ib * D.bs + kb * D.bs * D.n_vec2, D.n_vec2, false, ext3(ib, D.bs, D.n_vec2),
-                   ext3(kb, D.bs, D.n_aux), rexp + ib * D.bs, D.np, D.kp, D.nd, img + x * D.nd * (size_t)D.np * D.kp, false);
+    const size_t ib = x % D.nib, kb = x / D.nib, ibp = ib / D.J, j = ib % D.J;
+    bf16 *dst = img + (ibp + kb * D.nibp) * D.nd * (size_t)D.np * D.kp + j * D.bs * (size_t)D.kp;
+    oz_block_image_g(OzDenseGet{X + ib * D.bs + kb * D.bs * D.n_vec2, D.n_vec2, false}, ext3(ib, D.bs, D.n_vec2),
+                     ext3(kb, D.bs, D.n_aux), rexp + ib * D.bs, (int)D.bs, D.kp, D.nd, dst, false, threadIdx.x & 31, 32,
+                     D.np);
 }
 
 // M-side images of V^T blocks (jb, kb): image row = output column, index
@@ -96,10 +102,14 @@ __global__ void k_img_V(const double *__restrict__ V, const int *__restrict__ ce
                    cexp + jb * D.bs, D.mp, D.kp, D.nd, img + x * D.nd * (size_t)D.mp * D.kp, true);
 }
 
-// tiles and their steps; tile t covers output block row ib and block columns
-// jg*R .. jg*R+R-1.  Order: column groups of Gj slot groups (their V^T images,
-// Gj*R*nkb of them, stay resident in L2), within a group every block row ib
-// with its Gj tiles together (they share the X images of ib)
+// tiles and their steps; tile t covers output block rows J*ibp .. J*ibp+J-1
+// (N side) and block columns jg*R .. jg*R+R-1 (slots).  Order: column groups
+// of Gj slot groups (their V^T images, Gj*R*nkb of them, stay resident in
+// L2), within a group every block-row group with its Gj tiles together.
+// A step k carries the slots and N-side sub-blocks of a rectangle of
+// surviving (slot, sub-block) pairs: whether (jb, ib, kb) survives is
+// ||X_ib,kb|| ||V_kb,jb|| >= tpb, so for fixed kb the slot sets of the
+// sub-blocks are nested and split into at most J exact rectangles.
 __global__ void k_tiles_3c(size_t n_tiles, size_t n_jg, size_t Gj, const double *__restrict__ xn,
                            const double *__restrict__ vn, const int *__restrict__ rexp, const int *__restrict__ cexp,
                            double *__restrict__ out, Dense3c D, double tpb, OzTile *__restrict__ tiles,
@@ -107,9 +117,9 @@ __global__ void k_tiles_3c(size_t n_tiles, size_t n_jg, size_t Gj, const double 
                            unsigned long long *__restrict__ macs) {
     const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n_tiles) return;
-    const size_t q = t / (D.nib * Gj), rem = t % (D.nib * Gj);
+    const size_t q = t / (D.nibp * Gj), rem = t % (D.nibp * Gj);
     const size_t gsz = min(Gj, n_jg - q * Gj);  // only the last group is smaller
-    const size_t ib = rem / gsz, jg = q * Gj + rem % gsz;
+    const size_t ibp = rem / gsz, jg = q * Gj + rem % gsz;
     OzTile T;
     for (int s = 0; s < kOzMaxSlots; ++s) {
         T.c[s] = nullptr;
@@ -118,38 +128,68 @@ __global__ void k_tiles_3c(size_t n_tiles, size_t n_jg, size_t Gj, const double 
         T.rows[s] = 0;
         T.ldc[s] = 0;
     }
-    const int rows = ext3(ib, D.bs, D.n_vec2);
+    int nsub = 0, rows = 0, sub_rows[8];
+    for (int j = 0; j < D.J && ibp * D.J + j < D.nib; ++j) {
+        sub_rows[j] = ext3(ibp * D.J + j, D.bs, D.n_vec2);
+        rows += sub_rows[j];
+        ++nsub;
+    }
     for (int s = 0; s < D.R; ++s) {
         const size_t jb = jg * D.R + s;
         if (jb >= D.njb) break;
-        T.c[s] = out + ib * D.bs + jb * D.bs * D.n_vec2;
+        T.c[s] = out + ibp * D.J * D.bs + jb * D.bs * D.n_vec2;
         T.ldc[s] = (int)D.n_vec2;
         T.rows[s] = ext3(jb, D.bs, D.n_aux);  // slot rows are output columns
         T.rexp[s] = cexp + jb * D.bs;
     }
-    T.cols = rows;  // tile columns are output rows
-    T.cexp = rexp + ib * D.bs;
+    T.cols = rows;  // tile columns are output rows (J consecutive block rows)
+    T.cexp = rexp + ibp * D.J * D.bs;
     T.trans = 1;
     T.fresh_mask = 0xFFu;  // out = 0 + sum of the surviving products
-    T.s0 = (uint32_t)(t * D.nkb);
+    T.s0 = (uint32_t)(t * D.nkb * D.J);
     uint32_t n = 0;
     unsigned long long cnt = 0, m = 0;
     for (size_t kb = 0; kb < D.nkb; ++kb) {
-        OzStep st;
-        st.b = (uint32_t)(ib + kb * D.nib);
-        bool any = false;
-        const double x = xn[ib + kb * D.nib];
-        for (int s = 0; s < kOzMaxSlots; ++s) {
-            st.a[s] = kOzNone;
-            if (s >= D.R || !T.c[s]) continue;
-            const size_t jb = jg * D.R + s;
-            if (!(__dmul_rn(x, vn[kb + jb * D.nkb]) >= tpb)) continue;
-            st.a[s] = (uint32_t)(jb + kb * D.njb);
-            ++cnt;
-            m += (unsigned long long)rows * T.rows[s] * ext3(kb, D.bs, D.n_aux);
-            any = true;
+        uint32_t mask[8];
+        for (int j = 0; j < nsub; ++j) {
+            const double x = xn[ibp * D.J + j + kb * D.nib];
+            mask[j] = 0;
+            for (int s = 0; s < D.R; ++s) {
+                const size_t jb = jg * D.R + s;
+                if (jb >= D.njb) break;
+                if (__dmul_rn(x, vn[kb + jb * D.nkb]) >= tpb) {
+                    mask[j] |= 1u << s;
+                    ++cnt;
+                    m += (unsigned long long)sub_rows[j] * T.rows[s] * ext3(kb, D.bs, D.n_aux);
+                }
+            }
         }
-        if (any) steps[T.s0 + n++] = st;
+        // rectangles: the slots common to every sub-block that still has some
+        for (int guard = 0; guard < 8; ++guard) {
+            uint32_t common = 0xFFFFFFFFu, jset = 0;
+            for (int j = 0; j < nsub; ++j)
+                if (mask[j]) {
+                    common &= mask[j];
+                    jset |= 1u << j;
+                }
+            if (!jset) break;
+            if (!common) {  // not nested (cannot happen for a norm-product screen): one sub-block at a time
+                for (int j = 0; j < nsub; ++j)
+                    if (mask[j]) {
+                        common = mask[j];
+                        jset = 1u << j;
+                        break;
+                    }
+            }
+            OzStep st;
+            st.b = (uint32_t)(ibp + kb * D.nibp);
+            st.bmask = (jset == (1u << D.J) - 1u) ? kOzAllSub : jset;
+            for (int s = 0; s < kOzMaxSlots; ++s)
+                st.a[s] = ((common >> s) & 1u) ? (uint32_t)(jg * D.R + s + kb * D.njb) : kOzNone;
+            steps[T.s0 + n++] = st;
+            for (int j = 0; j < nsub; ++j)
+                if ((jset >> j) & 1u) mask[j] &= ~common;
+        }
     }
     T.ns = n;
     tiles[t] = T;
@@ -162,7 +202,14 @@ void transform_3c2c_ozaki(bsg_ctx ctx, size_t n_vec2, size_t n_aux, const double
     cudaStream_t s = ctx->stream;
     BSG_REQUIRE(bs <= 64, BSG_ERR_UNSUPPORTED, "Ozaki form supports blocks up to 64");
     const int nd = oz_default_digits(n_digits, (int)bs, (int)bs, (int)bs);
-    const OzShape sh = oz_shape((int)bs, (int)bs, (int)bs, nd);
+    // X block rows per tile on the N side.  Two rows (nd * 2*bs TMEM columns,
+    // bs % 8 == 0) halve the V^T image traffic per product, but on the 40-atom
+    // workload 35% of the steps split into two rectangles (the rows' screens
+    // differ) and the accumulator no longer fits twice in TMEM: measured 50 ms
+    // against 46 ms with one row, so one row it is.
+    const int J = 1;
+    OzShape sh = oz_shape((int)bs, (int)bs, (int)bs * J, nd);
+    sh.J = J;
     Dense3c D;
     D.n_vec2 = n_vec2;
     D.n_aux = n_aux;
@@ -174,10 +221,12 @@ void transform_3c2c_ozaki(bsg_ctx ctx, size_t n_vec2, size_t n_aux, const double
     D.np = sh.np;
     D.nd = nd;
     D.R = sh.R;
+    D.J = J;
+    D.nibp = ceil_div(D.nib, (size_t)J);
     if (!n_vec2 || !n_aux) return;
     const size_t a_img = (size_t)nd * sh.mp * sh.kp, b_img = (size_t)nd * sh.np * sh.kp;
     DevBuf xn(D.nib * D.nkb * 8, s), vn(D.nkb * D.njb * 8, s), rexp(n_vec2 * 4, s), cexp(n_aux * 4, s);
-    DevBuf ai(D.nkb * D.njb * a_img * 2, s), bi(D.nib * D.nkb * b_img * 2, s), cnt(16, s);
+    DevBuf ai(D.nkb * D.njb * a_img * 2, s), bi(D.nibp * D.nkb * b_img * 2, s), cnt(16, s);
     BSG_CUDA(cudaMemsetAsync(cnt.p, 0, 16, s));
     const int wpb = 8;
     k_dense_norms<<<(unsigned)ceil_div(D.nib * D.nkb, wpb), wpb * 32, 0, s>>>(X, n_vec2, n_vec2, n_aux, bs, D.nib,
@@ -190,9 +239,9 @@ void transform_3c2c_ozaki(bsg_ctx ctx, size_t n_vec2, size_t n_aux, const double
     k_img_V<<<oz_img_grid(D.nkb * D.njb), 32 * kOzImgWarps, 0, s>>>(V, cexp.as<int>(), D, ai.as<bf16>());
     ctx->note_launch(6);
     ctx->check_launch("3c2c ozaki prep");
-    const size_t n_jg = ceil_div(D.njb, (size_t)D.R), n_tiles = D.nib * n_jg;
-    BSG_REQUIRE(n_tiles * D.nkb < 0xffffffffull, BSG_ERR_UNSUPPORTED, "too many Ozaki steps in one call");
-    DevBuf dt(n_tiles * sizeof(OzTile), s), dst(n_tiles * D.nkb * sizeof(OzStep), s);
+    const size_t n_jg = ceil_div(D.njb, (size_t)D.R), n_tiles = D.nibp * n_jg;
+    BSG_REQUIRE(n_tiles * D.nkb * J < 0xffffffffull, BSG_ERR_UNSUPPORTED, "too many Ozaki steps in one call");
+    DevBuf dt(n_tiles * sizeof(OzTile), s), dst(n_tiles * D.nkb * J * sizeof(OzStep), s);
     const double tpb = thresh * (double)(bs * bs * bs);
     auto *c = cnt.as<unsigned long long>();
     // V^T images of one slot group: R * nkb images; keep about 48 MB of them in L2

@@ -81,6 +81,7 @@ int oz_default_digits(int requested, int bs_rows, int bs_k, int bs_cols) {
 
 struct OzKParams {
     int mp, kp, R, nd, S, F;
+    int J;               // N-side sub-blocks of a B image (NP / J rows each)
     uint32_t chunk;      // consecutive tiles per CTA turn
     int nbuf;            // TMEM accumulator sets (2: the MMA fills one while the epilogue drains the other)
     uint32_t tmem_cols;  // columns of one accumulator set
@@ -200,7 +201,20 @@ __global__ void __launch_bounds__(kOzThreads, 1)
                     const bf16 *src = live ? a_img + (size_t)ai * slot_elems : P.zero;
                     tc::bulk_g2s(sA + lane * slot_bytes, src, (uint32_t)len * slot_bytes, &full[stage]);
                 }
-                if (lane == 31) tc::bulk_g2s(sB, b_img + (size_t)st.b * b_img_elems, b_copy, &full[stage]);
+                const uint32_t jfull = (1u << P.J) - 1u;
+                if ((st.bmask & jfull) == jfull) {
+                    if (lane == 31) tc::bulk_g2s(sB, b_img + (size_t)st.b * b_img_elems, b_copy, &full[stage]);
+                } else {
+                    // some N-side sub-blocks are screened out for this step: per
+                    // (sub-block, digit) chunk, the image's rows or zeros
+                    const int npj = NP / P.J, c = lane - 16;
+                    if (c >= 0 && c < P.J * P.nd) {
+                        const int j = c / P.nd, i = c % P.nd;
+                        const size_t off = ((size_t)i * NP + (size_t)j * npj) * P.kp;
+                        const bf16 *src = ((st.bmask >> j) & 1u) ? b_img + (size_t)st.b * b_img_elems + off : P.zero;
+                        tc::bulk_g2s(sB + off * 2, src, (uint32_t)npj * P.kp * 2u, &full[stage]);
+                    }
+                }
                 if (++stage == (uint32_t)P.S) {
                     stage = 0;
                     ph ^= 1u;
@@ -277,12 +291,20 @@ __global__ void __launch_bounds__(kOzThreads, 1)
                         // region) overwrites the accumulator
                         uint32_t first = (k == c * P.F) ? 1u : 0u;
                         for (uint32_t q = 0; q < nq; ++q) {
+                            // the slice's descriptors first, then its MMAs back to back
                             const uint64_t aq = a0 + q * 16u, bq = b0 + q * 16u;
+                            uint64_t ad[kMaxPlan], bd[kMaxPlan];
+                            uint32_t dt[kMaxPlan], ac[kMaxPlan];
+#pragma unroll
+                            for (int e = 0; e < kMaxPlan; ++e) {
+                                ad[e] = aq + pa[e];
+                                bd[e] = bq + pb[e];
+                                dt[e] = dbase + (pd[e] & 0xFFFFu);
+                                ac[e] = (first & (pd[e] >> 16)) ? 0u : 1u;
+                            }
 #pragma unroll
                             for (int e = 0; e < kMaxPlan; ++e)
-                                if (e < n_plan)
-                                    tc::mma_bf16(dbase + (pd[e] & 0xFFFFu), aq + pa[e], bq + pb[e], pi[e],
-                                                 (first & (pd[e] >> 16)) ? 0u : 1u);
+                                if (e < n_plan) tc::mma_bf16(dt[e], ad[e], bd[e], pi[e], ac[e]);
                             first = 0;
                         }
                         tc::mma_commit(&empty[stage]);
@@ -415,6 +437,9 @@ static void launch_oz(bsg_ctx ctx, const OzShape &sh, const OzTile *tiles, size_
                       uint32_t chunk, cudaStream_t s) {
     OzKParams P;
     P.chunk = chunk;
+    P.J = sh.J;
+    BSG_REQUIRE(sh.J >= 1 && sh.J * sh.nd <= 16 && NP % sh.J == 0 && (NP / sh.J) % 8 == 0, BSG_ERR_UNSUPPORTED,
+                "Ozaki tile: N-side sub-blocks");
     P.mp = sh.mp;
     P.kp = sh.kp;
     P.R = sh.R;
@@ -565,6 +590,7 @@ __global__ void k_oz_steps(OzTile *__restrict__ tiles, size_t n_tiles, const uin
         const size_t bi = g.tB ? jb + kb * b_nrb : kb + jb * b_nrb;
         if (!B[bi]) continue;
         OzStep st;
+        st.bmask = kOzAllSub;
         st.b = b_base + (uint32_t)bi;
         bool any = false;
         for (int s = 0; s < kOzMaxSlots; ++s) {
@@ -859,6 +885,7 @@ void ozaki_grid_products(bsg_ctx ctx, size_t n_prod, size_t n, const std::vector
                 T.ns = (uint32_t)n;
                 for (size_t kb = 0; kb < n; ++kb) {
                     OzStep st;
+        st.bmask = kOzAllSub;
                     st.b = (uint32_t)(i * nn + kb + cb * n);
                     for (int sl = 0; sl < kOzMaxSlots; ++sl) {
                         const size_t rb = g * sh.R + sl;

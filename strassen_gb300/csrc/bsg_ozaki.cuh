@@ -35,6 +35,7 @@ struct OzShape {
     int nd;  // digits per operand
     int F;   // steps per exact chain (512 / kp)
     int S = 0;  // pipeline stages (0: as many as fit, at most 4)
+    int J = 1;  // N-side sub-blocks of np / J rows each (a B image holds J blocks)
 };
 OzShape oz_shape(int bs_rows, int bs_k, int bs_cols, int nd);
 // digits to use: `requested` (validated) or, for 0, 5 where it fits else 4
@@ -56,7 +57,9 @@ struct OzTile {
 struct OzStep {
     uint32_t b;                  // B image index
     uint32_t a[kOzMaxSlots];     // A image index per slot, kOzNone = zero
+    uint32_t bmask;              // N-side sub-blocks taken from B (bit j); the others are zero
 };
+constexpr uint32_t kOzAllSub = 0xFFFFFFFFu;
 
 // Runs the tiles: C_slot = alpha * sum_steps A_slot,step * B_step (+ C_slot
 // unless fresh).  a_img / b_img hold nd planes per image in the UMMA layout.
@@ -197,8 +200,10 @@ __device__ __forceinline__ uint32_t oz_digit_bf16(int d, int i) {
 template <class Get>
 __device__ __forceinline__ void oz_block_image_g(const Get &get, int rows, int k, const int *__restrict__ exps, int mpad,
                                                  int kp, int nd, __nv_bfloat16 *__restrict__ dst, bool m_side, int tid,
-                                                 int nthr) {
-    const size_t plane = oz_plane_stride(m_side, mpad, kp), rgs = oz_rg_stride(m_side, nd, kp);
+                                                 int nthr, int plane_rows = 0) {
+    // plane_rows (N side): rows of the image the block is part of (a group of
+    // blocks stacked along N), 0 = mpad
+    const size_t plane = oz_plane_stride(m_side, plane_rows ? plane_rows : mpad, kp), rgs = oz_rg_stride(m_side, nd, kp);
     const int hk = kp >> 3;
     for (int idx = tid; idx < mpad * hk; idx += nthr) {
         const int r = idx % mpad, h = idx / mpad;

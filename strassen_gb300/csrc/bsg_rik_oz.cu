@@ -310,6 +310,7 @@ __global__ void k_tiles_mui(const uint8_t *__restrict__ uflag, const double *__r
     uint32_t n = 0;
     for (size_t b = 0; b < D.nb; ++b) {
         OzStep st;
+        st.bmask = kOzAllSub;
         st.b = (uint32_t)(b + j * D.nb);
         bool any = false;
         for (int s = 0; s < kOzMaxSlots; ++s) {
@@ -370,6 +371,7 @@ __global__ void k_tiles_ij(const uint8_t *__restrict__ mflag, const double *__re
         const size_t mb = p * D.nb * D.nob + a + jb * D.nb;
         if (!mflag[mb]) continue;
         OzStep st;
+        st.bmask = kOzAllSub;
         st.b = (uint32_t)mb;
         bool any = false;
         for (int s = 0; s < kOzMaxSlots; ++s) {
@@ -432,6 +434,7 @@ __global__ void k_tiles_K(const uint8_t *__restrict__ mflag, const double *__res
             const size_t sb = p * D.nob * D.nob + ib + jb * D.nob;
             if (!sflag[sb]) continue;
             OzStep st;
+        st.bmask = kOzAllSub;
             st.b = (uint32_t)sb;
             bool any = false;
             for (int s = 0; s < kOzMaxSlots; ++s) {

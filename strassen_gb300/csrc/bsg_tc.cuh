@@ -123,14 +123,16 @@ __host__ __device__ constexpr uint32_t idesc_bf16_f32(uint32_t M, uint32_t N) {
            | ((M >> 4) & 0x1Fu) << 24;
 }
 
-// D[tmem] (+)= A[smem desc] * B[smem desc]; issued by one thread
+// D[tmem] (+)= A[smem desc] * B[smem desc]; issued by one thread.  No
+// memory clobber: the operands come from shared memory through the async
+// proxy, ordered by the mbarrier waits (volatile asm with memory clobbers)
+// around it, so the compiler may compute the next MMA's descriptors early.
 __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
                                          uint32_t accumulate) {
     asm volatile(
         "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
         " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
-        "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
-        : "memory");
+        "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate));
 }
 
 // arrive on the mbarrier once all previously issued MMAs of this thread are done
