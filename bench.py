@@ -265,6 +265,25 @@ def run_ours(args):
         extra = {"fp64_ms_per_step": ms64, "speedup_vs_fp64": ms64 / ms,
                  "rel_err_vs_fp64": float(np.linalg.norm(Kc - K64) / np.linalg.norm(K64)),
                  "rel_err_bound": 1e-9}
+        if not args.skip_kmn:
+            # adjacent contraction: symmetric K_mn = sum_P mui_P mui_P^T on the same B (FP64 3c->2c output)
+            Kmn = torch.empty((n_bf, n_bf), dtype=torch.float64, device=dev)
+            st = {}
+
+            def kmn_step(form_):
+                st[form_] = api.rik_kmn_step(B, keys, C, n_bf, n_aux, n_occ, bs, thr, n_part=1, form=form_,
+                                             n_digits=docc, out=Kmn, ctx=ctx, stats=True)[1]
+
+            kms_oz, _, _ = timed(lambda: kmn_step(api.FORM_OZAKI), 1, 1)
+            Kmn_oz = Kmn.cpu().numpy().copy()
+            kms_64, _, _ = timed(lambda: kmn_step(api.FORM_FP64), 1, 0)
+            Kmn_64 = Kmn.cpu().numpy()
+            mprod = bs ** 3 * st[api.FORM_FP64][5]  # block products x bs^3 multiply-adds (bound: edge blocks smaller)
+            extra["kmn"] = {"what": "K_mn = sum_P mui_P mui_P^T (n_bf x n_bf, lower blocks + mirror), mui_P recomputed",
+                            "mixed_ms": kms_oz, "fp64_ms": kms_64, "speedup_vs_fp64": kms_64 / kms_oz,
+                            "rel_err_vs_fp64": float(np.linalg.norm(Kmn_oz - Kmn_64) / np.linalg.norm(Kmn_64)),
+                            "block_products": st[api.FORM_FP64][5], "mixed_block_products": st[api.FORM_OZAKI][5],
+                            "kmn_product_flops_bound": 2.0 * mprod}
     if args.no_e2e:
         print(json.dumps({"metric": METRIC, "value": flops_total(n_bf, n_aux, n_occ, n_vec2) / (ms * 1e-3) / 1e12,
                           "unit": "TFLOP/s", "ms_per_step": ms, "note": "profiling run (no e2e / baselines)",
@@ -432,6 +451,7 @@ def main():
     ap.add_argument("--digits-occ", type=int, default=5)
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--skip-kmn", action="store_true", help="leave out the symmetric K_mn measurement")
     ap.add_argument("--no-e2e", action="store_true", help="profiling runs: timed device step only")
     ap.add_argument("--atoms", type=int, default=0, help="smaller system for profiler captures")
     ap.add_argument("--workload", default="rik", choices=["rik", "batched"],

@@ -237,6 +237,19 @@ typedef struct bsg_rik_args {
 bsg_status bsg_rik_occ_step(bsg_ctx ctx, const bsg_rik_args *args, double *K_out, int out_where,
                             uint64_t stats_out[5]);
 
+/* Symmetric exchange matrix K_mn = sum_{P,i} mui_P(m,i) mui_P(n,i), with
+ * mui_P = (mu i|P) the screened product U_P C the occ step builds
+ * (occ_ri_k_step.cpp:102-108).  No counterpart in the reference, whose driver
+ * stops at K_{mu j}: per P it adds matmult(Kmn_sub, mui_P, N, mui_P, T, thresh,
+ * 1, 1) the way :116 adds mui_P ijs_P, partitions as in bsg_rik_occ_step.
+ * Kmn_out: n_bf x n_bf column-major, exactly symmetric (lower blocks computed,
+ * upper mirrored; in the FP64 form the mirror equals the computed upper block
+ * bit for bit).  K_out (n_bf x n_occ, may be NULL) receives the occ step's K
+ * from the same pass.  stats_out (may be NULL): bsg_rik_occ_step's five
+ * counters, then the surviving block products of K_mn. */
+bsg_status bsg_rik_kmn_step(bsg_ctx ctx, const bsg_rik_args *args, double *Kmn_out, double *K_out, int out_where,
+                            uint64_t stats_out[6]);
+
 /* The occ-RI-K step above without any device allocation (no counterpart in
  * the reference, which runs on the host).  For callers that cannot allocate
  * device memory: code under a framework whose caching allocator owns the

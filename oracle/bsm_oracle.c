@@ -748,6 +748,56 @@ int ob_rik_occ_step(size_t n_bf, size_t n_aux, size_t n_occ, size_t n_vec2, cons
     return st;
 }
 
+/* Symmetric exchange matrix K_mn = sum_{P,i} mui_P(m,i) mui_P(n,i), N_bf x N_bf.
+ * The reference computes only K_{mu j} (occ_ri_k_step.cpp:83-130); this is the
+ * same pipeline's adjacent contraction written with its own operations: mui_P
+ * exactly as the occ step builds it (:102-108), then per P
+ * matmult(Kmn_sub, mui_P, N, mui_P, T, thresh, 1, 1) the way :116 adds
+ * mui_P ijs_P into K_sub, and the partition partials added in order (:119-122). */
+int ob_rik_kmn_step(size_t n_bf, size_t n_aux, size_t n_occ, size_t n_vec2, const double *ints, const uint64_t *keys,
+                    const double *c_occ, size_t bs, double thresh, int n_part, double *kmn_out) {
+    if (n_part < 1) return OB_EPRECOND;
+    for (size_t v = 0; v < n_vec2; ++v)
+        if (keys[v] >= n_bf * n_bf) return OB_EPRECOND;
+    ob_bsm *K = ob_create(n_bf, n_bf, bs, bs, 0.0);
+    ob_fill(K, 0.0);
+    ob_bsm *Cb = ob_create(n_bf, n_occ, bs, bs, 0.0);
+    ob_copy_from_dense(Cb, c_occ);
+    ob_bsm **Kpart = (ob_bsm **)calloc((size_t)n_part, sizeof(ob_bsm *));
+    int st = OB_OK;
+#pragma omp parallel for schedule(dynamic, 1) reduction(| : st)
+    for (int t = 0; t < n_part; ++t) {
+        double *U = (double *)calloc(n_bf * n_bf, sizeof(double));
+        ob_bsm *Ub = ob_create(n_bf, n_bf, bs, bs, 1e-20);
+        ob_bsm *mui = ob_create(n_bf, n_occ, bs, bs, 0.0);
+        ob_bsm *Ks = ob_create(n_bf, n_bf, bs, bs, 0.0);
+        ob_fill(Ks, 0.0);
+        size_t lo, hi;
+        static_range(n_aux, n_part, t, &lo, &hi);
+        int lst = OB_OK;
+        for (size_t P = lo; P < hi && !lst; ++P) {
+            decompress(U, n_bf, P, ints, n_vec2, keys);
+            ob_copy_from_dense(Ub, U);
+            lst = ob_matmult(mui, Ub, 0, Cb, 0, thresh, 1.0, 0.0, NULL);
+            if (lst) break;
+            ob_calc_norms(mui);
+            lst = ob_matmult(Ks, mui, 0, mui, 1, thresh, 1.0, 1.0, NULL);
+        }
+        Kpart[t] = Ks;
+        st |= lst;
+        free(U);
+        ob_free(Ub);
+        ob_free(mui);
+    }
+    for (int t = 0; t < n_part && !st; ++t) st = ob_add(K, Kpart[t]);
+    for (int t = 0; t < n_part; ++t) ob_free(Kpart[t]);
+    free(Kpart);
+    if (!st) ob_to_dense(K, kmn_out);
+    ob_free(K);
+    ob_free(Cb);
+    return st;
+}
+
 /* dense occ-RI-K occ_ri_k_step.cpp:39-77 */
 int ob_rik_occ_dense(size_t n_bf, size_t n_aux, size_t n_occ, size_t n_vec2, const double *ints, const uint64_t *keys,
                      const double *c_occ, int n_part, double *k_out) {

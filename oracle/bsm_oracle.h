@@ -58,6 +58,12 @@ int ob_matmult_strassen_sparse(ob_bsm *C, const ob_bsm *A, const ob_bsm *B, doub
 int ob_rik_occ_step(size_t n_bf, size_t n_aux, size_t n_occ, size_t n_vec2, const double *ints,
                     const uint64_t *keys, const double *c_occ, size_t bs, double thresh, int n_part,
                     double *k_out);
+/* symmetric K_mn = sum_{P,i} mui_P(m,i) mui_P(n,i) on the occ step's mui_P
+ * (occ_ri_k_step.cpp:102-108), per P matmult(Ks, mui, N, mui, T, thresh, 1, 1),
+ * partitions as above; kmn_out n_bf x n_bf column-major */
+int ob_rik_kmn_step(size_t n_bf, size_t n_aux, size_t n_occ, size_t n_vec2, const double *ints,
+                    const uint64_t *keys, const double *c_occ, size_t bs, double thresh, int n_part,
+                    double *kmn_out);
 /* dense occ-RI-K (occ_ri_k_step.cpp:39-77) on the same partition rule */
 int ob_rik_occ_dense(size_t n_bf, size_t n_aux, size_t n_occ, size_t n_vec2, const double *ints,
                      const uint64_t *keys, const double *c_occ, int n_part, double *k_out);

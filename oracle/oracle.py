@@ -74,6 +74,8 @@ def lib():
         L.ob_matmult_strassen_sparse.restype = c_int
         L.ob_rik_occ_step.argtypes = [c_size, c_size, c_size, c_size, c_vp, c_vp, c_vp, c_size, c_dbl, c_int, c_vp]
         L.ob_rik_occ_step.restype = c_int
+        L.ob_rik_kmn_step.argtypes = [c_size, c_size, c_size, c_size, c_vp, c_vp, c_vp, c_size, c_dbl, c_int, c_vp]
+        L.ob_rik_kmn_step.restype = c_int
         L.ob_rik_occ_dense.argtypes = [c_size, c_size, c_size, c_size, c_vp, c_vp, c_vp, c_int, c_vp]
         L.ob_rik_occ_dense.restype = c_int
         L.ob_3c2c_transform.argtypes = [c_size, c_size, c_vp, c_vp, c_size, c_dbl, c_vp]
@@ -105,6 +107,7 @@ def ref():
         R.ref_strassen.argtypes = [c_size, c_size, c_vp, c_vp, c_dbl, c_dbl, c_size, c_vp]
         R.ref_dryrun.argtypes = [c_size, c_size, c_vp, c_vp, c_dbl, c_dbl, C.POINTER(c_int), c_vp, c_size]
         R.ref_rik_occ_step.argtypes = [c_size, c_size, c_size, c_size, c_vp, c_vp, c_vp, c_size, c_dbl, c_int, c_vp]
+        R.ref_rik_kmn_step.argtypes = [c_size, c_size, c_size, c_size, c_vp, c_vp, c_vp, c_size, c_dbl, c_int, c_vp]
         R.ref_bsm_op.argtypes = [c_int, c_size, c_size, c_size, c_size, c_vp, c_dbl, c_vp, c_dbl, c_dbl, c_vp, c_vp,
                                  c_vp, c_vp]
         _REF = R
@@ -244,6 +247,19 @@ def rik_occ_step(ints, keys, c_occ, n_bf, n_aux, n_occ, bs, thresh, n_part=1):
     return out
 
 
+def rik_kmn_step(ints, keys, c_occ, n_bf, n_aux, n_occ, bs, thresh, n_part=1):
+    """K_mn = sum_{P,i} mui_P(m,i) mui_P(n,i) on the occ step's screened mui_P"""
+    ints = np.asfortranarray(ints, dtype=np.float64)
+    keys = np.ascontiguousarray(keys, dtype=np.uint64)
+    c_occ = np.asfortranarray(c_occ, dtype=np.float64)
+    out = np.zeros((n_bf, n_bf), dtype=np.float64, order="F")
+    st = lib().ob_rik_kmn_step(n_bf, n_aux, n_occ, ints.shape[0], _ptr(ints), _ptr(keys), _ptr(c_occ), bs, thresh,
+                               n_part, _ptr(out))
+    if st:
+        raise ValueError(f"oracle rik kmn status {st}")
+    return out
+
+
 def rik_occ_dense(ints, keys, c_occ, n_bf, n_aux, n_occ, n_part=1):
     ints = np.asfortranarray(ints, dtype=np.float64)
     keys = np.ascontiguousarray(keys, dtype=np.uint64)
@@ -321,6 +337,17 @@ def ref_rik_occ_step(ints, keys, c_occ, n_bf, n_aux, n_occ, bs, thresh, n_part=1
     c_occ = np.asfortranarray(c_occ, dtype=np.float64)
     out = np.zeros((n_bf, n_occ), dtype=np.float64, order="F")
     R.ref_rik_occ_step(n_bf, n_aux, n_occ, ints.shape[0], _ptr(ints), _ptr(keys), _ptr(c_occ), bs, thresh, n_part,
+                       _ptr(out))
+    return out
+
+
+def ref_rik_kmn_step(ints, keys, c_occ, n_bf, n_aux, n_occ, bs, thresh, n_part=1):
+    R = ref()
+    ints = np.asfortranarray(ints, dtype=np.float64)
+    keys = np.ascontiguousarray(keys, dtype=np.uint64)
+    c_occ = np.asfortranarray(c_occ, dtype=np.float64)
+    out = np.zeros((n_bf, n_bf), dtype=np.float64, order="F")
+    R.ref_rik_kmn_step(n_bf, n_aux, n_occ, ints.shape[0], _ptr(ints), _ptr(keys), _ptr(c_occ), bs, thresh, n_part,
                        _ptr(out))
     return out
 

@@ -134,6 +134,43 @@ int ref_rik_occ_step(size_t N_bf, size_t N_aux, size_t N_occ, size_t N_vec2, con
     return 0;
 }
 
+// K_mn = sum_{P,i} mui_P(m,i) mui_P(n,i) on the reference classes: the occ
+// step's mui_P (occ_ri_k_step.cpp:102-108) followed by the screened
+// matmult(Kmn_sub, mui, N, mui, T, thresh, 1, 1), partitions as above.
+int ref_rik_kmn_step(size_t N_bf, size_t N_aux, size_t N_occ, size_t N_vec2, const double* ints,
+                     const uint64_t* keys, const double* c_occ, size_t bs, double thresh, int n_part,
+                     double* kmn_out) {
+    omp_set_num_threads(1);
+    Matrix<double> ints_3c(ints, N_vec2, N_aux);
+    Matrix<double> occ_MOs(c_occ, N_bf, N_occ);
+    Matrix<size_t> v2m_keys(N_vec2, 1);
+    for (size_t v = 0; v < N_vec2; ++v) v2m_keys.elem(v, 0) = (size_t)keys[v];
+    BSM K_bsm(N_bf, N_bf, bs, bs, 0.0);
+    BSM C_bsm(occ_MOs, bs, bs, 0.0);
+    K_bsm.fill_with_values(0.e0);
+    for (int t = 0; t < n_part; ++t) {
+        Matrix<double> U(0.e0, N_bf, N_bf);
+        BSM U_bsm(N_bf, N_bf, bs, bs, 1e-20);
+        BSM mui(N_bf, N_occ, bs, bs, 0.0);
+        BSM Ksub(N_bf, N_bf, bs, bs, 0.0);
+        Ksub.fill_with_values(0.e0);
+        const size_t q = N_aux / (size_t)n_part, r = N_aux % (size_t)n_part, tt = (size_t)t;
+        const size_t lo = tt * q + (tt < r ? tt : r), hi = lo + q + (tt < r ? 1 : 0);
+        for (size_t P = lo; P < hi; ++P) {
+            double* u = U.data_ptr();
+            const double* cp = &ints_3c.elem(0, P);
+            for (size_t v = 0; v < N_vec2; ++v) u[v2m_keys.elem(v, 0)] = cp[v];
+            U_bsm.copy_from_input_matrix(U);
+            matmult(mui, U_bsm, false, C_bsm, false, thresh, 1.0, 0.0);
+            mui.calc_frobenius_norms();
+            matmult(Ksub, mui, false, mui, true, thresh, 1.0, 1.0);
+        }
+        K_bsm += Ksub;
+    }
+    export_bsm(K_bsm, kmn_out, nullptr, nullptr);
+    return 0;
+}
+
 // Sequence of container operations for parity of the block-level API:
 // op 0: lhs += rhs, 1: lhs -= rhs, 2: lhs.add_transpose(rhs), 3: lhs *= s,
 // 4: lhs.recompress(), 5: lhs.calc_frobenius_norms().  lhs/rhs built from

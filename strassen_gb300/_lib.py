@@ -91,6 +91,7 @@ _sig("bsg_matmult_strassen_sparse_form", [c_vp, c_vp, c_vp, c_dbl, c_size, c_int
 _sig("bsg_tensormult_contract", [c_vp, c_vp, c_int, c_vp, c_int, c_size, c_dbl, c_dbl, c_dbl])
 _sig("bsg_tensormult_batched", [c_vp, c_vp, c_int, c_vp, c_int, c_size, c_dbl, c_dbl, c_dbl])
 _sig("bsg_rik_occ_step", [c_vp, C.POINTER(RikArgs), c_vp, c_int, c_u64p])
+_sig("bsg_rik_kmn_step", [c_vp, C.POINTER(RikArgs), c_vp, c_vp, c_int, c_u64p])
 _sig("bsg_3c2c_transform", [c_vp, c_size, c_size, c_vp, c_vp, c_int, c_size, c_dbl, c_int, c_int, c_vp, c_int])
 _sig("bsg_probe_fp64_peak", [c_vp, C.POINTER(c_dbl)])
 c_flt = C.c_float

@@ -9,6 +9,7 @@ Names and argument meaning follow the reference's C++ API:
 * :func:`matmult_strassen_sparse`, :func:`matmult_strassen_dryrun` -- strassen.hpp:511,688
 * :func:`tensormult_contract`, :func:`tensormult_batched` -- blocksparse3d_tensor.h:11-24
 * :func:`rik_occ_step`       -- occ_ri_k_step.cpp:83-130
+* :func:`rik_kmn_step`       -- symmetric K_mn on the same step's mui_P (:102-108)
 * :func:`transform_3c2c`     -- 3c_2c_transform.cpp:44-57
 
 Errors the reference turns into assert/exit(1) raise :class:`BsgError`.
@@ -455,6 +456,47 @@ def rik_occ_step(ints, keys, c_occ, n_bf, n_aux, n_occ, bs, thresh, n_part=1, fo
         out[...] = ko
     del k1, k2, k3
     return (out, list(st)) if stats else out
+
+
+def rik_kmn_step(ints, keys, c_occ, n_bf, n_aux, n_occ, bs, thresh, n_part=1, form=FORM_FP64, n_digits=4,
+                 p_chunk=0, out=None, k_out=False, ctx=None, stats=False):
+    """Symmetric K_mn = sum_{P,i} mui_P(m,i) mui_P(n,i) on the occ step's
+    screened mui_P (occ_ri_k_step.cpp:102-108), n_bf x n_bf.
+
+    Inputs as rik_occ_step.  k_out=True also returns the occ step's K
+    (n_bf x n_occ) from the same pass: (Kmn, K).  stats=True appends the six
+    counters (the occ step's five, then the K_mn block products)."""
+    ctx = ctx or default_context()
+    pi, w1, k1 = _buf(ints)
+    pk, w2, k2 = _buf(keys, np.uint64)
+    pc, w3, k3 = _buf(c_occ)
+    if not (w1 == w2 == w3):
+        raise BsgError(1, "ints, keys and c_occ must all be host or all device arrays")
+    n_vec2 = ints.shape[0]
+    a = RikArgs(n_bf, n_aux, n_occ, n_vec2, pi, pk, pc, w1, bs, float(thresh), n_part, form, n_digits, p_chunk)
+    if out is None:
+        out = np.zeros((n_bf, n_bf), dtype=np.float64, order="F")
+    po, wo, ko = _buf(out)
+    kq = kk = None
+    pq = None
+    if k_out:
+        if wo == BSG_HOST:
+            kq = np.zeros((n_bf, n_occ), dtype=np.float64, order="F")
+        else:  # device output: a column-major n_bf x n_occ view
+            import torch
+            kq = torch.zeros((n_occ, n_bf), dtype=torch.float64, device=out.device).t()
+        pq, wq, kk = _buf(kq)
+    st = (C.c_uint64 * 6)()
+    check(lib.bsg_rik_kmn_step(ctx.h, C.byref(a), po, pq, wo, st))
+    if wo == BSG_HOST and ko is not out:
+        out[...] = ko
+    if k_out and wo == BSG_HOST and kk is not kq:
+        kq[...] = kk
+    del k1, k2, k3
+    res = (out, kq) if k_out else (out,)
+    if stats:
+        res = res + (list(st),)
+    return res[0] if len(res) == 1 else res
 
 
 def transform_3c2c(ints_3c, v_m12, bs, thresh, form=FORM_FP64, n_digits=4, out=None, ctx=None):

@@ -13,6 +13,7 @@
 //   ij       ij_P  = C^T * mui_P   screened
 //   ijs      ijs_P = ij_P + ij_P^T with the reference's norm bookkeeping
 //   kupd     Ksub[t] += mui_P * ijs_P, P in order within partition t
+//   kmn      Kmn_sub[t] += mui_P * mui_P^T (optional symmetric K_mn)
 //
 // and finally K = sum_t Ksub[t] in partition order (the critical section of
 // :119-122 with a fixed order).  The FP64 form performs the reference's
@@ -251,6 +252,57 @@ __global__ void k_kreduce(const double *__restrict__ Ksub, size_t n, int T, doub
     K[e] = acc;
 }
 
+// Kmn_sub[t](a, b) += mui_p(a,jb) * mui_p(b,jb)^T over p of partition t in
+// this chunk (in order) and surviving jb: matmult(Kmn_sub, mui, N, mui, T,
+// thresh, 1, 1) per P on a pre-filled Kmn_sub, the way :116 adds mui ijs.
+// Lower blocks a >= b only: an upper block's chains multiply the same pairs
+// in the same order (fma's product commutes), so it is the transpose bit for
+// bit and the reduce mirrors it.
+__global__ void __launch_bounds__(256) k_kmn_upd(const double *__restrict__ mui, const double *__restrict__ mnorm,
+                                                 const uint8_t *__restrict__ mflag, size_t n_bf, size_t n_occ,
+                                                 size_t bs, size_t nb, size_t nob, double tpb,
+                                                 const uint32_t *__restrict__ plo, const uint32_t *__restrict__ phi,
+                                                 double *__restrict__ Ksub, unsigned long long *__restrict__ nsig) {
+    const size_t x = blockIdx.x;  // (t, a, b)
+    const size_t t = x / (nb * nb), r = x % (nb * nb), a = r % nb, b = r / nb;
+    const uint32_t lo = plo[t], hi = phi[t];
+    if (a < b || lo >= hi) return;
+    const int rows = ext(a, bs, n_bf), cols = ext(b, bs, n_bf), n = rows * cols;
+    ElemMap m;
+    elem_map(m, rows, n);
+    double *K = Ksub + t * n_bf * n_bf + a * bs + b * bs * n_bf;
+    double acc[kREPT];
+#pragma unroll
+    for (int s = 0; s < kREPT; ++s) acc[s] = (threadIdx.x + s * blockDim.x < n) ? K[m.ii[s] + (size_t)m.jj[s] * n_bf] : 0.0;
+    uint32_t cnt = 0;
+    for (uint32_t p = lo; p < hi; ++p) {
+        const double *Mp = mui + (size_t)p * n_bf * n_occ;
+        for (size_t jb = 0; jb < nob; ++jb) {
+            const size_t ma = (size_t)p * nb * nob + a + jb * nb, mb = (size_t)p * nb * nob + b + jb * nb;
+            if (!mflag[ma] || !mflag[mb]) continue;
+            if (!(__dmul_rn(mnorm[ma], mnorm[mb]) >= tpb)) continue;
+            chain<false, true>(acc, false, m, n, Mp + a * bs + jb * bs * n_bf, n_bf, Mp + b * bs + jb * bs * n_bf, n_bf,
+                               ext(jb, bs, n_occ));
+            ++cnt;
+        }
+    }
+#pragma unroll
+    for (int s = 0; s < kREPT; ++s)
+        if (threadIdx.x + s * blockDim.x < n) K[m.ii[s] + (size_t)m.jj[s] * n_bf] = acc[s];
+    if (threadIdx.x == 0 && cnt) atomicAdd(nsig, (unsigned long long)cnt);
+}
+
+// K_mn = sum_t Kmn_sub[t] in partition order; upper blocks from the lower
+__global__ void k_kmn_reduce(const double *__restrict__ Ksub, size_t n_bf, size_t bs, int T, double *__restrict__ K) {
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n_bf * n_bf) return;
+    const size_t gi = e % n_bf, gj = e / n_bf;
+    const size_t src = (gi / bs >= gj / bs) ? e : gj + gi * n_bf;
+    double acc = 0.0;
+    for (int t = 0; t < T; ++t) acc = fma(1.0, Ksub[(size_t)t * n_bf * n_bf + src], acc);
+    K[e] = acc;
+}
+
 // per-block norms of the dense occupied coefficients (BlockSparseMatrix(C, bs, bs, 0.0), :85)
 __global__ void k_cnorms(const double *__restrict__ C, size_t n_bf, size_t n_occ, size_t bs, size_t nb, size_t nob,
                          double *__restrict__ cnorm) {
@@ -266,7 +318,7 @@ static unsigned threads_for(int rows, int cols) {
     return (unsigned)std::max<size_t>(32, ((ceil_div(e, kREPT) + 31) / 32) * 32);
 }
 
-void rik_fp64(bsg_ctx ctx, const RikDev &d, double *K_dev, uint64_t stats[5]) {
+void rik_fp64(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uint64_t stats[6]) {
     cudaStream_t s = ctx->stream;
     const size_t n_bf = d.n_bf, n_occ = d.n_occ, bs = d.bs, n_aux = d.n_aux;
     const size_t nb = ceil_div(n_bf, bs), nob = ceil_div(n_occ, bs);
@@ -287,10 +339,13 @@ void rik_fp64(bsg_ctx ctx, const RikDev &d, double *K_dev, uint64_t stats[5]) {
     DevBuf dmui(pc * n_bf * n_occ * 8, s), dmn(pc * nb * nob * 8, s), dmf(pc * nb * nob, s);
     DevBuf dij(pc * n_occ * n_occ * 8, s), dijf(pc * nob * nob, s);
     DevBuf dijs(pc * n_occ * n_occ * 8, s), dsn(pc * nob * nob * 8, s), dsf(pc * nob * nob, s);
-    DevBuf dK(std::max<size_t>(1, (size_t)T) * n_bf * n_occ * 8, s), dcn(nb * nob * 8, s);
-    DevBuf dplo(T * 4, s), dphi(T * 4, s), dcnt(5 * 8, s);
-    BSG_CUDA(cudaMemsetAsync(dK.p, 0, (size_t)T * n_bf * n_occ * 8, s));  // K_sub.fill_with_values(0) (:98)
-    BSG_CUDA(cudaMemsetAsync(dcnt.p, 0, 5 * 8, s));
+    const bool want_k = K_dev != nullptr, want_kmn = Kmn_dev != nullptr;
+    DevBuf dK(want_k ? (size_t)T * n_bf * n_occ * 8 : 0, s), dcn(nb * nob * 8, s);
+    DevBuf dKmn(want_kmn ? (size_t)T * n_bf * n_bf * 8 : 0, s);
+    DevBuf dplo(T * 4, s), dphi(T * 4, s), dcnt(6 * 8, s);
+    if (want_k) BSG_CUDA(cudaMemsetAsync(dK.p, 0, (size_t)T * n_bf * n_occ * 8, s));  // K_sub.fill_with_values(0) (:98)
+    if (want_kmn) BSG_CUDA(cudaMemsetAsync(dKmn.p, 0, (size_t)T * n_bf * n_bf * 8, s));
+    BSG_CUDA(cudaMemsetAsync(dcnt.p, 0, 6 * 8, s));
     auto *cnt = dcnt.as<unsigned long long>();
 
     const int wpb = 8;
@@ -314,13 +369,14 @@ void rik_fp64(bsg_ctx ctx, const RikDev &d, double *K_dev, uint64_t stats[5]) {
             dU.as<double>(), dun.as<double>(), duf.as<uint8_t>(), d.c_occ, dcn.as<double>(), n_bf, n_occ, bs, nb, nob,
             tpb, dmui.as<double>(), dmn.as<double>(), dmf.as<uint8_t>(), cnt + 0);
         ctx->note_launch();
-        k_ij<<<(unsigned)(np * nob * nob), threads_for((int)bs, (int)bs), 0, s>>>(
-            d.c_occ, dcn.as<double>(), dmui.as<double>(), dmn.as<double>(), dmf.as<uint8_t>(), n_bf, n_occ, bs, nb,
-            nob, tpb, dij.as<double>(), dijf.as<uint8_t>(), cnt + 1);
-        ctx->note_launch();
-        k_ijs<<<(unsigned)(np * nob * nob), 128, 0, s>>>(dij.as<double>(), dijf.as<uint8_t>(), n_occ, bs, nob,
-                                                          dijs.as<double>(), dsn.as<double>(), dsf.as<uint8_t>());
-        ctx->note_launch();
+        if (want_k) {
+            k_ij<<<(unsigned)(np * nob * nob), threads_for((int)bs, (int)bs), 0, s>>>(
+                d.c_occ, dcn.as<double>(), dmui.as<double>(), dmn.as<double>(), dmf.as<uint8_t>(), n_bf, n_occ, bs,
+                nb, nob, tpb, dij.as<double>(), dijf.as<uint8_t>(), cnt + 1);
+            k_ijs<<<(unsigned)(np * nob * nob), 128, 0, s>>>(dij.as<double>(), dijf.as<uint8_t>(), n_occ, bs, nob,
+                                                              dijs.as<double>(), dsn.as<double>(), dsf.as<uint8_t>());
+            ctx->note_launch(2);
+        }
         for (int t = 0; t < T; ++t) {
             const size_t lo = std::max<size_t>(plo_all[t], P0), hi = std::min<size_t>(phi_all[t], P0 + np);
             plo[t] = lo < hi ? (uint32_t)(lo - P0) : 0;
@@ -328,23 +384,37 @@ void rik_fp64(bsg_ctx ctx, const RikDev &d, double *K_dev, uint64_t stats[5]) {
         }
         BSG_CUDA(cudaMemcpyAsync(dplo.p, plo.data(), T * 4, cudaMemcpyHostToDevice, s));
         BSG_CUDA(cudaMemcpyAsync(dphi.p, phi.data(), T * 4, cudaMemcpyHostToDevice, s));
-        k_kupd<<<(unsigned)((size_t)T * nb * nob), threads_for((int)bs, (int)bs), 0, s>>>(
-            dmui.as<double>(), dmn.as<double>(), dmf.as<uint8_t>(), dijs.as<double>(), dsn.as<double>(),
-            dsf.as<uint8_t>(), n_bf, n_occ, bs, nb, nob, tpb, dplo.as<uint32_t>(), dphi.as<uint32_t>(),
-            dK.as<double>(), cnt + 2);
-        ctx->note_launch();
+        if (want_k) {
+            k_kupd<<<(unsigned)((size_t)T * nb * nob), threads_for((int)bs, (int)bs), 0, s>>>(
+                dmui.as<double>(), dmn.as<double>(), dmf.as<uint8_t>(), dijs.as<double>(), dsn.as<double>(),
+                dsf.as<uint8_t>(), n_bf, n_occ, bs, nb, nob, tpb, dplo.as<uint32_t>(), dphi.as<uint32_t>(),
+                dK.as<double>(), cnt + 2);
+            ctx->note_launch();
+        }
+        if (want_kmn) {
+            k_kmn_upd<<<(unsigned)((size_t)T * nb * nb), threads_for((int)bs, (int)bs), 0, s>>>(
+                dmui.as<double>(), dmn.as<double>(), dmf.as<uint8_t>(), n_bf, n_occ, bs, nb, nob, tpb,
+                dplo.as<uint32_t>(), dphi.as<uint32_t>(), dKmn.as<double>(), cnt + 5);
+            ctx->note_launch();
+        }
         ctx->check_launch("rik chunk");
         // the host-side partition table is reused by the next chunk
         BSG_CUDA(cudaStreamSynchronize(s));
     }
-    k_kreduce<<<(unsigned)ceil_div(n_bf * n_occ, 256), 256, 0, s>>>(dK.as<double>(), n_bf * n_occ, T, K_dev);
-    ctx->note_launch();
+    if (want_k) {
+        k_kreduce<<<(unsigned)ceil_div(n_bf * n_occ, 256), 256, 0, s>>>(dK.as<double>(), n_bf * n_occ, T, K_dev);
+        ctx->note_launch();
+    }
+    if (want_kmn) {
+        k_kmn_reduce<<<(unsigned)ceil_div(n_bf * n_bf, 256), 256, 0, s>>>(dKmn.as<double>(), n_bf, bs, T, Kmn_dev);
+        ctx->note_launch();
+    }
     ctx->check_launch("rik reduce");
     if (stats) {
-        unsigned long long h[5];
-        BSG_CUDA(cudaMemcpyAsync(h, cnt, 5 * 8, cudaMemcpyDeviceToHost, s));
+        unsigned long long h[6];
+        BSG_CUDA(cudaMemcpyAsync(h, cnt, 6 * 8, cudaMemcpyDeviceToHost, s));
         BSG_CUDA(cudaStreamSynchronize(s));
-        for (int i = 0; i < 5; ++i) stats[i] = h[i];
+        for (int i = 0; i < 6; ++i) stats[i] = h[i];
     }
 }
 
@@ -367,10 +437,13 @@ void check_keys(bsg_ctx ctx, const uint64_t *dkeys, size_t n, uint64_t limit) {
 
 using namespace bsg;
 
-extern "C" bsg_status bsg_rik_occ_step(bsg_ctx ctx, const bsg_rik_args *a, double *K_out, int out_where,
-                                       uint64_t stats_out[5]) {
+namespace {
+
+// shared body of the two RI-K entry points: either output may be NULL
+bsg_status rik_entry(bsg_ctx ctx, const bsg_rik_args *a, double *K_out, double *Kmn_out, int out_where,
+                     uint64_t *stats_out, int n_stats) {
     return guard([&] {
-        BSG_REQUIRE(ctx && a && K_out, BSG_ERR_ARG, "NULL argument");
+        BSG_REQUIRE(ctx && a && (K_out || Kmn_out), BSG_ERR_ARG, "NULL argument");
         BSG_REQUIRE(a->bs > 0 && a->n_part >= 1, BSG_ERR_ARG, "block size and partition count must be positive");
         BSG_REQUIRE(a->n_bf > 0 && a->n_occ > 0, BSG_ERR_ARG, "empty basis");
         BSG_REQUIRE(a->n_vec2 == 0 || (a->ints && a->keys), BSG_ERR_ARG, "integrals or keys missing");
@@ -387,7 +460,7 @@ extern "C" bsg_status bsg_rik_occ_step(bsg_ctx ctx, const bsg_rik_args *a, doubl
         d.n_part = a->n_part;
         d.p_chunk = a->p_chunk;
         d.n_digits = a->n_digits;
-        DevBuf dints, dkeys, dc, dk;
+        DevBuf dints, dkeys, dc, dk, dkmn;
         if (a->where == BSG_HOST) {
             dints = DevBuf(a->n_vec2 * a->n_aux * 8, s);
             dkeys = DevBuf(a->n_vec2 * 8, s);
@@ -405,26 +478,49 @@ extern "C" bsg_status bsg_rik_occ_step(bsg_ctx ctx, const bsg_rik_args *a, doubl
             d.c_occ = a->c_occ;
         }
         check_keys(ctx, d.keys, d.n_vec2, (uint64_t)(a->n_bf * a->n_bf));
-        double *Kd = K_out;
+        const size_t nk = a->n_bf * a->n_occ, nkmn = a->n_bf * a->n_bf;
+        double *Kd = K_out, *Kmnd = Kmn_out;
         if (out_where == BSG_HOST) {
-            dk = DevBuf(a->n_bf * a->n_occ * 8, s);
-            Kd = dk.as<double>();
+            if (K_out) {
+                dk = DevBuf(nk * 8, s);
+                Kd = dk.as<double>();
+            }
+            if (Kmn_out) {
+                dkmn = DevBuf(nkmn * 8, s);
+                Kmnd = dkmn.as<double>();
+            }
         }
-        uint64_t st[5] = {0, 0, 0, 0, 0};
-        if (a->form == BSG_FORM_FP64 || d.n_aux == 0) {
-            if (d.n_aux == 0)
-                BSG_CUDA(cudaMemsetAsync(Kd, 0, a->n_bf * a->n_occ * 8, s));
-            else
-                rik_fp64(ctx, d, Kd, st);
+        uint64_t st[6] = {0, 0, 0, 0, 0, 0};
+        if (d.n_aux == 0) {
+            if (Kd) BSG_CUDA(cudaMemsetAsync(Kd, 0, nk * 8, s));
+            if (Kmnd) BSG_CUDA(cudaMemsetAsync(Kmnd, 0, nkmn * 8, s));
+        } else if (a->form == BSG_FORM_FP64) {
+            rik_fp64(ctx, d, Kd, Kmnd, st);
         } else {
-            rik_ozaki(ctx, d, Kd, st);
+            rik_ozaki(ctx, d, Kd, Kmnd, st);
         }
-        if (out_where == BSG_HOST)
-            BSG_CUDA(cudaMemcpyAsync(K_out, Kd, a->n_bf * a->n_occ * 8, cudaMemcpyDeviceToHost, s));
+        if (out_where == BSG_HOST) {
+            if (K_out) BSG_CUDA(cudaMemcpyAsync(K_out, Kd, nk * 8, cudaMemcpyDeviceToHost, s));
+            if (Kmn_out) BSG_CUDA(cudaMemcpyAsync(Kmn_out, Kmnd, nkmn * 8, cudaMemcpyDeviceToHost, s));
+        }
         BSG_CUDA(cudaStreamSynchronize(s));
         if (stats_out)
-            for (int i = 0; i < 5; ++i) stats_out[i] = st[i];
+            for (int i = 0; i < n_stats; ++i) stats_out[i] = st[i];
     });
+}
+
+}  // namespace
+
+extern "C" bsg_status bsg_rik_occ_step(bsg_ctx ctx, const bsg_rik_args *a, double *K_out, int out_where,
+                                       uint64_t stats_out[5]) {
+    if (!K_out) return guard([] { BSG_REQUIRE(false, BSG_ERR_ARG, "NULL argument"); });
+    return rik_entry(ctx, a, K_out, nullptr, out_where, stats_out, 5);
+}
+
+extern "C" bsg_status bsg_rik_kmn_step(bsg_ctx ctx, const bsg_rik_args *a, double *Kmn_out, double *K_out,
+                                       int out_where, uint64_t stats_out[6]) {
+    if (!Kmn_out) return guard([] { BSG_REQUIRE(false, BSG_ERR_ARG, "NULL argument"); });
+    return rik_entry(ctx, a, K_out, Kmn_out, out_where, stats_out, 6);
 }
 
 extern "C" bsg_status bsg_3c2c_transform(bsg_ctx ctx, size_t n_vec2, size_t n_aux, const double *ints_3c,

@@ -15,7 +15,9 @@ struct RikDev {
     int n_digits = 4;
 };
 
-void rik_fp64(bsg_ctx ctx, const RikDev &d, double *K_dev, uint64_t stats[5]);
+// K_dev (n_bf x n_occ) and Kmn_dev (n_bf x n_bf) may each be NULL (that
+// output is skipped); stats: the five occ-step counters and the K_mn products
+void rik_fp64(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uint64_t stats[6]);
 
 // stage kernels shared by the FP64 and Ozaki pipelines (bsg_rik.cu)
 __global__ void k_scatter(const double *__restrict__ ints, const uint64_t *__restrict__ keys, size_t n_vec2,
@@ -26,7 +28,7 @@ __global__ void k_ijs(const double *__restrict__ ij, const uint8_t *__restrict__
                       size_t nob, double *__restrict__ ijs, double *__restrict__ snorm, uint8_t *__restrict__ sflag);
 __global__ void k_cnorms(const double *__restrict__ C, size_t n_bf, size_t n_occ, size_t bs, size_t nb, size_t nob,
                          double *__restrict__ cnorm);
-void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, uint64_t stats[5]);
+void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uint64_t stats[6]);
 // dense device 3c->2c in the Ozaki form (bsg_3c2c_oz.cu)
 void transform_3c2c_ozaki(bsg_ctx ctx, size_t n_vec2, size_t n_aux, const double *X, const double *V, size_t bs,
                           double thresh, int n_digits, double *out, uint64_t *nsig_out);

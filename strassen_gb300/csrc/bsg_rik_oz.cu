@@ -11,6 +11,8 @@
 //   ijs_P = ij + ij^T    FP64 (shared kernel)
 //   K    += mui_P ijs_P  tiles (P sub-range, jb, 5 block rows a), steps over
 //                        (P, ib); per-tile partial blocks summed in order
+//   Kmn  += mui_P mui_P^T  (optional) tiles (P sub-range, b, block rows a >= b),
+//                        steps over (P, jb); lower blocks, mirrored at the end
 // Operand scales: U rows per (P, mu); C columns per i (also the rows of C^T);
 // mui columns per (P, j) for the ij product; mui rows and ijs columns per
 // (P sub-range, mu / j) for the K product.  Every tile has one scale set, so
@@ -256,6 +258,18 @@ __global__ void k_img_mui_A(const double *__restrict__ mui, const uint8_t *__res
                 img + x * D.nd * (size_t)D.mp * D.kp, true);
 }
 
+// mui_p blocks (b, jb) as the B operand of K_mn = mui mui^T (rows b, k = jb; the
+// same digits as the A image, in the N-side layout); index p*nb*nob + b + jb*nb
+__global__ void k_img_mui_T(const double *__restrict__ mui, const uint8_t *__restrict__ mflag,
+                            const int *__restrict__ rexp, size_t Q, OzDims D, size_t n, bf16 *__restrict__ img) {
+    const size_t x = oz_warp_id();
+    if (x >= n || !mflag[x]) return;
+    const size_t p = x / (D.nb * D.nob), b = x % D.nb, jb = (x / D.nb) % D.nob;
+    oz_block_image(mui + p * D.n_bf * D.n_occ + b * D.bs + jb * D.bs * D.n_bf, D.n_bf, false, ext_r(b, D.bs, D.n_bf),
+                ext_r(jb, D.bs, D.n_occ), rexp + (p / Q) * D.n_bf + b * D.bs, D.np, D.kp, D.nd,
+                img + x * D.nd * (size_t)D.np * D.kp, false);
+}
+
 // ijs_p blocks (ib, jb) in the B role of the K product; index p*nob*nob + ib + jb*nob
 __global__ void k_img_ijs_B(const double *__restrict__ ijs, const uint8_t *__restrict__ sflag,
                             const int *__restrict__ cexp, size_t Q, OzDims D, size_t n, bf16 *__restrict__ img) {
@@ -470,6 +484,105 @@ __global__ void k_K_reduce(const double *__restrict__ Kpart, size_t n_sub, OzDim
     }
 }
 
+// (b, g) pairs of the K_mn tiles: block column b, group g of R block rows
+// a = g R .. g R + R - 1 with at least one a >= b; pairs ordered by b, then g
+__host__ __device__ inline size_t kmn_pairs(size_t nb, size_t R) {
+    const size_t ng = (nb + R - 1) / R;
+    size_t n = 0;
+    for (size_t b = 0; b < nb; ++b) n += ng - b / R;
+    return n;
+}
+
+// K_mn tiles: t = (sub-range, pair (b, g)), steps over (p, jb); slots a < b
+// are left out (their blocks are the mirrors of a > b)
+__global__ void k_tiles_Kmn(const uint8_t *__restrict__ mflag, const double *__restrict__ mnorm,
+                            const int *__restrict__ rexp_sub, double *__restrict__ Kpart, OzDims D, size_t np,
+                            size_t Q, size_t n_pairs, size_t n_tiles, double tpb, OzTile *__restrict__ tiles,
+                            OzStep *__restrict__ steps, unsigned long long *__restrict__ nsig,
+                            unsigned long long *__restrict__ macs) {
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_tiles) return;
+    const size_t ng = (D.nb + D.R - 1) / D.R, sub = t / n_pairs;
+    size_t rem = t % n_pairs, b = 0, g = 0;
+    for (; b < D.nb; ++b) {
+        const size_t c = ng - b / D.R;
+        if (rem < c) {
+            g = b / D.R + rem;
+            break;
+        }
+        rem -= c;
+    }
+    unsigned long long m = 0;
+    OzTile T;
+    tile_clear(T);
+    const size_t bs2 = D.bs * D.bs;
+    for (int s = 0; s < D.R; ++s) {
+        const size_t a = g * D.R + s;
+        if (a >= D.nb) break;
+        if (a < b) continue;
+        T.c[s] = Kpart + ((sub * D.nb + b) * D.nb + a) * bs2;
+        T.rows[s] = ext_r(a, D.bs, D.n_bf);
+        T.ldc[s] = T.rows[s];
+        T.rexp[s] = rexp_sub + sub * D.n_bf + a * D.bs;
+    }
+    T.cols = ext_r(b, D.bs, D.n_bf);
+    T.trans = 0;
+    T.cexp = rexp_sub + sub * D.n_bf + b * D.bs;
+    T.s0 = (uint32_t)(t * Q * D.nob);
+    uint32_t n = 0;
+    unsigned long long tot = 0;
+    const size_t p1 = min(np, (sub + 1) * Q);
+    for (size_t p = sub * Q; p < p1; ++p)
+        for (size_t jb = 0; jb < D.nob; ++jb) {
+            const size_t mb = p * D.nb * D.nob + b + jb * D.nb;
+            if (!mflag[mb]) continue;
+            OzStep st;
+            st.bmask = kOzAllSub;
+            st.b = (uint32_t)mb;
+            bool any = false;
+            for (int s = 0; s < kOzMaxSlots; ++s) {
+                st.a[s] = kOzNone;
+                if (s >= D.R || !T.c[s]) continue;
+                const size_t a = g * D.R + s, ma = p * D.nb * D.nob + a + jb * D.nb;
+                if (!mflag[ma]) continue;
+                if (!(__dmul_rn(mnorm[ma], mnorm[mb]) >= tpb)) continue;
+                st.a[s] = (uint32_t)ma;
+                m += (unsigned long long)T.rows[s] * T.cols * ext_r(jb, D.bs, D.n_occ);
+                ++tot;
+                any = true;
+            }
+            if (any) steps[T.s0 + n++] = st;
+        }
+    T.ns = n;
+    tiles[t] = T;
+    if (tot) atomicAdd(nsig, tot);
+    if (m) atomicAdd(macs, m);
+}
+
+// K_mn(a, b) += sum over sub-ranges (in order) of the tiles' partial blocks, a >= b
+__global__ void k_Kmn_reduce(const double *__restrict__ Kpart, size_t n_sub, OzDims D, double *__restrict__ K) {
+    const size_t blk = blockIdx.x;  // (b, a)
+    const size_t a = blk % D.nb, b = blk / D.nb;
+    if (a < b) return;
+    const int rows = ext_r(a, D.bs, D.n_bf), cols = ext_r(b, D.bs, D.n_bf);
+    const size_t bs2 = D.bs * D.bs;
+    for (int e = threadIdx.x; e < rows * cols; e += blockDim.x) {
+        const int r = e % rows, c = e / rows;
+        double acc = K[a * D.bs + r + (b * D.bs + c) * D.n_bf];
+        for (size_t sub = 0; sub < n_sub; ++sub) acc += Kpart[((sub * D.nb + b) * D.nb + a) * bs2 + e];
+        K[a * D.bs + r + (b * D.bs + c) * D.n_bf] = acc;
+    }
+}
+
+// upper triangle of K_mn from the lower one (diagonal blocks by element)
+__global__ void k_Kmn_mirror(double *__restrict__ K, size_t n_bf, size_t bs) {
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n_bf * n_bf) return;
+    const size_t gi = e % n_bf, gj = e / n_bf;
+    const size_t bi = gi / bs, bj = gj / bs;
+    if (bi < bj || (bi == bj && gi < gj)) K[e] = K[gj + gi * n_bf];
+}
+
 // FP64 block norms of mui (warp per present block)
 __global__ void k_mui_norms(const double *__restrict__ mui, const uint8_t *__restrict__ mflag, size_t n_bf,
                             size_t n_occ, size_t bs, size_t nb, size_t nob, size_t n, double *__restrict__ mnorm) {
@@ -481,7 +594,7 @@ __global__ void k_mui_norms(const double *__restrict__ mui, const uint8_t *__res
     if ((threadIdx.x & 31) == 0) mnorm[x] = est;
 }
 
-void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, uint64_t stats[5]) {
+void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uint64_t stats[6]) {
     cudaStream_t s = ctx->stream;
     const size_t n_bf = d.n_bf, n_occ = d.n_occ, bs = d.bs, n_aux = d.n_aux;
     BSG_REQUIRE(bs <= 64, BSG_ERR_UNSUPPORTED, "RI-K Ozaki form supports bs <= 64");
@@ -501,12 +614,13 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, uint64_t stats[5]) {
     const size_t nb = D.nb, nob = D.nob;
     const size_t a_img = (size_t)nd * sh.mp * sh.kp, b_img = (size_t)nd * sh.np * sh.kp;  // elements per image
     // bytes per aux function of every per-chunk buffer
+    const bool want_k = K_dev != nullptr, want_kmn = Kmn_dev != nullptr;
+    const size_t Q = 8;  // aux functions per K-product tile
     const size_t per_p = nb * nb * 9 + nb * nb * a_img * 2 + n_bf * n_occ * 8 + nb * nob * 9 +
                          nb * nob * (a_img + b_img) * 2 + 3 * n_occ * n_occ * 8 + 3 * nob * nob * 9 +
-                         nob * nob * b_img * 2;
+                         nob * nob * b_img * 2 + (want_kmn ? nb * nob * b_img * 2 + nb * nb * bs * bs * 8 / Q : 0);
     size_t pc = d.p_chunk ? d.p_chunk : std::max<size_t>(1, (size_t)(8ull << 30) / per_p);
     pc = std::max<size_t>(1, std::min(pc, n_aux));
-    const size_t Q = 8;  // aux functions per K-product tile
     const size_t n_sub_max = ceil_div(pc, Q);
 
     DevBuf dinv(n_bf * n_bf * 4, s), docc(nb * nb, s), dun(pc * nb * nb * 8, s), duf(pc * nb * nb, s);
@@ -524,14 +638,20 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, uint64_t stats[5]) {
     auto *bitsU = dbits.as<unsigned long long>(), *bitsM = bitsU + pc * n_bf, *bitsMs = bitsM + pc * n_occ,
          *bitsSs = bitsMs + n_sub_max * n_bf;
     DevBuf dimgMA(pc * nb * nob * a_img * 2, s), dimgSB(pc * nob * nob * b_img * 2, s);
-    DevBuf dKp(n_sub_max * nob * nb * bs * bs * 8, s), dcnt(5 * 8, s), dmacs(3 * 8, s);
+    DevBuf dKp(want_k ? n_sub_max * nob * nb * bs * bs * 8 : 0, s), dcnt(6 * 8, s), dmacs(4 * 8, s);
     const size_t ng_a = ceil_div(nb, (size_t)D.R), ng_i = ceil_div(nob, (size_t)D.R);
     const size_t tiles_mui = pc * nob * ng_a, tiles_ij = pc * nob * ng_i, tiles_K = n_sub_max * nob * ng_a;
     DevBuf dtm(tiles_mui * sizeof(OzTile), s), dsm(tiles_mui * nb * sizeof(OzStep), s);
     DevBuf dti(tiles_ij * sizeof(OzTile), s), dsi(tiles_ij * nb * sizeof(OzStep), s);
     DevBuf dtk(tiles_K * sizeof(OzTile), s), dsk(tiles_K * Q * nob * sizeof(OzStep), s);
-    BSG_CUDA(cudaMemsetAsync(K_dev, 0, n_bf * n_occ * 8, s));
-    BSG_CUDA(cudaMemsetAsync(dcnt.p, 0, 5 * 8, s));
+    // K_mn: images of mui in the B role, tiles over (sub-range, lower pair), partials
+    const size_t n_pairs = kmn_pairs(nb, (size_t)D.R), tiles_Kmn = want_kmn ? n_sub_max * n_pairs : 0;
+    DevBuf dimgMT(want_kmn ? pc * nb * nob * b_img * 2 : 0, s);
+    DevBuf dKmnp(want_kmn ? n_sub_max * nb * nb * bs * bs * 8 : 0, s);
+    DevBuf dtkm(tiles_Kmn * sizeof(OzTile), s), dskm(tiles_Kmn * Q * nob * sizeof(OzStep), s);
+    if (want_k) BSG_CUDA(cudaMemsetAsync(K_dev, 0, n_bf * n_occ * 8, s));
+    if (want_kmn) BSG_CUDA(cudaMemsetAsync(Kmn_dev, 0, n_bf * n_bf * 8, s));
+    BSG_CUDA(cudaMemsetAsync(dcnt.p, 0, 6 * 8, s));
     auto *cnt = dcnt.as<unsigned long long>();
     auto *macs = dmacs.as<unsigned long long>();
     const unsigned tb = (unsigned)std::max<size_t>(32, ((bs + 31) / 32) * 32);
@@ -553,7 +673,7 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, uint64_t stats[5]) {
     const double tpb = d.thresh * (double)(bs * bs * bs);
     for (size_t P0 = 0; P0 < n_aux; P0 += pc) {
         const size_t np = std::min(pc, n_aux - P0), n_sub = ceil_div(np, Q);
-        BSG_CUDA(cudaMemsetAsync(macs, 0, 3 * 8, s));
+        BSG_CUDA(cudaMemsetAsync(macs, 0, 4 * 8, s));
         // U_p block norms, keep flags, row exponents and digit images, all
         // gathered from the compressed integrals
         k_unorms_c<<<oz_img_grid(np * nb * nb), 32 * kOzImgWarps, 0, s>>>(
@@ -576,6 +696,31 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, uint64_t stats[5]) {
         oz_run(ctx, sh, dtm.as<OzTile>(), tm, dsm.as<OzStep>(), dimgU.as<bf16>(), dimgCB.as<bf16>(), 1.0, s, macs + 0);
         k_mui_norms<<<(unsigned)ceil_div(np * nb * nob, wpb), wpb * 32, 0, s>>>(
             dmui.as<double>(), dmf.as<uint8_t>(), n_bf, n_occ, bs, nb, nob, np * nb * nob, dmn.as<double>());
+        // mui row exponents per sub-range (A operand of K and of K_mn)
+        k_rowmax_mui_sub<<<oz_img_grid(np * nb * nob), 32 * kOzImgWarps, 0, s>>>(
+            dmui.as<double>(), dmf.as<uint8_t>(), n_bf, n_occ, bs, nb, nob, Q, np * nb * nob, bitsMs);
+        k_bits_exp<<<(unsigned)ceil_div(n_sub * n_bf, (size_t)256), 256, 0, s>>>(bitsMs, n_sub * n_bf,
+                                                                                 drexpMs.as<int>());
+        k_img_mui_A<<<oz_img_grid(np * nb * nob), 32 * kOzImgWarps, 0, s>>>(
+            dmui.as<double>(), dmf.as<uint8_t>(), drexpMs.as<int>(), Q, D, np * nb * nob, dimgMA.as<bf16>());
+        ctx->note_launch(4);
+        if (want_kmn) {
+            // K_mn += mui mui^T
+            k_img_mui_T<<<oz_img_grid(np * nb * nob), 32 * kOzImgWarps, 0, s>>>(
+                dmui.as<double>(), dmf.as<uint8_t>(), drexpMs.as<int>(), Q, D, np * nb * nob, dimgMT.as<bf16>());
+            const size_t tkm = n_sub * n_pairs;
+            k_tiles_Kmn<<<(unsigned)ceil_div(tkm, 128), 128, 0, s>>>(
+                dmf.as<uint8_t>(), dmn.as<double>(), drexpMs.as<int>(), dKmnp.as<double>(), D, np, Q, n_pairs, tkm,
+                tpb, dtkm.as<OzTile>(), dskm.as<OzStep>(), cnt + 5, macs + 3);
+            ctx->note_launch(2);
+            ctx->check_launch("rik ozaki Kmn prep");
+            oz_run(ctx, sh, dtkm.as<OzTile>(), tkm, dskm.as<OzStep>(), dimgMA.as<bf16>(), dimgMT.as<bf16>(), 1.0, s,
+                   macs + 3);
+            k_Kmn_reduce<<<(unsigned)(nb * nb), 256, 0, s>>>(dKmnp.as<double>(), n_sub, D, Kmn_dev);
+            ctx->note_launch();
+            ctx->check_launch("rik ozaki Kmn reduce");
+        }
+        if (!want_k) continue;
         // ij = C^T mui
         k_colmax_mui<<<oz_img_grid(np * nb * nob), 32 * kOzImgWarps, 0, s>>>(
             dmui.as<double>(), dmf.as<uint8_t>(), n_bf, n_occ, bs, nb, nob, np * nb * nob, bitsM);
@@ -586,23 +731,17 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, uint64_t stats[5]) {
         k_tiles_ij<<<(unsigned)ceil_div(ti, 128), 128, 0, s>>>(
             dmf.as<uint8_t>(), dmn.as<double>(), dcn.as<double>(), dcexpC.as<int>(), dcexpM.as<int>(),
             dij.as<double>(), D, ti, tpb, dti.as<OzTile>(), dsi.as<OzStep>(), dijf.as<uint8_t>(), cnt + 1, macs + 1);
-        ctx->note_launch(5);
+        ctx->note_launch(4);
         ctx->check_launch("rik ozaki ij prep");
         oz_run(ctx, sh, dti.as<OzTile>(), ti, dsi.as<OzStep>(), dimgCtA.as<bf16>(), dimgMB.as<bf16>(), 1.0, s, macs + 1);
         // ijs = ij + ij^T (FP64, with the reference's norm bookkeeping)
         k_ijs<<<(unsigned)(np * nob * nob), 128, 0, s>>>(dij.as<double>(), dijf.as<uint8_t>(), n_occ, bs, nob,
                                                           dijs.as<double>(), dsn.as<double>(), dsf.as<uint8_t>());
         // K += mui ijs
-        k_rowmax_mui_sub<<<oz_img_grid(np * nb * nob), 32 * kOzImgWarps, 0, s>>>(
-            dmui.as<double>(), dmf.as<uint8_t>(), n_bf, n_occ, bs, nb, nob, Q, np * nb * nob, bitsMs);
         k_colmax_ijs_sub<<<oz_img_grid(np * nob * nob), 32 * kOzImgWarps, 0, s>>>(
             dijs.as<double>(), dsf.as<uint8_t>(), n_occ, bs, nob, Q, np * nob * nob, bitsSs);
-        k_bits_exp<<<(unsigned)ceil_div(n_sub * n_bf, (size_t)256), 256, 0, s>>>(bitsMs, n_sub * n_bf,
-                                                                                 drexpMs.as<int>());
         k_bits_exp<<<(unsigned)ceil_div(n_sub * n_occ, (size_t)256), 256, 0, s>>>(bitsSs, n_sub * n_occ,
                                                                                   dcexpSs.as<int>());
-        k_img_mui_A<<<oz_img_grid(np * nb * nob), 32 * kOzImgWarps, 0, s>>>(
-            dmui.as<double>(), dmf.as<uint8_t>(), drexpMs.as<int>(), Q, D, np * nb * nob, dimgMA.as<bf16>());
         k_img_ijs_B<<<oz_img_grid(np * nob * nob), 32 * kOzImgWarps, 0, s>>>(
             dijs.as<double>(), dsf.as<uint8_t>(), dcexpSs.as<int>(), Q, D, np * nob * nob, dimgSB.as<bf16>());
         const size_t tk = n_sub * nob * ng_a;
@@ -610,19 +749,23 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, uint64_t stats[5]) {
             dmf.as<uint8_t>(), dmn.as<double>(), dsf.as<uint8_t>(), dsn.as<double>(), drexpMs.as<int>(),
             dcexpSs.as<int>(), dKp.as<double>(), D, np, Q, tk, tpb, dtk.as<OzTile>(), dsk.as<OzStep>(), cnt + 2,
             macs + 2);
-        ctx->note_launch(8);
+        ctx->note_launch(5);
         ctx->check_launch("rik ozaki K prep");
         oz_run(ctx, sh, dtk.as<OzTile>(), tk, dsk.as<OzStep>(), dimgMA.as<bf16>(), dimgSB.as<bf16>(), 1.0, s, macs + 2);
         k_K_reduce<<<(unsigned)(nb * nob), 256, 0, s>>>(dKp.as<double>(), n_sub, D, K_dev);
         ctx->note_launch();
         ctx->check_launch("rik ozaki K reduce");
     }
+    if (want_kmn) {
+        k_Kmn_mirror<<<(unsigned)ceil_div(n_bf * n_bf, (size_t)256), 256, 0, s>>>(Kmn_dev, n_bf, bs);
+        ctx->note_launch();
+    }
     ctx->gemm_check();
     if (stats) {
-        unsigned long long h[5];
-        BSG_CUDA(cudaMemcpyAsync(h, cnt, 5 * 8, cudaMemcpyDeviceToHost, s));
+        unsigned long long h[6];
+        BSG_CUDA(cudaMemcpyAsync(h, cnt, 6 * 8, cudaMemcpyDeviceToHost, s));
         BSG_CUDA(cudaStreamSynchronize(s));
-        for (int i = 0; i < 5; ++i) stats[i] = h[i];
+        for (int i = 0; i < 6; ++i) stats[i] = h[i];
     }
 }
 

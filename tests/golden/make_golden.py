@@ -9,6 +9,11 @@ Run where the reference sources are available (they are read from
   occ-RI-K K matrix (occ_ri_k_step.cpp:83-130, partitions 1 and 4) and the
   3c->2c transform (3c_2c_transform.cpp:44-57), plus the norm line printed by
   the reference's own driver binary.
+* ``h2o_kmn_golden.npz`` -- the symmetric exchange matrix K_mn =
+  sum_{P,i} mui_P(m,i) mui_P(n,i) built on the compiled reference's classes
+  (its mui_P, occ_ri_k_step.cpp:102-108, then matmult(Ks, mui, N, mui, T)),
+  partitions 1 and 4, thresholds 1e-20 and 1e-6.  ``make_golden.py kmn``
+  rewrites only this file.
 * ``ref_cases.npz`` -- small seeded matmult / Strassen / dry-run cases with
   the compiled reference's results, masks and norms (Strassen outputs as
   SHA-256 of their bytes).  Inputs are rebuilt from the stored per-block
@@ -40,8 +45,27 @@ H2O = {
 N_BF, N_AUX, N_OCC, N_VEC2, BS = 24, 113, 5, 322, 3
 
 
+def h2o_inputs():
+    ints = np.fromfile(os.path.join(HERE, "h2o_3c_ints_PQm12.bin")).reshape(N_AUX, N_VEC2).T
+    c = np.fromfile(os.path.join(HERE, "h2o_occ_mo.bin")).reshape(N_OCC, N_BF).T
+    keys = np.fromfile(os.path.join(HERE, "h2o_v2m_key.bin"), dtype=np.uint64)
+    return ints, keys, c
+
+
+def kmn():
+    ints, keys, c = h2o_inputs()
+    out = {}
+    for n_part in (1, 4):
+        for tag, thr in (("t20", 1e-20), ("t6", 1e-6)):
+            out[f"Kmn_part{n_part}_{tag}"] = O.ref_rik_kmn_step(ints, keys, c, N_BF, N_AUX, N_OCC, BS, thr, n_part)
+    np.savez(os.path.join(HERE, "h2o_kmn_golden.npz"), **out)
+
+
 def main():
     subprocess.check_call(["bash", os.path.join(ROOT, "oracle", "build_ref.sh")], env=dict(os.environ, REF_DIR=REF_DIR))
+    if sys.argv[1:] == ["kmn"]:
+        kmn()
+        return
     for dst, src in H2O.items():
         shutil.copyfile(os.path.join(REF_DIR, src), os.path.join(HERE, dst))
     ints = np.fromfile(os.path.join(HERE, "h2o_3c_ints_PQm12.bin")).reshape(N_AUX, N_VEC2).T
@@ -59,6 +83,7 @@ def main():
     norm_line = re.search(r"L2 norm of output = (\S+)", drv).group(1)
     np.savez(os.path.join(HERE, "h2o_golden.npz"), K_part1=k1, K_part4=k4, X_PQm12=t3,
              driver_norm_line=np.array(norm_line))
+    kmn()
 
     # Small seeded cases.  Inputs are rebuilt in the tests from (seed,
     # stream, per-block envelope table) with strassen_gb300.synth, which is

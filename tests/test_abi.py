@@ -16,7 +16,8 @@ def declared_symbols():
 
 def test_header_declares_entry_points():
     syms = declared_symbols()
-    for must in ("bsg_matmult", "bsg_matmult_strassen_sparse", "bsg_rik_occ_step", "bsg_3c2c_transform",
+    for must in ("bsg_matmult", "bsg_matmult_strassen_sparse", "bsg_rik_occ_step", "bsg_rik_kmn_step",
+                 "bsg_3c2c_transform",
                  "bsg_bsm_create", "bsg_pool_create", "bsg_tensormult_contract", "bsg_strassen_dryrun"):
         assert must in syms
 
@@ -39,3 +40,4 @@ def test_null_arguments_are_rejected(api):
     assert b"NULL" in api.lib.bsg_last_error()
     assert api.lib.bsg_matmult(None, None, 0, None, 0, 0.0, 1.0, 0.0, None) != 0
     assert api.lib.bsg_rik_occ_step(None, None, None, 0, None) != 0
+    assert api.lib.bsg_rik_kmn_step(None, None, None, None, 0, None) != 0

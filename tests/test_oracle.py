@@ -131,3 +131,54 @@ def test_oracle_rejects_bad_keys(oracle, h2o):
     keys[3] = d["n_bf"] ** 2
     with pytest.raises(ValueError):
         oracle.rik_occ_step(d["ints"], keys, d["c"], d["n_bf"], d["n_aux"], d["n_occ"], 3, 1e-20, 1)
+
+
+# ---- symmetric K_mn on the occ step's mui_P ----
+
+def _kmn_gold():
+    import os
+
+    from tests.conftest import GOLDEN
+    return np.load(os.path.join(GOLDEN, "h2o_kmn_golden.npz"))
+
+
+@pytest.mark.parametrize("n_part", [1, 4])
+@pytest.mark.parametrize("tag,thr", [("t20", 1e-20), ("t6", 1e-6)])
+def test_kmn_known_answer(oracle, h2o, n_part, tag, thr):
+    """K_mn restatement == the same contraction on the compiled reference's
+    classes (fixture), and exactly symmetric"""
+    d = h2o
+    K = oracle.rik_kmn_step(d["ints"], d["keys"], d["c"], d["n_bf"], d["n_aux"], d["n_occ"], 3, thr, n_part)
+    assert same_bits(K, _kmn_gold()[f"Kmn_part{n_part}_{tag}"])
+    assert np.array_equal(K, K.T)
+
+
+def test_kmn_dense_formula(oracle, h2o):
+    """at a negligible threshold K_mn = sum_P (U_P C)(U_P C)^T to rounding"""
+    d = h2o
+    n, keys = d["n_bf"], d["keys"].astype(np.int64)
+    K = oracle.rik_kmn_step(d["ints"], d["keys"], d["c"], n, d["n_aux"], d["n_occ"], 3, 1e-20, 1)
+    ref = np.zeros((n, n))
+    for P in range(d["n_aux"]):
+        U = np.zeros(n * n)
+        U[keys] = d["ints"][:, P]
+        m = U.reshape(n, n, order="F") @ d["c"]
+        ref += m @ m.T
+    assert np.linalg.norm(K - ref) / np.linalg.norm(ref) < 1e-13
+
+
+def test_kmn_symmetric_u_identity(oracle):
+    """for symmetric U_P the occ step's K_{mu j} = sum_P mui (ij + ji) equals
+    2 K_mn C: ties the new contraction to the reference's own output"""
+    rng = np.random.default_rng(3)
+    n_bf, n_aux, n_occ, bs = 20, 9, 6, 4
+    r, c = np.meshgrid(np.arange(n_bf), np.arange(n_bf), indexing="ij")
+    keys = (r + c * n_bf).ravel(order="F").astype(np.uint64)
+    ints = np.empty((n_bf * n_bf, n_aux), order="F")
+    for P in range(n_aux):
+        A = rng.standard_normal((n_bf, n_bf))
+        ints[:, P] = (A + A.T).ravel(order="F")
+    C = np.asfortranarray(rng.standard_normal((n_bf, n_occ)))
+    K = oracle.rik_occ_step(ints, keys, C, n_bf, n_aux, n_occ, bs, 1e-30, 1)
+    Kmn = oracle.rik_kmn_step(ints, keys, C, n_bf, n_aux, n_occ, bs, 1e-30, 1)
+    assert np.linalg.norm(K - 2 * Kmn @ C) / np.linalg.norm(K) < 1e-13
