@@ -46,25 +46,32 @@ static void *oz_zero_image() {
 
 static int round_up(int x, int m) { return (x + m - 1) / m * m; }
 
-OzShape oz_shape(int bs_rows, int bs_k, int bs_cols, int nd) {
-    OzShape s;
-    s.nd = nd;
-    s.mp = round_up(bs_rows, 8);
-    s.kp = round_up(bs_k, 16);
-    s.np = round_up(bs_cols, 8);
-    s.R = std::min(kOzMaxSlots, 128 / s.mp);
-    s.F = std::max(1, 512 / s.kp);
-    return s;
-}
-
 // B rows of a stage: the nd stacked digit planes, rounded up to the MMA's
 // N granularity of 16 (an MMA over an odd number of 8-row planes reads 8
 // zero rows past the stack)
 static uint32_t oz_b_rows(int nd, int np) { return (uint32_t)round_up(nd * np, 16); }
-static uint32_t oz_stage_bytes(const OzShape &sh) {
+// bytes of one step's A and B operands in shared memory
+static uint32_t oz_half_bytes(const OzShape &sh) {
     return (uint32_t)sh.nd * 128u * sh.kp * 2u + oz_b_rows(sh.nd, sh.np) * sh.kp * 2u;
 }
+static uint32_t oz_stage_bytes(const OzShape &sh) { return (sh.pair ? 2u : 1u) * oz_half_bytes(sh); }
 constexpr uint32_t kOzSmemBudget = 200u * 1024u;
+
+OzShape oz_shape(int bs_rows, int bs_k, int bs_cols, int nd) {
+    OzShape s;
+    s.nd = nd;
+    s.mp = round_up(bs_rows, 8);
+    s.np = round_up(bs_cols, 8);
+    s.R = std::min(kOzMaxSlots, 128 / s.mp);
+    // k rounded up to 8 leaves an odd number of 8-wide core columns: pair the
+    // steps (no zero padding in k) where two stages of pairs fit
+    s.kp = round_up(bs_k, 8);
+    s.pair = (s.kp % 16 == 8) ? 1 : 0;
+    if (s.pair && kOzSmemBudget / oz_stage_bytes(s) < 2) s.pair = 0;
+    if (!s.pair) s.kp = round_up(bs_k, 16);
+    s.F = s.pair ? 2 * std::max(1, 512 / (2 * s.kp)) : std::max(1, 512 / s.kp);
+    return s;
+}
 
 int oz_default_digits(int requested, int bs_rows, int bs_k, int bs_cols) {
     if (requested) {
@@ -81,6 +88,7 @@ int oz_default_digits(int requested, int bs_rows, int bs_k, int bs_cols) {
 
 struct OzKParams {
     int mp, kp, R, nd, S, F;
+    int pair;            // two steps per stage (OzShape::pair)
     int J;               // N-side sub-blocks of a B image (NP / J rows each)
     uint32_t chunk;      // consecutive tiles per CTA turn
     int nbuf;            // TMEM accumulator sets (2: the MMA fills one while the epilogue drains the other)
@@ -125,7 +133,8 @@ __global__ void __launch_bounds__(kOzThreads, 1)
     const uint32_t a_stage = (uint32_t)P.nd * 128u * P.kp * 2u;  // A: 128 rows x nd digits (M-side layout)
     const uint32_t b_copy = (uint32_t)P.nd * NP * P.kp * 2u;           // bytes of one B digit stack
     const uint32_t b_stage = (uint32_t)((P.nd * NP + 15) & ~15) * P.kp * 2u;  // stage room (N rounded to 16)
-    const uint32_t stage_bytes = a_stage + b_stage;
+    const uint32_t half_bytes = a_stage + b_stage;  // one step's operands; a pair stage holds two
+    const uint32_t stage_bytes = P.pair ? 2u * half_bytes : half_bytes;
     const uint32_t slot_bytes = (uint32_t)P.nd * P.mp * P.kp * 2u;  // one slot's full digit image
     const size_t slot_elems = (size_t)P.nd * P.mp * P.kp, b_img_elems = (size_t)P.nd * NP * P.kp;
     OzStep *sstep = reinterpret_cast<OzStep *>(smem + (size_t)P.S * stage_bytes);  // 32 prefetched steps
@@ -164,14 +173,45 @@ __global__ void __launch_bounds__(kOzThreads, 1)
 
     if (warp == 0) {
         // ---------------- producer ----------------
-        uint32_t it = 0;
+        uint32_t it = 0;  // stages filled
         unsigned long long w_empty = 0;
-        uint32_t stage = 0, ph = 0;  // ring position of step `it`
+        uint32_t stage = 0, ph = 0;  // ring position of stage `it`
+        const uint32_t jfull = (1u << P.J) - 1u;
+        // one step's A slots and B digit stack into the half-stage at sA / sB
+        auto copy_step = [&](const OzStep &st, uint8_t *sA, uint8_t *sB, uint64_t *bar) {
+            // slots whose images are consecutive in a_img (or all zero) go
+            // in one copy: a fully live step is one A copy and one B copy
+            const uint32_t ai = lane < P.R ? st.a[lane] : kOzNone;
+            const uint32_t prev = __shfl_up_sync(0xffffffffu, ai, 1);
+            const bool live = ai != kOzNone;
+            const bool joins = lane > 0 && (live ? (prev != kOzNone && prev + 1u == ai) : prev == kOzNone);
+            const uint32_t starts = __ballot_sync(0xffffffffu, lane < P.R && !joins) | (1u << P.R);
+            if (lane < P.R && !joins) {
+                const int len = __ffs(starts & ~((2u << lane) - 1u)) - 1 - lane;
+                const bf16 *src = live ? a_img + (size_t)ai * slot_elems : P.zero;
+                tc::bulk_g2s(sA + lane * slot_bytes, src, (uint32_t)len * slot_bytes, bar);
+            }
+            if ((st.bmask & jfull) == jfull) {
+                if (lane == 31) tc::bulk_g2s(sB, b_img + (size_t)st.b * b_img_elems, b_copy, bar);
+            } else {
+                // some N-side sub-blocks are screened out for this step: per
+                // (sub-block, digit) chunk, the image's rows or zeros
+                const int npj = NP / P.J, c = lane - 16;
+                if (c >= 0 && c < P.J * P.nd) {
+                    const int j = c / P.nd, i = c % P.nd;
+                    const size_t off = ((size_t)i * NP + (size_t)j * npj) * P.kp;
+                    const bf16 *src = ((st.bmask >> j) & 1u) ? b_img + (size_t)st.b * b_img_elems + off : P.zero;
+                    tc::bulk_g2s(sB + off * 2, src, (uint32_t)npj * P.kp * 2u, bar);
+                }
+            }
+        };
+        const uint32_t kstep = P.pair ? 2u : 1u;
         for (uint32_t t = oz_first_tile(P.chunk); t < n_tiles && !*abort; t = oz_next_tile(t, P.chunk)) {
             const uint32_t s0 = tiles[t].s0, ns = tiles[t].ns;
-            for (uint32_t k = 0; k < ns; ++k, ++it) {
+            for (uint32_t k = 0; k < ns; k += kstep, ++it) {
                 if ((k & 31u) == 0) {
-                    // the warp loads the next 32 step descriptors at once
+                    // the warp loads the next 32 step descriptors at once (a
+                    // pair never crosses a batch: k is even in pair mode)
                     __syncwarp();
                     if (k + lane < ns) sstep[lane] = steps[s0 + k + lane];
                     __syncwarp();
@@ -184,36 +224,20 @@ __global__ void __launch_bounds__(kOzThreads, 1)
                     if (prof) w_empty += clock64() - c0;
                 }
                 if (!__shfl_sync(0xffffffffu, okw, 0)) break;
-                const OzStep st = sstep[k & 31u];
                 uint8_t *sA = smem + (size_t)stage * stage_bytes;
                 uint8_t *sB = sA + a_stage;
-                if (lane == 0) tc::mbar_arrive_expect_tx(&full[stage], P.tx_bytes);
+                const bool two = P.pair && k + 1 < ns;
+                // a lone last step of a pair stage gets a zero B in the second
+                // half: the k16 slice that straddles into it then adds nothing
+                // (its A half holds earlier digits or zeros, always finite)
+                const uint32_t tx = two ? 2u * P.tx_bytes : (P.pair ? P.tx_bytes + b_copy : P.tx_bytes);
+                if (lane == 0) tc::mbar_arrive_expect_tx(&full[stage], tx);
                 __syncwarp();
-                // slots whose images are consecutive in a_img (or all zero) go
-                // in one copy: a fully live step is one A copy and one B copy
-                const uint32_t ai = lane < P.R ? st.a[lane] : kOzNone;
-                const uint32_t prev = __shfl_up_sync(0xffffffffu, ai, 1);
-                const bool live = ai != kOzNone;
-                const bool joins = lane > 0 && (live ? (prev != kOzNone && prev + 1u == ai) : prev == kOzNone);
-                const uint32_t starts = __ballot_sync(0xffffffffu, lane < P.R && !joins) | (1u << P.R);
-                if (lane < P.R && !joins) {
-                    const int len = __ffs(starts & ~((2u << lane) - 1u)) - 1 - lane;
-                    const bf16 *src = live ? a_img + (size_t)ai * slot_elems : P.zero;
-                    tc::bulk_g2s(sA + lane * slot_bytes, src, (uint32_t)len * slot_bytes, &full[stage]);
-                }
-                const uint32_t jfull = (1u << P.J) - 1u;
-                if ((st.bmask & jfull) == jfull) {
-                    if (lane == 31) tc::bulk_g2s(sB, b_img + (size_t)st.b * b_img_elems, b_copy, &full[stage]);
-                } else {
-                    // some N-side sub-blocks are screened out for this step: per
-                    // (sub-block, digit) chunk, the image's rows or zeros
-                    const int npj = NP / P.J, c = lane - 16;
-                    if (c >= 0 && c < P.J * P.nd) {
-                        const int j = c / P.nd, i = c % P.nd;
-                        const size_t off = ((size_t)i * NP + (size_t)j * npj) * P.kp;
-                        const bf16 *src = ((st.bmask >> j) & 1u) ? b_img + (size_t)st.b * b_img_elems + off : P.zero;
-                        tc::bulk_g2s(sB + off * 2, src, (uint32_t)npj * P.kp * 2u, &full[stage]);
-                    }
+                copy_step(sstep[k & 31u], sA, sB, &full[stage]);
+                if (two) {
+                    copy_step(sstep[(k + 1) & 31u], sA + half_bytes, sB + half_bytes, &full[stage]);
+                } else if (P.pair && lane == 31) {
+                    tc::bulk_g2s(sB + half_bytes, P.zero, b_copy, &full[stage]);
                 }
                 if (++stage == (uint32_t)P.S) {
                     stage = 0;
@@ -242,6 +266,13 @@ __global__ void __launch_bounds__(kOzThreads, 1)
             // 8-row groups: nd*kp*16 bytes apart on the M side (digits interleaved), kp*16 on the N side
             const uint64_t a_desc0 = tc::smem_desc(tc::smem_u32(smem), 128u, (uint32_t)P.nd * P.kp * 16u);
             const uint64_t b_desc0 = tc::smem_desc(tc::smem_u32(smem + a_stage), 128u, (uint32_t)P.kp * 16u);
+            // pair mode: the slice that straddles the two halves starts at the
+            // first half's last core column and finds its second one (column 0
+            // of the other half) one leading byte offset further
+            const uint32_t ncol = (uint32_t)P.kp / 8u;  // core columns per step
+            const uint32_t lbo_x = half_bytes - (ncol - 1u) * 128u;
+            const uint64_t a_descx = tc::smem_desc(tc::smem_u32(smem), lbo_x, (uint32_t)P.nd * P.kp * 16u);
+            const uint64_t b_descx = tc::smem_desc(tc::smem_u32(smem + a_stage), lbo_x, (uint32_t)P.kp * 16u);
             constexpr int kMaxPlanes = 256 / NP;  // B planes one MMA can take
             constexpr int kMaxPlan = kOzMaxDigits * ((kOzMaxDigits + kMaxPlanes - 1) / kMaxPlanes);
             uint32_t pd[kMaxPlan], pa[kMaxPlan], pb[kMaxPlan], pi[kMaxPlan];  // kept in registers (unrolled)
@@ -261,7 +292,7 @@ __global__ void __launch_bounds__(kOzThreads, 1)
                         }
                     ++n_plan;
                 }
-            const uint32_t nq = (uint32_t)P.kp / 16u;
+            const uint32_t kstep = P.pair ? 2u : 1u;
             bool ok = true;
             for (uint32_t t = oz_first_tile(P.chunk); t < n_tiles && ok; t = oz_next_tile(t, P.chunk)) {
                 const uint32_t ns = tiles[t].ns;
@@ -277,7 +308,7 @@ __global__ void __launch_bounds__(kOzThreads, 1)
                     tc::tc_fence_after();
                     const uint32_t dbase = tmem + buf * P.tmem_cols;
                     const uint32_t kend = min(ns, (c + 1) * (uint32_t)P.F);
-                    for (uint32_t k = c * P.F; k < kend; ++k, ++it) {
+                    for (uint32_t k = c * P.F; k < kend; k += kstep, ++it) {
                         c0 = prof ? clock64() : 0;
                         if (!tc::mbar_wait(&full[stage], ph, abort)) {
                             ok = false;
@@ -285,14 +316,33 @@ __global__ void __launch_bounds__(kOzThreads, 1)
                         }
                         if (prof) w_full += clock64() - c0;
                         tc::tc_fence_after();
-                        const uint64_t a0 = a_desc0 + stage * (stage_bytes >> 4);
-                        const uint64_t b0 = b_desc0 + stage * (stage_bytes >> 4);
+                        const uint32_t soff = stage * (stage_bytes >> 4);
+                        // k16 slices of this stage: kp / 16 of one step, or, for a
+                        // pair, the ncol (odd) slices over both halves' 2 ncol core
+                        // columns -- of a lone last step only those touching its half
+                        const uint32_t nq = !P.pair ? (uint32_t)P.kp / 16u : (k + 1 < ns ? ncol : (ncol + 1u) / 2u);
                         // the first MMA of a chain (digit 0, which spans every TMEM
                         // region) overwrites the accumulator
                         uint32_t first = (k == c * P.F) ? 1u : 0u;
                         for (uint32_t q = 0; q < nq; ++q) {
                             // the slice's descriptors first, then its MMAs back to back
-                            const uint64_t aq = a0 + q * 16u, bq = b0 + q * 16u;
+                            uint64_t aq, bq;
+                            if (!P.pair) {
+                                aq = a_desc0 + soff + q * 16u;
+                                bq = b_desc0 + soff + q * 16u;
+                            } else {
+                                const uint32_t g = 2u * q;  // first core column of the slice
+                                if (g + 1u < ncol) {        // both in the first half
+                                    aq = a_desc0 + soff + g * 8u;
+                                    bq = b_desc0 + soff + g * 8u;
+                                } else if (g + 1u == ncol) {  // straddles the halves
+                                    aq = a_descx + soff + g * 8u;
+                                    bq = b_descx + soff + g * 8u;
+                                } else {  // both in the second half
+                                    aq = a_desc0 + soff + ((half_bytes + (g - ncol) * 128u) >> 4);
+                                    bq = b_desc0 + soff + ((half_bytes + (g - ncol) * 128u) >> 4);
+                                }
+                            }
                             uint64_t ad[kMaxPlan], bd[kMaxPlan];
                             uint32_t dt[kMaxPlan], ac[kMaxPlan];
 #pragma unroll
@@ -445,6 +495,8 @@ static void launch_oz(bsg_ctx ctx, const OzShape &sh, const OzTile *tiles, size_
     P.R = sh.R;
     P.nd = sh.nd;
     P.F = sh.F;
+    P.pair = sh.pair;
+    BSG_REQUIRE(!sh.pair || (sh.F % 2 == 0 && sh.kp % 16 == 8), BSG_ERR_UNSUPPORTED, "Ozaki tile: step pairs");
     P.alpha = alpha;
     P.prof = prof;
     P.zero = static_cast<const bf16 *>(oz_zero_image());

@@ -29,13 +29,19 @@ constexpr uint32_t kOzNone = 0xFFFFFFFFu;
 // Padded tile geometry for one block size.
 struct OzShape {
     int mp;  // rows per slot (block rows rounded up to 8)
-    int kp;  // k per step (block k rounded up to 16)
+    int kp;  // k per step (block k rounded up to 16, or to 8 in pair mode)
     int np;  // output columns (block cols rounded up to 8)
     int R;   // slots per 128-row tile
     int nd;  // digits per operand
-    int F;   // steps per exact chain (512 / kp)
+    int F;   // steps per exact chain (F kp <= 512; even in pair mode)
     int S = 0;  // pipeline stages (0: as many as fit, at most 4)
     int J = 1;  // N-side sub-blocks of np / J rows each (a B image holds J blocks)
+    // Pair mode (kp = 8 mod 16, e.g. 24-wide blocks): a stage holds two steps
+    // side by side and the MMA's k16 slices run across them (the one slice
+    // that straddles the two takes its second core matrix from the other
+    // half through the descriptor's leading byte offset), so no step is
+    // padded to a multiple of 16 in k.
+    int pair = 0;
 };
 OzShape oz_shape(int bs_rows, int bs_k, int bs_cols, int nd);
 // digits to use: `requested` (validated) or, for 0, 5 where it fits else 4
