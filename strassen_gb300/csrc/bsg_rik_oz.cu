@@ -203,7 +203,15 @@ __global__ void k_colmax_ijs_sub(const double *__restrict__ ijs, const uint8_t *
 struct OzDims {
     size_t n_bf, n_occ, bs, nb, nob;
     int mp, kp, np, nd, R;
+    // N side of the ij and K products: J occupied block columns per tile
+    // (stacked along N in one image of npJ rows per digit plane), nobp groups
+    int J, npJ;
+    size_t nobp;
 };
+
+// N-side image rows of occupied block column jb = J*jbp + j inside its
+// group's image start at j*bs (J = 1: the image's own np rows)
+__device__ __forceinline__ int rows_in_group(const OzDims &D) { return D.J == 1 ? D.npJ : (int)D.bs; }
 
 // U_p blocks (M side), gathered from the compressed integrals; one warp per
 // (p, a, b), image index p*nb*nb + a + b*nb
@@ -236,15 +244,23 @@ __global__ void k_img_Ct_A(const double *__restrict__ C, const int *__restrict__
                 cexp + ib * D.bs, D.mp, D.kp, D.nd, img + x * D.nd * (size_t)D.mp * D.kp, true);
 }
 
-// mui_p blocks (a, jb) in the B role of ij; index p*nb*nob + a + jb*nb
+// mui_p blocks (a, jb) in the B role of ij, J block columns per image: image
+// index p*nb*nobp + a + jbp*nb, block jb = J*jbp + j at rows j*bs; one warp
+// per (p, a, jb) with jb < nobp*J (columns past n_occ get zero rows)
 __global__ void k_img_mui_B(const double *__restrict__ mui, const uint8_t *__restrict__ mflag,
                             const int *__restrict__ cexp, OzDims D, size_t n, bf16 *__restrict__ img) {
     const size_t x = oz_warp_id();
-    if (x >= n || !mflag[x]) return;
-    const size_t p = x / (D.nb * D.nob), a = x % D.nb, jb = (x / D.nb) % D.nob;
-    oz_block_image(mui + p * D.n_bf * D.n_occ + a * D.bs + jb * D.bs * D.n_bf, D.n_bf, true, ext_r(jb, D.bs, D.n_occ),
-                ext_r(a, D.bs, D.n_bf), cexp + p * D.n_occ + jb * D.bs, D.np, D.kp, D.nd,
-                img + x * D.nd * (size_t)D.np * D.kp, false);
+    if (x >= n) return;
+    const size_t nj = D.nobp * D.J, a = x % D.nb, jb = (x / D.nb) % nj, p = x / (D.nb * nj);
+    const size_t jbp = jb / D.J, j = jb % D.J;
+    bf16 *dst = img + ((p * D.nobp + jbp) * D.nb + a) * D.nd * (size_t)D.npJ * D.kp + j * D.bs * (size_t)D.kp;
+    const bool real = jb < D.nob;
+    if (real && !mflag[p * D.nb * D.nob + a + jb * D.nb]) return;
+    const size_t jc = real ? jb : 0;
+    oz_block_image_g(OzDenseGet{mui + p * D.n_bf * D.n_occ + a * D.bs + jc * D.bs * D.n_bf, D.n_bf, true},
+                     real ? ext_r(jb, D.bs, D.n_occ) : 0, real ? ext_r(a, D.bs, D.n_bf) : 0,
+                     cexp + p * D.n_occ + jc * D.bs, rows_in_group(D), D.kp, D.nd, dst, false, threadIdx.x & 31, 32,
+                     D.npJ);
 }
 
 // mui_p blocks (a, ib) in the A role of K += mui ijs; index p*nb*nob + a + ib*nb
@@ -270,15 +286,58 @@ __global__ void k_img_mui_T(const double *__restrict__ mui, const uint8_t *__res
                 img + x * D.nd * (size_t)D.np * D.kp, false);
 }
 
-// ijs_p blocks (ib, jb) in the B role of the K product; index p*nob*nob + ib + jb*nob
+// ijs_p blocks (ib, jb) in the B role of the K product, J block columns per
+// image: index p*nob*nobp + ib + jbp*nob; one warp per (p, ib, jb), jb < nobp*J
 __global__ void k_img_ijs_B(const double *__restrict__ ijs, const uint8_t *__restrict__ sflag,
                             const int *__restrict__ cexp, size_t Q, OzDims D, size_t n, bf16 *__restrict__ img) {
     const size_t x = oz_warp_id();
-    if (x >= n || !sflag[x]) return;
-    const size_t p = x / (D.nob * D.nob), ib = x % D.nob, jb = (x / D.nob) % D.nob;
-    oz_block_image(ijs + p * D.n_occ * D.n_occ + ib * D.bs + jb * D.bs * D.n_occ, D.n_occ, true, ext_r(jb, D.bs, D.n_occ),
-                ext_r(ib, D.bs, D.n_occ), cexp + (p / Q) * D.n_occ + jb * D.bs, D.np, D.kp, D.nd,
-                img + x * D.nd * (size_t)D.np * D.kp, false);
+    if (x >= n) return;
+    const size_t nj = D.nobp * D.J, ib = x % D.nob, jb = (x / D.nob) % nj, p = x / (D.nob * nj);
+    const size_t jbp = jb / D.J, j = jb % D.J;
+    bf16 *dst = img + ((p * D.nobp + jbp) * D.nob + ib) * D.nd * (size_t)D.npJ * D.kp + j * D.bs * (size_t)D.kp;
+    const bool real = jb < D.nob;
+    if (real && !sflag[p * D.nob * D.nob + ib + jb * D.nob]) return;
+    const size_t jc = real ? jb : 0;
+    oz_block_image_g(OzDenseGet{ijs + p * D.n_occ * D.n_occ + ib * D.bs + jc * D.bs * D.n_occ, D.n_occ, true},
+                     real ? ext_r(jb, D.bs, D.n_occ) : 0, real ? ext_r(ib, D.bs, D.n_occ) : 0,
+                     cexp + (p / Q) * D.n_occ + jc * D.bs, rows_in_group(D), D.kp, D.nd, dst, false,
+                     threadIdx.x & 31, 32, D.npJ);
+}
+
+// One k step of a tile whose N side holds J block columns: live[j] = slots
+// whose product with sub-block j survives.  The pairs are split into exact
+// rectangles (slot set x sub-block set), each one step: the slots common to
+// every sub-block that still has some, then the rest (at most J steps).
+// Sub-blocks past the last block column count as present: their image rows
+// are zero, so a rectangle may include them and keep the single B copy.
+__device__ __forceinline__ uint32_t emit_rect_steps(uint32_t (&live)[2], int J, uint32_t phantom, uint32_t b,
+                                                    const uint32_t (&a_idx)[kOzMaxSlots], OzStep *__restrict__ out) {
+    uint32_t n = 0;
+    for (int guard = 0; guard < 2 * 2; ++guard) {
+        uint32_t common = 0xFFFFFFFFu, jset = 0;
+        for (int j = 0; j < J; ++j)
+            if (live[j]) {
+                common &= live[j];
+                jset |= 1u << j;
+            }
+        if (!jset) break;
+        if (!common) {
+            for (int j = 0; j < J; ++j)
+                if (live[j]) {
+                    common = live[j];
+                    jset = 1u << j;
+                    break;
+                }
+        }
+        OzStep st;
+        st.b = b;
+        st.bmask = ((jset | phantom) == (1u << J) - 1u) ? kOzAllSub : jset;
+        for (int sl = 0; sl < kOzMaxSlots; ++sl) st.a[sl] = ((common >> sl) & 1u) ? a_idx[sl] : kOzNone;
+        out[n++] = st;
+        for (int j = 0; j < J; ++j)
+            if ((jset >> j) & 1u) live[j] &= ~common;
+    }
+    return n;
 }
 
 // ---- tiles and steps (one thread per tile) ----
@@ -353,7 +412,8 @@ __global__ void k_tiles_mui(const uint8_t *__restrict__ uflag, const double *__r
     if (m) atomicAdd(macs, m);
 }
 
-// ij tiles: t = (p, jb, group of R block rows ib)
+// ij tiles: t = (p, jbp, group of R block rows ib), N side J block columns
+// jb = J*jbp + j, steps over a (split into exact rectangles)
 __global__ void k_tiles_ij(const uint8_t *__restrict__ mflag, const double *__restrict__ mnorm,
                            const double *__restrict__ cnorm, const int *__restrict__ cexp_C,
                            const int *__restrict__ cexp_mui, double *__restrict__ ij, OzDims D, size_t n_tiles,
@@ -363,42 +423,50 @@ __global__ void k_tiles_ij(const uint8_t *__restrict__ mflag, const double *__re
     const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n_tiles) return;
     const size_t ng = (D.nob + D.R - 1) / D.R;
-    const size_t g = t % ng, jb = (t / ng) % D.nob, p = t / (ng * D.nob);
+    const size_t g = t % ng, jbp = (t / ng) % D.nobp, p = t / (ng * D.nobp);
     unsigned long long m = 0;
     OzTile T;
     tile_clear(T);
-    int cnt[kOzMaxSlots] = {0};
+    uint32_t cnt[kOzMaxSlots][2] = {};
     for (int s = 0; s < D.R; ++s) {
         const size_t ib = g * D.R + s;
         if (ib >= D.nob) break;
-        T.c[s] = ij + p * D.n_occ * D.n_occ + ib * D.bs + jb * D.bs * D.n_occ;
+        T.c[s] = ij + p * D.n_occ * D.n_occ + ib * D.bs + jbp * D.J * D.bs * D.n_occ;
         T.ldc[s] = (int)D.n_occ;
         T.rows[s] = ext_r(ib, D.bs, D.n_occ);
         T.rexp[s] = cexp_C + ib * D.bs;
     }
-    T.cols = ext_r(jb, D.bs, D.n_occ);
+    int cols = 0;
+    uint32_t phantom = 0;
+    for (int j = 0; j < D.J; ++j) {
+        const size_t jb = jbp * D.J + j;
+        if (jb < D.nob) cols = j * (int)D.bs + ext_r(jb, D.bs, D.n_occ);
+        else phantom |= 1u << j;
+    }
+    T.cols = cols;
     T.trans = 0;
-    T.cexp = cexp_mui + p * D.n_occ + jb * D.bs;
-    T.s0 = (uint32_t)(t * D.nb);
+    T.cexp = cexp_mui + p * D.n_occ + jbp * D.J * D.bs;
+    T.s0 = (uint32_t)(t * D.nb * D.J);
     uint32_t n = 0;
     for (size_t a = 0; a < D.nb; ++a) {
-        const size_t mb = p * D.nb * D.nob + a + jb * D.nb;
-        if (!mflag[mb]) continue;
-        OzStep st;
-        st.bmask = kOzAllSub;
-        st.b = (uint32_t)mb;
-        bool any = false;
-        for (int s = 0; s < kOzMaxSlots; ++s) {
-            st.a[s] = kOzNone;
-            if (s >= D.R || !T.c[s]) continue;
-            const size_t ib = g * D.R + s;
-            if (!(__dmul_rn(cnorm[a + ib * D.nb], mnorm[mb]) >= tpb)) continue;
-            st.a[s] = (uint32_t)(ib + a * D.nob);
-            m += (unsigned long long)T.rows[s] * ext_r(jb, D.bs, D.n_occ) * ext_r(a, D.bs, D.n_bf);
-            ++cnt[s];
-            any = true;
+        uint32_t live[2] = {0, 0};
+        uint32_t a_idx[kOzMaxSlots];
+        for (int s = 0; s < kOzMaxSlots; ++s) a_idx[s] = (uint32_t)(g * D.R + s + a * D.nob);
+        for (int j = 0; j < D.J; ++j) {
+            const size_t jb = jbp * D.J + j;
+            if (jb >= D.nob) continue;
+            const size_t mb = p * D.nb * D.nob + a + jb * D.nb;
+            if (!mflag[mb]) continue;
+            for (int s = 0; s < D.R; ++s) {
+                if (!T.c[s]) continue;
+                const size_t ib = g * D.R + s;
+                if (!(__dmul_rn(cnorm[a + ib * D.nb], mnorm[mb]) >= tpb)) continue;
+                live[j] |= 1u << s;
+                m += (unsigned long long)T.rows[s] * ext_r(jb, D.bs, D.n_occ) * ext_r(a, D.bs, D.n_bf);
+                ++cnt[s][j];
+            }
         }
-        if (any) steps[T.s0 + n++] = st;
+        n += emit_rect_steps(live, D.J, phantom, (uint32_t)((p * D.nobp + jbp) * D.nb + a), a_idx, steps + T.s0 + n);
     }
     T.ns = n;
     tiles[t] = T;
@@ -406,14 +474,21 @@ __global__ void k_tiles_ij(const uint8_t *__restrict__ mflag, const double *__re
     for (int s = 0; s < D.R; ++s) {
         const size_t ib = g * D.R + s;
         if (ib >= D.nob) break;
-        ijflag[p * D.nob * D.nob + ib + jb * D.nob] = cnt[s] > 0;
-        tot += cnt[s];
+        for (int j = 0; j < D.J; ++j) {
+            const size_t jb = jbp * D.J + j;
+            if (jb >= D.nob) continue;
+            ijflag[p * D.nob * D.nob + ib + jb * D.nob] = cnt[s][j] > 0;
+            tot += cnt[s][j];
+        }
     }
     if (tot) atomicAdd(nsig, tot);
     if (m) atomicAdd(macs, m);
 }
 
-// K tiles: t = (sub-range, jb, group of R block rows a), steps over (p, ib)
+// K tiles: t = (sub-range, jbp, group of R block rows a), N side J block
+// columns jb = J*jbp + j, steps over (p, ib) split into exact rectangles;
+// partial blocks of a tile: Kpart + ((sub*nobp + jbp)*nb + a) * bs * J*bs,
+// column-major with ld = the block's rows
 __global__ void k_tiles_K(const uint8_t *__restrict__ mflag, const double *__restrict__ mnorm,
                           const uint8_t *__restrict__ sflag, const double *__restrict__ snorm,
                           const int *__restrict__ rexp_sub, const int *__restrict__ cexp_sub, double *__restrict__ Kpart,
@@ -423,46 +498,55 @@ __global__ void k_tiles_K(const uint8_t *__restrict__ mflag, const double *__res
     const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n_tiles) return;
     const size_t ng = (D.nb + D.R - 1) / D.R;
-    const size_t g = t % ng, jb = (t / ng) % D.nob, sub = t / (ng * D.nob);
+    const size_t g = t % ng, jbp = (t / ng) % D.nobp, sub = t / (ng * D.nobp);
     unsigned long long m = 0;
     OzTile T;
     tile_clear(T);
-    const size_t bs2 = D.bs * D.bs;
+    const size_t blk = D.bs * D.bs * D.J;
     for (int s = 0; s < D.R; ++s) {
         const size_t a = g * D.R + s;
         if (a >= D.nb) break;
-        T.c[s] = Kpart + ((sub * D.nob + jb) * D.nb + a) * bs2;
+        T.c[s] = Kpart + ((sub * D.nobp + jbp) * D.nb + a) * blk;
         T.rows[s] = ext_r(a, D.bs, D.n_bf);
         T.ldc[s] = T.rows[s];
         T.rexp[s] = rexp_sub + sub * D.n_bf + a * D.bs;
     }
-    T.cols = ext_r(jb, D.bs, D.n_occ);
+    int cols = 0;
+    uint32_t phantom = 0;
+    for (int j = 0; j < D.J; ++j) {
+        const size_t jb = jbp * D.J + j;
+        if (jb < D.nob) cols = j * (int)D.bs + ext_r(jb, D.bs, D.n_occ);
+        else phantom |= 1u << j;
+    }
+    T.cols = cols;
     T.trans = 0;
-    T.cexp = cexp_sub + sub * D.n_occ + jb * D.bs;
-    T.s0 = (uint32_t)(t * Q * D.nob);
+    T.cexp = cexp_sub + sub * D.n_occ + jbp * D.J * D.bs;
+    T.s0 = (uint32_t)(t * Q * D.nob * D.J);
     uint32_t n = 0;
     unsigned long long tot = 0;
     const size_t p1 = min(np, (sub + 1) * Q);
     for (size_t p = sub * Q; p < p1; ++p)
         for (size_t ib = 0; ib < D.nob; ++ib) {
-            const size_t sb = p * D.nob * D.nob + ib + jb * D.nob;
-            if (!sflag[sb]) continue;
-            OzStep st;
-        st.bmask = kOzAllSub;
-            st.b = (uint32_t)sb;
-            bool any = false;
-            for (int s = 0; s < kOzMaxSlots; ++s) {
-                st.a[s] = kOzNone;
-                if (s >= D.R || !T.c[s]) continue;
-                const size_t a = g * D.R + s, mb = p * D.nb * D.nob + a + ib * D.nb;
-                if (!mflag[mb]) continue;
-                if (!(__dmul_rn(mnorm[mb], snorm[sb]) >= tpb)) continue;
-                st.a[s] = (uint32_t)mb;
-                m += (unsigned long long)T.rows[s] * T.cols * ext_r(ib, D.bs, D.n_occ);
-                ++tot;
-                any = true;
+            uint32_t live[2] = {0, 0};
+            uint32_t a_idx[kOzMaxSlots];
+            for (int s = 0; s < kOzMaxSlots; ++s) a_idx[s] = (uint32_t)(p * D.nb * D.nob + g * D.R + s + ib * D.nb);
+            for (int j = 0; j < D.J; ++j) {
+                const size_t jb = jbp * D.J + j;
+                if (jb >= D.nob) continue;
+                const size_t sb = p * D.nob * D.nob + ib + jb * D.nob;
+                if (!sflag[sb]) continue;
+                for (int s = 0; s < D.R; ++s) {
+                    if (!T.c[s]) continue;
+                    const size_t mb = p * D.nb * D.nob + g * D.R + s + ib * D.nb;
+                    if (!mflag[mb]) continue;
+                    if (!(__dmul_rn(mnorm[mb], snorm[sb]) >= tpb)) continue;
+                    live[j] |= 1u << s;
+                    m += (unsigned long long)T.rows[s] * ext_r(jb, D.bs, D.n_occ) * ext_r(ib, D.bs, D.n_occ);
+                    ++tot;
+                }
             }
-            if (any) steps[T.s0 + n++] = st;
+            n += emit_rect_steps(live, D.J, phantom, (uint32_t)((p * D.nobp + jbp) * D.nob + ib), a_idx,
+                                 steps + T.s0 + n);
         }
     T.ns = n;
     tiles[t] = T;
@@ -472,14 +556,15 @@ __global__ void k_tiles_K(const uint8_t *__restrict__ mflag, const double *__res
 
 // K(a, jb) += sum over sub-ranges (in order) of the tiles' partial blocks
 __global__ void k_K_reduce(const double *__restrict__ Kpart, size_t n_sub, OzDims D, double *__restrict__ K) {
-    const size_t blk = blockIdx.x;  // (jb, a)
-    const size_t a = blk % D.nb, jb = blk / D.nb;
+    const size_t x = blockIdx.x;  // (jb, a)
+    const size_t a = x % D.nb, jb = x / D.nb, jbp = jb / D.J, j = jb % D.J;
     const int rows = ext_r(a, D.bs, D.n_bf), cols = ext_r(jb, D.bs, D.n_occ);
-    const size_t bs2 = D.bs * D.bs;
+    const size_t blk = D.bs * D.bs * D.J;
     for (int e = threadIdx.x; e < rows * cols; e += blockDim.x) {
         const int r = e % rows, c = e / rows;
+        const size_t pe = (size_t)r + (j * D.bs + c) * (size_t)rows;
         double acc = K[a * D.bs + r + (jb * D.bs + c) * D.n_bf];
-        for (size_t sub = 0; sub < n_sub; ++sub) acc += Kpart[((sub * D.nob + jb) * D.nb + a) * bs2 + e];
+        for (size_t sub = 0; sub < n_sub; ++sub) acc += Kpart[((sub * D.nobp + jbp) * D.nb + a) * blk + pe];
         K[a * D.bs + r + (jb * D.bs + c) * D.n_bf] = acc;
     }
 }
@@ -611,14 +696,28 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
     D.np = sh.np;
     D.nd = nd;
     D.R = sh.R;
-    const size_t nb = D.nb, nob = D.nob;
+    // ij and K products: two occupied block columns per tile where they fit
+    // (N = 2 bs per digit plane, both accumulator sets in TMEM): the A images
+    // then serve twice the columns per copy and per MMA
+    int J = (bs % 8 == 0 && 2 * bs <= 64 && nd * 2 * (int)bs + 8 <= 256) ? 2 : 1;
+    OzShape shJ = oz_shape((int)bs, (int)bs, (int)bs * J, nd);
+    if (shJ.kp != sh.kp || shJ.pair != sh.pair) {  // the A images are laid out for sh's k steps
+        J = 1;
+        shJ = sh;
+    }
+    shJ.J = J;
+    D.J = J;
+    D.npJ = shJ.np;
+    D.nobp = ceil_div(D.nob, (size_t)J);
+    const size_t nb = D.nb, nob = D.nob, nobp = D.nobp;
     const size_t a_img = (size_t)nd * sh.mp * sh.kp, b_img = (size_t)nd * sh.np * sh.kp;  // elements per image
+    const size_t b_imgJ = (size_t)nd * shJ.np * shJ.kp;  // J-group images (N side of ij and K)
     // bytes per aux function of every per-chunk buffer
     const bool want_k = K_dev != nullptr, want_kmn = Kmn_dev != nullptr;
     const size_t Q = 8;  // aux functions per K-product tile
     const size_t per_p = nb * nb * 9 + nb * nb * a_img * 2 + n_bf * n_occ * 8 + nb * nob * 9 +
-                         nb * nob * (a_img + b_img) * 2 + 3 * n_occ * n_occ * 8 + 3 * nob * nob * 9 +
-                         nob * nob * b_img * 2 + (want_kmn ? nb * nob * b_img * 2 + nb * nb * bs * bs * 8 / Q : 0);
+                         nb * nob * a_img * 2 + nb * nobp * b_imgJ * 2 + 3 * n_occ * n_occ * 8 + 3 * nob * nob * 9 +
+                         nob * nobp * b_imgJ * 2 + (want_kmn ? nb * nob * b_img * 2 + nb * nb * bs * bs * 8 / Q : 0);
     size_t pc = d.p_chunk ? d.p_chunk : std::max<size_t>(1, (size_t)(8ull << 30) / per_p);
     pc = std::max<size_t>(1, std::min(pc, n_aux));
     const size_t n_sub_max = ceil_div(pc, Q);
@@ -630,20 +729,20 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
     DevBuf dcn(nb * nob * 8, s), dcexpC(nob * bs * 4, s), dimgCB(nb * nob * b_img * 2, s),
         dimgCtA(nob * nb * a_img * 2, s);
     DevBuf drexpU(pc * n_bf * 4, s), dimgU(pc * nb * nb * a_img * 2, s);
-    DevBuf dcexpM(pc * n_occ * 4, s), dimgMB(pc * nb * nob * b_img * 2, s);
+    DevBuf dcexpM(pc * n_occ * 4, s), dimgMB(pc * nb * nobp * b_imgJ * 2, s);
     DevBuf drexpMs(n_sub_max * n_bf * 4, s), dcexpSs(n_sub_max * n_occ * 4, s);
     // maxima bit patterns for the four exponent sets of a chunk
     const size_t nbits = pc * n_bf + pc * n_occ + n_sub_max * n_bf + n_sub_max * n_occ;
     DevBuf dbits(nbits * 8, s);
     auto *bitsU = dbits.as<unsigned long long>(), *bitsM = bitsU + pc * n_bf, *bitsMs = bitsM + pc * n_occ,
          *bitsSs = bitsMs + n_sub_max * n_bf;
-    DevBuf dimgMA(pc * nb * nob * a_img * 2, s), dimgSB(pc * nob * nob * b_img * 2, s);
-    DevBuf dKp(want_k ? n_sub_max * nob * nb * bs * bs * 8 : 0, s), dcnt(6 * 8, s), dmacs(4 * 8, s);
+    DevBuf dimgMA(pc * nb * nob * a_img * 2, s), dimgSB(pc * nob * nobp * b_imgJ * 2, s);
+    DevBuf dKp(want_k ? n_sub_max * nobp * nb * bs * bs * J * 8 : 0, s), dcnt(6 * 8, s), dmacs(4 * 8, s);
     const size_t ng_a = ceil_div(nb, (size_t)D.R), ng_i = ceil_div(nob, (size_t)D.R);
-    const size_t tiles_mui = pc * nob * ng_a, tiles_ij = pc * nob * ng_i, tiles_K = n_sub_max * nob * ng_a;
+    const size_t tiles_mui = pc * nob * ng_a, tiles_ij = pc * nobp * ng_i, tiles_K = n_sub_max * nobp * ng_a;
     DevBuf dtm(tiles_mui * sizeof(OzTile), s), dsm(tiles_mui * nb * sizeof(OzStep), s);
-    DevBuf dti(tiles_ij * sizeof(OzTile), s), dsi(tiles_ij * nb * sizeof(OzStep), s);
-    DevBuf dtk(tiles_K * sizeof(OzTile), s), dsk(tiles_K * Q * nob * sizeof(OzStep), s);
+    DevBuf dti(tiles_ij * sizeof(OzTile), s), dsi(tiles_ij * nb * J * sizeof(OzStep), s);
+    DevBuf dtk(tiles_K * sizeof(OzTile), s), dsk(tiles_K * Q * nob * J * sizeof(OzStep), s);
     // K_mn: images of mui in the B role, tiles over (sub-range, lower pair), partials
     const size_t n_pairs = kmn_pairs(nb, (size_t)D.R), tiles_Kmn = want_kmn ? n_sub_max * n_pairs : 0;
     DevBuf dimgMT(want_kmn ? pc * nb * nob * b_img * 2 : 0, s);
@@ -725,15 +824,16 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
         k_colmax_mui<<<oz_img_grid(np * nb * nob), 32 * kOzImgWarps, 0, s>>>(
             dmui.as<double>(), dmf.as<uint8_t>(), n_bf, n_occ, bs, nb, nob, np * nb * nob, bitsM);
         k_bits_exp<<<(unsigned)ceil_div(np * n_occ, (size_t)256), 256, 0, s>>>(bitsM, np * n_occ, dcexpM.as<int>());
-        k_img_mui_B<<<oz_img_grid(np * nb * nob), 32 * kOzImgWarps, 0, s>>>(
-            dmui.as<double>(), dmf.as<uint8_t>(), dcexpM.as<int>(), D, np * nb * nob, dimgMB.as<bf16>());
-        const size_t ti = np * nob * ng_i;
+        k_img_mui_B<<<oz_img_grid(np * nb * nobp * J), 32 * kOzImgWarps, 0, s>>>(
+            dmui.as<double>(), dmf.as<uint8_t>(), dcexpM.as<int>(), D, np * nb * nobp * J, dimgMB.as<bf16>());
+        const size_t ti = np * nobp * ng_i;
         k_tiles_ij<<<(unsigned)ceil_div(ti, 128), 128, 0, s>>>(
             dmf.as<uint8_t>(), dmn.as<double>(), dcn.as<double>(), dcexpC.as<int>(), dcexpM.as<int>(),
             dij.as<double>(), D, ti, tpb, dti.as<OzTile>(), dsi.as<OzStep>(), dijf.as<uint8_t>(), cnt + 1, macs + 1);
         ctx->note_launch(4);
         ctx->check_launch("rik ozaki ij prep");
-        oz_run(ctx, sh, dti.as<OzTile>(), ti, dsi.as<OzStep>(), dimgCtA.as<bf16>(), dimgMB.as<bf16>(), 1.0, s, macs + 1);
+        oz_run(ctx, shJ, dti.as<OzTile>(), ti, dsi.as<OzStep>(), dimgCtA.as<bf16>(), dimgMB.as<bf16>(), 1.0, s,
+               macs + 1);
         // ijs = ij + ij^T (FP64, with the reference's norm bookkeeping)
         k_ijs<<<(unsigned)(np * nob * nob), 128, 0, s>>>(dij.as<double>(), dijf.as<uint8_t>(), n_occ, bs, nob,
                                                           dijs.as<double>(), dsn.as<double>(), dsf.as<uint8_t>());
@@ -742,16 +842,17 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
             dijs.as<double>(), dsf.as<uint8_t>(), n_occ, bs, nob, Q, np * nob * nob, bitsSs);
         k_bits_exp<<<(unsigned)ceil_div(n_sub * n_occ, (size_t)256), 256, 0, s>>>(bitsSs, n_sub * n_occ,
                                                                                   dcexpSs.as<int>());
-        k_img_ijs_B<<<oz_img_grid(np * nob * nob), 32 * kOzImgWarps, 0, s>>>(
-            dijs.as<double>(), dsf.as<uint8_t>(), dcexpSs.as<int>(), Q, D, np * nob * nob, dimgSB.as<bf16>());
-        const size_t tk = n_sub * nob * ng_a;
+        k_img_ijs_B<<<oz_img_grid(np * nob * nobp * J), 32 * kOzImgWarps, 0, s>>>(
+            dijs.as<double>(), dsf.as<uint8_t>(), dcexpSs.as<int>(), Q, D, np * nob * nobp * J, dimgSB.as<bf16>());
+        const size_t tk = n_sub * nobp * ng_a;
         k_tiles_K<<<(unsigned)ceil_div(tk, 128), 128, 0, s>>>(
             dmf.as<uint8_t>(), dmn.as<double>(), dsf.as<uint8_t>(), dsn.as<double>(), drexpMs.as<int>(),
             dcexpSs.as<int>(), dKp.as<double>(), D, np, Q, tk, tpb, dtk.as<OzTile>(), dsk.as<OzStep>(), cnt + 2,
             macs + 2);
         ctx->note_launch(5);
         ctx->check_launch("rik ozaki K prep");
-        oz_run(ctx, sh, dtk.as<OzTile>(), tk, dsk.as<OzStep>(), dimgMA.as<bf16>(), dimgSB.as<bf16>(), 1.0, s, macs + 2);
+        oz_run(ctx, shJ, dtk.as<OzTile>(), tk, dsk.as<OzStep>(), dimgMA.as<bf16>(), dimgSB.as<bf16>(), 1.0, s,
+               macs + 2);
         k_K_reduce<<<(unsigned)(nb * nob), 256, 0, s>>>(dKp.as<double>(), n_sub, D, K_dev);
         ctx->note_launch();
         ctx->check_launch("rik ozaki K reduce");

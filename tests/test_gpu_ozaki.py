@@ -105,6 +105,23 @@ def test_ozaki_rik_synthetic(api, ctx, nd):
     assert err < 1e-9
 
 
+@pytest.mark.parametrize("n_occ", [24, 60, 77])
+def test_ozaki_rik_column_pairs(api, ctx, n_occ):
+    """occupied block columns paired on the N side of the ij and K products:
+    an odd number of column blocks (the last pair half empty), ragged last
+    blocks, and a single block; masks and K as in the FP64 form"""
+    s = S.RikSystem(seed=12, n_atoms=6, nbf=24, naux=10, n_occ=n_occ, box=6.5)
+    B = api.transform_3c2c(s.ints_3c(), s.v_m12(), 24, 1e-10, ctx=ctx)
+    C = s.c_occ()
+    K64, st64 = api.rik_occ_step(B, s.keys, C, s.n_bf, s.n_aux, s.n_occ, 24, 1e-10, ctx=ctx, stats=True)
+    Koz, stoz = api.rik_occ_step(B, s.keys, C, s.n_bf, s.n_aux, s.n_occ, 24, 1e-10, form=api.FORM_OZAKI,
+                                 n_digits=5, p_chunk=16, ctx=ctx, stats=True)
+    err = np.linalg.norm(Koz - K64) / np.linalg.norm(K64)
+    print("column pairs", n_occ, err, st64[:3], stoz[:3])
+    assert st64[:3] == stoz[:3]
+    assert err < 1e-9
+
+
 def test_ozaki_rik_h2o(api, ctx, h2o):
     d = h2o
     K = api.rik_occ_step(d["ints"], d["keys"], d["c"], d["n_bf"], d["n_aux"], d["n_occ"], 3, 1e-20,
