@@ -31,12 +31,12 @@ __global__ void k_dense_norms(const double *__restrict__ M, size_t ld, size_t nr
 }
 
 // exponent of every row of X (over all columns); one thread per row
-__global__ void k_rowexp_dense(const double *__restrict__ X, size_t nr, size_t nc, int *__restrict__ rexp) {
+__global__ void k_rowexp_dense(const double *__restrict__ X, size_t ld, size_t nr, size_t nc, int *__restrict__ rexp) {
     const size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= nr) return;
     long long mx = 0;
     for (size_t c = 0; c < nc; ++c) {
-        const long long b = oz_absbits(X[r + c * nr]);
+        const long long b = oz_absbits(X[r + c * ld]);
         mx = b > mx ? b : mx;
     }
     rexp[r] = oz_exp_of_bits(mx);
@@ -66,6 +66,7 @@ __global__ void k_colexp_dense(const double *__restrict__ V, size_t nr, int *__r
 
 struct Dense3c {
     size_t n_vec2, n_aux, bs, nib, nkb, njb;
+    size_t ldx, ldo;  // leading dimensions of X and of the output
     int mp, kp, np, nd, R;
     int J;        // X block rows per N-side group (np = J * bs rounded to 8)
     size_t nibp;  // groups of J block rows
@@ -87,7 +88,7 @@ __global__ void k_img_X(const double *__restrict__ X, const int *__restrict__ re
     if (x >= D.nib * D.nkb) return;
     const size_t ib = x % D.nib, kb = x / D.nib, ibp = ib / D.J, j = ib % D.J;
     bf16 *dst = img + (ibp + kb * D.nibp) * D.nd * (size_t)D.np * D.kp + j * D.bs * (size_t)D.kp;
-    oz_block_image_g(OzDenseGet{X + ib * D.bs + kb * D.bs * D.n_vec2, D.n_vec2, false}, ext3(ib, D.bs, D.n_vec2),
+    oz_block_image_g(OzDenseGet{X + ib * D.bs + kb * D.bs * D.ldx, D.ldx, false}, ext3(ib, D.bs, D.n_vec2),
                      ext3(kb, D.bs, D.n_aux), rexp + ib * D.bs, (int)D.bs, D.kp, D.nd, dst, false, threadIdx.x & 31, 32,
                      D.np);
 }
@@ -137,8 +138,8 @@ __global__ void k_tiles_3c(size_t n_tiles, size_t n_jg, size_t Gj, const double 
     for (int s = 0; s < D.R; ++s) {
         const size_t jb = jg * D.R + s;
         if (jb >= D.njb) break;
-        T.c[s] = out + ibp * D.J * D.bs + jb * D.bs * D.n_vec2;
-        T.ldc[s] = (int)D.n_vec2;
+        T.c[s] = out + ibp * D.J * D.bs + jb * D.bs * D.ldo;
+        T.ldc[s] = (int)D.ldo;
         T.rows[s] = ext3(jb, D.bs, D.n_aux);  // slot rows are output columns
         T.rexp[s] = cexp + jb * D.bs;
     }
@@ -197,24 +198,28 @@ __global__ void k_tiles_3c(size_t n_tiles, size_t n_jg, size_t Gj, const double 
     if (m) atomicAdd(macs, m);
 }
 
-void transform_3c2c_ozaki(bsg_ctx ctx, size_t n_vec2, size_t n_aux, const double *X, const double *V, size_t bs,
-                          double thresh, int n_digits, double *out, uint64_t *nsig_out) {
-    cudaStream_t s = ctx->stream;
-    BSG_REQUIRE(bs <= 64, BSG_ERR_UNSUPPORTED, "Ozaki form supports blocks up to 64");
-    const int nd = oz_default_digits(n_digits, (int)bs, (int)bs, (int)bs);
+namespace {
+
+// V-side operands (block norms, column exponents, M-side digit images of
+// V^T), shared by every row range of X
+struct Oz3cV {
+    DevBuf vn, cexp, ai;
+};
+
+Dense3c oz3c_dims(size_t n_aux, size_t bs, int nd, OzShape &sh) {
     // X block rows per tile on the N side.  Two rows (nd * 2*bs TMEM columns,
     // bs % 8 == 0) halve the V^T image traffic per product, but on the 40-atom
     // workload 35% of the steps split into two rectangles (the rows' screens
     // differ) and the accumulator no longer fits twice in TMEM: measured 50 ms
     // against 46 ms with one row, so one row it is.
     const int J = 1;
-    OzShape sh = oz_shape((int)bs, (int)bs, (int)bs * J, nd);
+    sh = oz_shape((int)bs, (int)bs, (int)bs * J, nd);
     sh.J = J;
     Dense3c D;
-    D.n_vec2 = n_vec2;
+    D.n_vec2 = D.ldx = D.ldo = 0;
     D.n_aux = n_aux;
     D.bs = bs;
-    D.nib = ceil_div(n_vec2, bs);
+    D.nib = D.nibp = 0;
     D.nkb = D.njb = ceil_div(n_aux, bs);
     D.mp = sh.mp;
     D.kp = sh.kp;
@@ -222,44 +227,140 @@ void transform_3c2c_ozaki(bsg_ctx ctx, size_t n_vec2, size_t n_aux, const double
     D.nd = nd;
     D.R = sh.R;
     D.J = J;
-    D.nibp = ceil_div(D.nib, (size_t)J);
-    if (!n_vec2 || !n_aux) return;
-    const size_t a_img = (size_t)nd * sh.mp * sh.kp, b_img = (size_t)nd * sh.np * sh.kp;
-    DevBuf xn(D.nib * D.nkb * 8, s), vn(D.nkb * D.njb * 8, s), rexp(n_vec2 * 4, s), cexp(n_aux * 4, s);
-    DevBuf ai(D.nkb * D.njb * a_img * 2, s), bi(D.nibp * D.nkb * b_img * 2, s), cnt(16, s);
-    BSG_CUDA(cudaMemsetAsync(cnt.p, 0, 16, s));
+    return D;
+}
+
+void oz3c_prepare_v(bsg_ctx ctx, const double *V, const Dense3c &D, Oz3cV &v) {
+    cudaStream_t s = ctx->stream;
+    const size_t n_aux = D.n_aux, a_img = (size_t)D.nd * D.mp * D.kp;
+    v.vn = DevBuf(D.nkb * D.njb * 8, s);
+    v.cexp = DevBuf(n_aux * 4, s);
+    v.ai = DevBuf(D.nkb * D.njb * a_img * 2, s);
     const int wpb = 8;
-    k_dense_norms<<<(unsigned)ceil_div(D.nib * D.nkb, wpb), wpb * 32, 0, s>>>(X, n_vec2, n_vec2, n_aux, bs, D.nib,
+    k_dense_norms<<<(unsigned)ceil_div(D.nkb * D.njb, wpb), wpb * 32, 0, s>>>(V, n_aux, n_aux, n_aux, D.bs, D.nkb,
+                                                                              D.nkb * D.njb, v.vn.as<double>());
+    k_colexp_dense<<<(unsigned)n_aux, 256, 0, s>>>(V, n_aux, v.cexp.as<int>());
+    k_img_V<<<oz_img_grid(D.nkb * D.njb), 32 * kOzImgWarps, 0, s>>>(V, v.cexp.as<int>(), D, v.ai.as<bf16>());
+    ctx->note_launch(3);
+    ctx->check_launch("3c2c ozaki V prep");
+}
+
+// rows [0, rows) of X (leading dimension ldx) into the same rows of out
+// (leading dimension ldo); stream-ordered on the context's stream, no sync
+void oz3c_rows(bsg_ctx ctx, Dense3c D, const OzShape &sh, const Oz3cV &v, const double *X, size_t ldx, size_t rows,
+               double *out, size_t ldo, double thresh, unsigned long long *cnt) {
+    cudaStream_t s = ctx->stream;
+    const size_t bs = D.bs, n_aux = D.n_aux;
+    D.n_vec2 = rows;
+    D.ldx = ldx;
+    D.ldo = ldo;
+    D.nib = ceil_div(rows, bs);
+    D.nibp = ceil_div(D.nib, (size_t)D.J);
+    const size_t a_img = (size_t)D.nd * sh.mp * sh.kp, b_img = (size_t)D.nd * sh.np * sh.kp;
+    DevBuf xn(D.nib * D.nkb * 8, s), rexp(rows * 4, s), bi(D.nibp * D.nkb * b_img * 2, s);
+    const int wpb = 8;
+    k_dense_norms<<<(unsigned)ceil_div(D.nib * D.nkb, wpb), wpb * 32, 0, s>>>(X, ldx, rows, n_aux, bs, D.nib,
                                                                               D.nib * D.nkb, xn.as<double>());
-    k_dense_norms<<<(unsigned)ceil_div(D.nkb * D.njb, wpb), wpb * 32, 0, s>>>(V, n_aux, n_aux, n_aux, bs, D.nkb,
-                                                                              D.nkb * D.njb, vn.as<double>());
-    k_rowexp_dense<<<(unsigned)ceil_div(n_vec2, 256), 256, 0, s>>>(X, n_vec2, n_aux, rexp.as<int>());
-    k_colexp_dense<<<(unsigned)n_aux, 256, 0, s>>>(V, n_aux, cexp.as<int>());
+    k_rowexp_dense<<<(unsigned)ceil_div(rows, 256), 256, 0, s>>>(X, ldx, rows, n_aux, rexp.as<int>());
     k_img_X<<<oz_img_grid(D.nib * D.nkb), 32 * kOzImgWarps, 0, s>>>(X, rexp.as<int>(), D, bi.as<bf16>());
-    k_img_V<<<oz_img_grid(D.nkb * D.njb), 32 * kOzImgWarps, 0, s>>>(V, cexp.as<int>(), D, ai.as<bf16>());
-    ctx->note_launch(6);
-    ctx->check_launch("3c2c ozaki prep");
+    ctx->note_launch(3);
+    ctx->check_launch("3c2c ozaki X prep");
     const size_t n_jg = ceil_div(D.njb, (size_t)D.R), n_tiles = D.nibp * n_jg;
-    BSG_REQUIRE(n_tiles * D.nkb * J < 0xffffffffull, BSG_ERR_UNSUPPORTED, "too many Ozaki steps in one call");
-    DevBuf dt(n_tiles * sizeof(OzTile), s), dst(n_tiles * D.nkb * J * sizeof(OzStep), s);
+    BSG_REQUIRE(n_tiles * D.nkb * D.J < 0xffffffffull, BSG_ERR_UNSUPPORTED, "too many Ozaki steps in one call");
+    DevBuf dt(n_tiles * sizeof(OzTile), s), dst(n_tiles * D.nkb * D.J * sizeof(OzStep), s);
     const double tpb = thresh * (double)(bs * bs * bs);
-    auto *c = cnt.as<unsigned long long>();
     // V^T images of one slot group: R * nkb images; keep about 48 MB of them in L2
     const size_t grp_bytes = (size_t)D.R * D.nkb * a_img * 2;
     const size_t Gj = std::max<size_t>(1, std::min<size_t>(n_jg, (48ull << 20) / std::max<size_t>(grp_bytes, 1)));
-    k_tiles_3c<<<(unsigned)ceil_div(n_tiles, 128), 128, 0, s>>>(n_tiles, n_jg, Gj, xn.as<double>(), vn.as<double>(),
-                                                                rexp.as<int>(), cexp.as<int>(), out, D, tpb,
-                                                                dt.as<OzTile>(), dst.as<OzStep>(), c, c + 1);
+    k_tiles_3c<<<(unsigned)ceil_div(n_tiles, 128), 128, 0, s>>>(n_tiles, n_jg, Gj, xn.as<double>(), v.vn.as<double>(),
+                                                                rexp.as<int>(), v.cexp.as<int>(), out, D, tpb,
+                                                                dt.as<OzTile>(), dst.as<OzStep>(), cnt, cnt + 1);
     ctx->note_launch();
     ctx->check_launch("3c2c ozaki tiles");
     // tiles go round-robin (chunk 1): the Gj tiles of one block row run on
     // neighbouring CTAs at about the same time and share its X images in L2
     // (a chunk of Gj tiles per CTA puts 152 block rows in flight at once and
     // measured more DRAM traffic)
-    oz_run(ctx, sh, dt.as<OzTile>(), n_tiles, dst.as<OzStep>(), ai.as<bf16>(), bi.as<bf16>(), 1.0, s, c + 1, 1);
+    oz_run(ctx, sh, dt.as<OzTile>(), n_tiles, dst.as<OzStep>(), v.ai.as<bf16>(), bi.as<bf16>(), 1.0, s, cnt + 1, 1);
+}
+
+struct EventPair {
+    cudaEvent_t e[2] = {nullptr, nullptr};
+    EventPair() {
+        for (auto &x : e) BSG_CUDA(cudaEventCreateWithFlags(&x, cudaEventDisableTiming));
+    }
+    ~EventPair() {
+        for (auto &x : e)
+            if (x) cudaEventDestroy(x);
+    }
+};
+
+}  // namespace
+
+void transform_3c2c_ozaki(bsg_ctx ctx, size_t n_vec2, size_t n_aux, const double *X, const double *V, size_t bs,
+                          double thresh, int n_digits, double *out, uint64_t *nsig_out) {
+    cudaStream_t s = ctx->stream;
+    BSG_REQUIRE(bs <= 64, BSG_ERR_UNSUPPORTED, "Ozaki form supports blocks up to 64");
+    const int nd = oz_default_digits(n_digits, (int)bs, (int)bs, (int)bs);
+    OzShape sh;
+    const Dense3c D = oz3c_dims(n_aux, bs, nd, sh);
+    if (!n_vec2 || !n_aux) return;
+    DevBuf cnt(16, s);
+    BSG_CUDA(cudaMemsetAsync(cnt.p, 0, 16, s));
+    Oz3cV v;
+    oz3c_prepare_v(ctx, V, D, v);
+    oz3c_rows(ctx, D, sh, v, X, n_vec2, n_vec2, out, n_vec2, thresh, cnt.as<unsigned long long>());
     ctx->gemm_check();
     if (nsig_out) {
-        BSG_CUDA(cudaMemcpyAsync(nsig_out, c, 8, cudaMemcpyDeviceToHost, s));
+        BSG_CUDA(cudaMemcpyAsync(nsig_out, cnt.p, 8, cudaMemcpyDeviceToHost, s));
+        BSG_CUDA(cudaStreamSynchronize(s));
+    }
+}
+
+// Host X: uploaded in row ranges on the context's upload stream, each range
+// transformed on the compute stream while the next one is in flight (two
+// device range buffers).  The rows of the output are independent, so the
+// result equals transform_3c2c_ozaki's bit for bit.
+void transform_3c2c_ozaki_upload(bsg_ctx ctx, size_t n_vec2, size_t n_aux, const double *X_host, const double *V,
+                                 size_t bs, double thresh, int n_digits, double *out, uint64_t *nsig_out) {
+    cudaStream_t s = ctx->stream;
+    BSG_REQUIRE(bs <= 64, BSG_ERR_UNSUPPORTED, "Ozaki form supports blocks up to 64");
+    const int nd = oz_default_digits(n_digits, (int)bs, (int)bs, (int)bs);
+    OzShape sh;
+    const Dense3c D = oz3c_dims(n_aux, bs, nd, sh);
+    if (!n_vec2 || !n_aux) return;
+    // about eight ranges of whole block rows
+    const size_t nib = ceil_div(n_vec2, bs), rc = std::max<size_t>(1, ceil_div(nib, (size_t)8)) * bs;
+    const size_t n_ch = ceil_div(n_vec2, rc);
+    DevBuf cnt(16, s), xb0(rc * n_aux * 8, s), xb1(n_ch > 1 ? rc * n_aux * 8 : 0, s);
+    double *xb[2] = {xb0.as<double>(), xb1.as<double>()};
+    BSG_CUDA(cudaMemsetAsync(cnt.p, 0, 16, s));
+    Oz3cV v;
+    oz3c_prepare_v(ctx, V, D, v);
+    cudaStream_t up = ctx->upload_stream();
+    EventPair copied, used, ready;
+    BSG_CUDA(cudaEventRecord(ready.e[0], s));  // the range buffers exist (stream-ordered allocation)
+    BSG_CUDA(cudaStreamWaitEvent(up, ready.e[0], 0));
+    auto upload = [&](size_t c) {
+        const size_t r0 = c * rc, rows = std::min(rc, n_vec2 - r0);
+        BSG_CUDA(cudaMemcpy2DAsync(xb[c & 1], rows * 8, X_host + r0, n_vec2 * 8, rows * 8, n_aux,
+                                   cudaMemcpyHostToDevice, up));
+        BSG_CUDA(cudaEventRecord(copied.e[c & 1], up));
+    };
+    upload(0);
+    for (size_t c = 0; c < n_ch; ++c) {
+        if (c + 1 < n_ch) {
+            if (c >= 1) BSG_CUDA(cudaStreamWaitEvent(up, used.e[(c + 1) & 1], 0));  // range c-1 is done with it
+            upload(c + 1);
+        }
+        BSG_CUDA(cudaStreamWaitEvent(s, copied.e[c & 1], 0));
+        const size_t r0 = c * rc, rows = std::min(rc, n_vec2 - r0);
+        oz3c_rows(ctx, D, sh, v, xb[c & 1], rows, rows, out + r0, n_vec2, thresh, cnt.as<unsigned long long>());
+        BSG_CUDA(cudaEventRecord(used.e[c & 1], s));
+    }
+    ctx->gemm_check();
+    if (nsig_out) {
+        BSG_CUDA(cudaMemcpyAsync(nsig_out, cnt.p, 8, cudaMemcpyDeviceToHost, s));
         BSG_CUDA(cudaStreamSynchronize(s));
     }
 }

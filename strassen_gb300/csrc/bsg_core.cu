@@ -47,6 +47,10 @@ void ctx_release(bsg_ctx c) {
     if (c->refs.fetch_sub(1) == 1) {
         cudaStreamSynchronize(c->stream);
         if (c->d_gemm_err) cudaFree(c->d_gemm_err);
+        if (c->copy_stream) {
+            cudaStreamSynchronize(c->copy_stream);
+            cudaStreamDestroy(c->copy_stream);
+        }
         if (c->own_stream) cudaStreamDestroy(c->stream);
         delete c;
     }
@@ -62,6 +66,11 @@ extern "C" int bsg_version(void) { return 10000; }
 void bsg_ctx_s::check_launch(const char *what) {
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) throw Error{BSG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e)};
+}
+
+cudaStream_t bsg_ctx_s::upload_stream() {
+    if (!copy_stream) BSG_CUDA(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking));
+    return copy_stream;
 }
 
 int *bsg_ctx_s::gemm_err_flag() {

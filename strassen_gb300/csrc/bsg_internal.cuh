@@ -104,6 +104,10 @@ struct bsg_ctx_s {
     // GEMM per (block rows, block k, block cols, digits)
     bool autotune = true;
     std::map<std::array<int, 4>, std::array<int, 2>> oz_tune;
+    // second stream for host->device uploads that overlap compute on `stream`
+    // (created on first use, released with the context)
+    cudaStream_t copy_stream = 0;
+    cudaStream_t upload_stream();
     void note_launch(uint64_t n = 1) { launches += n; }
     void check_launch(const char *what);
     int *gemm_err_flag();  // the device flag, cleared before the first launch of a call

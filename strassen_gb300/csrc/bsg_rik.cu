@@ -533,22 +533,22 @@ extern "C" bsg_status bsg_3c2c_transform(bsg_ctx ctx, size_t n_vec2, size_t n_au
             // dense device path: same norms and screen as the block-sparse
             // path below, products on tensor cores, output written directly
             cudaStream_t s = ctx->stream;
-            DevBuf dx, dv, dout;
-            const double *x = ints_3c, *v = v_m12;
+            DevBuf dv, dout;
+            const double *v = v_m12;
             double *o = out;
             if (where == BSG_HOST) {
-                dx = DevBuf(n_vec2 * n_aux * 8, s);
                 dv = DevBuf(n_aux * n_aux * 8, s);
-                BSG_CUDA(cudaMemcpyAsync(dx.p, ints_3c, n_vec2 * n_aux * 8, cudaMemcpyHostToDevice, s));
                 BSG_CUDA(cudaMemcpyAsync(dv.p, v_m12, n_aux * n_aux * 8, cudaMemcpyHostToDevice, s));
-                x = dx.as<double>();
                 v = dv.as<double>();
             }
             if (out_where == BSG_HOST) {
                 dout = DevBuf(n_vec2 * n_aux * 8, s);
                 o = dout.as<double>();
             }
-            transform_3c2c_ozaki(ctx, n_vec2, n_aux, x, v, bs, thresh, n_digits, o, nullptr);
+            if (where == BSG_HOST)  // the integrals stream in by row ranges, overlapping the transform
+                transform_3c2c_ozaki_upload(ctx, n_vec2, n_aux, ints_3c, v, bs, thresh, n_digits, o, nullptr);
+            else
+                transform_3c2c_ozaki(ctx, n_vec2, n_aux, ints_3c, v, bs, thresh, n_digits, o, nullptr);
             if (out_where == BSG_HOST)
                 BSG_CUDA(cudaMemcpyAsync(out, o, n_vec2 * n_aux * 8, cudaMemcpyDeviceToHost, s));
             BSG_CUDA(cudaStreamSynchronize(s));

@@ -32,5 +32,9 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
 // dense device 3c->2c in the Ozaki form (bsg_3c2c_oz.cu)
 void transform_3c2c_ozaki(bsg_ctx ctx, size_t n_vec2, size_t n_aux, const double *X, const double *V, size_t bs,
                           double thresh, int n_digits, double *out, uint64_t *nsig_out);
+// the same with X in host memory: uploaded in row ranges that overlap the
+// transform of the previous range (V and out on the device)
+void transform_3c2c_ozaki_upload(bsg_ctx ctx, size_t n_vec2, size_t n_aux, const double *X_host, const double *V,
+                                 size_t bs, double thresh, int n_digits, double *out, uint64_t *nsig_out);
 
 }  // namespace bsg
