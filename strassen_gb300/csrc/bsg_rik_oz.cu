@@ -5,7 +5,8 @@
 //
 // Per chunk of aux functions P:
 //   scatter + U block norms / flags        (FP64 kernels shared with bsg_rik.cu)
-//   mui_P = U_P C        tiles (P, j, 5 block rows a), steps over b
+//   mui_P = U_P C        as mui_P^T = C^T U_P^T: tiles (P, a, 5 occupied block
+//                        columns j), steps over the present U_P(a, b)
 //   mui norms            FP64, from the computed mui blocks
 //   ij_P  = C^T mui_P    tiles (P, jb, 5 block rows ib), steps over a
 //   ijs_P = ij + ij^T    FP64 (shared kernel)
@@ -213,8 +214,9 @@ struct OzDims {
 // group's image start at j*bs (J = 1: the image's own np rows)
 __device__ __forceinline__ int rows_in_group(const OzDims &D) { return D.J == 1 ? D.npJ : (int)D.bs; }
 
-// U_p blocks (M side), gathered from the compressed integrals; one warp per
-// (p, a, b), image index p*nb*nb + a + b*nb
+// U_p blocks (a, b) as the N side of mui^T = C^T U^T (image rows = the
+// block's rows mu, k = its columns), gathered from the compressed integrals;
+// one warp per (p, a, b), image index p*nb*nb + a + b*nb
 __global__ void k_img_U(const double *__restrict__ ints, const int *__restrict__ inv, size_t n_vec2, size_t P0,
                         const uint8_t *__restrict__ uflag, const int *__restrict__ rexp, OzDims D, size_t n,
                         bf16 *__restrict__ img) {
@@ -222,20 +224,11 @@ __global__ void k_img_U(const double *__restrict__ ints, const int *__restrict__
     if (x >= n || !uflag[x]) return;
     const size_t p = x / (D.nb * D.nb), a = x % D.nb, b = (x / D.nb) % D.nb;
     const UGet get{inv, ints + (P0 + p) * n_vec2, D.n_bf, a * D.bs, b * D.bs};
-    oz_block_image_g(get, ext_r(a, D.bs, D.n_bf), ext_r(b, D.bs, D.n_bf), rexp + p * D.n_bf + a * D.bs, D.mp, D.kp,
-                     D.nd, img + x * D.nd * (size_t)D.mp * D.kp, true, threadIdx.x & 31, 32);
+    oz_block_image_g(get, ext_r(a, D.bs, D.n_bf), ext_r(b, D.bs, D.n_bf), rexp + p * D.n_bf + a * D.bs, D.np, D.kp,
+                     D.nd, img + x * D.nd * (size_t)D.np * D.kp, false, threadIdx.x & 31, 32);
 }
 
-// C blocks (b, j) in the B role of mui = U C; index b + j*nb
-__global__ void k_img_C_B(const double *__restrict__ C, const int *__restrict__ cexp, OzDims D, bf16 *__restrict__ img) {
-    const size_t x = oz_warp_id();
-    if (x >= D.nb * D.nob) return;
-    const size_t b = x % D.nb, j = x / D.nb;
-    oz_block_image(C + b * D.bs + j * D.bs * D.n_bf, D.n_bf, true, ext_r(j, D.bs, D.n_occ), ext_r(b, D.bs, D.n_bf),
-                cexp + j * D.bs, D.np, D.kp, D.nd, img + x * D.nd * (size_t)D.np * D.kp, false);
-}
-
-// C^T blocks (ib, a) in the A role of ij = C^T mui; index ib + a*nob
+// C^T blocks (ib, a) in the A role of ij = C^T mui and of mui^T = C^T U^T; index ib + a*nob
 __global__ void k_img_Ct_A(const double *__restrict__ C, const int *__restrict__ cexp, OzDims D, bf16 *__restrict__ img) {
     const size_t x = oz_warp_id();
     if (x >= D.nob * D.nb) return;
@@ -353,7 +346,10 @@ __device__ __forceinline__ void tile_clear(OzTile &T) {
     T.fresh_mask = 0xFFu;
 }
 
-// mui tiles: t = (p, j, group g of R block rows a)
+// mui tiles, transposed: mui_p^T(j, a) = sum_b C^T(j, b) U_p(a, b)^T, so the
+// dense C^T blocks fill the slots (R occupied block columns j) and the
+// block-sparse U_p supplies one N-side block per step (every present
+// U_p(a, b)); t = (p, a, group g of R block columns j), written transposed
 __global__ void k_tiles_mui(const uint8_t *__restrict__ uflag, const double *__restrict__ unorm,
                             const double *__restrict__ cnorm, const int *__restrict__ rexp_U,
                             const int *__restrict__ cexp_C, double *__restrict__ mui, OzDims D, size_t n_tiles,
@@ -362,38 +358,39 @@ __global__ void k_tiles_mui(const uint8_t *__restrict__ uflag, const double *__r
                             unsigned long long *__restrict__ macs) {
     const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n_tiles) return;
-    const size_t ng = (D.nb + D.R - 1) / D.R;
-    const size_t g = t % ng, j = (t / ng) % D.nob, p = t / (ng * D.nob);
+    const size_t ng = (D.nob + D.R - 1) / D.R;
+    const size_t g = t % ng, a = (t / ng) % D.nb, p = t / (ng * D.nb);
     unsigned long long m = 0;
     OzTile T;
     tile_clear(T);
     int cnt[kOzMaxSlots] = {0};
     for (int s = 0; s < D.R; ++s) {
-        const size_t a = g * D.R + s;
-        if (a >= D.nb) break;
+        const size_t j = g * D.R + s;
+        if (j >= D.nob) break;
         T.c[s] = mui + p * D.n_bf * D.n_occ + a * D.bs + j * D.bs * D.n_bf;
         T.ldc[s] = (int)D.n_bf;
-        T.rows[s] = ext_r(a, D.bs, D.n_bf);
-        T.rexp[s] = rexp_U + p * D.n_bf + a * D.bs;
+        T.rows[s] = ext_r(j, D.bs, D.n_occ);  // slot rows are mui columns
+        T.rexp[s] = cexp_C + j * D.bs;
     }
-    T.cols = ext_r(j, D.bs, D.n_occ);
-    T.trans = 0;
-    T.cexp = cexp_C + j * D.bs;
+    T.cols = ext_r(a, D.bs, D.n_bf);  // tile columns are mui rows
+    T.trans = 1;
+    T.cexp = rexp_U + p * D.n_bf + a * D.bs;
     T.s0 = (uint32_t)(t * D.nb);
     uint32_t n = 0;
     for (size_t b = 0; b < D.nb; ++b) {
+        const size_t ub = p * D.nb * D.nb + a + b * D.nb;
+        if (!uflag[ub]) continue;
         OzStep st;
         st.bmask = kOzAllSub;
-        st.b = (uint32_t)(b + j * D.nb);
+        st.b = (uint32_t)ub;
         bool any = false;
         for (int s = 0; s < kOzMaxSlots; ++s) {
             st.a[s] = kOzNone;
             if (s >= D.R || !T.c[s]) continue;
-            const size_t a = g * D.R + s, ub = p * D.nb * D.nb + a + b * D.nb;
-            if (!uflag[ub]) continue;
+            const size_t j = g * D.R + s;
             if (!(__dmul_rn(unorm[ub], cnorm[b + j * D.nb]) >= tpb)) continue;
-            st.a[s] = (uint32_t)ub;
-            m += (unsigned long long)T.rows[s] * ext_r(j, D.bs, D.n_occ) * ext_r(b, D.bs, D.n_bf);
+            st.a[s] = (uint32_t)(j + b * D.nob);
+            m += (unsigned long long)T.rows[s] * T.cols * ext_r(b, D.bs, D.n_bf);
             ++cnt[s];
             any = true;
         }
@@ -403,8 +400,8 @@ __global__ void k_tiles_mui(const uint8_t *__restrict__ uflag, const double *__r
     tiles[t] = T;
     unsigned long long tot = 0;
     for (int s = 0; s < D.R; ++s) {
-        const size_t a = g * D.R + s;
-        if (a >= D.nb) break;
+        const size_t j = g * D.R + s;
+        if (j >= D.nob) break;
         mflag[p * D.nb * D.nob + a + j * D.nb] = cnt[s] > 0;
         tot += cnt[s];
     }
@@ -715,7 +712,7 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
     // bytes per aux function of every per-chunk buffer
     const bool want_k = K_dev != nullptr, want_kmn = Kmn_dev != nullptr;
     const size_t Q = 8;  // aux functions per K-product tile
-    const size_t per_p = nb * nb * 9 + nb * nb * a_img * 2 + n_bf * n_occ * 8 + nb * nob * 9 +
+    const size_t per_p = nb * nb * 9 + nb * nb * b_img * 2 + n_bf * n_occ * 8 + nb * nob * 9 +
                          nb * nob * a_img * 2 + nb * nobp * b_imgJ * 2 + 3 * n_occ * n_occ * 8 + 3 * nob * nob * 9 +
                          nob * nobp * b_imgJ * 2 + (want_kmn ? nb * nob * b_img * 2 + nb * nb * bs * bs * 8 / Q : 0);
     size_t pc = d.p_chunk ? d.p_chunk : std::max<size_t>(1, (size_t)(8ull << 30) / per_p);
@@ -726,9 +723,8 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
     DevBuf dmui(pc * n_bf * n_occ * 8, s), dmn(pc * nb * nob * 8, s), dmf(pc * nb * nob, s);
     DevBuf dij(pc * n_occ * n_occ * 8, s), dijf(pc * nob * nob, s);
     DevBuf dijs(pc * n_occ * n_occ * 8, s), dsn(pc * nob * nob * 8, s), dsf(pc * nob * nob, s);
-    DevBuf dcn(nb * nob * 8, s), dcexpC(nob * bs * 4, s), dimgCB(nb * nob * b_img * 2, s),
-        dimgCtA(nob * nb * a_img * 2, s);
-    DevBuf drexpU(pc * n_bf * 4, s), dimgU(pc * nb * nb * a_img * 2, s);
+    DevBuf dcn(nb * nob * 8, s), dcexpC(nob * bs * 4, s), dimgCtA(nob * nb * a_img * 2, s);
+    DevBuf drexpU(pc * n_bf * 4, s), dimgU(pc * nb * nb * b_img * 2, s);
     DevBuf dcexpM(pc * n_occ * 4, s), dimgMB(pc * nb * nobp * b_imgJ * 2, s);
     DevBuf drexpMs(n_sub_max * n_bf * 4, s), dcexpSs(n_sub_max * n_occ * 4, s);
     // maxima bit patterns for the four exponent sets of a chunk
@@ -739,7 +735,7 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
     DevBuf dimgMA(pc * nb * nob * a_img * 2, s), dimgSB(pc * nob * nobp * b_imgJ * 2, s);
     DevBuf dKp(want_k ? n_sub_max * nobp * nb * bs * bs * J * 8 : 0, s), dcnt(6 * 8, s), dmacs(4 * 8, s);
     const size_t ng_a = ceil_div(nb, (size_t)D.R), ng_i = ceil_div(nob, (size_t)D.R);
-    const size_t tiles_mui = pc * nob * ng_a, tiles_ij = pc * nobp * ng_i, tiles_K = n_sub_max * nobp * ng_a;
+    const size_t tiles_mui = pc * nb * ng_i, tiles_ij = pc * nobp * ng_i, tiles_K = n_sub_max * nobp * ng_a;
     DevBuf dtm(tiles_mui * sizeof(OzTile), s), dsm(tiles_mui * nb * sizeof(OzStep), s);
     DevBuf dti(tiles_ij * sizeof(OzTile), s), dsi(tiles_ij * nb * J * sizeof(OzStep), s);
     DevBuf dtk(tiles_K * sizeof(OzTile), s), dsk(tiles_K * Q * nob * J * sizeof(OzStep), s);
@@ -755,11 +751,10 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
     auto *macs = dmacs.as<unsigned long long>();
     const unsigned tb = (unsigned)std::max<size_t>(32, ((bs + 31) / 32) * 32);
 
-    // call-constant operands: C norms, C column exponents, C images in both roles
+    // call-constant operands: C norms, C column exponents, C^T images
     const int wpb = 8;
     k_cnorms<<<(unsigned)ceil_div(nb * nob, wpb), wpb * 32, 0, s>>>(d.c_occ, n_bf, n_occ, bs, nb, nob, dcn.as<double>());
     k_cexp_C<<<(unsigned)nob, tb, 0, s>>>(d.c_occ, n_bf, n_occ, bs, dcexpC.as<int>());
-    k_img_C_B<<<oz_img_grid(nb * nob), 32 * kOzImgWarps, 0, s>>>(d.c_occ, dcexpC.as<int>(), D, dimgCB.as<bf16>());
     k_img_Ct_A<<<oz_img_grid(nob * nb), 32 * kOzImgWarps, 0, s>>>(d.c_occ, dcexpC.as<int>(), D, dimgCtA.as<bf16>());
     // inverse key map of the compressed integrals (replaces the per-P dense rebuild)
     BSG_CUDA(cudaMemsetAsync(dinv.p, 0xFF, n_bf * n_bf * 4, s));
@@ -767,7 +762,7 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
     if (d.n_vec2)
         k_key_inverse<<<(unsigned)ceil_div(d.n_vec2, 256), 256, 0, s>>>(d.keys, d.n_vec2, n_bf, bs, nb, dinv.as<int>(),
                                                                         docc.as<uint8_t>());
-    ctx->note_launch(5);
+    ctx->note_launch(4);
     const double tpb_u = 1e-20 * (double)(bs * bs);
     const double tpb = d.thresh * (double)(bs * bs * bs);
     for (size_t P0 = 0; P0 < n_aux; P0 += pc) {
@@ -786,13 +781,14 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
         k_img_U<<<oz_img_grid(np * nb * nb), 32 * kOzImgWarps, 0, s>>>(d.ints, dinv.as<int>(), d.n_vec2, P0,
                                                                        duf.as<uint8_t>(), drexpU.as<int>(), D,
                                                                        np * nb * nb, dimgU.as<bf16>());
-        const size_t tm = np * nob * ng_a;
+        const size_t tm = np * nb * ng_i;
         k_tiles_mui<<<(unsigned)ceil_div(tm, 128), 128, 0, s>>>(
             duf.as<uint8_t>(), dun.as<double>(), dcn.as<double>(), drexpU.as<int>(), dcexpC.as<int>(),
             dmui.as<double>(), D, tm, tpb, dtm.as<OzTile>(), dsm.as<OzStep>(), dmf.as<uint8_t>(), cnt + 0, macs + 0);
         ctx->note_launch(5);
         ctx->check_launch("rik ozaki mui prep");
-        oz_run(ctx, sh, dtm.as<OzTile>(), tm, dsm.as<OzStep>(), dimgU.as<bf16>(), dimgCB.as<bf16>(), 1.0, s, macs + 0);
+        oz_run(ctx, sh, dtm.as<OzTile>(), tm, dsm.as<OzStep>(), dimgCtA.as<bf16>(), dimgU.as<bf16>(), 1.0, s,
+               macs + 0);
         k_mui_norms<<<(unsigned)ceil_div(np * nb * nob, wpb), wpb * 32, 0, s>>>(
             dmui.as<double>(), dmf.as<uint8_t>(), n_bf, n_occ, bs, nb, nob, np * nb * nob, dmn.as<double>());
         // mui row exponents per sub-range (A operand of K and of K_mn)
