@@ -450,7 +450,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--form", default="ozaki", choices=["fp64", "ozaki"])
-    ap.add_argument("--digits-3c2c", type=int, default=6)
+    ap.add_argument("--digits-3c2c", type=int, default=5)
     ap.add_argument("--digits-occ", type=int, default=5)
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")

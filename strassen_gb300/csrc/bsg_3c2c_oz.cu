@@ -208,12 +208,21 @@ struct Oz3cV {
 
 Dense3c oz3c_dims(size_t n_aux, size_t bs, int nd, OzShape &sh) {
     // X block rows per tile on the N side.  Two rows (nd * 2*bs TMEM columns,
-    // bs % 8 == 0) halve the V^T image traffic per product, but on the 40-atom
-    // workload 35% of the steps split into two rectangles (the rows' screens
-    // differ) and the accumulator no longer fits twice in TMEM: measured 50 ms
-    // against 46 ms with one row, so one row it is.
-    const int J = 1;
+    // bs % 8 == 0) halve the shared-memory bytes of the V^T operand per
+    // product; 35% of the steps split into two rectangles (the rows' screens
+    // differ).  Measured on the 40-atom workload: 5 digits 34.1 ms with two
+    // rows against 36.2 with one; 6 digits 41.1 against 39.5 (the two
+    // accumulator sets no longer fit TMEM together), so two rows only where
+    // both sets fit.
+    int J = (bs % 8 == 0 && 2 * bs <= 64 && nd * 2 * (int)bs + 8 <= 256) ? 2 : 1;
     sh = oz_shape((int)bs, (int)bs, (int)bs * J, nd);
+    if (J == 2) {  // the V^T images are laid out for the one-row shape's k steps
+        const OzShape s1 = oz_shape((int)bs, (int)bs, (int)bs, nd);
+        if (s1.kp != sh.kp || s1.pair != sh.pair) {
+            J = 1;
+            sh = s1;
+        }
+    }
     sh.J = J;
     Dense3c D;
     D.n_vec2 = D.ldx = D.ldo = 0;

@@ -145,19 +145,21 @@ def test_ozaki_pipeline(api, ctx):
     assert err < 1e-9
 
 
+@pytest.mark.parametrize("nd,tol", [(6, 1e-10), (5, 1e-7)])
 @pytest.mark.parametrize("n_atoms,bs", [(8, 24), (3, 16), (1, 24)])
-def test_3c2c_host_upload_matches_device(api, ctx, n_atoms, bs):
+def test_3c2c_host_upload_matches_device(api, ctx, n_atoms, bs, nd, tol):
     """host integrals stream in by row ranges overlapping the transform: the
     output equals the device-input transform bit for bit (ranges of whole
-    block rows, a ragged last range, and a single range)"""
+    block rows, a ragged last range, and a single range); at 5 digits the
+    tiles carry two X block rows (split into exact rectangles)"""
     torch = pytest.importorskip("torch")
     s = S.RikSystem(seed=4, n_atoms=n_atoms, nbf=24, naux=12, n_occ=10, box=5.0)
     X, V = s.ints_3c(), s.v_m12()
-    out_h = api.transform_3c2c(X, V, bs, 1e-10, form=api.FORM_OZAKI, n_digits=6, ctx=ctx)
+    out_h = api.transform_3c2c(X, V, bs, 1e-10, form=api.FORM_OZAKI, n_digits=nd, ctx=ctx)
     Xd = torch.from_numpy(np.ascontiguousarray(X.T)).cuda().T
     Vd = torch.from_numpy(np.ascontiguousarray(V.T)).cuda().T
     out_d = torch.zeros((X.shape[1], X.shape[0]), dtype=torch.float64, device="cuda").T
-    api.transform_3c2c(Xd, Vd, bs, 1e-10, form=api.FORM_OZAKI, n_digits=6, out=out_d, ctx=ctx)
+    api.transform_3c2c(Xd, Vd, bs, 1e-10, form=api.FORM_OZAKI, n_digits=nd, out=out_d, ctx=ctx)
     assert same_bits(out_h, out_d.cpu().numpy())
     ref = api.transform_3c2c(X, V, bs, 1e-10, ctx=ctx)
-    assert np.linalg.norm(out_h - ref) / np.linalg.norm(ref) < 1e-10
+    assert np.linalg.norm(out_h - ref) / np.linalg.norm(ref) < tol
