@@ -145,33 +145,29 @@ __device__ __forceinline__ size_t oz_plane_stride(bool m_side, int mpad, int kp)
 }
 
 // Fixed-point value of v with row/column exponent e, integer arithmetic only:
-// N = round(v 2^(K - e)) with ties to even (|N| <= 2^K).
+// N = round(v 2^(K - e)) with ties to even (|N| <= 2^K).  With q = M >> s
+// the rounded quotient is (M + 2^(s-1) - 1 + (q & 1)) >> s, one add chain
+// instead of compares; s is capped at 63 (any s >= 54 rounds to 0 either way).
 __device__ __forceinline__ long long oz_fixed(double v, int e, int K) {
-    const long long bits = __double_as_longlong(v);
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
     const int E = (int)((bits >> 52) & 0x7FF);
-    const long long M = (bits & 0xFFFFFFFFFFFFFll) | (E ? (1ll << 52) : 0ll);
+    const unsigned long long M = (bits & 0xFFFFFFFFFFFFFull) | (E ? (1ull << 52) : 0ull);
     const int sh = (E ? E : 1) - 1075 + K - e;  // N = M * 2^sh
-    long long N;
-    if (M == 0) {
-        N = 0;
-    } else if (sh >= 0) {
+    unsigned long long N;
+    if (sh >= 0) {
         N = M << sh;
     } else {
-        const int s = -sh;
-        if (s > 54) {
-            N = 0;
-        } else {
-            const long long q = M >> s, rem = M & ((1ll << s) - 1), half = 1ll << (s - 1);
-            N = q + ((rem > half || (rem == half && (q & 1))) ? 1 : 0);
-        }
+        const int s = -sh < 63 ? -sh : 63;
+        N = (M + ((1ull << (s - 1)) - 1ull) + ((M >> s) & 1ull)) >> s;
     }
-    return bits < 0 ? -N : N;
+    return (bits >> 63) ? -(long long)N : (long long)N;
 }
 
 // Split into nd balanced base-256 digits: N = d_0 256^(nd-1) + ... + d_{nd-1}
 // with d_1.. in [-128, 127] and d_0 in [-128, 128], K = 7 + 8(nd-1).  Adding
 // 128 to each of the nd-1 low bytes (the constant 0x80..80) makes them plain
-// bytes of T = N + C (d_i = byte - 128) and leaves d_0 = T >> 8(nd-1).
+// bytes of T = N + C (d_i = byte - 128) and leaves d_0 = T >> 8(nd-1).  Up to
+// 5 digits the low bytes sit in T's low 32 bits and are read from there.
 struct OzDigits {
     long long T;
     int lowb;  // 8 (nd - 1)
@@ -187,6 +183,7 @@ struct OzDigits {
             const int d0 = (int)(T >> lowb);
             return (d0 < 0 && !neg) ? d0 + 256 : d0;  // nd = 8: N = +2^63 wraps
         }
+        if (lowb <= 32) return (int)(((unsigned int)T >> (lowb - 8 * i)) & 255u) - 128;
         return (int)((T >> (lowb - 8 * i)) & 255) - 128;
     }
 };
@@ -194,8 +191,8 @@ struct OzDigits {
 // bf16 bits of d 2^(-8i) for an integer |d| <= 128 (exact; built from the
 // float bits of d with the exponent lowered by 8i)
 __device__ __forceinline__ uint32_t oz_digit_bf16(int d, int i) {
-    if (!d) return 0u;
-    return (__float_as_uint((float)d) - ((uint32_t)(8 * i) << 23)) >> 16;
+    const uint32_t f = (__float_as_uint((float)d) - ((uint32_t)(8 * i) << 23)) >> 16;
+    return d ? f : 0u;
 }
 
 // Digit image of one block from a value source get(r, l) (image row r, k l),

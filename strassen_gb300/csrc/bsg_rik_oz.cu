@@ -64,24 +64,24 @@ struct UGet {
     }
 };
 
-// block norms and keep flags of U_p, one warp per (p, a, b); the elements are
-// visited in the order of the dense block norm (lane-strided column-major),
-// so the result is bit-identical to it
-__global__ void k_unorms_c(const double *__restrict__ ints, const int *__restrict__ inv, const uint8_t *__restrict__ occ,
-                           size_t n_vec2, size_t P0, size_t n_bf, size_t bs, size_t nb, size_t n_p, double tpb,
-                           double *__restrict__ norm, uint8_t *__restrict__ flag) {
-    const size_t x = oz_warp_id();
-    if (x >= n_p * nb * nb) return;
-    const size_t p = x / (nb * nb), rr = x % (nb * nb), a = rr % nb, b = rr / nb;
-    if (!occ[rr]) {  // no entry: the dense block is zero, its norm 0 (< tpb)
-        if ((threadIdx.x & 31) == 0) {
-            norm[x] = 0.0;
-            flag[x] = !(0.0 < tpb);
-        }
-        return;
-    }
+// block norms and keep flags of U_p, one warp per (p, occupied block w =
+// p*n_ob + ob); the elements are visited in the order of the dense block norm
+// (lane-strided column-major), so the result is bit-identical to it.  Blocks
+// without any integral keep the zero norm and flag the caller cleared.  The
+// gathered elements are also stored densely (ucomp + w*bs*bs, column-major
+// with the block's row count as leading dimension) for the row maxima and
+// the digit images.
+__global__ void k_unorms_c(const double *__restrict__ ints, const int *__restrict__ inv,
+                           const uint32_t *__restrict__ ob_list, size_t n_ob, size_t n_vec2, size_t P0, size_t n_bf,
+                           size_t bs, size_t nb, size_t n_p, double tpb, double *__restrict__ norm,
+                           uint8_t *__restrict__ flag, double *__restrict__ ucomp) {
+    const size_t w = oz_warp_id();
+    if (w >= n_p * n_ob) return;
+    const size_t p = w / n_ob, rr = ob_list[w % n_ob], a = rr % nb, b = rr / nb;
+    const size_t x = p * nb * nb + rr;
     const int rs = ext_r(a, bs, n_bf), cs = ext_r(b, bs, n_bf);
     const UGet get{inv, ints + (P0 + p) * n_vec2, n_bf, a * bs, b * bs};
+    double *dense = ucomp + w * bs * bs;
     const int lane = threadIdx.x & 31, n = rs * cs;
     double acc = 0.0;
     for (int i0 = lane; i0 < n; i0 += 32 * 8) {
@@ -93,7 +93,10 @@ __global__ void k_unorms_c(const double *__restrict__ ints, const int *__restric
         }
 #pragma unroll
         for (int u = 0; u < 8; ++u)
-            if (i0 + 32 * u < n) acc = fma(v[u], v[u], acc);
+            if (i0 + 32 * u < n) {
+                acc = fma(v[u], v[u], acc);
+                dense[i0 + 32 * u] = v[u];
+            }
     }
 #pragma unroll
     for (int o = 16; o >= 1; o >>= 1) acc = __dadd_rn(acc, __shfl_down_sync(0xffffffffu, acc, o));
@@ -123,21 +126,21 @@ __global__ void k_bits_exp(const unsigned long long *__restrict__ bits, size_t n
     if (i < n) exps[i] = oz_exp_of_bits((long long)bits[i]);
 }
 
-// rows of U_p over its present blocks, gathered from the compressed integrals
-__global__ void k_rowmax_U_c(const double *__restrict__ ints, const int *__restrict__ inv, size_t n_vec2, size_t P0,
-                             const uint8_t *__restrict__ uflag, size_t n_bf, size_t bs, size_t nb, size_t n,
+// rows of U_p over its kept blocks, from the dense copies; one warp per
+// occupied block w
+__global__ void k_rowmax_U_c(const double *__restrict__ ucomp, const uint32_t *__restrict__ ob_list, size_t n_ob,
+                             size_t n_p, const uint8_t *__restrict__ uflag, size_t n_bf, size_t bs, size_t nb,
                              unsigned long long *__restrict__ bits) {
-    const size_t x = oz_warp_id();
-    if (x >= n || !uflag[x]) return;
-    const size_t p = x / (nb * nb), a = x % nb, b = (x / nb) % nb;
+    const size_t w = oz_warp_id();
+    if (w >= n_p * n_ob) return;
+    const size_t p = w / n_ob, rr = ob_list[w % n_ob], a = rr % nb, b = rr / nb;
+    if (!uflag[p * nb * nb + rr]) return;
     const int rows = ext_r(a, bs, n_bf), k = ext_r(b, bs, n_bf);
-    const double *col = ints + (P0 + p) * n_vec2;
+    const double *dense = ucomp + w * bs * bs;
     for (int r = threadIdx.x & 31; r < rows; r += 32) {
         long long mx = 0;
         for (int l = 0; l < k; ++l) {
-            const int v = inv[a * bs + r + (b * bs + l) * n_bf];
-            if (v < 0) continue;
-            const long long bb_ = oz_absbits(col[v]);
+            const long long bb_ = oz_absbits(dense[r + l * rows]);
             mx = bb_ > mx ? bb_ : mx;
         }
         if (mx) atomicMax(&bits[p * n_bf + a * bs + r], (unsigned long long)mx);
@@ -214,18 +217,22 @@ struct OzDims {
 // group's image start at j*bs (J = 1: the image's own np rows)
 __device__ __forceinline__ int rows_in_group(const OzDims &D) { return D.J == 1 ? D.npJ : (int)D.bs; }
 
+
+
 // U_p blocks (a, b) as the N side of mui^T = C^T U^T (image rows = the
-// block's rows mu, k = its columns), gathered from the compressed integrals;
-// one warp per (p, a, b), image index p*nb*nb + a + b*nb
-__global__ void k_img_U(const double *__restrict__ ints, const int *__restrict__ inv, size_t n_vec2, size_t P0,
-                        const uint8_t *__restrict__ uflag, const int *__restrict__ rexp, OzDims D, size_t n,
+// block's rows mu, k = its columns), from the dense copies; one warp per
+// occupied block w, image index p*nb*nb + a + b*nb
+__global__ void k_img_U(const double *__restrict__ ucomp, const uint32_t *__restrict__ ob_list, size_t n_ob,
+                        size_t n_p, const uint8_t *__restrict__ uflag, const int *__restrict__ rexp, OzDims D,
                         bf16 *__restrict__ img) {
-    const size_t x = oz_warp_id();
-    if (x >= n || !uflag[x]) return;
-    const size_t p = x / (D.nb * D.nb), a = x % D.nb, b = (x / D.nb) % D.nb;
-    const UGet get{inv, ints + (P0 + p) * n_vec2, D.n_bf, a * D.bs, b * D.bs};
-    oz_block_image_g(get, ext_r(a, D.bs, D.n_bf), ext_r(b, D.bs, D.n_bf), rexp + p * D.n_bf + a * D.bs, D.np, D.kp,
-                     D.nd, img + x * D.nd * (size_t)D.np * D.kp, false, threadIdx.x & 31, 32);
+    const size_t w = oz_warp_id();
+    if (w >= n_p * n_ob) return;
+    const size_t p = w / n_ob, rr = ob_list[w % n_ob], a = rr % D.nb, b = rr / D.nb;
+    const size_t x = p * D.nb * D.nb + rr;
+    if (!uflag[x]) return;
+    const int rows = ext_r(a, D.bs, D.n_bf);
+    oz_block_image(ucomp + w * D.bs * D.bs, (size_t)rows, false, rows, ext_r(b, D.bs, D.n_bf),
+                   rexp + p * D.n_bf + a * D.bs, D.np, D.kp, D.nd, img + x * D.nd * (size_t)D.np * D.kp, false);
 }
 
 // C^T blocks (ib, a) in the A role of ij = C^T mui and of mui^T = C^T U^T; index ib + a*nob
@@ -763,6 +770,16 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
         k_key_inverse<<<(unsigned)ceil_div(d.n_vec2, 256), 256, 0, s>>>(d.keys, d.n_vec2, n_bf, bs, nb, dinv.as<int>(),
                                                                         docc.as<uint8_t>());
     ctx->note_launch(4);
+    // the U blocks that hold any integral (the same for every P), in block order
+    std::vector<uint8_t> hocc(nb * nb);
+    BSG_CUDA(cudaMemcpyAsync(hocc.data(), docc.p, nb * nb, cudaMemcpyDeviceToHost, s));
+    BSG_CUDA(cudaStreamSynchronize(s));
+    std::vector<uint32_t> hob;
+    for (size_t rr = 0; rr < nb * nb; ++rr)
+        if (hocc[rr]) hob.push_back((uint32_t)rr);
+    const size_t n_ob = hob.size();
+    DevBuf dob(std::max<size_t>(1, n_ob) * 4, s), ducomp(std::max<size_t>(1, pc * n_ob) * bs * bs * 8, s);
+    if (n_ob) BSG_CUDA(cudaMemcpyAsync(dob.p, hob.data(), n_ob * 4, cudaMemcpyHostToDevice, s));
     const double tpb_u = 1e-20 * (double)(bs * bs);
     const double tpb = d.thresh * (double)(bs * bs * bs);
     for (size_t P0 = 0; P0 < n_aux; P0 += pc) {
@@ -770,17 +787,22 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
         BSG_CUDA(cudaMemsetAsync(macs, 0, 4 * 8, s));
         // U_p block norms, keep flags, row exponents and digit images, all
         // gathered from the compressed integrals
-        k_unorms_c<<<oz_img_grid(np * nb * nb), 32 * kOzImgWarps, 0, s>>>(
-            d.ints, dinv.as<int>(), docc.as<uint8_t>(), d.n_vec2, P0, n_bf, bs, nb, np, tpb_u, dun.as<double>(),
-            duf.as<uint8_t>());
+        BSG_CUDA(cudaMemsetAsync(dun.p, 0, np * nb * nb * 8, s));
+        BSG_CUDA(cudaMemsetAsync(duf.p, 0, np * nb * nb, s));
         // mui = U C
         BSG_CUDA(cudaMemsetAsync(dbits.p, 0, nbits * 8, s));
-        k_rowmax_U_c<<<oz_img_grid(np * nb * nb), 32 * kOzImgWarps, 0, s>>>(
-            d.ints, dinv.as<int>(), d.n_vec2, P0, duf.as<uint8_t>(), n_bf, bs, nb, np * nb * nb, bitsU);
+        if (n_ob) {
+            k_unorms_c<<<oz_img_grid(np * n_ob), 32 * kOzImgWarps, 0, s>>>(
+                d.ints, dinv.as<int>(), dob.as<uint32_t>(), n_ob, d.n_vec2, P0, n_bf, bs, nb, np, tpb_u,
+                dun.as<double>(), duf.as<uint8_t>(), ducomp.as<double>());
+            k_rowmax_U_c<<<oz_img_grid(np * n_ob), 32 * kOzImgWarps, 0, s>>>(
+                ducomp.as<double>(), dob.as<uint32_t>(), n_ob, np, duf.as<uint8_t>(), n_bf, bs, nb, bitsU);
+        }
         k_bits_exp<<<(unsigned)ceil_div(np * n_bf, (size_t)256), 256, 0, s>>>(bitsU, np * n_bf, drexpU.as<int>());
-        k_img_U<<<oz_img_grid(np * nb * nb), 32 * kOzImgWarps, 0, s>>>(d.ints, dinv.as<int>(), d.n_vec2, P0,
-                                                                       duf.as<uint8_t>(), drexpU.as<int>(), D,
-                                                                       np * nb * nb, dimgU.as<bf16>());
+        if (n_ob)
+            k_img_U<<<oz_img_grid(np * n_ob), 32 * kOzImgWarps, 0, s>>>(ducomp.as<double>(), dob.as<uint32_t>(), n_ob,
+                                                                       np, duf.as<uint8_t>(), drexpU.as<int>(), D,
+                                                                       dimgU.as<bf16>());
         const size_t tm = np * nb * ng_i;
         k_tiles_mui<<<(unsigned)ceil_div(tm, 128), 128, 0, s>>>(
             duf.as<uint8_t>(), dun.as<double>(), dcn.as<double>(), drexpU.as<int>(), dcexpC.as<int>(),
