@@ -74,7 +74,8 @@ struct UGet {
 __global__ void k_unorms_c(const double *__restrict__ ints, const int *__restrict__ inv,
                            const uint32_t *__restrict__ ob_list, size_t n_ob, size_t n_vec2, size_t P0, size_t n_bf,
                            size_t bs, size_t nb, size_t n_p, double tpb, double *__restrict__ norm,
-                           uint8_t *__restrict__ flag, double *__restrict__ ucomp) {
+                           uint8_t *__restrict__ flag, double *__restrict__ ucomp,
+                           unsigned long long *__restrict__ row_bits) {
     const size_t w = oz_warp_id();
     if (w >= n_p * n_ob) return;
     const size_t p = w / n_ob, rr = ob_list[w % n_ob], a = rr % nb, b = rr / nb;
@@ -100,10 +101,23 @@ __global__ void k_unorms_c(const double *__restrict__ ints, const int *__restric
     }
 #pragma unroll
     for (int o = 16; o >= 1; o >>= 1) acc = __dadd_rn(acc, __shfl_down_sync(0xffffffffu, acc, o));
+    const double est = sqrt(__shfl_sync(0xffffffffu, acc, 0));
+    const bool keep = !(est < tpb);
     if (lane == 0) {
-        const double est = sqrt(acc);
         norm[x] = est;
-        flag[x] = !(est < tpb);
+        flag[x] = keep;
+    }
+    if (!keep) return;
+    // row maxima of the kept block (the scale exponents of U's rows), from
+    // the dense copy this warp just wrote
+    __syncwarp();
+    for (int r = lane; r < rs; r += 32) {
+        long long mx = 0;
+        for (int l = 0; l < cs; ++l) {
+            const long long bb_ = oz_absbits(dense[r + l * rs]);
+            mx = bb_ > mx ? bb_ : mx;
+        }
+        if (mx) atomicMax(&row_bits[p * n_bf + a * bs + r], (unsigned long long)mx);
     }
 }
 
@@ -124,64 +138,6 @@ __global__ void k_cexp_C(const double *__restrict__ C, size_t n_bf, size_t n_occ
 __global__ void k_bits_exp(const unsigned long long *__restrict__ bits, size_t n, int *__restrict__ exps) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) exps[i] = oz_exp_of_bits((long long)bits[i]);
-}
-
-// rows of U_p over its kept blocks, from the dense copies; one warp per
-// occupied block w
-__global__ void k_rowmax_U_c(const double *__restrict__ ucomp, const uint32_t *__restrict__ ob_list, size_t n_ob,
-                             size_t n_p, const uint8_t *__restrict__ uflag, size_t n_bf, size_t bs, size_t nb,
-                             unsigned long long *__restrict__ bits) {
-    const size_t w = oz_warp_id();
-    if (w >= n_p * n_ob) return;
-    const size_t p = w / n_ob, rr = ob_list[w % n_ob], a = rr % nb, b = rr / nb;
-    if (!uflag[p * nb * nb + rr]) return;
-    const int rows = ext_r(a, bs, n_bf), k = ext_r(b, bs, n_bf);
-    const double *dense = ucomp + w * bs * bs;
-    for (int r = threadIdx.x & 31; r < rows; r += 32) {
-        long long mx = 0;
-        for (int l = 0; l < k; ++l) {
-            const long long bb_ = oz_absbits(dense[r + l * rows]);
-            mx = bb_ > mx ? bb_ : mx;
-        }
-        if (mx) atomicMax(&bits[p * n_bf + a * bs + r], (unsigned long long)mx);
-    }
-}
-
-// columns of mui_p (per p) over its present blocks
-__global__ void k_colmax_mui(const double *__restrict__ mui, const uint8_t *__restrict__ mflag, size_t n_bf,
-                             size_t n_occ, size_t bs, size_t nb, size_t nob, size_t n, unsigned long long *__restrict__ bits) {
-    const size_t x = oz_warp_id();
-    if (x >= n || !mflag[x]) return;
-    const size_t p = x / (nb * nob), a = x % nb, jb = (x / nb) % nob;
-    const int rows = ext_r(a, bs, n_bf), cols = ext_r(jb, bs, n_occ);
-    const double *M = mui + p * n_bf * n_occ;
-    for (int c = threadIdx.x & 31; c < cols; c += 32) {
-        long long mx = 0;
-        for (int r = 0; r < rows; ++r) {
-            const long long bb_ = oz_absbits(M[a * bs + r + (jb * bs + c) * n_bf]);
-            mx = bb_ > mx ? bb_ : mx;
-        }
-        if (mx) atomicMax(&bits[p * n_occ + jb * bs + c], (unsigned long long)mx);
-    }
-}
-
-// rows of mui over the aux sub-range p / Q
-__global__ void k_rowmax_mui_sub(const double *__restrict__ mui, const uint8_t *__restrict__ mflag, size_t n_bf,
-                                 size_t n_occ, size_t bs, size_t nb, size_t nob, size_t Q, size_t n,
-                                 unsigned long long *__restrict__ bits) {
-    const size_t x = oz_warp_id();
-    if (x >= n || !mflag[x]) return;
-    const size_t p = x / (nb * nob), a = x % nb, ib = (x / nb) % nob;
-    const int rows = ext_r(a, bs, n_bf), k = ext_r(ib, bs, n_occ);
-    const double *M = mui + p * n_bf * n_occ;
-    for (int r = threadIdx.x & 31; r < rows; r += 32) {
-        long long mx = 0;
-        for (int l = 0; l < k; ++l) {
-            const long long bb_ = oz_absbits(M[a * bs + r + (ib * bs + l) * n_bf]);
-            mx = bb_ > mx ? bb_ : mx;
-        }
-        if (mx) atomicMax(&bits[(p / Q) * n_bf + a * bs + r], (unsigned long long)mx);
-    }
 }
 
 // columns of ijs over the aux sub-range p / Q
@@ -340,6 +296,29 @@ __device__ __forceinline__ uint32_t emit_rect_steps(uint32_t (&live)[2], int J, 
     return n;
 }
 
+// Warp-built step lists: lane l holds the (at most 2) steps of the tile's
+// k step base + l; they are written after the n steps already there, in
+// lane order, which is the order a serial loop over the k steps gives.
+__device__ __forceinline__ void warp_append_steps(const OzStep (&mine)[2], uint32_t cnt, OzStep *__restrict__ out,
+                                                  uint32_t &n) {
+    const int lane = threadIdx.x & 31;
+    uint32_t incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    const uint32_t excl = incl - cnt;
+    for (uint32_t i = 0; i < cnt; ++i) out[n + excl + i] = mine[i];
+    n += __shfl_sync(0xffffffffu, incl, 31);
+}
+
+__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
 // ---- tiles and steps (one thread per tile) ----
 
 __device__ __forceinline__ void tile_clear(OzTile &T) {
@@ -417,21 +396,22 @@ __global__ void k_tiles_mui(const uint8_t *__restrict__ uflag, const double *__r
 }
 
 // ij tiles: t = (p, jbp, group of R block rows ib), N side J block columns
-// jb = J*jbp + j, steps over a (split into exact rectangles)
+// jb = J*jbp + j, steps over a (split into exact rectangles); one warp per
+// tile, lanes over a
 __global__ void k_tiles_ij(const uint8_t *__restrict__ mflag, const double *__restrict__ mnorm,
                            const double *__restrict__ cnorm, const int *__restrict__ cexp_C,
                            const int *__restrict__ cexp_mui, double *__restrict__ ij, OzDims D, size_t n_tiles,
                            double tpb, OzTile *__restrict__ tiles, OzStep *__restrict__ steps,
                            uint8_t *__restrict__ ijflag, unsigned long long *__restrict__ nsig,
                            unsigned long long *__restrict__ macs) {
-    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t t = oz_warp_id();
     if (t >= n_tiles) return;
+    const int lane = threadIdx.x & 31;
     const size_t ng = (D.nob + D.R - 1) / D.R;
     const size_t g = t % ng, jbp = (t / ng) % D.nobp, p = t / (ng * D.nobp);
     unsigned long long m = 0;
     OzTile T;
     tile_clear(T);
-    uint32_t cnt[kOzMaxSlots][2] = {};
     for (int s = 0; s < D.R; ++s) {
         const size_t ib = g * D.R + s;
         if (ib >= D.nob) break;
@@ -451,59 +431,71 @@ __global__ void k_tiles_ij(const uint8_t *__restrict__ mflag, const double *__re
     T.trans = 0;
     T.cexp = cexp_mui + p * D.n_occ + jbp * D.J * D.bs;
     T.s0 = (uint32_t)(t * D.nb * D.J);
-    uint32_t n = 0;
-    for (size_t a = 0; a < D.nb; ++a) {
-        uint32_t live[2] = {0, 0};
-        uint32_t a_idx[kOzMaxSlots];
-        for (int s = 0; s < kOzMaxSlots; ++s) a_idx[s] = (uint32_t)(g * D.R + s + a * D.nob);
-        for (int j = 0; j < D.J; ++j) {
-            const size_t jb = jbp * D.J + j;
-            if (jb >= D.nob) continue;
-            const size_t mb = p * D.nb * D.nob + a + jb * D.nb;
-            if (!mflag[mb]) continue;
-            for (int s = 0; s < D.R; ++s) {
-                if (!T.c[s]) continue;
-                const size_t ib = g * D.R + s;
-                if (!(__dmul_rn(cnorm[a + ib * D.nb], mnorm[mb]) >= tpb)) continue;
-                live[j] |= 1u << s;
-                m += (unsigned long long)T.rows[s] * ext_r(jb, D.bs, D.n_occ) * ext_r(a, D.bs, D.n_bf);
-                ++cnt[s][j];
+    uint32_t n = 0, seen[kOzMaxSlots][2] = {};  // per (slot, sub-block): products in this lane
+    for (size_t base = 0; base < D.nb; base += 32) {
+        const size_t a = base + lane;
+        OzStep mine[2];
+        uint32_t cnt = 0;
+        if (a < D.nb) {
+            uint32_t live[2] = {0, 0};
+            uint32_t a_idx[kOzMaxSlots];
+            for (int s = 0; s < kOzMaxSlots; ++s) a_idx[s] = (uint32_t)(g * D.R + s + a * D.nob);
+            for (int j = 0; j < D.J; ++j) {
+                const size_t jb = jbp * D.J + j;
+                if (jb >= D.nob) continue;
+                const size_t mb = p * D.nb * D.nob + a + jb * D.nb;
+                if (!mflag[mb]) continue;
+                for (int s = 0; s < D.R; ++s) {
+                    if (!T.c[s]) continue;
+                    const size_t ib = g * D.R + s;
+                    if (!(__dmul_rn(cnorm[a + ib * D.nb], mnorm[mb]) >= tpb)) continue;
+                    live[j] |= 1u << s;
+                    m += (unsigned long long)T.rows[s] * ext_r(jb, D.bs, D.n_occ) * ext_r(a, D.bs, D.n_bf);
+                    ++seen[s][j];
+                }
             }
+            cnt = emit_rect_steps(live, D.J, phantom, (uint32_t)((p * D.nobp + jbp) * D.nb + a), a_idx, mine);
         }
-        n += emit_rect_steps(live, D.J, phantom, (uint32_t)((p * D.nobp + jbp) * D.nb + a), a_idx, steps + T.s0 + n);
+        warp_append_steps(mine, cnt, steps + T.s0, n);
     }
-    T.ns = n;
-    tiles[t] = T;
     unsigned long long tot = 0;
     for (int s = 0; s < D.R; ++s) {
         const size_t ib = g * D.R + s;
         if (ib >= D.nob) break;
         for (int j = 0; j < D.J; ++j) {
             const size_t jb = jbp * D.J + j;
+            const unsigned long long c = warp_sum_u64(seen[s][j]);  // lane 0 holds the tile's count
             if (jb >= D.nob) continue;
-            ijflag[p * D.nob * D.nob + ib + jb * D.nob] = cnt[s][j] > 0;
-            tot += cnt[s][j];
+            if (lane == 0) ijflag[p * D.nob * D.nob + ib + jb * D.nob] = c > 0;
+            tot += c;
         }
     }
-    if (tot) atomicAdd(nsig, tot);
-    if (m) atomicAdd(macs, m);
+    m = warp_sum_u64(m);
+    if (lane == 0) {
+        T.ns = n;
+        tiles[t] = T;
+        if (tot) atomicAdd(nsig, tot);
+        if (m) atomicAdd(macs, m);
+    }
 }
 
 // K tiles: t = (sub-range, jbp, group of R block rows a), N side J block
 // columns jb = J*jbp + j, steps over (p, ib) split into exact rectangles;
 // partial blocks of a tile: Kpart + ((sub*nobp + jbp)*nb + a) * bs * J*bs,
-// column-major with ld = the block's rows
+// column-major with ld = the block's rows.  One warp per tile, lanes over
+// the (p, ib) steps.
 __global__ void k_tiles_K(const uint8_t *__restrict__ mflag, const double *__restrict__ mnorm,
                           const uint8_t *__restrict__ sflag, const double *__restrict__ snorm,
                           const int *__restrict__ rexp_sub, const int *__restrict__ cexp_sub, double *__restrict__ Kpart,
                           OzDims D, size_t np, size_t Q, size_t n_tiles, double tpb, OzTile *__restrict__ tiles,
                           OzStep *__restrict__ steps, unsigned long long *__restrict__ nsig,
                           unsigned long long *__restrict__ macs) {
-    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t t = oz_warp_id();
     if (t >= n_tiles) return;
+    const int lane = threadIdx.x & 31;
     const size_t ng = (D.nb + D.R - 1) / D.R;
     const size_t g = t % ng, jbp = (t / ng) % D.nobp, sub = t / (ng * D.nobp);
-    unsigned long long m = 0;
+    unsigned long long m = 0, tot = 0;
     OzTile T;
     tile_clear(T);
     const size_t blk = D.bs * D.bs * D.J;
@@ -527,10 +519,13 @@ __global__ void k_tiles_K(const uint8_t *__restrict__ mflag, const double *__res
     T.cexp = cexp_sub + sub * D.n_occ + jbp * D.J * D.bs;
     T.s0 = (uint32_t)(t * Q * D.nob * D.J);
     uint32_t n = 0;
-    unsigned long long tot = 0;
-    const size_t p1 = min(np, (sub + 1) * Q);
-    for (size_t p = sub * Q; p < p1; ++p)
-        for (size_t ib = 0; ib < D.nob; ++ib) {
+    const size_t p0 = sub * Q, p1 = min(np, (sub + 1) * Q), n_k = (p1 - p0) * D.nob;
+    for (size_t base = 0; base < n_k; base += 32) {
+        const size_t idx = base + lane;
+        OzStep mine[2];
+        uint32_t cnt = 0;
+        if (idx < n_k) {
+            const size_t p = p0 + idx / D.nob, ib = idx % D.nob;
             uint32_t live[2] = {0, 0};
             uint32_t a_idx[kOzMaxSlots];
             for (int s = 0; s < kOzMaxSlots; ++s) a_idx[s] = (uint32_t)(p * D.nb * D.nob + g * D.R + s + ib * D.nb);
@@ -549,13 +544,18 @@ __global__ void k_tiles_K(const uint8_t *__restrict__ mflag, const double *__res
                     ++tot;
                 }
             }
-            n += emit_rect_steps(live, D.J, phantom, (uint32_t)((p * D.nobp + jbp) * D.nob + ib), a_idx,
-                                 steps + T.s0 + n);
+            cnt = emit_rect_steps(live, D.J, phantom, (uint32_t)((p * D.nobp + jbp) * D.nob + ib), a_idx, mine);
         }
-    T.ns = n;
-    tiles[t] = T;
-    if (tot) atomicAdd(nsig, tot);
-    if (m) atomicAdd(macs, m);
+        warp_append_steps(mine, cnt, steps + T.s0, n);
+    }
+    m = warp_sum_u64(m);
+    tot = warp_sum_u64(tot);
+    if (lane == 0) {
+        T.ns = n;
+        tiles[t] = T;
+        if (tot) atomicAdd(nsig, tot);
+        if (m) atomicAdd(macs, m);
+    }
 }
 
 // K(a, jb) += sum over sub-ranges (in order) of the tiles' partial blocks
@@ -672,15 +672,40 @@ __global__ void k_Kmn_mirror(double *__restrict__ K, size_t n_bf, size_t bs) {
     if (bi < bj || (bi == bj && gi < gj)) K[e] = K[gj + gi * n_bf];
 }
 
-// FP64 block norms of mui (warp per present block)
-__global__ void k_mui_norms(const double *__restrict__ mui, const uint8_t *__restrict__ mflag, size_t n_bf,
-                            size_t n_occ, size_t bs, size_t nb, size_t nob, size_t n, double *__restrict__ mnorm) {
-    const size_t x = (size_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+// One pass over each present mui_p block (warp per block): its FP64 norm
+// (the deterministic block-norm order), its row maxima per aux sub-range p/Q
+// (rows of the A operand of K and K_mn) and, when col_bits is given, its
+// column maxima per p (columns of the B operand of ij).  The block is read
+// from DRAM once; the second and third walks hit L1.
+__global__ void k_mui_stats(const double *__restrict__ mui, const uint8_t *__restrict__ mflag, size_t n_bf,
+                            size_t n_occ, size_t bs, size_t nb, size_t nob, size_t Q, size_t n,
+                            double *__restrict__ mnorm, unsigned long long *__restrict__ row_bits,
+                            unsigned long long *__restrict__ col_bits) {
+    const size_t x = oz_warp_id();
     if (x >= n || !mflag[x]) return;
-    const size_t p = x / (nb * nob), a = x % nb, j = (x / nb) % nob;
-    const double est = warp_block_norm(mui + p * n_bf * n_occ + a * bs + j * bs * n_bf, ext_r(a, bs, n_bf),
-                                       ext_r(j, bs, n_occ), n_bf);
-    if ((threadIdx.x & 31) == 0) mnorm[x] = est;
+    const size_t p = x / (nb * nob), a = x % nb, jb = (x / nb) % nob;
+    const int rows = ext_r(a, bs, n_bf), cols = ext_r(jb, bs, n_occ);
+    const double *M = mui + p * n_bf * n_occ + a * bs + jb * bs * n_bf;
+    const double est = warp_block_norm(M, rows, cols, n_bf);
+    const int lane = threadIdx.x & 31;
+    if (lane == 0) mnorm[x] = est;
+    for (int r = lane; r < rows; r += 32) {
+        long long mx = 0;
+        for (int l = 0; l < cols; ++l) {
+            const long long bb_ = oz_absbits(M[r + (size_t)l * n_bf]);
+            mx = bb_ > mx ? bb_ : mx;
+        }
+        if (mx) atomicMax(&row_bits[(p / Q) * n_bf + a * bs + r], (unsigned long long)mx);
+    }
+    if (!col_bits) return;
+    for (int c = lane; c < cols; c += 32) {
+        long long mx = 0;
+        for (int r = 0; r < rows; ++r) {
+            const long long bb_ = oz_absbits(M[r + (size_t)c * n_bf]);
+            mx = bb_ > mx ? bb_ : mx;
+        }
+        if (mx) atomicMax(&col_bits[p * n_occ + jb * bs + c], (unsigned long long)mx);
+    }
 }
 
 void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uint64_t stats[6]) {
@@ -794,9 +819,7 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
         if (n_ob) {
             k_unorms_c<<<oz_img_grid(np * n_ob), 32 * kOzImgWarps, 0, s>>>(
                 d.ints, dinv.as<int>(), dob.as<uint32_t>(), n_ob, d.n_vec2, P0, n_bf, bs, nb, np, tpb_u,
-                dun.as<double>(), duf.as<uint8_t>(), ducomp.as<double>());
-            k_rowmax_U_c<<<oz_img_grid(np * n_ob), 32 * kOzImgWarps, 0, s>>>(
-                ducomp.as<double>(), dob.as<uint32_t>(), n_ob, np, duf.as<uint8_t>(), n_bf, bs, nb, bitsU);
+                dun.as<double>(), duf.as<uint8_t>(), ducomp.as<double>(), bitsU);
         }
         k_bits_exp<<<(unsigned)ceil_div(np * n_bf, (size_t)256), 256, 0, s>>>(bitsU, np * n_bf, drexpU.as<int>());
         if (n_ob)
@@ -807,20 +830,20 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
         k_tiles_mui<<<(unsigned)ceil_div(tm, 128), 128, 0, s>>>(
             duf.as<uint8_t>(), dun.as<double>(), dcn.as<double>(), drexpU.as<int>(), dcexpC.as<int>(),
             dmui.as<double>(), D, tm, tpb, dtm.as<OzTile>(), dsm.as<OzStep>(), dmf.as<uint8_t>(), cnt + 0, macs + 0);
-        ctx->note_launch(5);
+        ctx->note_launch(4);
         ctx->check_launch("rik ozaki mui prep");
         oz_run(ctx, sh, dtm.as<OzTile>(), tm, dsm.as<OzStep>(), dimgCtA.as<bf16>(), dimgU.as<bf16>(), 1.0, s,
                macs + 0);
-        k_mui_norms<<<(unsigned)ceil_div(np * nb * nob, wpb), wpb * 32, 0, s>>>(
-            dmui.as<double>(), dmf.as<uint8_t>(), n_bf, n_occ, bs, nb, nob, np * nb * nob, dmn.as<double>());
-        // mui row exponents per sub-range (A operand of K and of K_mn)
-        k_rowmax_mui_sub<<<oz_img_grid(np * nb * nob), 32 * kOzImgWarps, 0, s>>>(
-            dmui.as<double>(), dmf.as<uint8_t>(), n_bf, n_occ, bs, nb, nob, Q, np * nb * nob, bitsMs);
+        // mui norms, row exponents per sub-range (A operand of K and of K_mn)
+        // and column exponents per aux function (B operand of ij)
+        k_mui_stats<<<oz_img_grid(np * nb * nob), 32 * kOzImgWarps, 0, s>>>(
+            dmui.as<double>(), dmf.as<uint8_t>(), n_bf, n_occ, bs, nb, nob, Q, np * nb * nob, dmn.as<double>(), bitsMs,
+            want_k ? bitsM : nullptr);
         k_bits_exp<<<(unsigned)ceil_div(n_sub * n_bf, (size_t)256), 256, 0, s>>>(bitsMs, n_sub * n_bf,
                                                                                  drexpMs.as<int>());
         k_img_mui_A<<<oz_img_grid(np * nb * nob), 32 * kOzImgWarps, 0, s>>>(
             dmui.as<double>(), dmf.as<uint8_t>(), drexpMs.as<int>(), Q, D, np * nb * nob, dimgMA.as<bf16>());
-        ctx->note_launch(4);
+        ctx->note_launch(3);
         if (want_kmn) {
             // K_mn += mui mui^T
             k_img_mui_T<<<oz_img_grid(np * nb * nob), 32 * kOzImgWarps, 0, s>>>(
@@ -839,16 +862,14 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
         }
         if (!want_k) continue;
         // ij = C^T mui
-        k_colmax_mui<<<oz_img_grid(np * nb * nob), 32 * kOzImgWarps, 0, s>>>(
-            dmui.as<double>(), dmf.as<uint8_t>(), n_bf, n_occ, bs, nb, nob, np * nb * nob, bitsM);
         k_bits_exp<<<(unsigned)ceil_div(np * n_occ, (size_t)256), 256, 0, s>>>(bitsM, np * n_occ, dcexpM.as<int>());
         k_img_mui_B<<<oz_img_grid(np * nb * nobp * J), 32 * kOzImgWarps, 0, s>>>(
             dmui.as<double>(), dmf.as<uint8_t>(), dcexpM.as<int>(), D, np * nb * nobp * J, dimgMB.as<bf16>());
         const size_t ti = np * nobp * ng_i;
-        k_tiles_ij<<<(unsigned)ceil_div(ti, 128), 128, 0, s>>>(
+        k_tiles_ij<<<oz_img_grid(ti), 32 * kOzImgWarps, 0, s>>>(
             dmf.as<uint8_t>(), dmn.as<double>(), dcn.as<double>(), dcexpC.as<int>(), dcexpM.as<int>(),
             dij.as<double>(), D, ti, tpb, dti.as<OzTile>(), dsi.as<OzStep>(), dijf.as<uint8_t>(), cnt + 1, macs + 1);
-        ctx->note_launch(4);
+        ctx->note_launch(3);
         ctx->check_launch("rik ozaki ij prep");
         oz_run(ctx, shJ, dti.as<OzTile>(), ti, dsi.as<OzStep>(), dimgCtA.as<bf16>(), dimgMB.as<bf16>(), 1.0, s,
                macs + 1);
@@ -863,7 +884,7 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
         k_img_ijs_B<<<oz_img_grid(np * nob * nobp * J), 32 * kOzImgWarps, 0, s>>>(
             dijs.as<double>(), dsf.as<uint8_t>(), dcexpSs.as<int>(), Q, D, np * nob * nobp * J, dimgSB.as<bf16>());
         const size_t tk = n_sub * nobp * ng_a;
-        k_tiles_K<<<(unsigned)ceil_div(tk, 128), 128, 0, s>>>(
+        k_tiles_K<<<oz_img_grid(tk), 32 * kOzImgWarps, 0, s>>>(
             dmf.as<uint8_t>(), dmn.as<double>(), dsf.as<uint8_t>(), dsn.as<double>(), drexpMs.as<int>(),
             dcexpSs.as<int>(), dKp.as<double>(), D, np, Q, tk, tpb, dtk.as<OzTile>(), dsk.as<OzStep>(), cnt + 2,
             macs + 2);
