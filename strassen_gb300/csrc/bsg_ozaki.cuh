@@ -216,21 +216,19 @@ __device__ __forceinline__ void oz_block_image_g(const Get &get, int rows, int k
             continue;
         }
         const int e = exps[r];
-        uint32_t w[kOzMaxDigits][4];
+        double v[8];  // the eight loads first, then the splits
 #pragma unroll
-        for (int i = 0; i < kOzMaxDigits; ++i) w[i][0] = w[i][1] = w[i][2] = w[i][3] = 0u;
+        for (int j = 0; j < 8; ++j) v[j] = h * 8 + j < k ? get(r, h * 8 + j) : 0.0;
+        OzDigits D[8] = {OzDigits(v[0], e, nd), OzDigits(v[1], e, nd), OzDigits(v[2], e, nd), OzDigits(v[3], e, nd),
+                         OzDigits(v[4], e, nd), OzDigits(v[5], e, nd), OzDigits(v[6], e, nd), OzDigits(v[7], e, nd)};
+        // one digit plane at a time: four packed words live, not nd x 4
+        for (int i = 0; i < nd; ++i) {
+            uint32_t w[4];
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            const int l = h * 8 + j;
-            const OzDigits D(l < k ? get(r, l) : 0.0, e, nd);
-#pragma unroll
-            for (int i = 0; i < kOzMaxDigits; ++i)
-                if (i < nd) w[i][j >> 1] |= oz_digit_bf16(D.digit(i), i) << (16 * (j & 1));
+            for (int q = 0; q < 4; ++q)
+                w[q] = oz_digit_bf16(D[2 * q].digit(i), i) | (oz_digit_bf16(D[2 * q + 1].digit(i), i) << 16);
+            *reinterpret_cast<uint4 *>(dst + i * plane + off) = make_uint4(w[0], w[1], w[2], w[3]);
         }
-#pragma unroll
-        for (int i = 0; i < kOzMaxDigits; ++i)
-            if (i < nd)
-                *reinterpret_cast<uint4 *>(dst + i * plane + off) = make_uint4(w[i][0], w[i][1], w[i][2], w[i][3]);
     }
 }
 
