@@ -10,9 +10,10 @@
  *
  * Arithmetic: the FP64 form performs, for every output element, the same
  * sequence of IEEE-754 operations as the reference linked against the
- * deterministic BLAS definition documented in the design doc (fma chains over k in
- * order, per-block accumulation C = alpha*t + C, 32-lane norm tree), so its
- * results, block masks and cached norms are bit-identical to that reference.
+ * deterministic BLAS definition (dgemm: for every element an fma chain over k
+ * in order from zero, then C = alpha*t + beta*C; nrm2: 32 lane-strided fma
+ * chains combined by a shuffle tree), so its results, block masks and cached
+ * norms are bit-identical to that reference.
  *
  * Threading: a bsg_ctx owns one CUDA stream; calls on one context are
  * ordered on that stream.  Host threads may call concurrently only on
