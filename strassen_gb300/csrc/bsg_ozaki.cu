@@ -114,6 +114,39 @@ enum OzProf {
 
 constexpr int kOzThreads = 320;  // producer, MMA issuer, 8 epilogue warps
 
+// Conversions for the epilogue with integer operations instead of the FP64
+// pipe (GB300 runs FP64 at a small fraction of its integer rate).
+// x exactly as a double, for |x| < 2^53
+__device__ __forceinline__ double oz_i64_to_f64(long long x) {
+    if (x == 0) return 0.0;
+    const unsigned long long sgn = x < 0 ? (1ull << 63) : 0ull;
+    const unsigned long long a = x < 0 ? 0ull - (unsigned long long)x : (unsigned long long)x;
+    const int msb = 63 - __clzll((long long)a);
+    const unsigned long long m = (a << (52 - msb)) & 0xFFFFFFFFFFFFFull;
+    return __longlong_as_double((long long)(sgn | ((unsigned long long)(msb + 1023) << 52) | m));
+}
+// an FP32 value as a double (exact; zero and subnormal inputs take the
+// hardware conversion)
+__device__ __forceinline__ double oz_f32_to_f64(float f) {
+    const uint32_t u = __float_as_uint(f);
+    const uint32_t ex = (u >> 23) & 0xFFu;
+    if (ex == 0u || ex == 0xFFu) return (double)f;
+    return __longlong_as_double((long long)(((unsigned long long)(u >> 31) << 63) |
+                                            ((unsigned long long)(ex - 127u + 1023u) << 52) |
+                                            ((unsigned long long)(u & 0x7FFFFFu) << 29)));
+}
+// v 2^e: the exponent field moves when the result stays a normal number;
+// otherwise (and for zero) an ordinary multiplication by the power of two
+__device__ __forceinline__ double oz_scale_pow2(double v, int e) {
+    const long long b = __double_as_longlong(v);
+    const int ev = (int)((b >> 52) & 0x7FF);
+    const int en = ev + e;
+    if (ev != 0 && ev != 0x7FF && en > 0 && en < 0x7FF)
+        return __longlong_as_double(b + ((long long)e << 52));
+    const double sc = (e >= -1022 && e <= 1023) ? __longlong_as_double((long long)(e + 1023) << 52) : ldexp(1.0, e);
+    return __dmul_rn(v, sc);
+}
+
 // Tile sequence of a CTA: chunks of `chunk` consecutive tiles, chunk
 // blockIdx.x, then every gridDim.x-th chunk (tiles of one chunk share operand
 // images, which then stay hot in L2 between them).  Every role walks the same
@@ -451,17 +484,28 @@ __global__ void __launch_bounds__(kOzThreads, 1)
                 const int ldc = T.ldc[s];
                 const bool fresh = (T.fresh_mask >> s) & 1u;
                 const bool unit = P.alpha == 1.0;
+                // sub-blocks stored apart (J <= 2, so a group's NP/2 columns cross at
+                // most one sub-block boundary)
+                const bool subm = T.sub_cols != 0;
+                const int npj = NP / P.J, js0 = cbase / npj;
 #pragma unroll
                 for (int j = 0; j < NPH; ++j) {
                     const int c = cbase + j;
-                    if (c < T.cols) {
-                        const double tot = __dadd_rn((double)hi[j], (double)(lo[j] * 65536.f));
-                        const int e = er + T.cexp[c];
-                        const double sc = (e >= -1022 && e <= 1023) ? __longlong_as_double((long long)(e + 1023) << 52)
-                                                                    : ldexp(1.0, e);
-                        double out = __dmul_rn(tot, sc);
+                    int cc = c, js = 0;
+                    if (subm) {
+                        js = c >= (js0 + 1) * npj ? js0 + 1 : js0;
+                        cc = c - js * npj;
+                    }
+                    if (c < T.cols && (!subm || cc < T.sub_cols)) {
+                        // both terms are exact doubles built with integer operations
+                        // (|hi| < 2^53, lo 2^16 an FP32 value): one FP64 add rounds,
+                        // and the power of two goes into the exponent field
+                        const double tot = __dadd_rn(oz_i64_to_f64(hi[j]), oz_f32_to_f64(lo[j] * 65536.f));
+                        const int e = er + T.cexp[subm ? js * T.cexp_sub + cc : c];
+                        double out = oz_scale_pow2(tot, e);
                         if (!unit) out = __dmul_rn(P.alpha, out);
-                        double *dst = T.trans ? cp + c + (size_t)r * ldc : cp + r + (size_t)c * ldc;
+                        double *base = subm ? cp + js * T.sub_stride : cp;
+                        double *dst = T.trans ? base + cc + (size_t)r * ldc : base + r + (size_t)cc * ldc;
                         *dst = fresh ? out : __dadd_rn(*dst, out);
                     }
                 }

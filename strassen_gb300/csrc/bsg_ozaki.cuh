@@ -58,6 +58,13 @@ struct OzTile {
     int trans;                     // 1: slot rows are output columns, tile columns output rows
     uint32_t fresh_mask;           // slot s overwrites C (bit set) or adds to it
     uint32_t s0, ns;               // step range
+    // N-side sub-blocks stored apart (0: the tile's columns are contiguous):
+    // with J = 2 sub-blocks of NP/2 columns, sub-block js holds sub_cols
+    // valid columns at output offset js * sub_stride (elements) with column
+    // exponents at cexp + js * cexp_sub
+    int sub_cols = 0;
+    long long sub_stride = 0;
+    int cexp_sub = 0;
 };
 
 struct OzStep {

@@ -167,6 +167,9 @@ struct OzDims {
     // (stacked along N in one image of npJ rows per digit plane), nobp groups
     int J, npJ;
     size_t nobp;
+    // N side of mui^T = C^T U^T: U blocks of Jm consecutive aux functions per
+    // image (npm rows per digit plane)
+    int Jm, npm;
 };
 
 // N-side image rows of occupied block column jb = J*jbp + j inside its
@@ -177,18 +180,21 @@ __device__ __forceinline__ int rows_in_group(const OzDims &D) { return D.J == 1 
 
 // U_p blocks (a, b) as the N side of mui^T = C^T U^T (image rows = the
 // block's rows mu, k = its columns), from the dense copies; one warp per
-// occupied block w, image index p*nb*nb + a + b*nb
+// occupied block w.  The blocks of Jm consecutive aux functions p = Jm*pp + j
+// share one image (index pp*nb*nb + a + b*nb), aux function j at rows j*bs.
 __global__ void k_img_U(const double *__restrict__ ucomp, const uint32_t *__restrict__ ob_list, size_t n_ob,
                         size_t n_p, const uint8_t *__restrict__ uflag, const int *__restrict__ rexp, OzDims D,
                         bf16 *__restrict__ img) {
     const size_t w = oz_warp_id();
     if (w >= n_p * n_ob) return;
     const size_t p = w / n_ob, rr = ob_list[w % n_ob], a = rr % D.nb, b = rr / D.nb;
-    const size_t x = p * D.nb * D.nb + rr;
-    if (!uflag[x]) return;
+    if (!uflag[p * D.nb * D.nb + rr]) return;
+    const size_t pp = p / D.Jm, j = p % D.Jm;
     const int rows = ext_r(a, D.bs, D.n_bf);
-    oz_block_image(ucomp + w * D.bs * D.bs, (size_t)rows, false, rows, ext_r(b, D.bs, D.n_bf),
-                   rexp + p * D.n_bf + a * D.bs, D.np, D.kp, D.nd, img + x * D.nd * (size_t)D.np * D.kp, false);
+    bf16 *dst = img + (pp * D.nb * D.nb + rr) * D.nd * (size_t)D.npm * D.kp + j * D.bs * (size_t)D.kp;
+    oz_block_image_g(OzDenseGet{ucomp + w * D.bs * D.bs, (size_t)rows, false}, rows, ext_r(b, D.bs, D.n_bf),
+                     rexp + p * D.n_bf + a * D.bs, D.Jm == 1 ? D.npm : (int)D.bs, D.kp, D.nd, dst, false,
+                     threadIdx.x & 31, 32, D.npm);
 }
 
 // C^T blocks (ib, a) in the A role of ij = C^T mui and of mui^T = C^T U^T; index ib + a*nob
@@ -334,53 +340,64 @@ __device__ __forceinline__ void tile_clear(OzTile &T) {
 
 // mui tiles, transposed: mui_p^T(j, a) = sum_b C^T(j, b) U_p(a, b)^T, so the
 // dense C^T blocks fill the slots (R occupied block columns j) and the
-// block-sparse U_p supplies one N-side block per step (every present
-// U_p(a, b)); t = (p, a, group g of R block columns j), written transposed
+// block-sparse U_p supplies the N side: per step the present U blocks (a, b)
+// of Jm consecutive aux functions p = Jm*pp + j (their C^T operand is the
+// same).  t = (pp, a, group g of R block columns j), written transposed; the
+// aux functions' outputs are n_bf*n_occ apart (sub-blocks stored apart).
 __global__ void k_tiles_mui(const uint8_t *__restrict__ uflag, const double *__restrict__ unorm,
                             const double *__restrict__ cnorm, const int *__restrict__ rexp_U,
-                            const int *__restrict__ cexp_C, double *__restrict__ mui, OzDims D, size_t n_tiles,
-                            double tpb, OzTile *__restrict__ tiles, OzStep *__restrict__ steps,
+                            const int *__restrict__ cexp_C, double *__restrict__ mui, OzDims D, size_t np,
+                            size_t n_tiles, double tpb, OzTile *__restrict__ tiles, OzStep *__restrict__ steps,
                             uint8_t *__restrict__ mflag, unsigned long long *__restrict__ nsig,
                             unsigned long long *__restrict__ macs) {
     const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n_tiles) return;
     const size_t ng = (D.nob + D.R - 1) / D.R;
-    const size_t g = t % ng, a = (t / ng) % D.nb, p = t / (ng * D.nb);
+    const size_t g = t % ng, a = (t / ng) % D.nb, pp = t / (ng * D.nb), p0 = pp * D.Jm;
+    const int nsub = (int)min((size_t)D.Jm, np - p0);
     unsigned long long m = 0;
     OzTile T;
     tile_clear(T);
-    int cnt[kOzMaxSlots] = {0};
+    int cnt[kOzMaxSlots][2] = {};
     for (int s = 0; s < D.R; ++s) {
         const size_t j = g * D.R + s;
         if (j >= D.nob) break;
-        T.c[s] = mui + p * D.n_bf * D.n_occ + a * D.bs + j * D.bs * D.n_bf;
+        T.c[s] = mui + p0 * D.n_bf * D.n_occ + a * D.bs + j * D.bs * D.n_bf;
         T.ldc[s] = (int)D.n_bf;
         T.rows[s] = ext_r(j, D.bs, D.n_occ);  // slot rows are mui columns
         T.rexp[s] = cexp_C + j * D.bs;
     }
-    T.cols = ext_r(a, D.bs, D.n_bf);  // tile columns are mui rows
+    const int npj = D.npm / D.Jm;
     T.trans = 1;
-    T.cexp = rexp_U + p * D.n_bf + a * D.bs;
-    T.s0 = (uint32_t)(t * D.nb);
+    T.cexp = rexp_U + p0 * D.n_bf + a * D.bs;
+    if (D.Jm == 1) {
+        T.cols = ext_r(a, D.bs, D.n_bf);  // tile columns are mui rows
+    } else {
+        T.cols = nsub * npj;  // no columns of an aux function past the chunk
+        T.sub_cols = ext_r(a, D.bs, D.n_bf);
+        T.sub_stride = (long long)(D.n_bf * D.n_occ);
+        T.cexp_sub = (int)D.n_bf;
+    }
+    T.s0 = (uint32_t)(t * D.nb * D.Jm);
     uint32_t n = 0;
     for (size_t b = 0; b < D.nb; ++b) {
-        const size_t ub = p * D.nb * D.nb + a + b * D.nb;
-        if (!uflag[ub]) continue;
-        OzStep st;
-        st.bmask = kOzAllSub;
-        st.b = (uint32_t)ub;
-        bool any = false;
-        for (int s = 0; s < kOzMaxSlots; ++s) {
-            st.a[s] = kOzNone;
-            if (s >= D.R || !T.c[s]) continue;
-            const size_t j = g * D.R + s;
-            if (!(__dmul_rn(unorm[ub], cnorm[b + j * D.nb]) >= tpb)) continue;
-            st.a[s] = (uint32_t)(j + b * D.nob);
-            m += (unsigned long long)T.rows[s] * T.cols * ext_r(b, D.bs, D.n_bf);
-            ++cnt[s];
-            any = true;
+        uint32_t live[2] = {0, 0};
+        uint32_t a_idx[kOzMaxSlots];
+        for (int s = 0; s < kOzMaxSlots; ++s) a_idx[s] = (uint32_t)(g * D.R + s + b * D.nob);
+        for (int js = 0; js < nsub; ++js) {
+            const size_t ub = (p0 + js) * D.nb * D.nb + a + b * D.nb;
+            if (!uflag[ub]) continue;
+            for (int s = 0; s < D.R; ++s) {
+                if (!T.c[s]) continue;
+                const size_t j = g * D.R + s;
+                if (!(__dmul_rn(unorm[ub], cnorm[b + j * D.nb]) >= tpb)) continue;
+                live[js] |= 1u << s;
+                m += (unsigned long long)T.rows[s] * ext_r(a, D.bs, D.n_bf) * ext_r(b, D.bs, D.n_bf);
+                ++cnt[s][js];
+            }
         }
-        if (any) steps[T.s0 + n++] = st;
+        // a missing aux function (odd chunk end) counts as absent: its image rows are never written
+        n += emit_rect_steps(live, D.Jm, 0u, (uint32_t)(pp * D.nb * D.nb + a + b * D.nb), a_idx, steps + T.s0 + n);
     }
     T.ns = n;
     tiles[t] = T;
@@ -388,8 +405,10 @@ __global__ void k_tiles_mui(const uint8_t *__restrict__ uflag, const double *__r
     for (int s = 0; s < D.R; ++s) {
         const size_t j = g * D.R + s;
         if (j >= D.nob) break;
-        mflag[p * D.nb * D.nob + a + j * D.nb] = cnt[s] > 0;
-        tot += cnt[s];
+        for (int js = 0; js < nsub; ++js) {
+            mflag[(p0 + js) * D.nb * D.nob + a + j * D.nb] = cnt[s][js] > 0;
+            tot += cnt[s][js];
+        }
     }
     if (tot) atomicAdd(nsig, tot);
     if (m) atomicAdd(macs, m);
@@ -736,6 +755,17 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
     }
     shJ.J = J;
     D.J = J;
+    // mui^T = C^T U^T: the U blocks of two aux functions per tile on the N side
+    int Jm = (bs % 8 == 0 && 2 * bs <= 64 && nd * 2 * (int)bs + 8 <= 256) ? 2 : 1;
+    OzShape shM = oz_shape((int)bs, (int)bs, (int)bs * Jm, nd);
+    if (shM.kp != sh.kp || shM.pair != sh.pair) {
+        Jm = 1;
+        shM = sh;
+    }
+    shM.J = Jm;
+    D.Jm = Jm;
+    D.npm = shM.np;
+    const size_t b_imgM = (size_t)nd * shM.np * shM.kp;  // elements per U image (Jm aux functions)
     D.npJ = shJ.np;
     D.nobp = ceil_div(D.nob, (size_t)J);
     const size_t nb = D.nb, nob = D.nob, nobp = D.nobp;
@@ -756,7 +786,7 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
     DevBuf dij(pc * n_occ * n_occ * 8, s), dijf(pc * nob * nob, s);
     DevBuf dijs(pc * n_occ * n_occ * 8, s), dsn(pc * nob * nob * 8, s), dsf(pc * nob * nob, s);
     DevBuf dcn(nb * nob * 8, s), dcexpC(nob * bs * 4, s), dimgCtA(nob * nb * a_img * 2, s);
-    DevBuf drexpU(pc * n_bf * 4, s), dimgU(pc * nb * nb * b_img * 2, s);
+    DevBuf drexpU(pc * n_bf * 4, s), dimgU(ceil_div(pc, (size_t)Jm) * nb * nb * b_imgM * 2, s);
     DevBuf dcexpM(pc * n_occ * 4, s), dimgMB(pc * nb * nobp * b_imgJ * 2, s);
     DevBuf drexpMs(n_sub_max * n_bf * 4, s), dcexpSs(n_sub_max * n_occ * 4, s);
     // maxima bit patterns for the four exponent sets of a chunk
@@ -767,8 +797,8 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
     DevBuf dimgMA(pc * nb * nob * a_img * 2, s), dimgSB(pc * nob * nobp * b_imgJ * 2, s);
     DevBuf dKp(want_k ? n_sub_max * nobp * nb * bs * bs * J * 8 : 0, s), dcnt(6 * 8, s), dmacs(4 * 8, s);
     const size_t ng_a = ceil_div(nb, (size_t)D.R), ng_i = ceil_div(nob, (size_t)D.R);
-    const size_t tiles_mui = pc * nb * ng_i, tiles_ij = pc * nobp * ng_i, tiles_K = n_sub_max * nobp * ng_a;
-    DevBuf dtm(tiles_mui * sizeof(OzTile), s), dsm(tiles_mui * nb * sizeof(OzStep), s);
+    const size_t tiles_mui = ceil_div(pc, (size_t)Jm) * nb * ng_i, tiles_ij = pc * nobp * ng_i, tiles_K = n_sub_max * nobp * ng_a;
+    DevBuf dtm(tiles_mui * sizeof(OzTile), s), dsm(tiles_mui * nb * Jm * sizeof(OzStep), s);
     DevBuf dti(tiles_ij * sizeof(OzTile), s), dsi(tiles_ij * nb * J * sizeof(OzStep), s);
     DevBuf dtk(tiles_K * sizeof(OzTile), s), dsk(tiles_K * Q * nob * J * sizeof(OzStep), s);
     // K_mn: images of mui in the B role, tiles over (sub-range, lower pair), partials
@@ -826,13 +856,14 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
             k_img_U<<<oz_img_grid(np * n_ob), 32 * kOzImgWarps, 0, s>>>(ducomp.as<double>(), dob.as<uint32_t>(), n_ob,
                                                                        np, duf.as<uint8_t>(), drexpU.as<int>(), D,
                                                                        dimgU.as<bf16>());
-        const size_t tm = np * nb * ng_i;
+        const size_t tm = ceil_div(np, (size_t)Jm) * nb * ng_i;
         k_tiles_mui<<<(unsigned)ceil_div(tm, 128), 128, 0, s>>>(
             duf.as<uint8_t>(), dun.as<double>(), dcn.as<double>(), drexpU.as<int>(), dcexpC.as<int>(),
-            dmui.as<double>(), D, tm, tpb, dtm.as<OzTile>(), dsm.as<OzStep>(), dmf.as<uint8_t>(), cnt + 0, macs + 0);
+            dmui.as<double>(), D, np, tm, tpb, dtm.as<OzTile>(), dsm.as<OzStep>(), dmf.as<uint8_t>(), cnt + 0,
+            macs + 0);
         ctx->note_launch(4);
         ctx->check_launch("rik ozaki mui prep");
-        oz_run(ctx, sh, dtm.as<OzTile>(), tm, dsm.as<OzStep>(), dimgCtA.as<bf16>(), dimgU.as<bf16>(), 1.0, s,
+        oz_run(ctx, shM, dtm.as<OzTile>(), tm, dsm.as<OzStep>(), dimgCtA.as<bf16>(), dimgU.as<bf16>(), 1.0, s,
                macs + 0);
         // mui norms, row exponents per sub-range (A operand of K and of K_mn)
         // and column exponents per aux function (B operand of ij)

@@ -106,17 +106,19 @@ def test_ozaki_rik_synthetic(api, ctx, nd):
     assert err < 1e-9
 
 
-@pytest.mark.parametrize("n_occ", [24, 60, 77])
-def test_ozaki_rik_column_pairs(api, ctx, n_occ):
-    """occupied block columns paired on the N side of the ij and K products:
-    an odd number of column blocks (the last pair half empty), ragged last
-    blocks, and a single block; masks and K as in the FP64 form"""
-    s = S.RikSystem(seed=12, n_atoms=6, nbf=24, naux=10, n_occ=n_occ, box=6.5)
+@pytest.mark.parametrize("n_occ,nbf,p_chunk", [(24, 24, 16), (60, 24, 16), (77, 24, 16), (50, 22, 7)])
+def test_ozaki_rik_column_pairs(api, ctx, n_occ, nbf, p_chunk):
+    """occupied block columns paired on the N side of the ij and K products
+    and aux functions paired on the N side of mui: an odd number of column
+    blocks (the last pair half empty), ragged last blocks, a single block,
+    ragged basis blocks and odd chunks of aux functions (the last pair a
+    single one); masks and K as in the FP64 form"""
+    s = S.RikSystem(seed=12, n_atoms=6, nbf=nbf, naux=10, n_occ=n_occ, box=6.5)
     B = api.transform_3c2c(s.ints_3c(), s.v_m12(), 24, 1e-10, ctx=ctx)
     C = s.c_occ()
     K64, st64 = api.rik_occ_step(B, s.keys, C, s.n_bf, s.n_aux, s.n_occ, 24, 1e-10, ctx=ctx, stats=True)
     Koz, stoz = api.rik_occ_step(B, s.keys, C, s.n_bf, s.n_aux, s.n_occ, 24, 1e-10, form=api.FORM_OZAKI,
-                                 n_digits=5, p_chunk=16, ctx=ctx, stats=True)
+                                 n_digits=5, p_chunk=p_chunk, ctx=ctx, stats=True)
     err = np.linalg.norm(Koz - K64) / np.linalg.norm(K64)
     print("column pairs", n_occ, err, st64[:3], stoz[:3])
     assert st64[:3] == stoz[:3]
