@@ -488,25 +488,38 @@ __global__ void __launch_bounds__(kOzThreads, 1)
                 // most one sub-block boundary)
                 const bool subm = T.sub_cols != 0;
                 const int npj = NP / P.J, js0 = cbase / npj;
-#pragma unroll
-                for (int j = 0; j < NPH; ++j) {
+                // column j of this group: output address (null = not stored) and value
+                auto col_out = [&](int j, double *&dst) -> double {
                     const int c = cbase + j;
                     int cc = c, js = 0;
                     if (subm) {
                         js = c >= (js0 + 1) * npj ? js0 + 1 : js0;
                         cc = c - js * npj;
                     }
-                    if (c < T.cols && (!subm || cc < T.sub_cols)) {
-                        // both terms are exact doubles built with integer operations
-                        // (|hi| < 2^53, lo 2^16 an FP32 value): one FP64 add rounds,
-                        // and the power of two goes into the exponent field
-                        const double tot = __dadd_rn(oz_i64_to_f64(hi[j]), oz_f32_to_f64(lo[j] * 65536.f));
-                        const int e = er + T.cexp[subm ? js * T.cexp_sub + cc : c];
-                        double out = oz_scale_pow2(tot, e);
-                        if (!unit) out = __dmul_rn(P.alpha, out);
-                        double *base = subm ? cp + js * T.sub_stride : cp;
-                        double *dst = T.trans ? base + cc + (size_t)r * ldc : base + r + (size_t)cc * ldc;
-                        *dst = fresh ? out : __dadd_rn(*dst, out);
+                    dst = nullptr;
+                    if (!(c < T.cols && (!subm || cc < T.sub_cols))) return 0.0;
+                    // both terms are exact doubles built with integer operations
+                    // (|hi| < 2^53, lo 2^16 an FP32 value): one FP64 add rounds,
+                    // and the power of two goes into the exponent field
+                    const double tot = __dadd_rn(oz_i64_to_f64(hi[j]), oz_f32_to_f64(lo[j] * 65536.f));
+                    const int e = er + T.cexp[subm ? js * T.cexp_sub + cc : c];
+                    double out = oz_scale_pow2(tot, e);
+                    if (!unit) out = __dmul_rn(P.alpha, out);
+                    double *base = subm ? cp + js * T.sub_stride : cp;
+                    dst = T.trans ? base + cc + (size_t)r * ldc : base + r + (size_t)cc * ldc;
+                    return out;
+                };
+#pragma unroll
+                for (int j = 0; j < NPH; j += 2) {
+                    double *d0, *d1;
+                    const double o0 = col_out(j, d0), o1 = col_out(j + 1, d1);
+                    // a transposed tile's row is contiguous in the output: pairs of
+                    // columns go as one 16-byte store when adjacent and aligned
+                    if (fresh && d0 && d1 == d0 + 1 && ((reinterpret_cast<uintptr_t>(d0) & 15u) == 0u)) {
+                        *reinterpret_cast<double2 *>(d0) = make_double2(o0, o1);
+                    } else {
+                        if (d0) *d0 = fresh ? o0 : __dadd_rn(*d0, o0);
+                        if (d1) *d1 = fresh ? o1 : __dadd_rn(*d1, o1);
                     }
                 }
                 if (fresh && r == 0 && grp == 0 && T.cnorm[s]) *T.cnorm[s] = 0.0;
