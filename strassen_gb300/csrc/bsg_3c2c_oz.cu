@@ -30,16 +30,25 @@ __global__ void k_dense_norms(const double *__restrict__ M, size_t ld, size_t nr
     if ((threadIdx.x & 31) == 0) norm[b] = est;
 }
 
-// exponent of every row of X (over all columns); one thread per row
-__global__ void k_rowexp_dense(const double *__restrict__ X, size_t ld, size_t nr, size_t nc, int *__restrict__ rexp) {
-    const size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= nr) return;
-    long long mx = 0;
-    for (size_t c = 0; c < nc; ++c) {
-        const long long b = oz_absbits(X[r + c * ld]);
-        mx = b > mx ? b : mx;
+// block norms of X (warp per block, the deterministic order) and the block's
+// row maxima folded into row_bits (bit patterns of |x|, atomicMax), one pass
+__global__ void k_xnorm_rowmax(const double *__restrict__ X, size_t ld, size_t nr, size_t nc, size_t bs, size_t nrb,
+                               size_t nblk, double *__restrict__ norm, unsigned long long *__restrict__ row_bits) {
+    const size_t b = (size_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    if (b >= nblk) return;
+    const size_t rb = b % nrb, cb = b / nrb;
+    const int rows = ext3(rb, bs, nr), cols = ext3(cb, bs, nc);
+    const double *M = X + rb * bs + cb * bs * ld;
+    const double est = warp_block_norm(M, rows, cols, ld);
+    if ((threadIdx.x & 31) == 0) norm[b] = est;
+    for (int r = threadIdx.x & 31; r < rows; r += 32) {
+        long long mx = 0;
+        for (int l = 0; l < cols; ++l) {
+            const long long v = oz_absbits(M[r + (size_t)l * ld]);
+            mx = v > mx ? v : mx;
+        }
+        if (mx) atomicMax(&row_bits[rb * bs + r], (unsigned long long)mx);
     }
-    rexp[r] = oz_exp_of_bits(mx);
 }
 
 // exponent of every column of V (over all rows); one block per column
@@ -116,8 +125,9 @@ __global__ void k_tiles_3c(size_t n_tiles, size_t n_jg, size_t Gj, const double 
                            double *__restrict__ out, Dense3c D, double tpb, OzTile *__restrict__ tiles,
                            OzStep *__restrict__ steps, unsigned long long *__restrict__ nsig,
                            unsigned long long *__restrict__ macs) {
-    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t t = oz_warp_id();  // one warp per tile, lanes over the k steps
     if (t >= n_tiles) return;
+    const int lane = threadIdx.x & 31;
     const size_t q = t / (D.nibp * Gj), rem = t % (D.nibp * Gj);
     const size_t gsz = min(Gj, n_jg - q * Gj);  // only the last group is smaller
     const size_t ibp = rem / gsz, jg = q * Gj + rem % gsz;
@@ -150,52 +160,39 @@ __global__ void k_tiles_3c(size_t n_tiles, size_t n_jg, size_t Gj, const double 
     T.s0 = (uint32_t)(t * D.nkb * D.J);
     uint32_t n = 0;
     unsigned long long cnt = 0, m = 0;
-    for (size_t kb = 0; kb < D.nkb; ++kb) {
-        uint32_t mask[8];
-        for (int j = 0; j < nsub; ++j) {
-            const double x = xn[ibp * D.J + j + kb * D.nib];
-            mask[j] = 0;
-            for (int s = 0; s < D.R; ++s) {
-                const size_t jb = jg * D.R + s;
-                if (jb >= D.njb) break;
-                if (__dmul_rn(x, vn[kb + jb * D.nkb]) >= tpb) {
-                    mask[j] |= 1u << s;
-                    ++cnt;
-                    m += (unsigned long long)sub_rows[j] * T.rows[s] * ext3(kb, D.bs, D.n_aux);
-                }
-            }
-        }
-        // rectangles: the slots common to every sub-block that still has some
-        for (int guard = 0; guard < 8; ++guard) {
-            uint32_t common = 0xFFFFFFFFu, jset = 0;
-            for (int j = 0; j < nsub; ++j)
-                if (mask[j]) {
-                    common &= mask[j];
-                    jset |= 1u << j;
-                }
-            if (!jset) break;
-            if (!common) {  // not nested (cannot happen for a norm-product screen): one sub-block at a time
-                for (int j = 0; j < nsub; ++j)
-                    if (mask[j]) {
-                        common = mask[j];
-                        jset = 1u << j;
-                        break;
+    for (size_t base = 0; base < D.nkb; base += 32) {
+        const size_t kb = base + lane;
+        OzStep mine[2];
+        uint32_t c = 0;
+        if (kb < D.nkb) {
+            uint32_t live[2] = {0, 0};
+            for (int j = 0; j < nsub; ++j) {
+                const double x = xn[ibp * D.J + j + kb * D.nib];
+                for (int s = 0; s < D.R; ++s) {
+                    const size_t jb = jg * D.R + s;
+                    if (jb >= D.njb) break;
+                    if (__dmul_rn(x, vn[kb + jb * D.nkb]) >= tpb) {
+                        live[j] |= 1u << s;
+                        ++cnt;
+                        m += (unsigned long long)sub_rows[j] * T.rows[s] * ext3(kb, D.bs, D.n_aux);
                     }
+                }
             }
-            OzStep st;
-            st.b = (uint32_t)(ibp + kb * D.nibp);
-            st.bmask = (jset == (1u << D.J) - 1u) ? kOzAllSub : jset;
-            for (int s = 0; s < kOzMaxSlots; ++s)
-                st.a[s] = ((common >> s) & 1u) ? (uint32_t)(jg * D.R + s + kb * D.njb) : kOzNone;
-            steps[T.s0 + n++] = st;
-            for (int j = 0; j < nsub; ++j)
-                if ((jset >> j) & 1u) mask[j] &= ~common;
+            uint32_t a_idx[kOzMaxSlots];
+            for (int s = 0; s < kOzMaxSlots; ++s) a_idx[s] = (uint32_t)(jg * D.R + s + kb * D.njb);
+            // exact rectangles (the slot sets of a norm-product screen are nested)
+            c = emit_rect_steps(live, D.J, 0u, (uint32_t)(ibp + kb * D.nibp), a_idx, mine);
         }
+        warp_append_steps(mine, c, steps + T.s0, n);
     }
-    T.ns = n;
-    tiles[t] = T;
-    if (cnt) atomicAdd(nsig, cnt);
-    if (m) atomicAdd(macs, m);
+    cnt = warp_sum_u64(cnt);
+    m = warp_sum_u64(m);
+    if (lane == 0) {
+        T.ns = n;
+        tiles[t] = T;
+        if (cnt) atomicAdd(nsig, cnt);
+        if (m) atomicAdd(macs, m);
+    }
 }
 
 namespace {
@@ -268,9 +265,12 @@ void oz3c_rows(bsg_ctx ctx, Dense3c D, const OzShape &sh, const Oz3cV &v, const 
     const size_t a_img = (size_t)D.nd * sh.mp * sh.kp, b_img = (size_t)D.nd * sh.np * sh.kp;
     DevBuf xn(D.nib * D.nkb * 8, s), rexp(rows * 4, s), bi(D.nibp * D.nkb * b_img * 2, s);
     const int wpb = 8;
-    k_dense_norms<<<(unsigned)ceil_div(D.nib * D.nkb, wpb), wpb * 32, 0, s>>>(X, ldx, rows, n_aux, bs, D.nib,
-                                                                              D.nib * D.nkb, xn.as<double>());
-    k_rowexp_dense<<<(unsigned)ceil_div(rows, 256), 256, 0, s>>>(X, ldx, rows, n_aux, rexp.as<int>());
+    DevBuf rbits(rows * 8, s);
+    BSG_CUDA(cudaMemsetAsync(rbits.p, 0, rows * 8, s));
+    k_xnorm_rowmax<<<(unsigned)ceil_div(D.nib * D.nkb, wpb), wpb * 32, 0, s>>>(
+        X, ldx, rows, n_aux, bs, D.nib, D.nib * D.nkb, xn.as<double>(), rbits.as<unsigned long long>());
+    k_bits_to_exp<<<(unsigned)ceil_div(rows, (size_t)256), 256, 0, s>>>(rbits.as<unsigned long long>(), rows,
+                                                                        rexp.as<int>());
     k_img_X<<<oz_img_grid(D.nib * D.nkb), 32 * kOzImgWarps, 0, s>>>(X, rexp.as<int>(), D, bi.as<bf16>());
     ctx->note_launch(3);
     ctx->check_launch("3c2c ozaki X prep");
@@ -281,7 +281,7 @@ void oz3c_rows(bsg_ctx ctx, Dense3c D, const OzShape &sh, const Oz3cV &v, const 
     // V^T images of one slot group: R * nkb images; keep about 48 MB of them in L2
     const size_t grp_bytes = (size_t)D.R * D.nkb * a_img * 2;
     const size_t Gj = std::max<size_t>(1, std::min<size_t>(n_jg, (48ull << 20) / std::max<size_t>(grp_bytes, 1)));
-    k_tiles_3c<<<(unsigned)ceil_div(n_tiles, 128), 128, 0, s>>>(n_tiles, n_jg, Gj, xn.as<double>(), v.vn.as<double>(),
+    k_tiles_3c<<<oz_img_grid(n_tiles), 32 * kOzImgWarps, 0, s>>>(n_tiles, n_jg, Gj, xn.as<double>(), v.vn.as<double>(),
                                                                 rexp.as<int>(), v.cexp.as<int>(), out, D, tpb,
                                                                 dt.as<OzTile>(), dst.as<OzStep>(), cnt, cnt + 1);
     ctx->note_launch();

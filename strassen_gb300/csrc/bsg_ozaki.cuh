@@ -257,6 +257,68 @@ __device__ __forceinline__ void oz_block_image(const double *__restrict__ src, s
     oz_block_image_g(OzDenseGet{src, ld, b_role}, rows, k, exps, mpad, kp, nd, dst, m_side, threadIdx.x & 31, 32);
 }
 
+// One k step of a tile whose N side holds J block columns: live[j] = slots
+// whose product with sub-block j survives.  The pairs are split into exact
+// rectangles (slot set x sub-block set), each one step: the slots common to
+// every sub-block that still has some, then the rest (at most J steps).
+// Sub-blocks past the last block column count as present: their image rows
+// are zero, so a rectangle may include them and keep the single B copy.
+__device__ __forceinline__ uint32_t emit_rect_steps(uint32_t (&live)[2], int J, uint32_t phantom, uint32_t b,
+                                                    const uint32_t (&a_idx)[kOzMaxSlots], OzStep *__restrict__ out) {
+    uint32_t n = 0;
+    for (int guard = 0; guard < 2 * 2; ++guard) {
+        uint32_t common = 0xFFFFFFFFu, jset = 0;
+        for (int j = 0; j < J; ++j)
+            if (live[j]) {
+                common &= live[j];
+                jset |= 1u << j;
+            }
+        if (!jset) break;
+        if (!common) {
+            for (int j = 0; j < J; ++j)
+                if (live[j]) {
+                    common = live[j];
+                    jset = 1u << j;
+                    break;
+                }
+        }
+        OzStep st;
+        st.b = b;
+        st.bmask = ((jset | phantom) == (1u << J) - 1u) ? kOzAllSub : jset;
+        for (int sl = 0; sl < kOzMaxSlots; ++sl) st.a[sl] = ((common >> sl) & 1u) ? a_idx[sl] : kOzNone;
+        out[n++] = st;
+        for (int j = 0; j < J; ++j)
+            if ((jset >> j) & 1u) live[j] &= ~common;
+    }
+    return n;
+}
+
+// Warp-built step lists: lane l holds the (at most 2) steps of the tile's
+// k step base + l; they are written after the n steps already there, in
+// lane order, which is the order a serial loop over the k steps gives.
+__device__ __forceinline__ void warp_append_steps(const OzStep (&mine)[2], uint32_t cnt, OzStep *__restrict__ out,
+                                                  uint32_t &n) {
+    const int lane = threadIdx.x & 31;
+    uint32_t incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    const uint32_t excl = incl - cnt;
+    for (uint32_t i = 0; i < cnt; ++i) out[n + excl + i] = mine[i];
+    n += __shfl_sync(0xffffffffu, incl, 31);
+}
+
+__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// exponents from maxima bit patterns (bsg_ozaki.cu): exps[i] = frexp exponent of bits[i]
+__global__ void k_bits_to_exp(const unsigned long long *__restrict__ bits, size_t n, int *__restrict__ exps);
+
 // one warp per item: global warp index and a guard for launches of 8 warps per CTA
 constexpr int kOzImgWarps = 8;
 __device__ __forceinline__ size_t oz_warp_id() { return (size_t)blockIdx.x * kOzImgWarps + (threadIdx.x >> 5); }

@@ -135,11 +135,6 @@ __global__ void k_cexp_C(const double *__restrict__ C, size_t n_bf, size_t n_occ
 // Bit patterns of |x| (non-negative doubles order like their bits) are
 // combined with atomicMax; the exponents follow from the maxima.
 
-__global__ void k_bits_exp(const unsigned long long *__restrict__ bits, size_t n, int *__restrict__ exps) {
-    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) exps[i] = oz_exp_of_bits((long long)bits[i]);
-}
-
 // columns of ijs over the aux sub-range p / Q
 __global__ void k_colmax_ijs_sub(const double *__restrict__ ijs, const uint8_t *__restrict__ sflag, size_t n_occ,
                                  size_t bs, size_t nob, size_t Q, size_t n, unsigned long long *__restrict__ bits) {
@@ -206,46 +201,36 @@ __global__ void k_img_Ct_A(const double *__restrict__ C, const int *__restrict__
                 cexp + ib * D.bs, D.mp, D.kp, D.nd, img + x * D.nd * (size_t)D.mp * D.kp, true);
 }
 
-// mui_p blocks (a, jb) in the B role of ij, J block columns per image: image
-// index p*nb*nobp + a + jbp*nb, block jb = J*jbp + j at rows j*bs; one warp
-// per (p, a, jb) with jb < nobp*J (columns past n_occ get zero rows)
-__global__ void k_img_mui_B(const double *__restrict__ mui, const uint8_t *__restrict__ mflag,
-                            const int *__restrict__ cexp, OzDims D, size_t n, bf16 *__restrict__ img) {
+// All digit images of one mui_p block in one pass (warp per (p, a, jb), jb <
+// nobp*J): the A image of the K and K_mn products (rows a, row exponents per
+// aux sub-range, index p*nb*nob + a + jb*nb), the J-grouped B image of ij
+// (imgB, rows jb, column exponents per aux function; columns past n_occ get
+// zero rows) and the B image of K_mn (imgT, rows a); null images are skipped.
+// The block is read from DRAM once, the second and third splits hit L1.
+__global__ void k_img_mui_all(const double *__restrict__ mui, const uint8_t *__restrict__ mflag,
+                              const int *__restrict__ rexp, size_t Q, const int *__restrict__ cexp, OzDims D, size_t n,
+                              bf16 *__restrict__ imgA, bf16 *__restrict__ imgB, bf16 *__restrict__ imgT) {
     const size_t x = oz_warp_id();
     if (x >= n) return;
     const size_t nj = D.nobp * D.J, a = x % D.nb, jb = (x / D.nb) % nj, p = x / (D.nb * nj);
     const size_t jbp = jb / D.J, j = jb % D.J;
-    bf16 *dst = img + ((p * D.nobp + jbp) * D.nb + a) * D.nd * (size_t)D.npJ * D.kp + j * D.bs * (size_t)D.kp;
     const bool real = jb < D.nob;
-    if (real && !mflag[p * D.nb * D.nob + a + jb * D.nb]) return;
+    const size_t xb = p * D.nb * D.nob + a + jb * D.nb;
+    if (real && !mflag[xb]) return;
     const size_t jc = real ? jb : 0;
-    oz_block_image_g(OzDenseGet{mui + p * D.n_bf * D.n_occ + a * D.bs + jc * D.bs * D.n_bf, D.n_bf, true},
-                     real ? ext_r(jb, D.bs, D.n_occ) : 0, real ? ext_r(a, D.bs, D.n_bf) : 0,
-                     cexp + p * D.n_occ + jc * D.bs, rows_in_group(D), D.kp, D.nd, dst, false, threadIdx.x & 31, 32,
-                     D.npJ);
-}
-
-// mui_p blocks (a, ib) in the A role of K += mui ijs; index p*nb*nob + a + ib*nb
-__global__ void k_img_mui_A(const double *__restrict__ mui, const uint8_t *__restrict__ mflag,
-                            const int *__restrict__ rexp, size_t Q, OzDims D, size_t n, bf16 *__restrict__ img) {
-    const size_t x = oz_warp_id();
-    if (x >= n || !mflag[x]) return;
-    const size_t p = x / (D.nb * D.nob), a = x % D.nb, ib = (x / D.nb) % D.nob;
-    oz_block_image(mui + p * D.n_bf * D.n_occ + a * D.bs + ib * D.bs * D.n_bf, D.n_bf, false, ext_r(a, D.bs, D.n_bf),
-                ext_r(ib, D.bs, D.n_occ), rexp + (p / Q) * D.n_bf + a * D.bs, D.mp, D.kp, D.nd,
-                img + x * D.nd * (size_t)D.mp * D.kp, true);
-}
-
-// mui_p blocks (b, jb) as the B operand of K_mn = mui mui^T (rows b, k = jb; the
-// same digits as the A image, in the N-side layout); index p*nb*nob + b + jb*nb
-__global__ void k_img_mui_T(const double *__restrict__ mui, const uint8_t *__restrict__ mflag,
-                            const int *__restrict__ rexp, size_t Q, OzDims D, size_t n, bf16 *__restrict__ img) {
-    const size_t x = oz_warp_id();
-    if (x >= n || !mflag[x]) return;
-    const size_t p = x / (D.nb * D.nob), b = x % D.nb, jb = (x / D.nb) % D.nob;
-    oz_block_image(mui + p * D.n_bf * D.n_occ + b * D.bs + jb * D.bs * D.n_bf, D.n_bf, false, ext_r(b, D.bs, D.n_bf),
-                ext_r(jb, D.bs, D.n_occ), rexp + (p / Q) * D.n_bf + b * D.bs, D.np, D.kp, D.nd,
-                img + x * D.nd * (size_t)D.np * D.kp, false);
+    const double *M = mui + p * D.n_bf * D.n_occ + a * D.bs + jc * D.bs * D.n_bf;
+    const int ra = ext_r(a, D.bs, D.n_bf), rj = real ? ext_r(jb, D.bs, D.n_occ) : 0;
+    if (imgB)
+        oz_block_image_g(OzDenseGet{M, D.n_bf, true}, rj, real ? ra : 0, cexp + p * D.n_occ + jc * D.bs,
+                         rows_in_group(D), D.kp, D.nd,
+                         imgB + ((p * D.nobp + jbp) * D.nb + a) * D.nd * (size_t)D.npJ * D.kp + j * D.bs * (size_t)D.kp,
+                         false, threadIdx.x & 31, 32, D.npJ);
+    if (!real) return;
+    const int *re = rexp + (p / Q) * D.n_bf + a * D.bs;
+    if (imgA)
+        oz_block_image(M, D.n_bf, false, ra, rj, re, D.mp, D.kp, D.nd, imgA + xb * D.nd * (size_t)D.mp * D.kp, true);
+    if (imgT)
+        oz_block_image(M, D.n_bf, false, ra, rj, re, D.np, D.kp, D.nd, imgT + xb * D.nd * (size_t)D.np * D.kp, false);
 }
 
 // ijs_p blocks (ib, jb) in the B role of the K product, J block columns per
@@ -264,65 +249,6 @@ __global__ void k_img_ijs_B(const double *__restrict__ ijs, const uint8_t *__res
                      real ? ext_r(jb, D.bs, D.n_occ) : 0, real ? ext_r(ib, D.bs, D.n_occ) : 0,
                      cexp + (p / Q) * D.n_occ + jc * D.bs, rows_in_group(D), D.kp, D.nd, dst, false,
                      threadIdx.x & 31, 32, D.npJ);
-}
-
-// One k step of a tile whose N side holds J block columns: live[j] = slots
-// whose product with sub-block j survives.  The pairs are split into exact
-// rectangles (slot set x sub-block set), each one step: the slots common to
-// every sub-block that still has some, then the rest (at most J steps).
-// Sub-blocks past the last block column count as present: their image rows
-// are zero, so a rectangle may include them and keep the single B copy.
-__device__ __forceinline__ uint32_t emit_rect_steps(uint32_t (&live)[2], int J, uint32_t phantom, uint32_t b,
-                                                    const uint32_t (&a_idx)[kOzMaxSlots], OzStep *__restrict__ out) {
-    uint32_t n = 0;
-    for (int guard = 0; guard < 2 * 2; ++guard) {
-        uint32_t common = 0xFFFFFFFFu, jset = 0;
-        for (int j = 0; j < J; ++j)
-            if (live[j]) {
-                common &= live[j];
-                jset |= 1u << j;
-            }
-        if (!jset) break;
-        if (!common) {
-            for (int j = 0; j < J; ++j)
-                if (live[j]) {
-                    common = live[j];
-                    jset = 1u << j;
-                    break;
-                }
-        }
-        OzStep st;
-        st.b = b;
-        st.bmask = ((jset | phantom) == (1u << J) - 1u) ? kOzAllSub : jset;
-        for (int sl = 0; sl < kOzMaxSlots; ++sl) st.a[sl] = ((common >> sl) & 1u) ? a_idx[sl] : kOzNone;
-        out[n++] = st;
-        for (int j = 0; j < J; ++j)
-            if ((jset >> j) & 1u) live[j] &= ~common;
-    }
-    return n;
-}
-
-// Warp-built step lists: lane l holds the (at most 2) steps of the tile's
-// k step base + l; they are written after the n steps already there, in
-// lane order, which is the order a serial loop over the k steps gives.
-__device__ __forceinline__ void warp_append_steps(const OzStep (&mine)[2], uint32_t cnt, OzStep *__restrict__ out,
-                                                  uint32_t &n) {
-    const int lane = threadIdx.x & 31;
-    uint32_t incl = cnt;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += v;
-    }
-    const uint32_t excl = incl - cnt;
-    for (uint32_t i = 0; i < cnt; ++i) out[n + excl + i] = mine[i];
-    n += __shfl_sync(0xffffffffu, incl, 31);
-}
-
-__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
-#pragma unroll
-    for (int o = 16; o >= 1; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    return v;
 }
 
 // ---- tiles and steps (one thread per tile) ----
@@ -350,8 +276,9 @@ __global__ void k_tiles_mui(const uint8_t *__restrict__ uflag, const double *__r
                             size_t n_tiles, double tpb, OzTile *__restrict__ tiles, OzStep *__restrict__ steps,
                             uint8_t *__restrict__ mflag, unsigned long long *__restrict__ nsig,
                             unsigned long long *__restrict__ macs) {
-    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t t = oz_warp_id();  // one warp per tile, lanes over b
     if (t >= n_tiles) return;
+    const int lane = threadIdx.x & 31;
     const size_t ng = (D.nob + D.R - 1) / D.R;
     const size_t g = t % ng, a = (t / ng) % D.nb, pp = t / (ng * D.nb), p0 = pp * D.Jm;
     const int nsub = (int)min((size_t)D.Jm, np - p0);
@@ -380,38 +307,48 @@ __global__ void k_tiles_mui(const uint8_t *__restrict__ uflag, const double *__r
     }
     T.s0 = (uint32_t)(t * D.nb * D.Jm);
     uint32_t n = 0;
-    for (size_t b = 0; b < D.nb; ++b) {
-        uint32_t live[2] = {0, 0};
-        uint32_t a_idx[kOzMaxSlots];
-        for (int s = 0; s < kOzMaxSlots; ++s) a_idx[s] = (uint32_t)(g * D.R + s + b * D.nob);
-        for (int js = 0; js < nsub; ++js) {
-            const size_t ub = (p0 + js) * D.nb * D.nb + a + b * D.nb;
-            if (!uflag[ub]) continue;
-            for (int s = 0; s < D.R; ++s) {
-                if (!T.c[s]) continue;
-                const size_t j = g * D.R + s;
-                if (!(__dmul_rn(unorm[ub], cnorm[b + j * D.nb]) >= tpb)) continue;
-                live[js] |= 1u << s;
-                m += (unsigned long long)T.rows[s] * ext_r(a, D.bs, D.n_bf) * ext_r(b, D.bs, D.n_bf);
-                ++cnt[s][js];
+    for (size_t base = 0; base < D.nb; base += 32) {
+        const size_t b = base + lane;
+        OzStep mine[2];
+        uint32_t c = 0;
+        if (b < D.nb) {
+            uint32_t live[2] = {0, 0};
+            uint32_t a_idx[kOzMaxSlots];
+            for (int s = 0; s < kOzMaxSlots; ++s) a_idx[s] = (uint32_t)(g * D.R + s + b * D.nob);
+            for (int js = 0; js < nsub; ++js) {
+                const size_t ub = (p0 + js) * D.nb * D.nb + a + b * D.nb;
+                if (!uflag[ub]) continue;
+                for (int s = 0; s < D.R; ++s) {
+                    if (!T.c[s]) continue;
+                    const size_t j = g * D.R + s;
+                    if (!(__dmul_rn(unorm[ub], cnorm[b + j * D.nb]) >= tpb)) continue;
+                    live[js] |= 1u << s;
+                    m += (unsigned long long)T.rows[s] * ext_r(a, D.bs, D.n_bf) * ext_r(b, D.bs, D.n_bf);
+                    ++cnt[s][js];
+                }
             }
+            // a missing aux function (odd chunk end) counts as absent: its image rows are never written
+            c = emit_rect_steps(live, D.Jm, 0u, (uint32_t)(pp * D.nb * D.nb + a + b * D.nb), a_idx, mine);
         }
-        // a missing aux function (odd chunk end) counts as absent: its image rows are never written
-        n += emit_rect_steps(live, D.Jm, 0u, (uint32_t)(pp * D.nb * D.nb + a + b * D.nb), a_idx, steps + T.s0 + n);
+        warp_append_steps(mine, c, steps + T.s0, n);
     }
-    T.ns = n;
-    tiles[t] = T;
     unsigned long long tot = 0;
     for (int s = 0; s < D.R; ++s) {
         const size_t j = g * D.R + s;
         if (j >= D.nob) break;
         for (int js = 0; js < nsub; ++js) {
-            mflag[(p0 + js) * D.nb * D.nob + a + j * D.nb] = cnt[s][js] > 0;
-            tot += cnt[s][js];
+            const unsigned long long cs = warp_sum_u64((unsigned long long)cnt[s][js]);  // lane 0 holds the sum
+            if (lane == 0) mflag[(p0 + js) * D.nb * D.nob + a + j * D.nb] = cs > 0;
+            tot += cs;
         }
     }
-    if (tot) atomicAdd(nsig, tot);
-    if (m) atomicAdd(macs, m);
+    m = warp_sum_u64(m);
+    if (lane == 0) {
+        T.ns = n;
+        tiles[t] = T;
+        if (tot) atomicAdd(nsig, tot);
+        if (m) atomicAdd(macs, m);
+    }
 }
 
 // ij tiles: t = (p, jbp, group of R block rows ib), N side J block columns
@@ -851,13 +788,13 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
                 d.ints, dinv.as<int>(), dob.as<uint32_t>(), n_ob, d.n_vec2, P0, n_bf, bs, nb, np, tpb_u,
                 dun.as<double>(), duf.as<uint8_t>(), ducomp.as<double>(), bitsU);
         }
-        k_bits_exp<<<(unsigned)ceil_div(np * n_bf, (size_t)256), 256, 0, s>>>(bitsU, np * n_bf, drexpU.as<int>());
+        k_bits_to_exp<<<(unsigned)ceil_div(np * n_bf, (size_t)256), 256, 0, s>>>(bitsU, np * n_bf, drexpU.as<int>());
         if (n_ob)
             k_img_U<<<oz_img_grid(np * n_ob), 32 * kOzImgWarps, 0, s>>>(ducomp.as<double>(), dob.as<uint32_t>(), n_ob,
                                                                        np, duf.as<uint8_t>(), drexpU.as<int>(), D,
                                                                        dimgU.as<bf16>());
         const size_t tm = ceil_div(np, (size_t)Jm) * nb * ng_i;
-        k_tiles_mui<<<(unsigned)ceil_div(tm, 128), 128, 0, s>>>(
+        k_tiles_mui<<<oz_img_grid(tm), 32 * kOzImgWarps, 0, s>>>(
             duf.as<uint8_t>(), dun.as<double>(), dcn.as<double>(), drexpU.as<int>(), dcexpC.as<int>(),
             dmui.as<double>(), D, np, tm, tpb, dtm.as<OzTile>(), dsm.as<OzStep>(), dmf.as<uint8_t>(), cnt + 0,
             macs + 0);
@@ -870,20 +807,23 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
         k_mui_stats<<<oz_img_grid(np * nb * nob), 32 * kOzImgWarps, 0, s>>>(
             dmui.as<double>(), dmf.as<uint8_t>(), n_bf, n_occ, bs, nb, nob, Q, np * nb * nob, dmn.as<double>(), bitsMs,
             want_k ? bitsM : nullptr);
-        k_bits_exp<<<(unsigned)ceil_div(n_sub * n_bf, (size_t)256), 256, 0, s>>>(bitsMs, n_sub * n_bf,
+        k_bits_to_exp<<<(unsigned)ceil_div(n_sub * n_bf, (size_t)256), 256, 0, s>>>(bitsMs, n_sub * n_bf,
                                                                                  drexpMs.as<int>());
-        k_img_mui_A<<<oz_img_grid(np * nb * nob), 32 * kOzImgWarps, 0, s>>>(
-            dmui.as<double>(), dmf.as<uint8_t>(), drexpMs.as<int>(), Q, D, np * nb * nob, dimgMA.as<bf16>());
-        ctx->note_launch(3);
+        if (want_k)
+            k_bits_to_exp<<<(unsigned)ceil_div(np * n_occ, (size_t)256), 256, 0, s>>>(bitsM, np * n_occ,
+                                                                                     dcexpM.as<int>());
+        // every digit image of mui in one pass
+        k_img_mui_all<<<oz_img_grid(np * nb * nobp * J), 32 * kOzImgWarps, 0, s>>>(
+            dmui.as<double>(), dmf.as<uint8_t>(), drexpMs.as<int>(), Q, dcexpM.as<int>(), D, np * nb * nobp * J,
+            dimgMA.as<bf16>(), want_k ? dimgMB.as<bf16>() : nullptr, want_kmn ? dimgMT.as<bf16>() : nullptr);
+        ctx->note_launch(want_k ? 4 : 3);
         if (want_kmn) {
             // K_mn += mui mui^T
-            k_img_mui_T<<<oz_img_grid(np * nb * nob), 32 * kOzImgWarps, 0, s>>>(
-                dmui.as<double>(), dmf.as<uint8_t>(), drexpMs.as<int>(), Q, D, np * nb * nob, dimgMT.as<bf16>());
             const size_t tkm = n_sub * n_pairs;
             k_tiles_Kmn<<<(unsigned)ceil_div(tkm, 128), 128, 0, s>>>(
                 dmf.as<uint8_t>(), dmn.as<double>(), drexpMs.as<int>(), dKmnp.as<double>(), D, np, Q, n_pairs, tkm,
                 tpb, dtkm.as<OzTile>(), dskm.as<OzStep>(), cnt + 5, macs + 3);
-            ctx->note_launch(2);
+            ctx->note_launch();
             ctx->check_launch("rik ozaki Kmn prep");
             oz_run(ctx, sh, dtkm.as<OzTile>(), tkm, dskm.as<OzStep>(), dimgMA.as<bf16>(), dimgMT.as<bf16>(), 1.0, s,
                    macs + 3);
@@ -893,14 +833,11 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
         }
         if (!want_k) continue;
         // ij = C^T mui
-        k_bits_exp<<<(unsigned)ceil_div(np * n_occ, (size_t)256), 256, 0, s>>>(bitsM, np * n_occ, dcexpM.as<int>());
-        k_img_mui_B<<<oz_img_grid(np * nb * nobp * J), 32 * kOzImgWarps, 0, s>>>(
-            dmui.as<double>(), dmf.as<uint8_t>(), dcexpM.as<int>(), D, np * nb * nobp * J, dimgMB.as<bf16>());
         const size_t ti = np * nobp * ng_i;
         k_tiles_ij<<<oz_img_grid(ti), 32 * kOzImgWarps, 0, s>>>(
             dmf.as<uint8_t>(), dmn.as<double>(), dcn.as<double>(), dcexpC.as<int>(), dcexpM.as<int>(),
             dij.as<double>(), D, ti, tpb, dti.as<OzTile>(), dsi.as<OzStep>(), dijf.as<uint8_t>(), cnt + 1, macs + 1);
-        ctx->note_launch(3);
+        ctx->note_launch();
         ctx->check_launch("rik ozaki ij prep");
         oz_run(ctx, shJ, dti.as<OzTile>(), ti, dsi.as<OzStep>(), dimgCtA.as<bf16>(), dimgMB.as<bf16>(), 1.0, s,
                macs + 1);
@@ -910,7 +847,7 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
         // K += mui ijs
         k_colmax_ijs_sub<<<oz_img_grid(np * nob * nob), 32 * kOzImgWarps, 0, s>>>(
             dijs.as<double>(), dsf.as<uint8_t>(), n_occ, bs, nob, Q, np * nob * nob, bitsSs);
-        k_bits_exp<<<(unsigned)ceil_div(n_sub * n_occ, (size_t)256), 256, 0, s>>>(bitsSs, n_sub * n_occ,
+        k_bits_to_exp<<<(unsigned)ceil_div(n_sub * n_occ, (size_t)256), 256, 0, s>>>(bitsSs, n_sub * n_occ,
                                                                                   dcexpSs.as<int>());
         k_img_ijs_B<<<oz_img_grid(np * nob * nobp * J), 32 * kOzImgWarps, 0, s>>>(
             dijs.as<double>(), dsf.as<uint8_t>(), dcexpSs.as<int>(), Q, D, np * nob * nobp * J, dimgSB.as<bf16>());
