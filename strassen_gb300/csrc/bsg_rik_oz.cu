@@ -165,6 +165,10 @@ struct OzDims {
     // N side of mui^T = C^T U^T: U blocks of Jm consecutive aux functions per
     // image (npm rows per digit plane)
     int Jm, npm;
+    // N side of K_mn = mui mui^T: Jk consecutive basis block rows per image
+    // (npk rows per digit plane), nbp groups
+    int Jk, npk;
+    size_t nbp;
 };
 
 // N-side image rows of occupied block column jb = J*jbp + j inside its
@@ -229,8 +233,11 @@ __global__ void k_img_mui_all(const double *__restrict__ mui, const uint8_t *__r
     const int *re = rexp + (p / Q) * D.n_bf + a * D.bs;
     if (imgA)
         oz_block_image(M, D.n_bf, false, ra, rj, re, D.mp, D.kp, D.nd, imgA + xb * D.nd * (size_t)D.mp * D.kp, true);
-    if (imgT)
-        oz_block_image(M, D.n_bf, false, ra, rj, re, D.np, D.kp, D.nd, imgT + xb * D.nd * (size_t)D.np * D.kp, false);
+    if (imgT)  // K_mn's N side: block rows a of Jk-groups, image (p, jb, a / Jk), rows (a % Jk) * bs
+        oz_block_image_g(OzDenseGet{M, D.n_bf, false}, ra, rj, re, D.Jk == 1 ? D.npk : (int)D.bs, D.kp, D.nd,
+                         imgT + ((p * D.nob + jb) * D.nbp + a / D.Jk) * D.nd * (size_t)D.npk * D.kp +
+                             (a % D.Jk) * D.bs * (size_t)D.kp,
+                         false, threadIdx.x & 31, 32, D.npk);
 }
 
 // ijs_p blocks (ib, jb) in the B role of the K product, J block columns per
@@ -529,17 +536,20 @@ __global__ void k_K_reduce(const double *__restrict__ Kpart, size_t n_sub, OzDim
     }
 }
 
-// (b, g) pairs of the K_mn tiles: block column b, group g of R block rows
-// a = g R .. g R + R - 1 with at least one a >= b; pairs ordered by b, then g
-__host__ __device__ inline size_t kmn_pairs(size_t nb, size_t R) {
+// (bp, g) pairs of the K_mn tiles: a group of Jk block columns b = Jk*bp + j
+// and a group g of R block rows a = g R .. g R + R - 1 with at least one
+// a >= Jk*bp; pairs ordered by bp, then g
+__host__ __device__ inline size_t kmn_pairs(size_t nbp, size_t Jk, size_t nb, size_t R) {
     const size_t ng = (nb + R - 1) / R;
     size_t n = 0;
-    for (size_t b = 0; b < nb; ++b) n += ng - b / R;
+    for (size_t bp = 0; bp < nbp; ++bp) n += ng - (Jk * bp) / R;
     return n;
 }
 
-// K_mn tiles: t = (sub-range, pair (b, g)), steps over (p, jb); slots a < b
-// are left out (their blocks are the mirrors of a > b)
+// K_mn tiles: t = (sub-range, pair (bp, g)), N side Jk block columns, steps
+// over (p, jb) split into exact rectangles; a product (a, b) enters only for
+// a >= b (the upper blocks are the mirrors).  Partial blocks of a tile:
+// Kpart + ((sub*nbp + bp)*nb + a) * bs * Jk*bs, column-major, ld = rows.
 __global__ void k_tiles_Kmn(const uint8_t *__restrict__ mflag, const double *__restrict__ mnorm,
                             const int *__restrict__ rexp_sub, double *__restrict__ Kpart, OzDims D, size_t np,
                             size_t Q, size_t n_pairs, size_t n_tiles, double tpb, OzTile *__restrict__ tiles,
@@ -548,55 +558,60 @@ __global__ void k_tiles_Kmn(const uint8_t *__restrict__ mflag, const double *__r
     const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n_tiles) return;
     const size_t ng = (D.nb + D.R - 1) / D.R, sub = t / n_pairs;
-    size_t rem = t % n_pairs, b = 0, g = 0;
-    for (; b < D.nb; ++b) {
-        const size_t c = ng - b / D.R;
+    size_t rem = t % n_pairs, bp = 0, g = 0;
+    for (; bp < D.nbp; ++bp) {
+        const size_t c = ng - (D.Jk * bp) / D.R;
         if (rem < c) {
-            g = b / D.R + rem;
+            g = (D.Jk * bp) / D.R + rem;
             break;
         }
         rem -= c;
     }
+    const size_t b0 = bp * D.Jk;
     unsigned long long m = 0;
     OzTile T;
     tile_clear(T);
-    const size_t bs2 = D.bs * D.bs;
+    const size_t blk = D.bs * D.bs * D.Jk;
     for (int s = 0; s < D.R; ++s) {
         const size_t a = g * D.R + s;
         if (a >= D.nb) break;
-        if (a < b) continue;
-        T.c[s] = Kpart + ((sub * D.nb + b) * D.nb + a) * bs2;
+        if (a < b0) continue;
+        T.c[s] = Kpart + ((sub * D.nbp + bp) * D.nb + a) * blk;
         T.rows[s] = ext_r(a, D.bs, D.n_bf);
         T.ldc[s] = T.rows[s];
         T.rexp[s] = rexp_sub + sub * D.n_bf + a * D.bs;
     }
-    T.cols = ext_r(b, D.bs, D.n_bf);
+    int cols = 0;
+    for (int j = 0; j < D.Jk; ++j)
+        if (b0 + j < D.nb) cols = j * (int)D.bs + ext_r(b0 + j, D.bs, D.n_bf);
+    T.cols = cols;
     T.trans = 0;
-    T.cexp = rexp_sub + sub * D.n_bf + b * D.bs;
-    T.s0 = (uint32_t)(t * Q * D.nob);
+    T.cexp = rexp_sub + sub * D.n_bf + b0 * D.bs;
+    T.s0 = (uint32_t)(t * Q * D.nob * D.Jk);
     uint32_t n = 0;
     unsigned long long tot = 0;
     const size_t p1 = min(np, (sub + 1) * Q);
     for (size_t p = sub * Q; p < p1; ++p)
         for (size_t jb = 0; jb < D.nob; ++jb) {
-            const size_t mb = p * D.nb * D.nob + b + jb * D.nb;
-            if (!mflag[mb]) continue;
-            OzStep st;
-            st.bmask = kOzAllSub;
-            st.b = (uint32_t)mb;
-            bool any = false;
-            for (int s = 0; s < kOzMaxSlots; ++s) {
-                st.a[s] = kOzNone;
-                if (s >= D.R || !T.c[s]) continue;
-                const size_t a = g * D.R + s, ma = p * D.nb * D.nob + a + jb * D.nb;
-                if (!mflag[ma]) continue;
-                if (!(__dmul_rn(mnorm[ma], mnorm[mb]) >= tpb)) continue;
-                st.a[s] = (uint32_t)ma;
-                m += (unsigned long long)T.rows[s] * T.cols * ext_r(jb, D.bs, D.n_occ);
-                ++tot;
-                any = true;
+            uint32_t live[2] = {0, 0};
+            uint32_t a_idx[kOzMaxSlots];
+            for (int s = 0; s < kOzMaxSlots; ++s) a_idx[s] = (uint32_t)(p * D.nb * D.nob + g * D.R + s + jb * D.nb);
+            for (int j = 0; j < D.Jk; ++j) {
+                const size_t b = b0 + j;
+                if (b >= D.nb) continue;
+                const size_t mb = p * D.nb * D.nob + b + jb * D.nb;
+                if (!mflag[mb]) continue;
+                for (int s = 0; s < D.R; ++s) {
+                    if (!T.c[s]) continue;
+                    const size_t a = g * D.R + s, ma = p * D.nb * D.nob + a + jb * D.nb;
+                    if (a < b || !mflag[ma]) continue;
+                    if (!(__dmul_rn(mnorm[ma], mnorm[mb]) >= tpb)) continue;
+                    live[j] |= 1u << s;
+                    m += (unsigned long long)T.rows[s] * ext_r(b, D.bs, D.n_bf) * ext_r(jb, D.bs, D.n_occ);
+                    ++tot;
+                }
             }
-            if (any) steps[T.s0 + n++] = st;
+            n += emit_rect_steps(live, D.Jk, 0u, (uint32_t)((p * D.nob + jb) * D.nbp + bp), a_idx, steps + T.s0 + n);
         }
     T.ns = n;
     tiles[t] = T;
@@ -606,15 +621,16 @@ __global__ void k_tiles_Kmn(const uint8_t *__restrict__ mflag, const double *__r
 
 // K_mn(a, b) += sum over sub-ranges (in order) of the tiles' partial blocks, a >= b
 __global__ void k_Kmn_reduce(const double *__restrict__ Kpart, size_t n_sub, OzDims D, double *__restrict__ K) {
-    const size_t blk = blockIdx.x;  // (b, a)
-    const size_t a = blk % D.nb, b = blk / D.nb;
+    const size_t x = blockIdx.x;  // (b, a)
+    const size_t a = x % D.nb, b = x / D.nb, bp = b / D.Jk, j = b % D.Jk;
     if (a < b) return;
     const int rows = ext_r(a, D.bs, D.n_bf), cols = ext_r(b, D.bs, D.n_bf);
-    const size_t bs2 = D.bs * D.bs;
+    const size_t blk = D.bs * D.bs * D.Jk;
     for (int e = threadIdx.x; e < rows * cols; e += blockDim.x) {
         const int r = e % rows, c = e / rows;
+        const size_t pe = (size_t)r + (j * D.bs + c) * (size_t)rows;
         double acc = K[a * D.bs + r + (b * D.bs + c) * D.n_bf];
-        for (size_t sub = 0; sub < n_sub; ++sub) acc += Kpart[((sub * D.nb + b) * D.nb + a) * bs2 + e];
+        for (size_t sub = 0; sub < n_sub; ++sub) acc += Kpart[((sub * D.nbp + bp) * D.nb + a) * blk + pe];
         K[a * D.bs + r + (b * D.bs + c) * D.n_bf] = acc;
     }
 }
@@ -702,6 +718,14 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
     shM.J = Jm;
     D.Jm = Jm;
     D.npm = shM.np;
+    // K_mn: two basis block rows per tile on the N side where they fit
+    int Jk = Jm;
+    OzShape shK = Jk == 2 ? shM : sh;
+    shK.J = Jk;
+    D.Jk = Jk;
+    D.npk = shK.np;
+    D.nbp = ceil_div(D.nb, (size_t)Jk);
+    const size_t b_imgK = (size_t)nd * shK.np * shK.kp;
     const size_t b_imgM = (size_t)nd * shM.np * shM.kp;  // elements per U image (Jm aux functions)
     D.npJ = shJ.np;
     D.nobp = ceil_div(D.nob, (size_t)J);
@@ -739,10 +763,11 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
     DevBuf dti(tiles_ij * sizeof(OzTile), s), dsi(tiles_ij * nb * J * sizeof(OzStep), s);
     DevBuf dtk(tiles_K * sizeof(OzTile), s), dsk(tiles_K * Q * nob * J * sizeof(OzStep), s);
     // K_mn: images of mui in the B role, tiles over (sub-range, lower pair), partials
-    const size_t n_pairs = kmn_pairs(nb, (size_t)D.R), tiles_Kmn = want_kmn ? n_sub_max * n_pairs : 0;
-    DevBuf dimgMT(want_kmn ? pc * nb * nob * b_img * 2 : 0, s);
-    DevBuf dKmnp(want_kmn ? n_sub_max * nb * nb * bs * bs * 8 : 0, s);
-    DevBuf dtkm(tiles_Kmn * sizeof(OzTile), s), dskm(tiles_Kmn * Q * nob * sizeof(OzStep), s);
+    const size_t n_pairs = kmn_pairs(D.nbp, (size_t)Jk, nb, (size_t)D.R);
+    const size_t tiles_Kmn = want_kmn ? n_sub_max * n_pairs : 0;
+    DevBuf dimgMT(want_kmn ? pc * nob * D.nbp * b_imgK * 2 : 0, s);
+    DevBuf dKmnp(want_kmn ? n_sub_max * D.nbp * nb * bs * bs * Jk * 8 : 0, s);
+    DevBuf dtkm(tiles_Kmn * sizeof(OzTile), s), dskm(tiles_Kmn * Q * nob * Jk * sizeof(OzStep), s);
     if (want_k) BSG_CUDA(cudaMemsetAsync(K_dev, 0, n_bf * n_occ * 8, s));
     if (want_kmn) BSG_CUDA(cudaMemsetAsync(Kmn_dev, 0, n_bf * n_bf * 8, s));
     BSG_CUDA(cudaMemsetAsync(dcnt.p, 0, 6 * 8, s));
@@ -825,7 +850,7 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
                 tpb, dtkm.as<OzTile>(), dskm.as<OzStep>(), cnt + 5, macs + 3);
             ctx->note_launch();
             ctx->check_launch("rik ozaki Kmn prep");
-            oz_run(ctx, sh, dtkm.as<OzTile>(), tkm, dskm.as<OzStep>(), dimgMA.as<bf16>(), dimgMT.as<bf16>(), 1.0, s,
+            oz_run(ctx, shK, dtkm.as<OzTile>(), tkm, dskm.as<OzStep>(), dimgMA.as<bf16>(), dimgMT.as<bf16>(), 1.0, s,
                    macs + 3);
             k_Kmn_reduce<<<(unsigned)(nb * nb), 256, 0, s>>>(dKmnp.as<double>(), n_sub, D, Kmn_dev);
             ctx->note_launch();

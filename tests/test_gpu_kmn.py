@@ -99,13 +99,16 @@ def test_mixed_form(api, ctx, bs, nd, tol):
     assert em < tol and ek < tol
 
 
-def test_mixed_kmn_only(api, ctx):
-    """K_mn without the occ step's K (the ij and K products are skipped)"""
-    s = S.RikSystem(seed=10, n_atoms=6, nbf=24, naux=12, n_occ=30, box=6.0)
+@pytest.mark.parametrize("n_atoms,p_chunk", [(6, 0), (5, 7)])
+def test_mixed_kmn_only(api, ctx, n_atoms, p_chunk):
+    """K_mn without the occ step's K (the ij and K products are skipped);
+    an odd number of basis block rows leaves the last N-side pair half empty"""
+    s = S.RikSystem(seed=10, n_atoms=n_atoms, nbf=24, naux=12, n_occ=30, box=6.0)
     B = api.transform_3c2c(s.ints_3c(), s.v_m12(), 24, 1e-10, ctx=ctx)
     C = s.c_occ()
     K64 = api.rik_kmn_step(B, s.keys, C, s.n_bf, s.n_aux, s.n_occ, 24, 1e-10, ctx=ctx)
     Koz, st = api.rik_kmn_step(B, s.keys, C, s.n_bf, s.n_aux, s.n_occ, 24, 1e-10, form=api.FORM_OZAKI, n_digits=5,
-                               ctx=ctx, stats=True)
+                               p_chunk=p_chunk, ctx=ctx, stats=True)
+    assert np.array_equal(Koz, Koz.T)
     assert st[1] == 0 and st[2] == 0 and st[5] > 0
     assert np.linalg.norm(Koz - K64) / np.linalg.norm(K64) < 1e-9
