@@ -3,17 +3,24 @@
 // screening (block norms, masks, surviving pairs), the transpose-add and the
 // K accumulation stay FP64.
 //
-// Per chunk of aux functions P:
-//   scatter + U block norms / flags        (FP64 kernels shared with bsg_rik.cu)
-//   mui_P = U_P C        as mui_P^T = C^T U_P^T: tiles (P, a, 5 occupied block
-//                        columns j), steps over the present U_P(a, b)
-//   mui norms            FP64, from the computed mui blocks
-//   ij_P  = C^T mui_P    tiles (P, jb, 5 block rows ib), steps over a
+// Per chunk of aux functions P (N-side groups of two blocks where both TMEM
+// accumulator sets fit):
+//   U_P                  block norms, flags, row maxima and dense copies of the
+//                        occupied blocks, gathered once from the compressed
+//                        integrals (bit-identical FP64 norms)
+//   mui_P = U_P C        as mui_P^T = C^T U_P^T: tiles (P pair, a, 5 occupied
+//                        block columns j), steps over the present U_P(a, b)
+//   mui statistics       FP64 norms, row and column maxima in one pass; all
+//                        digit images of mui in one pass
+//   ij_P  = C^T mui_P    tiles (P, jb pair, 5 block rows ib), steps over a
 //   ijs_P = ij + ij^T    FP64 (shared kernel)
-//   K    += mui_P ijs_P  tiles (P sub-range, jb, 5 block rows a), steps over
-//                        (P, ib); per-tile partial blocks summed in order
-//   Kmn  += mui_P mui_P^T  (optional) tiles (P sub-range, b, block rows a >= b),
-//                        steps over (P, jb); lower blocks, mirrored at the end
+//   K    += mui_P ijs_P  tiles (P sub-range, jb pair, 5 block rows a), steps
+//                        over (P, ib); per-tile partial blocks summed in order
+//   Kmn  += mui_P mui_P^T  (optional) tiles (P sub-range, b pair, block rows
+//                        a >= b), steps over (P, jb); lower blocks, mirrored
+//                        at the end
+// Steps whose N-side sub-blocks have different surviving slot sets split into
+// exact rectangles, so every product the FP64 screen drops stays out.
 // Operand scales: U rows per (P, mu); C columns per i (also the rows of C^T);
 // mui columns per (P, j) for the ij product; mui rows and ijs columns per
 // (P sub-range, mu / j) for the K product.  Every tile has one scale set, so
