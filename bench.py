@@ -362,6 +362,74 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def run_rik_large(args):
+    """The large RI-K configuration: 125 atoms in a 20 A box (n_bf 3000,
+    n_aux 10500, n_occ 500), uniform 24-wide blocks (the per-atom shells of
+    sizes 8-32 are not modelled), tau swept over 1e-6 .. 1e-12.  Per tau: one
+    timed mixed-form step on device-resident inputs (X is 45 GB), and the
+    error of each stage against the FP64 form on a sixteenth of it -- the
+    3c->2c transform on the first rows of X, the occ step on the first aux
+    functions of the mixed B (the full FP64 step does not fit the time budget:
+    about 35 x the mixed one).  A measurement case, not the bench line."""
+    import torch
+
+    from strassen_gb300 import api
+    from strassen_gb300 import synth as S
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    t0 = time.time()
+    sysm = S.RikSystem(seed=CFG["seed"], n_atoms=125, nbf=24, naux=84, n_occ=500, box=20.0)
+    n_bf, n_aux, n_occ, n_vec2, bs = sysm.n_bf, sysm.n_aux, sysm.n_occ, sysm.n_vec2, CFG["bs"]
+    Xt = sysm.ints_3c_torch(dev)  # n_aux x n_vec2 row-major == n_vec2 x n_aux column-major
+    X = Xt.T
+    V = torch.from_numpy(np.ascontiguousarray(sysm.v_m12().T)).to(dev).T
+    Cn = sysm.c_occ()
+    C = torch.from_numpy(np.ascontiguousarray(Cn.T)).to(dev).T
+    keys = torch.from_numpy(sysm.keys.view(np.int64)).to(dev)
+    B = torch.empty((n_aux, n_vec2), dtype=torch.float64, device=dev).T
+    K = torch.empty((n_occ, n_bf), dtype=torch.float64, device=dev).T
+    setup_s = time.time() - t0
+    ctx = api.Context(0)
+    f3c, focc = step_flops(n_bf, n_aux, n_occ, n_vec2)
+    rows = n_vec2 // 16
+    p_sub = n_aux // 16
+    Xs = np.asfortranarray(X[:rows].cpu().numpy())
+    Vn = np.asfortranarray(V.cpu().numpy())
+    res = []
+    for thr in (1e-6, 1e-8, 1e-10, 1e-12):
+        def step():
+            api.transform_3c2c(X, V, bs, thr, form=api.FORM_OZAKI, n_digits=args.digits_3c2c, out=B, ctx=ctx)
+            api.rik_occ_step(B, keys, C, n_bf, n_aux, n_occ, bs, thr, form=api.FORM_OZAKI, n_digits=args.digits_occ,
+                             out=K, ctx=ctx)
+
+        step()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        step()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        # stage errors against the FP64 form on a sixteenth of each stage
+        b_oz = api.transform_3c2c(Xs, Vn, bs, thr, form=api.FORM_OZAKI, n_digits=args.digits_3c2c, ctx=ctx)
+        b_64 = api.transform_3c2c(Xs, Vn, bs, thr, ctx=ctx)
+        Bs = np.asfortranarray(B[:, :p_sub].cpu().numpy())
+        k_oz = api.rik_occ_step(Bs, sysm.keys, Cn, n_bf, p_sub, n_occ, bs, thr, form=api.FORM_OZAKI,
+                                n_digits=args.digits_occ, ctx=ctx)
+        k_64 = api.rik_occ_step(Bs, sysm.keys, Cn, n_bf, p_sub, n_occ, bs, thr, ctx=ctx)
+        rel = lambda a, b: float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+        res.append({"tau": thr, "ms_per_step": ms, "tflops_dense_equiv": (f3c + focc) / (ms * 1e-3) / 1e12,
+                    "rel_err_3c2c_rows_1_16": rel(b_oz, b_64), "rel_err_occ_aux_1_16": rel(k_oz, k_64)})
+        del b_oz, b_64, Bs
+    print(json.dumps({"metric": "large RI-K step, mixed form, per tau", "unit": "ms",
+                      "config": {"workload": f"125 atoms in a 20 A box, n_bf {n_bf}, n_aux {n_aux}, n_occ {n_occ}, "
+                                             f"n_vec2 {n_vec2}, bs {bs} (uniform)",
+                                 "digits": {"3c2c": args.digits_3c2c, "occ": args.digits_occ},
+                                 "X_GB": n_vec2 * n_aux * 8 / 1e9}, "setup_s": setup_s,
+                      "flops_dense_equiv": f3c + focc, "results": res}))
+
+
 def run_batched(args):
     """Batched screened GEMMs (the batched-launch configuration): `--count`
     independent products C_i = A_i B_i, sizes uniform in [256, 4096] (rounded
@@ -457,12 +525,15 @@ def main():
     ap.add_argument("--skip-kmn", action="store_true", help="leave out the symmetric K_mn measurement")
     ap.add_argument("--no-e2e", action="store_true", help="profiling runs: timed device step only")
     ap.add_argument("--atoms", type=int, default=0, help="smaller system for profiler captures")
-    ap.add_argument("--workload", default="rik", choices=["rik", "batched"],
+    ap.add_argument("--workload", default="rik", choices=["rik", "batched", "rik-large"],
                     help="rik: the RI-K step (default); batched: the batched-GEMM configuration")
     ap.add_argument("--count", type=int, default=512, help="products of the batched workload")
     args = ap.parse_args()
     if args.workload == "batched":
         run_batched(args)
+        return
+    if args.workload == "rik-large":
+        run_rik_large(args)
         return
     if args.impl == "reference":
         run_reference(args)

@@ -318,7 +318,15 @@ void transform_3c2c_ozaki(bsg_ctx ctx, size_t n_vec2, size_t n_aux, const double
     BSG_CUDA(cudaMemsetAsync(cnt.p, 0, 16, s));
     Oz3cV v;
     oz3c_prepare_v(ctx, V, D, v);
-    oz3c_rows(ctx, D, sh, v, X, n_vec2, n_vec2, out, n_vec2, thresh, cnt.as<unsigned long long>());
+    // row ranges whose X digit images stay within 16 GB (one range for the
+    // 40-atom workload); the rows are independent, so ranges change nothing
+    const size_t row_img = D.nkb * (size_t)D.nd * sh.np * sh.kp * 2 / (size_t)D.J;  // image bytes per block row
+    const size_t nib = ceil_div(n_vec2, bs);
+    const size_t rb = std::max<size_t>(1, std::min(nib, (size_t)(16ull << 30) / std::max<size_t>(row_img, 1)));
+    const size_t rr = (rb >= nib ? nib : rb / (size_t)D.J * (size_t)D.J + (rb < (size_t)D.J ? (size_t)D.J : 0)) * bs;
+    for (size_t r0 = 0; r0 < n_vec2; r0 += rr)
+        oz3c_rows(ctx, D, sh, v, X + r0, n_vec2, std::min(rr, n_vec2 - r0), out + r0, n_vec2, thresh,
+                  cnt.as<unsigned long long>());
     ctx->gemm_check();
     if (nsig_out) {
         BSG_CUDA(cudaMemcpyAsync(nsig_out, cnt.p, 8, cudaMemcpyDeviceToHost, s));
