@@ -366,11 +366,11 @@ def run_rik_large(args):
     """The large RI-K configuration: 125 atoms in a 20 A box (n_bf 3000,
     n_aux 10500, n_occ 500), uniform 24-wide blocks (the per-atom shells of
     sizes 8-32 are not modelled), tau swept over 1e-6 .. 1e-12.  Per tau: one
-    timed mixed-form step on device-resident inputs (X is 45 GB), and the
-    error of each stage against the FP64 form on a sixteenth of it -- the
-    3c->2c transform on the first rows of X, the occ step on the first aux
-    functions of the mixed B (the full FP64 step does not fit the time budget:
-    about 35 x the mixed one).  A measurement case, not the bench line."""
+    timed mixed-form step on device-resident inputs (X is 45 GB), and errors
+    against the FP64 form on a sixteenth of the work: the 3c->2c output on the
+    first rows of X, and K of the whole pipeline over the first aux functions
+    (the full FP64 step does not fit the time budget: about 35 x the mixed
+    one).  A measurement case, not the bench line."""
     import torch
 
     from strassen_gb300 import api
@@ -411,17 +411,33 @@ def run_rik_large(args):
         e1.record()
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
-        # stage errors against the FP64 form on a sixteenth of each stage
+        # errors against the FP64 form: the 3c->2c output on the first sixteenth of
+        # the rows, and K of the whole pipeline (both forms from the same X) over
+        # the first sixteenth of the aux functions, which needs only those
+        # columns of B: FP64 B[:, :p_sub] = X V[:, :p_sub]
         b_oz = api.transform_3c2c(Xs, Vn, bs, thr, form=api.FORM_OZAKI, n_digits=args.digits_3c2c, ctx=ctx)
         b_64 = api.transform_3c2c(Xs, Vn, bs, thr, ctx=ctx)
-        Bs = np.asfortranarray(B[:, :p_sub].cpu().numpy())
-        k_oz = api.rik_occ_step(Bs, sysm.keys, Cn, n_bf, p_sub, n_occ, bs, thr, form=api.FORM_OZAKI,
-                                n_digits=args.digits_occ, ctx=ctx)
-        k_64 = api.rik_occ_step(Bs, sysm.keys, Cn, n_bf, p_sub, n_occ, bs, thr, ctx=ctx)
+        # FP64 form of those columns: matmult on block-sparse copies at threshold 0
+        # with the output pre-filled with zeros, as 3c_2c_transform.cpp:44-57 does
+        Xb = api.BlockSparseMatrix.from_dense(X, bs, bs, 0.0, ctx=ctx)
+        Vb = api.BlockSparseMatrix.from_dense(V[:, :p_sub], bs, bs, 0.0, ctx=ctx)
+        Cb = api.BlockSparseMatrix(n_vec2, p_sub, bs, bs, 0.0, ctx=ctx)
+        Cb.fill_with_values(0.0)
+        api.matmult(Cb, Xb, 0, Vb, 0, thr, 1.0, 1.0)
+        del Xb, Vb
+        B64 = torch.empty((p_sub, n_vec2), dtype=torch.float64, device=dev).T
+        Cb.to_matrix(out=B64)
+        del Cb
+        k_64 = api.rik_occ_step(B64, keys, C, n_bf, p_sub, n_occ, bs, thr, ctx=ctx,
+                                out=torch.empty((n_occ, n_bf), dtype=torch.float64, device=dev).T).cpu().numpy()
+        del B64
+        k_oz = api.rik_occ_step(B[:, :p_sub], keys, C, n_bf, p_sub, n_occ, bs, thr, form=api.FORM_OZAKI,
+                                n_digits=args.digits_occ, ctx=ctx,
+                                out=torch.empty((n_occ, n_bf), dtype=torch.float64, device=dev).T).cpu().numpy()
         rel = lambda a, b: float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
         res.append({"tau": thr, "ms_per_step": ms, "tflops_dense_equiv": (f3c + focc) / (ms * 1e-3) / 1e12,
-                    "rel_err_3c2c_rows_1_16": rel(b_oz, b_64), "rel_err_occ_aux_1_16": rel(k_oz, k_64)})
-        del b_oz, b_64, Bs
+                    "rel_err_3c2c_rows_1_16": rel(b_oz, b_64), "rel_err_K_aux_1_16": rel(k_oz, k_64)})
+        del b_oz, b_64
     print(json.dumps({"metric": "large RI-K step, mixed form, per tau", "unit": "ms",
                       "config": {"workload": f"125 atoms in a 20 A box, n_bf {n_bf}, n_aux {n_aux}, n_occ {n_occ}, "
                                              f"n_vec2 {n_vec2}, bs {bs} (uniform)",
