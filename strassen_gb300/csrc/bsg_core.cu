@@ -12,17 +12,12 @@
 
 namespace bsg {
 
-static thread_local int g_code = 0;
+// the message of the last failed call on this host thread (the status code
+// itself is what the call returns)
 static thread_local std::string g_msg;
 
-void set_error(int code, const std::string &msg) {
-    g_code = code;
-    g_msg = msg;
-}
-void clear_error() {
-    g_code = 0;
-    g_msg.clear();
-}
+void set_error(int, const std::string &msg) { g_msg = msg; }
+void clear_error() { g_msg.clear(); }
 
 DevBuf::DevBuf(size_t n, cudaStream_t st) : bytes(n), s(st) {
     if (n) {

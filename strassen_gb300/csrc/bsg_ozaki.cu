@@ -798,8 +798,7 @@ void oz_build_tiles(bsg_ctx ctx, const ScreenItems &si, const OzShape &sh, const
     size_t slot_no = 0;
     const size_t blk_elems = g.ibs * g.jbs;
     while (i < items.size()) {
-        OzTile T;
-        std::memset(&T, 0, sizeof(T));
+        OzTile T{};
         const uint32_t jb = si.item_jb[i];
         T.cexp = cexp + jb * g.jbs;
         T.cols = items[i].cols;
@@ -977,8 +976,7 @@ void ozaki_grid_products(bsg_ctx ctx, size_t n_prod, size_t n, const std::vector
     for (size_t i = 0; i < n_prod; ++i)
         for (size_t cb = 0; cb < n; ++cb)
             for (size_t g = 0; g < ng; ++g) {
-                OzTile T;
-                std::memset(&T, 0, sizeof(T));
+                OzTile T{};
                 for (int sl = 0; sl < sh.R; ++sl) {
                     const size_t rb = g * sh.R + sl;
                     if (rb >= n) break;

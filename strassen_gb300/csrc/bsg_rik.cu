@@ -465,7 +465,7 @@ bsg_status rik_entry(bsg_ctx ctx, const bsg_rik_args *a, double *K_out, double *
             dints = DevBuf(a->n_vec2 * a->n_aux * 8, s);
             dkeys = DevBuf(a->n_vec2 * 8, s);
             dc = DevBuf(a->n_bf * a->n_occ * 8, s);
-            if (a->n_vec2 * a->n_aux)
+            if (a->n_vec2 && a->n_aux)
                 BSG_CUDA(cudaMemcpyAsync(dints.p, a->ints, a->n_vec2 * a->n_aux * 8, cudaMemcpyHostToDevice, s));
             if (a->n_vec2) BSG_CUDA(cudaMemcpyAsync(dkeys.p, a->keys, a->n_vec2 * 8, cudaMemcpyHostToDevice, s));
             BSG_CUDA(cudaMemcpyAsync(dc.p, a->c_occ, a->n_bf * a->n_occ * 8, cudaMemcpyHostToDevice, s));
