@@ -357,38 +357,46 @@ __global__ void __launch_bounds__(kOzThreads, 1)
                         // the first MMA of a chain (digit 0, which spans every TMEM
                         // region) overwrites the accumulator
                         uint32_t first = (k == c * P.F) ? 1u : 0u;
-                        for (uint32_t q = 0; q < nq; ++q) {
-                            // the slice's descriptors first, then its MMAs back to back
-                            uint64_t aq, bq;
-                            if (!P.pair) {
-                                aq = a_desc0 + soff + q * 16u;
-                                bq = b_desc0 + soff + q * 16u;
-                            } else {
-                                const uint32_t g = 2u * q;  // first core column of the slice
-                                if (g + 1u < ncol) {        // both in the first half
-                                    aq = a_desc0 + soff + g * 8u;
-                                    bq = b_desc0 + soff + g * 8u;
-                                } else if (g + 1u == ncol) {  // straddles the halves
-                                    aq = a_descx + soff + g * 8u;
-                                    bq = b_descx + soff + g * 8u;
-                                } else {  // both in the second half
-                                    aq = a_desc0 + soff + ((half_bytes + (g - ncol) * 128u) >> 4);
-                                    bq = b_desc0 + soff + ((half_bytes + (g - ncol) * 128u) >> 4);
+                        // slice descriptors of this stage
+                        uint64_t aqs[8], bqs[8];
+#pragma unroll
+                        for (uint32_t q = 0; q < 8; ++q) {
+                            uint64_t aq = 0, bq = 0;
+                            if (q < nq) {
+                                if (!P.pair) {
+                                    aq = a_desc0 + soff + q * 16u;
+                                    bq = b_desc0 + soff + q * 16u;
+                                } else {
+                                    const uint32_t g = 2u * q;  // first core column of the slice
+                                    if (g + 1u < ncol) {        // both in the first half
+                                        aq = a_desc0 + soff + g * 8u;
+                                        bq = b_desc0 + soff + g * 8u;
+                                    } else if (g + 1u == ncol) {  // straddles the halves
+                                        aq = a_descx + soff + g * 8u;
+                                        bq = b_descx + soff + g * 8u;
+                                    } else {  // both in the second half
+                                        aq = a_desc0 + soff + ((half_bytes + (g - ncol) * 128u) >> 4);
+                                        bq = b_desc0 + soff + ((half_bytes + (g - ncol) * 128u) >> 4);
+                                    }
                                 }
                             }
-                            uint64_t ad[kMaxPlan], bd[kMaxPlan];
-                            uint32_t dt[kMaxPlan], ac[kMaxPlan];
+                            aqs[q] = aq;
+                            bqs[q] = bq;
+                        }
+                        // digit by digit, each over the stage's k16 slices: consecutive
+                        // MMAs accumulate into the same TMEM columns (a k chain), and
+                        // the first MMA of a chain (digit 0, which spans every region)
+                        // overwrites the accumulator
 #pragma unroll
-                            for (int e = 0; e < kMaxPlan; ++e) {
-                                ad[e] = aq + pa[e];
-                                bd[e] = bq + pb[e];
-                                dt[e] = dbase + (pd[e] & 0xFFFFu);
-                                ac[e] = (first & (pd[e] >> 16)) ? 0u : 1u;
+                        for (int e = 0; e < kMaxPlan; ++e) {
+                            if (e >= n_plan) break;
+                            const uint32_t dt = dbase + (pd[e] & 0xFFFFu);
+#pragma unroll
+                            for (uint32_t q = 0; q < 8; ++q) {
+                                if (q >= nq) break;
+                                const uint32_t ac = (first && q == 0 && (pd[e] >> 16)) ? 0u : 1u;
+                                tc::mma_bf16(dt, aqs[q] + pa[e], bqs[q] + pb[e], pi[e], ac);
                             }
-#pragma unroll
-                            for (int e = 0; e < kMaxPlan; ++e)
-                                if (e < n_plan) tc::mma_bf16(dt[e], ad[e], bd[e], pi[e], ac[e]);
-                            first = 0;
                         }
                         tc::mma_commit(&empty[stage]);
                         if (++stage == (uint32_t)P.S) {
