@@ -494,8 +494,24 @@ __global__ void __launch_bounds__(kOzThreads, 1)
                 const bool unit = P.alpha == 1.0;
                 // sub-blocks stored apart (J <= 2, so a group's NP/2 columns cross at
                 // most one sub-block boundary)
-                const bool subm = T.sub_cols != 0;
+                const int tcols = T.cols, tsub = T.sub_cols, tcexp_sub = T.cexp_sub, ttrans = T.trans;
+                const long long tsub_stride = T.sub_stride;
+                const int *tcexp = T.cexp;
+                const bool subm = tsub != 0;
                 const int npj = NP / P.J, js0 = cbase / npj;
+                // every column's exponent loaded before the first store (the stores
+                // could alias the exponent array, which would serialize the loads)
+                int cex[NPH];
+#pragma unroll
+                for (int j = 0; j < NPH; ++j) {
+                    const int c = cbase + j;
+                    int cc = c, js = 0;
+                    if (subm) {
+                        js = c >= (js0 + 1) * npj ? js0 + 1 : js0;
+                        cc = c - js * npj;
+                    }
+                    cex[j] = (c < tcols && (!subm || cc < tsub)) ? tcexp[subm ? js * tcexp_sub + cc : c] : 0;
+                }
                 // column j of this group: output address (null = not stored) and value
                 auto col_out = [&](int j, double *&dst) -> double {
                     const int c = cbase + j;
@@ -505,16 +521,15 @@ __global__ void __launch_bounds__(kOzThreads, 1)
                         cc = c - js * npj;
                     }
                     dst = nullptr;
-                    if (!(c < T.cols && (!subm || cc < T.sub_cols))) return 0.0;
+                    if (!(c < tcols && (!subm || cc < tsub))) return 0.0;
                     // both terms are exact doubles built with integer operations
                     // (|hi| < 2^53, lo 2^16 an FP32 value): one FP64 add rounds,
                     // and the power of two goes into the exponent field
                     const double tot = __dadd_rn(oz_i64_to_f64(hi[j]), oz_f32_to_f64(lo[j] * 65536.f));
-                    const int e = er + T.cexp[subm ? js * T.cexp_sub + cc : c];
-                    double out = oz_scale_pow2(tot, e);
+                    double out = oz_scale_pow2(tot, er + cex[j]);
                     if (!unit) out = __dmul_rn(P.alpha, out);
-                    double *base = subm ? cp + js * T.sub_stride : cp;
-                    dst = T.trans ? base + cc + (size_t)r * ldc : base + r + (size_t)cc * ldc;
+                    double *base = subm ? cp + js * tsub_stride : cp;
+                    dst = ttrans ? base + cc + (size_t)r * ldc : base + r + (size_t)cc * ldc;
                     return out;
                 };
 #pragma unroll
