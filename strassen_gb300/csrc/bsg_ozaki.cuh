@@ -182,25 +182,32 @@ struct OzDigits {
         lowb = 8 * (nd - 1);
         const long long C = nd > 1 ? (long long)(0x8080808080808080ull >> (64 - lowb)) : 0;
         T = oz_fixed(v, e, 7 + lowb) + C;
-        neg = v < 0;
+        neg = __double_as_longlong(v) < 0;  // the sign bit (an integer test, not an FP64 compare)
     }
     bool neg;
     __device__ __forceinline__ int digit(int i) const {
         if (i == 0) {
             const int d0 = (int)(T >> lowb);
-            return (d0 < 0 && !neg) ? d0 + 256 : d0;  // nd = 8: N = +2^63 wraps
+            // only at 8 digits can T overflow (N = +2^63 wraps)
+            return (lowb == 56 && d0 < 0 && !neg) ? d0 + 256 : d0;
         }
         if (lowb <= 32) return (int)(((unsigned int)T >> (lowb - 8 * i)) & 255u) - 128;
         return (int)((T >> (lowb - 8 * i)) & 255) - 128;
     }
+    // float bits of d_i 2^(-8i), sc = 2^(-8i): exact (a digit has at most 8
+    // significant bits, the product stays a normal float for i <= 7, zero
+    // stays zero), and the high half is the bf16 of the same value.  FP32
+    // multiplies and fmas stand in for integer subtracts and zero tests: the
+    // split is bound by the integer pipe.  Up to 5 digits a low digit is a
+    // byte of T's low word (one byte permute) and (byte - 128) sc is one fma.
+    __device__ __forceinline__ uint32_t digit_f32(int i, float sc) const {
+        if (i > 0 && lowb <= 32) {
+            const uint32_t b = __byte_perm((uint32_t)T, 0u, 0x4440u | (uint32_t)((lowb >> 3) - i));
+            return __float_as_uint(fmaf((float)b, sc, -128.0f * sc));
+        }
+        return __float_as_uint((float)digit(i) * sc);
+    }
 };
-
-// bf16 bits of d 2^(-8i) for an integer |d| <= 128 (exact; built from the
-// float bits of d with the exponent lowered by 8i)
-__device__ __forceinline__ uint32_t oz_digit_bf16(int d, int i) {
-    const uint32_t f = (__float_as_uint((float)d) - ((uint32_t)(8 * i) << 23)) >> 16;
-    return d ? f : 0u;
-}
 
 // Digit image of one block from a value source get(r, l) (image row r, k l),
 // 8 consecutive k per item and one 16-byte store per digit plane; items are
@@ -230,10 +237,11 @@ __device__ __forceinline__ void oz_block_image_g(const Get &get, int rows, int k
                          OzDigits(v[4], e, nd), OzDigits(v[5], e, nd), OzDigits(v[6], e, nd), OzDigits(v[7], e, nd)};
         // one digit plane at a time: four packed words live, not nd x 4
         for (int i = 0; i < nd; ++i) {
-            uint32_t w[4];
+            const float sc = __int_as_float((127 - 8 * i) << 23);  // 2^(-8i)
+            uint32_t w[4];  // two bf16 = the high halves of two floats (one byte permute)
 #pragma unroll
             for (int q = 0; q < 4; ++q)
-                w[q] = oz_digit_bf16(D[2 * q].digit(i), i) | (oz_digit_bf16(D[2 * q + 1].digit(i), i) << 16);
+                w[q] = __byte_perm(D[2 * q].digit_f32(i, sc), D[2 * q + 1].digit_f32(i, sc), 0x7632);
             *reinterpret_cast<uint4 *>(dst + i * plane + off) = make_uint4(w[0], w[1], w[2], w[3]);
         }
     }
