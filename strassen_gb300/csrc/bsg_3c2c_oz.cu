@@ -91,15 +91,29 @@ struct Dense3c {
 
 // N-side images of X: J consecutive block rows stacked along N, one image
 // per (group ibp, kb), index ibp + kb*nibp; block ib = J*ibp + j fills rows
-// j*bs.. of its group's image (rows of missing blocks are never read)
+// j*bs.. of its group's image (rows of missing blocks are never read).
+// kImgXBlocks consecutive blocks x = ib + kb*nib per warp.
+constexpr int kImgXBlocks = 4;
 __global__ void k_img_X(const double *__restrict__ X, const int *__restrict__ rexp, Dense3c D, bf16 *__restrict__ img) {
-    const size_t x = oz_warp_id();
-    if (x >= D.nib * D.nkb) return;
-    const size_t ib = x % D.nib, kb = x / D.nib, ibp = ib / D.J, j = ib % D.J;
-    bf16 *dst = img + (ibp + kb * D.nibp) * D.nd * (size_t)D.np * D.kp + j * D.bs * (size_t)D.kp;
-    oz_block_image_g(OzDenseGet{X + ib * D.bs + kb * D.bs * D.ldx, D.ldx, false}, ext3(ib, D.bs, D.n_vec2),
-                     ext3(kb, D.bs, D.n_aux), rexp + ib * D.bs, (int)D.bs, D.kp, D.nd, dst, false, threadIdx.x & 31, 32,
-                     D.np);
+    __shared__ OzImgJob sj[kOzImgWarps][kImgXBlocks];
+    const size_t x0 = oz_warp_id() * kImgXBlocks, n = D.nib * D.nkb;
+    if (x0 >= n) return;
+    oz_jobs_image(
+        kImgXBlocks,
+        [&](int q, OzImgJob &J) {
+            const size_t x = x0 + q;
+            if (x >= n) return false;
+            const size_t ib = x % D.nib, kb = x / D.nib, ibp = ib / D.J, j = ib % D.J;
+            J.get = OzDenseGet{X + ib * D.bs + kb * D.bs * D.ldx, D.ldx, false};
+            J.rows = ext3(ib, D.bs, D.n_vec2);
+            J.k = ext3(kb, D.bs, D.n_aux);
+            J.exps = rexp + ib * D.bs;
+            J.dst = img + (ibp + kb * D.nibp) * D.nd * (size_t)D.np * D.kp + j * D.bs * (size_t)D.kp;
+            J.m_side = false;
+            J.plane_rows = D.np;
+            return true;
+        },
+        (int)D.bs, D.kp, D.nd, sj[threadIdx.x >> 5]);
 }
 
 // M-side images of V^T blocks (jb, kb): image row = output column, index
@@ -271,7 +285,8 @@ void oz3c_rows(bsg_ctx ctx, Dense3c D, const OzShape &sh, const Oz3cV &v, const 
         X, ldx, rows, n_aux, bs, D.nib, D.nib * D.nkb, xn.as<double>(), rbits.as<unsigned long long>());
     k_bits_to_exp<<<(unsigned)ceil_div(rows, (size_t)256), 256, 0, s>>>(rbits.as<unsigned long long>(), rows,
                                                                         rexp.as<int>());
-    k_img_X<<<oz_img_grid(D.nib * D.nkb), 32 * kOzImgWarps, 0, s>>>(X, rexp.as<int>(), D, bi.as<bf16>());
+    k_img_X<<<oz_img_grid(ceil_div(D.nib * D.nkb, (size_t)kImgXBlocks)), 32 * kOzImgWarps, 0, s>>>(X, rexp.as<int>(), D,
+                                                                                              bi.as<bf16>());
     ctx->note_launch(3);
     ctx->check_launch("3c2c ozaki X prep");
     const size_t n_jg = ceil_div(D.njb, (size_t)D.R), n_tiles = D.nibp * n_jg;

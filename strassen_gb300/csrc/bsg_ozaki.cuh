@@ -209,42 +209,46 @@ struct OzDigits {
     }
 };
 
-// Digit image of one block from a value source get(r, l) (image row r, k l),
-// 8 consecutive k per item and one 16-byte store per digit plane; items are
-// spread over threads tid, tid + nthr, ...  exps[r] is the scale exponent of
-// image row r; rows >= `rows` and k >= `k` are zero.  m_side selects the
-// layout (M side of the MMA, or N side).
+// One item of a block's digit image from a value source get(r, l) (image row
+// r, k l): image row r = idx % mpad, 8 consecutive k from h*8, h = idx / mpad,
+// one 16-byte store per digit plane.  exps[r] is the scale exponent of image
+// row r; rows >= `rows` and k >= `k` are zero.  m_side selects the layout (M
+// side of the MMA, or N side); plane_rows (N side): rows of the image the
+// block is part of (a group of blocks stacked along N), 0 = mpad.
+template <class Get>
+__device__ __forceinline__ void oz_image_item(const Get &get, int rows, int k, const int *__restrict__ exps, int mpad,
+                                              int kp, int nd, __nv_bfloat16 *__restrict__ dst, bool m_side,
+                                              int plane_rows, int idx) {
+    const size_t plane = oz_plane_stride(m_side, plane_rows ? plane_rows : mpad, kp), rgs = oz_rg_stride(m_side, nd, kp);
+    const int r = idx % mpad, h = idx / mpad;
+    const size_t off = (size_t)(r >> 3) * rgs + (size_t)h * 64 + (size_t)(r & 7) * 8;
+    if (r >= rows || h * 8 >= k) {  // padding: all digits zero
+        for (int i = 0; i < nd; ++i) *reinterpret_cast<uint4 *>(dst + i * plane + off) = make_uint4(0, 0, 0, 0);
+        return;
+    }
+    const int e = exps[r];
+    double v[8];  // the eight loads first, then the splits
+#pragma unroll
+    for (int j = 0; j < 8; ++j) v[j] = h * 8 + j < k ? get(r, h * 8 + j) : 0.0;
+    OzDigits D[8] = {OzDigits(v[0], e, nd), OzDigits(v[1], e, nd), OzDigits(v[2], e, nd), OzDigits(v[3], e, nd),
+                     OzDigits(v[4], e, nd), OzDigits(v[5], e, nd), OzDigits(v[6], e, nd), OzDigits(v[7], e, nd)};
+    // one digit plane at a time: four packed words live, not nd x 4
+    for (int i = 0; i < nd; ++i) {
+        const float sc = __int_as_float((127 - 8 * i) << 23);  // 2^(-8i)
+        uint32_t w[4];  // two bf16 = the high halves of two floats (one byte permute)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) w[q] = __byte_perm(D[2 * q].digit_f32(i, sc), D[2 * q + 1].digit_f32(i, sc), 0x7632);
+        *reinterpret_cast<uint4 *>(dst + i * plane + off) = make_uint4(w[0], w[1], w[2], w[3]);
+    }
+}
+
+// Digit image of one block, items spread over threads tid, tid + nthr, ...
 template <class Get>
 __device__ __forceinline__ void oz_block_image_g(const Get &get, int rows, int k, const int *__restrict__ exps, int mpad,
                                                  int kp, int nd, __nv_bfloat16 *__restrict__ dst, bool m_side, int tid,
                                                  int nthr, int plane_rows = 0) {
-    // plane_rows (N side): rows of the image the block is part of (a group of
-    // blocks stacked along N), 0 = mpad
-    const size_t plane = oz_plane_stride(m_side, plane_rows ? plane_rows : mpad, kp), rgs = oz_rg_stride(m_side, nd, kp);
-    const int hk = kp >> 3;
-    for (int idx = tid; idx < mpad * hk; idx += nthr) {
-        const int r = idx % mpad, h = idx / mpad;
-        const size_t off = (size_t)(r >> 3) * rgs + (size_t)h * 64 + (size_t)(r & 7) * 8;
-        if (r >= rows || h * 8 >= k) {  // padding: all digits zero
-            for (int i = 0; i < nd; ++i) *reinterpret_cast<uint4 *>(dst + i * plane + off) = make_uint4(0, 0, 0, 0);
-            continue;
-        }
-        const int e = exps[r];
-        double v[8];  // the eight loads first, then the splits
-#pragma unroll
-        for (int j = 0; j < 8; ++j) v[j] = h * 8 + j < k ? get(r, h * 8 + j) : 0.0;
-        OzDigits D[8] = {OzDigits(v[0], e, nd), OzDigits(v[1], e, nd), OzDigits(v[2], e, nd), OzDigits(v[3], e, nd),
-                         OzDigits(v[4], e, nd), OzDigits(v[5], e, nd), OzDigits(v[6], e, nd), OzDigits(v[7], e, nd)};
-        // one digit plane at a time: four packed words live, not nd x 4
-        for (int i = 0; i < nd; ++i) {
-            const float sc = __int_as_float((127 - 8 * i) << 23);  // 2^(-8i)
-            uint32_t w[4];  // two bf16 = the high halves of two floats (one byte permute)
-#pragma unroll
-            for (int q = 0; q < 4; ++q)
-                w[q] = __byte_perm(D[2 * q].digit_f32(i, sc), D[2 * q + 1].digit_f32(i, sc), 0x7632);
-            *reinterpret_cast<uint4 *>(dst + i * plane + off) = make_uint4(w[0], w[1], w[2], w[3]);
-        }
-    }
+    for (int idx = tid; idx < mpad * (kp >> 3); idx += nthr)
+        oz_image_item(get, rows, k, exps, mpad, kp, nd, dst, m_side, plane_rows, idx);
 }
 
 // value source of a column-major block: b_role false: src[r + l*ld] (image
@@ -263,6 +267,42 @@ __device__ __forceinline__ void oz_block_image(const double *__restrict__ src, s
                                                int k, const int *__restrict__ exps, int mpad, int kp, int nd,
                                                __nv_bfloat16 *__restrict__ dst, bool m_side) {
     oz_block_image_g(OzDenseGet{src, ld, b_role}, rows, k, exps, mpad, kp, nd, dst, m_side, threadIdx.x & 31, 32);
+}
+
+// One block image of a warp's job list (see oz_jobs_image); rows < 0: none
+struct OzImgJob {
+    OzDenseGet get;
+    int rows, k;
+    const int *exps;
+    __nv_bfloat16 *dst;
+    int plane_rows;
+    bool m_side;
+};
+
+// Digit images of n_jobs <= 32 blocks by one warp, the items of consecutive
+// jobs back to back: a 24 x 24 block has 72 items, so one block per warp
+// leaves a quarter of the lanes idle in its last pass (the image kernels are
+// bound by the integer pipe).  Lane j describes job j once, job(j, J)
+// returning false for a job without an image, into the warp's table sj in
+// shared memory, which the items read.  Every job has the same mpad, kp and
+// nd.  The whole warp calls this.
+template <class JobFn>
+__device__ __forceinline__ void oz_jobs_image(int n_jobs, const JobFn &job, int mpad, int kp, int nd,
+                                              OzImgJob *__restrict__ sj) {
+    const int lane = threadIdx.x & 31, per = mpad * (kp >> 3);
+    if (lane < n_jobs) {
+        OzImgJob J;
+        if (!job(lane, J)) J.rows = -1;
+        sj[lane] = J;
+    }
+    __syncwarp();
+    for (int it = lane; it < n_jobs * per; it += 32) {
+        const int j = it / per;
+        const OzImgJob &J = sj[j];
+        if (J.rows >= 0)
+            oz_image_item(J.get, J.rows, J.k, J.exps, mpad, kp, nd, J.dst, J.m_side, J.plane_rows, it - j * per);
+    }
+    __syncwarp();
 }
 
 // One k step of a tile whose N side holds J block columns: live[j] = slots

@@ -185,22 +185,36 @@ __device__ __forceinline__ int rows_in_group(const OzDims &D) { return D.J == 1 
 
 
 // U_p blocks (a, b) as the N side of mui^T = C^T U^T (image rows = the
-// block's rows mu, k = its columns), from the dense copies; one warp per
-// occupied block w.  The blocks of Jm consecutive aux functions p = Jm*pp + j
-// share one image (index pp*nb*nb + a + b*nb), aux function j at rows j*bs.
+// block's rows mu, k = its columns), from the dense copies; kImgUBlocks
+// consecutive occupied blocks w per warp.  The blocks of Jm consecutive aux
+// functions p = Jm*pp + j share one image (index pp*nb*nb + a + b*nb), aux
+// function j at rows j*bs.
+constexpr int kImgUBlocks = 4;
 __global__ void k_img_U(const double *__restrict__ ucomp, const uint32_t *__restrict__ ob_list, size_t n_ob,
                         size_t n_p, const uint8_t *__restrict__ uflag, const int *__restrict__ rexp, OzDims D,
                         bf16 *__restrict__ img) {
-    const size_t w = oz_warp_id();
-    if (w >= n_p * n_ob) return;
-    const size_t p = w / n_ob, rr = ob_list[w % n_ob], a = rr % D.nb, b = rr / D.nb;
-    if (!uflag[p * D.nb * D.nb + rr]) return;
-    const size_t pp = p / D.Jm, j = p % D.Jm;
-    const int rows = ext_r(a, D.bs, D.n_bf);
-    bf16 *dst = img + (pp * D.nb * D.nb + rr) * D.nd * (size_t)D.npm * D.kp + j * D.bs * (size_t)D.kp;
-    oz_block_image_g(OzDenseGet{ucomp + w * D.bs * D.bs, (size_t)rows, false}, rows, ext_r(b, D.bs, D.n_bf),
-                     rexp + p * D.n_bf + a * D.bs, D.Jm == 1 ? D.npm : (int)D.bs, D.kp, D.nd, dst, false,
-                     threadIdx.x & 31, 32, D.npm);
+    __shared__ OzImgJob sj[kOzImgWarps][kImgUBlocks];
+    const size_t w0 = oz_warp_id() * kImgUBlocks, nw = n_p * n_ob;
+    if (w0 >= nw) return;
+    oz_jobs_image(
+        kImgUBlocks,
+        [&](int q, OzImgJob &J) {
+            const size_t w = w0 + q;
+            if (w >= nw) return false;
+            const size_t p = w / n_ob, rr = ob_list[w % n_ob], a = rr % D.nb, b = rr / D.nb;
+            if (!uflag[p * D.nb * D.nb + rr]) return false;
+            const size_t pp = p / D.Jm, j = p % D.Jm;
+            const int rows = ext_r(a, D.bs, D.n_bf);
+            J.get = OzDenseGet{ucomp + w * D.bs * D.bs, (size_t)rows, false};
+            J.rows = rows;
+            J.k = ext_r(b, D.bs, D.n_bf);
+            J.exps = rexp + p * D.n_bf + a * D.bs;
+            J.dst = img + (pp * D.nb * D.nb + rr) * D.nd * (size_t)D.npm * D.kp + j * D.bs * (size_t)D.kp;
+            J.m_side = false;
+            J.plane_rows = D.npm;
+            return true;
+        },
+        D.Jm == 1 ? D.npm : (int)D.bs, D.kp, D.nd, sj[threadIdx.x >> 5]);
 }
 
 // C^T blocks (ib, a) in the A role of ij = C^T mui and of mui^T = C^T U^T; index ib + a*nob
@@ -212,57 +226,107 @@ __global__ void k_img_Ct_A(const double *__restrict__ C, const int *__restrict__
                 cexp + ib * D.bs, D.mp, D.kp, D.nd, img + x * D.nd * (size_t)D.mp * D.kp, true);
 }
 
-// All digit images of one mui_p block in one pass (warp per (p, a, jb), jb <
-// nobp*J): the A image of the K and K_mn products (rows a, row exponents per
-// aux sub-range, index p*nb*nob + a + jb*nb), the J-grouped B image of ij
-// (imgB, rows jb, column exponents per aux function; columns past n_occ get
-// zero rows) and the B image of K_mn (imgT, rows a); null images are skipped.
-// The block is read from DRAM once, the second and third splits hit L1.
+// All digit images of mui_p blocks x = (p, a, jb), jb < nobp*J, kImgMBlocks
+// consecutive blocks per warp: the A image of the K and K_mn products (rows
+// a, row exponents per aux sub-range, index p*nb*nob + a + jb*nb), the
+// J-grouped B image of ij (imgB, rows jb, column exponents per aux function;
+// columns past n_occ get zero rows) and the B image of K_mn (imgT, rows a);
+// null images are skipped.  A block's B and A images are neighbouring jobs,
+// so the block is read from DRAM once and the second split hits L1.
+constexpr int kImgMBlocks = 2;
 __global__ void k_img_mui_all(const double *__restrict__ mui, const uint8_t *__restrict__ mflag,
                               const int *__restrict__ rexp, size_t Q, const int *__restrict__ cexp, OzDims D, size_t n,
                               bf16 *__restrict__ imgA, bf16 *__restrict__ imgB, bf16 *__restrict__ imgT) {
-    const size_t x = oz_warp_id();
-    if (x >= n) return;
-    const size_t nj = D.nobp * D.J, a = x % D.nb, jb = (x / D.nb) % nj, p = x / (D.nb * nj);
-    const size_t jbp = jb / D.J, j = jb % D.J;
-    const bool real = jb < D.nob;
-    const size_t xb = p * D.nb * D.nob + a + jb * D.nb;
-    if (real && !mflag[xb]) return;
-    const size_t jc = real ? jb : 0;
-    const double *M = mui + p * D.n_bf * D.n_occ + a * D.bs + jc * D.bs * D.n_bf;
-    const int ra = ext_r(a, D.bs, D.n_bf), rj = real ? ext_r(jb, D.bs, D.n_occ) : 0;
-    if (imgB)
-        oz_block_image_g(OzDenseGet{M, D.n_bf, true}, rj, real ? ra : 0, cexp + p * D.n_occ + jc * D.bs,
-                         rows_in_group(D), D.kp, D.nd,
-                         imgB + ((p * D.nobp + jbp) * D.nb + a) * D.nd * (size_t)D.npJ * D.kp + j * D.bs * (size_t)D.kp,
-                         false, threadIdx.x & 31, 32, D.npJ);
-    if (!real) return;
-    const int *re = rexp + (p / Q) * D.n_bf + a * D.bs;
-    if (imgA)
-        oz_block_image(M, D.n_bf, false, ra, rj, re, D.mp, D.kp, D.nd, imgA + xb * D.nd * (size_t)D.mp * D.kp, true);
-    if (imgT)  // K_mn's N side: block rows a of Jk-groups, image (p, jb, a / Jk), rows (a % Jk) * bs
-        oz_block_image_g(OzDenseGet{M, D.n_bf, false}, ra, rj, re, D.Jk == 1 ? D.npk : (int)D.bs, D.kp, D.nd,
+    __shared__ OzImgJob sj[kOzImgWarps][2 * kImgMBlocks];
+    const size_t x0 = oz_warp_id() * kImgMBlocks;
+    if (x0 >= n) return;
+    const size_t nj = D.nobp * D.J;
+    // job 2q: B image of block x0 + q, job 2q + 1: its A image
+    auto job = [&](int jj, OzImgJob &J) {
+        const size_t x = x0 + jj / 2;
+        if (x >= n) return false;
+        const size_t a = x % D.nb, jb = (x / D.nb) % nj, p = x / (D.nb * nj);
+        const bool real = jb < D.nob;
+        const size_t xb = p * D.nb * D.nob + a + jb * D.nb;
+        if (real && !mflag[xb]) return false;
+        const size_t jc = real ? jb : 0;
+        const double *M = mui + p * D.n_bf * D.n_occ + a * D.bs + jc * D.bs * D.n_bf;
+        const int ra = ext_r(a, D.bs, D.n_bf), rj = real ? ext_r(jb, D.bs, D.n_occ) : 0;
+        if (jj & 1) {
+            if (!real || !imgA) return false;
+            J.get = OzDenseGet{M, D.n_bf, false};
+            J.rows = ra;
+            J.k = rj;
+            J.exps = rexp + (p / Q) * D.n_bf + a * D.bs;
+            J.dst = imgA + xb * D.nd * (size_t)D.mp * D.kp;
+            J.m_side = true;
+            J.plane_rows = 0;
+        } else {
+            if (!imgB) return false;
+            const size_t jbp = jb / D.J, j = jb % D.J;
+            J.get = OzDenseGet{M, D.n_bf, true};
+            J.rows = rj;
+            J.k = real ? ra : 0;
+            J.exps = cexp + p * D.n_occ + jc * D.bs;
+            J.dst = imgB + ((p * D.nobp + jbp) * D.nb + a) * D.nd * (size_t)D.npJ * D.kp + j * D.bs * (size_t)D.kp;
+            J.m_side = false;
+            J.plane_rows = D.npJ;
+        }
+        return true;
+    };
+    OzImgJob *tab = sj[threadIdx.x >> 5];
+    const int mpB = rows_in_group(D);
+    if (mpB == D.mp) {
+        oz_jobs_image(2 * kImgMBlocks, job, D.mp, D.kp, D.nd, tab);
+    } else {  // different image heights: the B images, then the A images
+        oz_jobs_image(kImgMBlocks, [&](int q, OzImgJob &J) { return job(2 * q, J); }, mpB, D.kp, D.nd, tab);
+        oz_jobs_image(kImgMBlocks, [&](int q, OzImgJob &J) { return job(2 * q + 1, J); }, D.mp, D.kp, D.nd, tab);
+    }
+    if (!imgT) return;
+    for (int q = 0; q < kImgMBlocks; ++q) {
+        // K_mn's N side: block rows a of Jk-groups, image (p, jb, a / Jk), rows (a % Jk) * bs
+        const size_t x = x0 + q;
+        if (x >= n) break;
+        const size_t a = x % D.nb, jb = (x / D.nb) % nj, p = x / (D.nb * nj);
+        if (jb >= D.nob || !mflag[p * D.nb * D.nob + a + jb * D.nb]) continue;
+        const double *M = mui + p * D.n_bf * D.n_occ + a * D.bs + jb * D.bs * D.n_bf;
+        oz_block_image_g(OzDenseGet{M, D.n_bf, false}, ext_r(a, D.bs, D.n_bf), ext_r(jb, D.bs, D.n_occ),
+                         rexp + (p / Q) * D.n_bf + a * D.bs, D.Jk == 1 ? D.npk : (int)D.bs, D.kp, D.nd,
                          imgT + ((p * D.nob + jb) * D.nbp + a / D.Jk) * D.nd * (size_t)D.npk * D.kp +
                              (a % D.Jk) * D.bs * (size_t)D.kp,
                          false, threadIdx.x & 31, 32, D.npk);
+    }
 }
 
 // ijs_p blocks (ib, jb) in the B role of the K product, J block columns per
-// image: index p*nob*nobp + ib + jbp*nob; one warp per (p, ib, jb), jb < nobp*J
+// image: index p*nob*nobp + ib + jbp*nob; blocks x = (p, ib, jb), jb < nobp*J,
+// kImgSBlocks consecutive blocks per warp
+constexpr int kImgSBlocks = 4;
 __global__ void k_img_ijs_B(const double *__restrict__ ijs, const uint8_t *__restrict__ sflag,
                             const int *__restrict__ cexp, size_t Q, OzDims D, size_t n, bf16 *__restrict__ img) {
-    const size_t x = oz_warp_id();
-    if (x >= n) return;
-    const size_t nj = D.nobp * D.J, ib = x % D.nob, jb = (x / D.nob) % nj, p = x / (D.nob * nj);
-    const size_t jbp = jb / D.J, j = jb % D.J;
-    bf16 *dst = img + ((p * D.nobp + jbp) * D.nob + ib) * D.nd * (size_t)D.npJ * D.kp + j * D.bs * (size_t)D.kp;
-    const bool real = jb < D.nob;
-    if (real && !sflag[p * D.nob * D.nob + ib + jb * D.nob]) return;
-    const size_t jc = real ? jb : 0;
-    oz_block_image_g(OzDenseGet{ijs + p * D.n_occ * D.n_occ + ib * D.bs + jc * D.bs * D.n_occ, D.n_occ, true},
-                     real ? ext_r(jb, D.bs, D.n_occ) : 0, real ? ext_r(ib, D.bs, D.n_occ) : 0,
-                     cexp + (p / Q) * D.n_occ + jc * D.bs, rows_in_group(D), D.kp, D.nd, dst, false,
-                     threadIdx.x & 31, 32, D.npJ);
+    __shared__ OzImgJob sj[kOzImgWarps][kImgSBlocks];
+    const size_t x0 = oz_warp_id() * kImgSBlocks;
+    if (x0 >= n) return;
+    oz_jobs_image(
+        kImgSBlocks,
+        [&](int q, OzImgJob &J) {
+            const size_t x = x0 + q;
+            if (x >= n) return false;
+            const size_t nj = D.nobp * D.J, ib = x % D.nob, jb = (x / D.nob) % nj, p = x / (D.nob * nj);
+            const size_t jbp = jb / D.J, j = jb % D.J;
+            const bool real = jb < D.nob;
+            if (real && !sflag[p * D.nob * D.nob + ib + jb * D.nob]) return false;
+            const size_t jc = real ? jb : 0;
+            J.get = OzDenseGet{ijs + p * D.n_occ * D.n_occ + ib * D.bs + jc * D.bs * D.n_occ, D.n_occ, true};
+            J.rows = real ? ext_r(jb, D.bs, D.n_occ) : 0;
+            J.k = real ? ext_r(ib, D.bs, D.n_occ) : 0;
+            J.exps = cexp + (p / Q) * D.n_occ + jc * D.bs;
+            J.dst = img + ((p * D.nobp + jbp) * D.nob + ib) * D.nd * (size_t)D.npJ * D.kp + j * D.bs * (size_t)D.kp;
+            J.m_side = false;
+            J.plane_rows = D.npJ;
+            return true;
+        },
+        rows_in_group(D), D.kp, D.nd, sj[threadIdx.x >> 5]);
 }
 
 // ---- tiles and steps (one thread per tile) ----
@@ -822,7 +886,7 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
         }
         k_bits_to_exp<<<(unsigned)ceil_div(np * n_bf, (size_t)256), 256, 0, s>>>(bitsU, np * n_bf, drexpU.as<int>());
         if (n_ob)
-            k_img_U<<<oz_img_grid(np * n_ob), 32 * kOzImgWarps, 0, s>>>(ducomp.as<double>(), dob.as<uint32_t>(), n_ob,
+            k_img_U<<<oz_img_grid(ceil_div(np * n_ob, (size_t)kImgUBlocks)), 32 * kOzImgWarps, 0, s>>>(ducomp.as<double>(), dob.as<uint32_t>(), n_ob,
                                                                        np, duf.as<uint8_t>(), drexpU.as<int>(), D,
                                                                        dimgU.as<bf16>());
         const size_t tm = ceil_div(np, (size_t)Jm) * nb * ng_i;
@@ -845,7 +909,7 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
             k_bits_to_exp<<<(unsigned)ceil_div(np * n_occ, (size_t)256), 256, 0, s>>>(bitsM, np * n_occ,
                                                                                      dcexpM.as<int>());
         // every digit image of mui in one pass
-        k_img_mui_all<<<oz_img_grid(np * nb * nobp * J), 32 * kOzImgWarps, 0, s>>>(
+        k_img_mui_all<<<oz_img_grid(ceil_div(np * nb * nobp * J, (size_t)kImgMBlocks)), 32 * kOzImgWarps, 0, s>>>(
             dmui.as<double>(), dmf.as<uint8_t>(), drexpMs.as<int>(), Q, dcexpM.as<int>(), D, np * nb * nobp * J,
             dimgMA.as<bf16>(), want_k ? dimgMB.as<bf16>() : nullptr, want_kmn ? dimgMT.as<bf16>() : nullptr);
         ctx->note_launch(want_k ? 4 : 3);
@@ -881,7 +945,7 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
             dijs.as<double>(), dsf.as<uint8_t>(), n_occ, bs, nob, Q, np * nob * nob, bitsSs);
         k_bits_to_exp<<<(unsigned)ceil_div(n_sub * n_occ, (size_t)256), 256, 0, s>>>(bitsSs, n_sub * n_occ,
                                                                                   dcexpSs.as<int>());
-        k_img_ijs_B<<<oz_img_grid(np * nob * nobp * J), 32 * kOzImgWarps, 0, s>>>(
+        k_img_ijs_B<<<oz_img_grid(ceil_div(np * nob * nobp * J, (size_t)kImgSBlocks)), 32 * kOzImgWarps, 0, s>>>(
             dijs.as<double>(), dsf.as<uint8_t>(), dcexpSs.as<int>(), Q, D, np * nob * nobp * J, dimgSB.as<bf16>());
         const size_t tk = n_sub * nobp * ng_a;
         k_tiles_K<<<oz_img_grid(tk), 32 * kOzImgWarps, 0, s>>>(
