@@ -30,25 +30,34 @@ __global__ void k_dense_norms(const double *__restrict__ M, size_t ld, size_t nr
     if ((threadIdx.x & 31) == 0) norm[b] = est;
 }
 
-// block norms of X (warp per block, the deterministic order) and the block's
-// row maxima folded into row_bits (bit patterns of |x|, atomicMax), one pass
+// block norms of X (the deterministic order) and the blocks' row maxima
+// folded into row_bits (bit patterns of |x|, atomicMax), one pass;
+// kNormBlocks consecutive blocks per warp, their norms finished from the
+// warp's table of chains (norm_from_chains), kXnWarps warps per CTA
+constexpr int kXnWarps = 8;
 __global__ void k_xnorm_rowmax(const double *__restrict__ X, size_t ld, size_t nr, size_t nc, size_t bs, size_t nrb,
                                size_t nblk, double *__restrict__ norm, unsigned long long *__restrict__ row_bits) {
-    const size_t b = (size_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
-    if (b >= nblk) return;
-    const size_t rb = b % nrb, cb = b / nrb;
-    const int rows = ext3(rb, bs, nr), cols = ext3(cb, bs, nc);
-    const double *M = X + rb * bs + cb * bs * ld;
-    const double est = warp_block_norm(M, rows, cols, ld);
-    if ((threadIdx.x & 31) == 0) norm[b] = est;
-    for (int r = threadIdx.x & 31; r < rows; r += 32) {
-        long long mx = 0;
-        for (int l = 0; l < cols; ++l) {
-            const long long v = oz_absbits(M[r + (size_t)l * ld]);
-            mx = v > mx ? v : mx;
+    __shared__ NormTable tab[kXnWarps];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const size_t b0 = ((size_t)blockIdx.x * kXnWarps + w) * kNormBlocks;
+    if (b0 >= nblk) return;
+    const int nq = (int)min((size_t)kNormBlocks, nblk - b0);
+    for (int q = 0; q < nq; ++q) {
+        const size_t b = b0 + q, rb = b % nrb, cb = b / nrb;
+        const int rows = ext3(rb, bs, nr), cols = ext3(cb, bs, nc);
+        const double *M = X + rb * bs + cb * bs * ld;
+        tab[w][q][lane] = warp_norm_chain(M, rows, cols, ld);
+        for (int r = lane; r < rows; r += 32) {
+            long long mx = 0;
+            for (int l = 0; l < cols; ++l) {
+                const long long v = oz_absbits(M[r + (size_t)l * ld]);
+                mx = v > mx ? v : mx;
+            }
+            if (mx) atomicMax(&row_bits[rb * bs + r], (unsigned long long)mx);
         }
-        if (mx) atomicMax(&row_bits[rb * bs + r], (unsigned long long)mx);
     }
+    __syncwarp();
+    if (lane < nq) norm[b0 + lane] = norm_from_chains(tab[w][lane]);
 }
 
 // exponent of every column of V (over all rows); one block per column
@@ -278,10 +287,9 @@ void oz3c_rows(bsg_ctx ctx, Dense3c D, const OzShape &sh, const Oz3cV &v, const 
     D.nibp = ceil_div(D.nib, (size_t)D.J);
     const size_t a_img = (size_t)D.nd * sh.mp * sh.kp, b_img = (size_t)D.nd * sh.np * sh.kp;
     DevBuf xn(D.nib * D.nkb * 8, s), rexp(rows * 4, s), bi(D.nibp * D.nkb * b_img * 2, s);
-    const int wpb = 8;
     DevBuf rbits(rows * 8, s);
     BSG_CUDA(cudaMemsetAsync(rbits.p, 0, rows * 8, s));
-    k_xnorm_rowmax<<<(unsigned)ceil_div(D.nib * D.nkb, wpb), wpb * 32, 0, s>>>(
+    k_xnorm_rowmax<<<(unsigned)ceil_div(D.nib * D.nkb, (size_t)kXnWarps * kNormBlocks), kXnWarps * 32, 0, s>>>(
         X, ldx, rows, n_aux, bs, D.nib, D.nib * D.nkb, xn.as<double>(), rbits.as<unsigned long long>());
     k_bits_to_exp<<<(unsigned)ceil_div(rows, (size_t)256), 256, 0, s>>>(rbits.as<unsigned long long>(), rows,
                                                                         rexp.as<int>());

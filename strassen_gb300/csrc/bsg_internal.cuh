@@ -165,7 +165,8 @@ void launch_zero_blocks(bsg_bsm m, const uint8_t *d_sel, cudaStream_t s);
 // computed by one full warp in the fixed order: lane l accumulates
 // fma(x_i, x_i, s) over column-major element indices i = l, l+32, ...; then
 // s_l += s_{l+o} for o = 16..1; lane 0 returns sqrt(s_0).
-__device__ __forceinline__ double warp_block_norm(const double *__restrict__ p, int rs, int cs, size_t ld) {
+// The lane's chain s_l (the first half of the definition).
+__device__ __forceinline__ double warp_norm_chain(const double *__restrict__ p, int rs, int cs, size_t ld) {
     const int lane = threadIdx.x & 31;
     double acc = 0.0;
     const int n = rs * cs;
@@ -174,7 +175,34 @@ __device__ __forceinline__ double warp_block_norm(const double *__restrict__ p, 
         const double v = p[(size_t)r + (size_t)c * ld];
         acc = fma(v, v, acc);
     }
+    return acc;
+}
+
+__device__ __forceinline__ double warp_block_norm(const double *__restrict__ p, int rs, int cs, size_t ld) {
+    double acc = warp_norm_chain(p, rs, cs, ld);
 #pragma unroll
     for (int o = 16; o >= 1; o >>= 1) acc = __dadd_rn(acc, __shfl_down_sync(0xffffffffu, acc, o));
     return sqrt(acc);
 }
+
+// The same norm from the 32 chains s[0..31] of one block, by one thread: the
+// shuffle tree above as plain adds (level o adds s_{l+o} to s_l, l < o, o =
+// 16 .. 1) and the square root.  Kernels that hold several blocks' chains in
+// shared memory let lane q finish block q, so the FP64 pipe (the bound of the
+// norm passes on this part) runs the tree and the square root once per
+// kNormBlocks blocks instead of warp-wide for every block.
+__device__ __forceinline__ double norm_from_chains(const double *s) {
+    double t[16];
+#pragma unroll
+    for (int l = 0; l < 16; ++l) t[l] = __dadd_rn(s[l], s[l + 16]);
+#pragma unroll
+    for (int o = 8; o >= 1; o >>= 1)
+#pragma unroll
+        for (int l = 0; l < o; ++l) t[l] = __dadd_rn(t[l], t[l + o]);
+    return sqrt(t[0]);
+}
+
+// blocks per warp of the batched norm passes, and the per-warp table of their
+// chains (33 doubles per block: lane q reading row q meets no bank conflict)
+constexpr int kNormBlocks = 8;
+using NormTable = double[kNormBlocks][33];

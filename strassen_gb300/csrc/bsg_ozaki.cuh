@@ -364,6 +364,14 @@ __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
     return v;
 }
 
+// warp maximum of a 64-bit value by two 32-bit reductions: the high words,
+// then the low words of the lanes that hold the high maximum
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
+    const uint32_t hi = __reduce_max_sync(0xffffffffu, (uint32_t)(v >> 32));
+    const uint32_t lo = __reduce_max_sync(0xffffffffu, (uint32_t)(v >> 32) == hi ? (uint32_t)v : 0u);
+    return ((unsigned long long)hi << 32) | lo;
+}
+
 // exponents from maxima bit patterns (bsg_ozaki.cu): exps[i] = frexp exponent of bits[i]
 __global__ void k_bits_to_exp(const unsigned long long *__restrict__ bits, size_t n, int *__restrict__ exps);
 

@@ -715,40 +715,58 @@ __global__ void k_Kmn_mirror(double *__restrict__ K, size_t n_bf, size_t bs) {
     if (bi < bj || (bi == bj && gi < gj)) K[e] = K[gj + gi * n_bf];
 }
 
-// One pass over each present mui_p block (warp per block): its FP64 norm
-// (the deterministic block-norm order), its row maxima per aux sub-range p/Q
-// (rows of the A operand of K and K_mn) and, when col_bits is given, its
-// column maxima per p (columns of the B operand of ij).  The block is read
-// from DRAM once; the second and third walks hit L1.
+// One pass over each present mui_p block (kNormBlocks consecutive blocks per
+// warp): its FP64 norm (the deterministic block-norm order, finished from the
+// warp's table of chains), its row maxima per aux sub-range p/Q (rows of the
+// A operand of K and K_mn) and, when col_bits is given, its column maxima per
+// p (columns of the B operand of ij).  The block is read from DRAM once; the
+// maxima walk hits L1.
 __global__ void k_mui_stats(const double *__restrict__ mui, const uint8_t *__restrict__ mflag, size_t n_bf,
                             size_t n_occ, size_t bs, size_t nb, size_t nob, size_t Q, size_t n,
                             double *__restrict__ mnorm, unsigned long long *__restrict__ row_bits,
                             unsigned long long *__restrict__ col_bits) {
-    const size_t x = oz_warp_id();
-    if (x >= n || !mflag[x]) return;
-    const size_t p = x / (nb * nob), a = x % nb, jb = (x / nb) % nob;
-    const int rows = ext_r(a, bs, n_bf), cols = ext_r(jb, bs, n_occ);
-    const double *M = mui + p * n_bf * n_occ + a * bs + jb * bs * n_bf;
-    const double est = warp_block_norm(M, rows, cols, n_bf);
-    const int lane = threadIdx.x & 31;
-    if (lane == 0) mnorm[x] = est;
-    for (int r = lane; r < rows; r += 32) {
-        long long mx = 0;
+    __shared__ NormTable tab[kOzImgWarps];
+    const size_t x0 = oz_warp_id() * kNormBlocks;
+    if (x0 >= n) return;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nq = (int)min((size_t)kNormBlocks, n - x0);
+    for (int q = 0; q < nq; ++q) {
+        const size_t x = x0 + q;
+        if (!mflag[x]) continue;
+        const size_t p = x / (nb * nob), a = x % nb, jb = (x / nb) % nob;
+        const int rows = ext_r(a, bs, n_bf), cols = ext_r(jb, bs, n_occ);
+        const double *M = mui + p * n_bf * n_occ + a * bs + jb * bs * n_bf;
+        tab[w][q][lane] = warp_norm_chain(M, rows, cols, n_bf);
+        // one walk over the columns with the lanes over rows (bs <= 64: rows
+        // lane and lane + 32), so every step reads one column coalesced; a
+        // column's maximum is a warp reduction, kept by lane l % 32
+        unsigned long long rmx[2] = {0, 0}, cmx[2] = {0, 0};
+#pragma unroll 4
         for (int l = 0; l < cols; ++l) {
-            const long long bb_ = oz_absbits(M[r + (size_t)l * n_bf]);
-            mx = bb_ > mx ? bb_ : mx;
+            const double *col = M + (size_t)l * n_bf;
+            unsigned long long cm = 0;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int r = lane + 32 * h;
+                if (r < rows) {
+                    const unsigned long long bb = (unsigned long long)oz_absbits(col[r]);
+                    rmx[h] = bb > rmx[h] ? bb : rmx[h];
+                    cm = bb > cm ? bb : cm;
+                }
+            }
+            if (col_bits) {
+                cm = warp_max_u64(cm);
+                if (lane == (l & 31)) (l < 32 ? cmx[0] : cmx[1]) = cm;
+            }
         }
-        if (mx) atomicMax(&row_bits[(p / Q) * n_bf + a * bs + r], (unsigned long long)mx);
-    }
-    if (!col_bits) return;
-    for (int c = lane; c < cols; c += 32) {
-        long long mx = 0;
-        for (int r = 0; r < rows; ++r) {
-            const long long bb_ = oz_absbits(M[r + (size_t)c * n_bf]);
-            mx = bb_ > mx ? bb_ : mx;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int r = lane + 32 * h;
+            if (r < rows && rmx[h]) atomicMax(&row_bits[(p / Q) * n_bf + a * bs + r], rmx[h]);
+            if (col_bits && r < cols && cmx[h]) atomicMax(&col_bits[p * n_occ + jb * bs + r], cmx[h]);
         }
-        if (mx) atomicMax(&col_bits[p * n_occ + jb * bs + c], (unsigned long long)mx);
     }
+    __syncwarp();
+    if (lane < nq && mflag[x0 + lane]) mnorm[x0 + lane] = norm_from_chains(tab[w][lane]);
 }
 
 void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uint64_t stats[6]) {
@@ -900,7 +918,7 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
                macs + 0);
         // mui norms, row exponents per sub-range (A operand of K and of K_mn)
         // and column exponents per aux function (B operand of ij)
-        k_mui_stats<<<oz_img_grid(np * nb * nob), 32 * kOzImgWarps, 0, s>>>(
+        k_mui_stats<<<oz_img_grid(ceil_div(np * nb * nob, (size_t)kNormBlocks)), 32 * kOzImgWarps, 0, s>>>(
             dmui.as<double>(), dmf.as<uint8_t>(), n_bf, n_occ, bs, nb, nob, Q, np * nb * nob, dmn.as<double>(), bitsMs,
             want_k ? bitsM : nullptr);
         k_bits_to_exp<<<(unsigned)ceil_div(n_sub * n_bf, (size_t)256), 256, 0, s>>>(bitsMs, n_sub * n_bf,
