@@ -42,10 +42,11 @@ void ctx_release(bsg_ctx c) {
     if (c->refs.fetch_sub(1) == 1) {
         cudaStreamSynchronize(c->stream);
         if (c->d_gemm_err) cudaFree(c->d_gemm_err);
-        if (c->copy_stream) {
-            cudaStreamSynchronize(c->copy_stream);
-            cudaStreamDestroy(c->copy_stream);
-        }
+        for (cudaStream_t x : {c->copy_stream, c->chain_hi, c->side_lo})
+            if (x) {
+                cudaStreamSynchronize(x);
+                cudaStreamDestroy(x);
+            }
         if (c->own_stream) cudaStreamDestroy(c->stream);
         delete c;
     }
@@ -66,6 +67,24 @@ void bsg_ctx_s::check_launch(const char *what) {
 cudaStream_t bsg_ctx_s::upload_stream() {
     if (!copy_stream) BSG_CUDA(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking));
     return copy_stream;
+}
+
+cudaStream_t bsg_ctx_s::chain_stream() {
+    if (!chain_hi) {
+        int least = 0, greatest = 0;
+        BSG_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        BSG_CUDA(cudaStreamCreateWithPriority(&chain_hi, cudaStreamNonBlocking, greatest));
+    }
+    return chain_hi;
+}
+
+cudaStream_t bsg_ctx_s::side_stream() {
+    if (!side_lo) {
+        int least = 0, greatest = 0;
+        BSG_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        BSG_CUDA(cudaStreamCreateWithPriority(&side_lo, cudaStreamNonBlocking, least));
+    }
+    return side_lo;
 }
 
 int *bsg_ctx_s::gemm_err_flag() {

@@ -108,6 +108,13 @@ struct bsg_ctx_s {
     // (created on first use, released with the context)
     cudaStream_t copy_stream = 0;
     cudaStream_t upload_stream();
+    // a highest-priority stream for a dependent kernel chain and a lowest-
+    // priority one for work overlapped with it: with the chain's persistent
+    // GEMM at the higher priority, blocks of the side work never hold it back
+    // (both created on first use, released with the context)
+    cudaStream_t chain_hi = 0, side_lo = 0;
+    cudaStream_t chain_stream();
+    cudaStream_t side_stream();
     void note_launch(uint64_t n = 1) { launches += n; }
     void check_launch(const char *what);
     int *gemm_err_flag();  // the device flag, cleared before the first launch of a call

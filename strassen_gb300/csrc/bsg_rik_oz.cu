@@ -769,6 +769,54 @@ __global__ void k_mui_stats(const double *__restrict__ mui, const uint8_t *__res
     if (lane < nq && mflag[x0 + lane]) mnorm[x0 + lane] = norm_from_chains(tab[w][lane]);
 }
 
+// Two streams forked off a caller's stream: both wait for the caller's work
+// so far; join() makes the caller's stream wait for both.  The destructor
+// joins too when join() was not reached (an error path), so no kernel of the
+// fork outlives the stream-ordered frees of the caller's buffers.  Also holds
+// the events that order the U sets between the two streams.
+struct StreamFork {
+    cudaStream_t base, a, b;
+    cudaEvent_t start = nullptr, end_a = nullptr, end_b = nullptr;
+    cudaEvent_t u_ready[2] = {nullptr, nullptr}, u_done[2] = {nullptr, nullptr};
+    bool joined = false;
+    StreamFork(cudaStream_t base_, cudaStream_t a_, cudaStream_t b_) : base(base_), a(a_), b(b_) {
+        for (cudaEvent_t *e : {&start, &end_a, &end_b, &u_ready[0], &u_ready[1], &u_done[0], &u_done[1]})
+            if (cudaEventCreateWithFlags(e, cudaEventDisableTiming) != cudaSuccess) {
+                *e = nullptr;
+                release();
+                throw Error{BSG_ERR_CUDA, "stream fork: event creation failed"};
+            }
+        if (cudaEventRecord(start, base) != cudaSuccess || cudaStreamWaitEvent(a, start, 0) != cudaSuccess ||
+            cudaStreamWaitEvent(b, start, 0) != cudaSuccess) {
+            release();
+            throw Error{BSG_ERR_CUDA, "stream fork: ordering the streams failed"};
+        }
+    }
+    void join() {
+        BSG_CUDA(cudaEventRecord(end_a, a));
+        BSG_CUDA(cudaEventRecord(end_b, b));
+        BSG_CUDA(cudaStreamWaitEvent(base, end_a, 0));
+        BSG_CUDA(cudaStreamWaitEvent(base, end_b, 0));
+        joined = true;
+    }
+    void release() {
+        for (cudaEvent_t e : {start, end_a, end_b, u_ready[0], u_ready[1], u_done[0], u_done[1]})
+            if (e) cudaEventDestroy(e);
+        start = end_a = end_b = u_ready[0] = u_ready[1] = u_done[0] = u_done[1] = nullptr;
+    }
+    ~StreamFork() {
+        if (!joined && end_a && end_b) {  // error path; nothing here throws
+            cudaEventRecord(end_a, a);
+            cudaEventRecord(end_b, b);
+            cudaStreamWaitEvent(base, end_a, 0);
+            cudaStreamWaitEvent(base, end_b, 0);
+        }
+        release();
+    }
+    StreamFork(const StreamFork &) = delete;
+    StreamFork &operator=(const StreamFork &) = delete;
+};
+
 void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uint64_t stats[6]) {
     cudaStream_t s = ctx->stream;
     const size_t n_bf = d.n_bf, n_occ = d.n_occ, bs = d.bs, n_aux = d.n_aux;
@@ -831,19 +879,26 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
     pc = std::max<size_t>(1, std::min(pc, n_aux));
     const size_t n_sub_max = ceil_div(pc, Q);
 
-    DevBuf dinv(n_bf * n_bf * 4, s), docc(nb * nb, s), dun(pc * nb * nb * 8, s), duf(pc * nb * nb, s);
+    DevBuf dinv(n_bf * n_bf * 4, s), docc(nb * nb, s);
+    // the U set (norms, flags, row maxima, row exponents, dense copies,
+    // images) twice: the next chunk's U pass runs on a side stream while this
+    // chunk's products run
+    DevBuf dun[2] = {DevBuf(pc * nb * nb * 8, s), DevBuf(pc * nb * nb * 8, s)};
+    DevBuf duf[2] = {DevBuf(pc * nb * nb, s), DevBuf(pc * nb * nb, s)};
     DevBuf dmui(pc * n_bf * n_occ * 8, s), dmn(pc * nb * nob * 8, s), dmf(pc * nb * nob, s);
     DevBuf dij(pc * n_occ * n_occ * 8, s), dijf(pc * nob * nob, s);
     DevBuf dijs(pc * n_occ * n_occ * 8, s), dsn(pc * nob * nob * 8, s), dsf(pc * nob * nob, s);
     DevBuf dcn(nb * nob * 8, s), dcexpC(nob * bs * 4, s), dimgCtA(nob * nb * a_img * 2, s);
-    DevBuf drexpU(pc * n_bf * 4, s), dimgU(ceil_div(pc, (size_t)Jm) * nb * nb * b_imgM * 2, s);
+    DevBuf drexpU[2] = {DevBuf(pc * n_bf * 4, s), DevBuf(pc * n_bf * 4, s)};
+    DevBuf dbitsU[2] = {DevBuf(pc * n_bf * 8, s), DevBuf(pc * n_bf * 8, s)};
+    const size_t u_img_bytes = ceil_div(pc, (size_t)Jm) * nb * nb * b_imgM * 2;
+    DevBuf dimgU[2] = {DevBuf(u_img_bytes, s), DevBuf(u_img_bytes, s)};
     DevBuf dcexpM(pc * n_occ * 4, s), dimgMB(pc * nb * nobp * b_imgJ * 2, s);
     DevBuf drexpMs(n_sub_max * n_bf * 4, s), dcexpSs(n_sub_max * n_occ * 4, s);
-    // maxima bit patterns for the four exponent sets of a chunk
-    const size_t nbits = pc * n_bf + pc * n_occ + n_sub_max * n_bf + n_sub_max * n_occ;
+    // maxima bit patterns for the three exponent sets of a chunk's mui and ijs
+    const size_t nbits = pc * n_occ + n_sub_max * n_bf + n_sub_max * n_occ;
     DevBuf dbits(nbits * 8, s);
-    auto *bitsU = dbits.as<unsigned long long>(), *bitsM = bitsU + pc * n_bf, *bitsMs = bitsM + pc * n_occ,
-         *bitsSs = bitsMs + n_sub_max * n_bf;
+    auto *bitsM = dbits.as<unsigned long long>(), *bitsMs = bitsM + pc * n_occ, *bitsSs = bitsMs + n_sub_max * n_bf;
     DevBuf dimgMA(pc * nb * nob * a_img * 2, s), dimgSB(pc * nob * nobp * b_imgJ * 2, s);
     DevBuf dKp(want_k ? n_sub_max * nobp * nb * bs * bs * J * 8 : 0, s), dcnt(6 * 8, s), dmacs(4 * 8, s);
     const size_t ng_a = ceil_div(nb, (size_t)D.R), ng_i = ceil_div(nob, (size_t)D.R);
@@ -884,38 +939,71 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
     for (size_t rr = 0; rr < nb * nb; ++rr)
         if (hocc[rr]) hob.push_back((uint32_t)rr);
     const size_t n_ob = hob.size();
-    DevBuf dob(std::max<size_t>(1, n_ob) * 4, s), ducomp(std::max<size_t>(1, pc * n_ob) * bs * bs * 8, s);
+    const size_t ucomp_bytes = std::max<size_t>(1, pc * n_ob) * bs * bs * 8;
+    DevBuf dob(std::max<size_t>(1, n_ob) * 4, s), ducomp[2] = {DevBuf(ucomp_bytes, s), DevBuf(ucomp_bytes, s)};
     if (n_ob) BSG_CUDA(cudaMemcpyAsync(dob.p, hob.data(), n_ob * 4, cudaMemcpyHostToDevice, s));
     const double tpb_u = 1e-20 * (double)(bs * bs);
     const double tpb = d.thresh * (double)(bs * bs * bs);
-    for (size_t P0 = 0; P0 < n_aux; P0 += pc) {
-        const size_t np = std::min(pc, n_aux - P0), n_sub = ceil_div(np, Q);
-        BSG_CUDA(cudaMemsetAsync(macs, 0, 4 * 8, s));
+
+    // Two streams from here on: the products of each chunk on a high-priority
+    // chain stream, the U pass of the next chunk on a low-priority side
+    // stream.  u_ready[x]: U set x written; u_done[x]: the mui product that
+    // read U set x finished (the set may be overwritten).  Both join the
+    // caller's stream before the checks and the statistics, and on any exit.
+    ctx->gemm_err_flag();  // cleared on the caller's stream, ahead of the fork
+    const cudaStream_t hs = ctx->chain_stream(), ss = ctx->side_stream();
+    StreamFork fork(s, hs, ss);
+    auto u_pass = [&](size_t P0, int x) {
         // U_p block norms, keep flags, row exponents and digit images, all
         // gathered from the compressed integrals
-        BSG_CUDA(cudaMemsetAsync(dun.p, 0, np * nb * nb * 8, s));
-        BSG_CUDA(cudaMemsetAsync(duf.p, 0, np * nb * nb, s));
+        const size_t np = std::min(pc, n_aux - P0);
+        BSG_CUDA(cudaMemsetAsync(dun[x].p, 0, np * nb * nb * 8, ss));
+        BSG_CUDA(cudaMemsetAsync(duf[x].p, 0, np * nb * nb, ss));
+        BSG_CUDA(cudaMemsetAsync(dbitsU[x].p, 0, np * n_bf * 8, ss));
+        auto *bitsU = dbitsU[x].as<unsigned long long>();
+        if (n_ob) {
+            k_unorms_c<<<oz_img_grid(np * n_ob), 32 * kOzImgWarps, 0, ss>>>(
+                d.ints, dinv.as<int>(), dob.as<uint32_t>(), n_ob, d.n_vec2, P0, n_bf, bs, nb, np, tpb_u,
+                dun[x].as<double>(), duf[x].as<uint8_t>(), ducomp[x].as<double>(), bitsU);
+        }
+        k_bits_to_exp<<<(unsigned)ceil_div(np * n_bf, (size_t)256), 256, 0, ss>>>(bitsU, np * n_bf,
+                                                                                   drexpU[x].as<int>());
+        if (n_ob)
+            k_img_U<<<oz_img_grid(ceil_div(np * n_ob, (size_t)kImgUBlocks)), 32 * kOzImgWarps, 0, ss>>>(
+                ducomp[x].as<double>(), dob.as<uint32_t>(), n_ob, np, duf[x].as<uint8_t>(), drexpU[x].as<int>(), D,
+                dimgU[x].as<bf16>());
+        ctx->note_launch(n_ob ? 3 : 1);
+        ctx->check_launch("rik ozaki U pass");
+        BSG_CUDA(cudaEventRecord(fork.u_ready[x], ss));
+    };
+    s = hs;
+    u_pass(0, 0);
+    int ux = 0;  // U set of the current chunk
+    for (size_t P0 = 0; P0 < n_aux; P0 += pc, ux ^= 1) {
+        const size_t np = std::min(pc, n_aux - P0), n_sub = ceil_div(np, Q);
+        BSG_CUDA(cudaStreamWaitEvent(s, fork.u_ready[ux], 0));
+        auto &dun_ = dun[ux], &duf_ = duf[ux], &drexpU_ = drexpU[ux], &dimgU_ = dimgU[ux];
+        BSG_CUDA(cudaMemsetAsync(macs, 0, 4 * 8, s));
         // mui = U C
         BSG_CUDA(cudaMemsetAsync(dbits.p, 0, nbits * 8, s));
-        if (n_ob) {
-            k_unorms_c<<<oz_img_grid(np * n_ob), 32 * kOzImgWarps, 0, s>>>(
-                d.ints, dinv.as<int>(), dob.as<uint32_t>(), n_ob, d.n_vec2, P0, n_bf, bs, nb, np, tpb_u,
-                dun.as<double>(), duf.as<uint8_t>(), ducomp.as<double>(), bitsU);
-        }
-        k_bits_to_exp<<<(unsigned)ceil_div(np * n_bf, (size_t)256), 256, 0, s>>>(bitsU, np * n_bf, drexpU.as<int>());
-        if (n_ob)
-            k_img_U<<<oz_img_grid(ceil_div(np * n_ob, (size_t)kImgUBlocks)), 32 * kOzImgWarps, 0, s>>>(ducomp.as<double>(), dob.as<uint32_t>(), n_ob,
-                                                                       np, duf.as<uint8_t>(), drexpU.as<int>(), D,
-                                                                       dimgU.as<bf16>());
         const size_t tm = ceil_div(np, (size_t)Jm) * nb * ng_i;
         k_tiles_mui<<<oz_img_grid(tm), 32 * kOzImgWarps, 0, s>>>(
-            duf.as<uint8_t>(), dun.as<double>(), dcn.as<double>(), drexpU.as<int>(), dcexpC.as<int>(),
+            duf_.as<uint8_t>(), dun_.as<double>(), dcn.as<double>(), drexpU_.as<int>(), dcexpC.as<int>(),
             dmui.as<double>(), D, np, tm, tpb, dtm.as<OzTile>(), dsm.as<OzStep>(), dmf.as<uint8_t>(), cnt + 0,
             macs + 0);
-        ctx->note_launch(4);
+        ctx->note_launch();
         ctx->check_launch("rik ozaki mui prep");
-        oz_run(ctx, shM, dtm.as<OzTile>(), tm, dsm.as<OzStep>(), dimgCtA.as<bf16>(), dimgU.as<bf16>(), 1.0, s,
+        oz_run(ctx, shM, dtm.as<OzTile>(), tm, dsm.as<OzStep>(), dimgCtA.as<bf16>(), dimgU_.as<bf16>(), 1.0, s,
                macs + 0);
+        BSG_CUDA(cudaEventRecord(fork.u_done[ux], s));
+        if (P0 + pc < n_aux) {
+            // the next chunk's U pass into the other set (the chunk before
+            // this one has finished reading it), issued after this chunk's
+            // mui product so that it runs beside the statistics and image
+            // passes rather than beside a persistent GEMM's start
+            if (P0 > 0) BSG_CUDA(cudaStreamWaitEvent(ss, fork.u_done[ux ^ 1], 0));
+            u_pass(P0 + pc, ux ^ 1);
+        }
         // mui norms, row exponents per sub-range (A operand of K and of K_mn)
         // and column exponents per aux function (B operand of ij)
         k_mui_stats<<<oz_img_grid(ceil_div(np * nb * nob, (size_t)kNormBlocks)), 32 * kOzImgWarps, 0, s>>>(
@@ -982,6 +1070,8 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
         k_Kmn_mirror<<<(unsigned)ceil_div(n_bf * n_bf, (size_t)256), 256, 0, s>>>(Kmn_dev, n_bf, bs);
         ctx->note_launch();
     }
+    fork.join();
+    s = ctx->stream;
     ctx->gemm_check();
     if (stats) {
         unsigned long long h[6];
