@@ -19,6 +19,9 @@
 //   Kmn  += mui_P mui_P^T  (optional) tiles (P sub-range, b pair, block rows
 //                        a >= b), steps over (P, jb); lower blocks, mirrored
 //                        at the end
+// The U pass of chunk c+1 runs on a low-priority side stream beside chunk c's
+// statistics and image passes (two U sets, ordered by events); the products
+// run on a high-priority chain stream; both join the caller's stream.
 // Steps whose N-side sub-blocks have different surviving slot sets split into
 // exact rectangles, so every product the FP64 screen drops stays out.
 // Operand scales: U rows per (P, mu); C columns per i (also the rows of C^T);
