@@ -145,8 +145,9 @@ bsg_status bsg_matmult_strassen_sparse(bsg_bsm C, bsg_bsm A, int tA, bsg_bsm B, 
 bsg_status bsg_matmult_strassen_sparse_form(bsg_bsm C, bsg_bsm A, bsg_bsm B, double thresh,
                                             size_t min_size_for_strassen, int form, int n_digits);
 
-/* ---- batched products (BASELINE config 3; no single counterpart in the
- *      reference, which calls matmult once per product) ----
+/* ---- batched products (many independent screened products of mixed sizes
+ *      in one call; no single counterpart in the reference, which calls
+ *      matmult once per product) ----
  * C_i = alpha A_i B_i + beta C_i for i < n, each with matmult's semantics
  * (no transposes), any sizes and block sizes.  Mixed form: products are
  * grouped by block sizes and each group runs as ONE persistent tensor-core
