@@ -44,3 +44,16 @@ def test_reference_arm_other_ranks_exit_quietly():
     r = _run(RANK="1", WORLD_SIZE="2", LOCAL_RANK="1")
     assert r.returncode == 0, r.stderr[-2000:]
     assert _json_lines(r.stdout) == []
+
+
+def test_our_arm_fails_loudly_without_a_gpu():
+    """no CPU fallback: without a GPU our arm exits non-zero and prints no line"""
+    import pytest
+
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present: the arm would run the full benchmark")
+    r = subprocess.run([sys.executable, "bench.py", "--steps", "1", "--warmup", "3"], cwd=ROOT,
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode != 0
+    assert _json_lines(r.stdout) == []
