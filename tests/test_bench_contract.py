@@ -7,6 +7,8 @@ import os
 import subprocess
 import sys
 
+import pytest
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 KEYS = ("impl", "metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
         "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e")
@@ -48,8 +50,6 @@ def test_reference_arm_other_ranks_exit_quietly():
 
 def test_our_arm_fails_loudly_without_a_gpu():
     """no CPU fallback: without a GPU our arm exits non-zero and prints no line"""
-    import pytest
-
     torch = pytest.importorskip("torch")
     if torch.cuda.is_available():
         pytest.skip("a GPU is present: the arm would run the full benchmark")
