@@ -56,7 +56,8 @@ typedef struct bsg_batch_plan_s *bsg_batch_plan;
 const char *bsg_last_error(void);
 int bsg_version(void);
 
-/* ---- context (device + stream) ---- */
+/* ---- context (device + stream; no counterpart in the reference, which runs
+ *      on the host: every call below takes the context or an object made on it) ---- */
 bsg_status bsg_ctx_create(int device, void *cuda_stream, bsg_ctx *out);
 bsg_status bsg_ctx_destroy(bsg_ctx ctx);
 bsg_status bsg_ctx_sync(bsg_ctx ctx);
@@ -91,8 +92,10 @@ bsg_status bsg_pool_stats(bsg_pool pool, size_t *blocks_total, size_t *blocks_fr
  * pool may be NULL (a fresh pool of bsr*bsc-element blocks, :15) */
 bsg_status bsg_bsm_create(bsg_ctx ctx, size_t nr, size_t nc, size_t bsr, size_t bsc, double thresh, bsg_pool pool,
                           bsg_bsm *out);
-bsg_status bsg_bsm_destroy(bsg_bsm m);
-/* dims[0..5] = nr, nc, bsr, bsc, nrb, ncb; *thresh = the per-element threshold */
+bsg_status bsg_bsm_destroy(bsg_bsm m); /* end of the BlockSparseMatrix's life; its blocks go back to its pool */
+/* dims[0..5] = nr, nc, bsr, bsc, nrb, ncb; *thresh = the per-element threshold:
+ * nrow/ncol/max_blocksize_row/max_blocksize_col/nrowblocks/ncolblocks/thresh
+ * accessors, blocksparsematrix.h:49-55 */
 bsg_status bsg_bsm_info(bsg_bsm m, size_t dims[6], double *thresh);
 bsg_status bsg_bsm_pool(bsg_bsm m, bsg_pool *out); /* mem_pool_ptr() blocksparsematrix.h:81 */
 /* copy assignment: blocks and cached norms (used as `ijs = ij`, occ_ri_k_step.cpp:112) */
@@ -113,7 +116,9 @@ bsg_status bsg_bsm_no_of_alloc_blocks(bsg_bsm m, size_t *out);   /* no_of_alloc_
 bsg_status bsg_bsm_calc_alloc_dim(bsg_bsm m, size_t *out);       /* calc_alloc_dim :164-168 */
 /* to_pointer / to_matrix :103-131 (absent blocks read as zero) */
 bsg_status bsg_bsm_to_dense(bsg_bsm m, double *out, int where);
-/* block presence (1/0) and cached norms, block (r,c) at index r + c*nrb */
+/* block presence (1/0) and cached norms, block (r,c) at index r + c*nrb (the
+ * reference's block(r, c) storage order, blocksparsematrix.h:71-72, and each
+ * block's frobenius_norm(), matrix.h:52-53; for mask parity tests) */
 bsg_status bsg_bsm_get_mask(bsg_bsm m, uint8_t *mask_host);
 bsg_status bsg_bsm_get_norms(bsg_bsm m, double *norms_host);
 
