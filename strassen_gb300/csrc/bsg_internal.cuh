@@ -163,16 +163,16 @@ void ctx_release(bsg_ctx c);
 // kernels + launchers shared between translation units
 void launch_block_norms(bsg_bsm m, const uint8_t *d_sel, cudaStream_t s);  // recompute norms where sel (all if null)
 void launch_zero_blocks(bsg_bsm m, const uint8_t *d_sel, cudaStream_t s);
-// warp-level norm of n elements (column-major block, rows rs, ld) with the
-// fixed 32-lane order of the deterministic BLAS definition
 }  // namespace bsg
 
 // ---- device helpers ----
 // Frobenius norm of an rs x cs column-major block with leading dimension ld,
-// computed by one full warp in the fixed order: lane l accumulates
-// fma(x_i, x_i, s) over column-major element indices i = l, l+32, ...; then
-// s_l += s_{l+o} for o = 16..1; lane 0 returns sqrt(s_0).
-// The lane's chain s_l (the first half of the definition).
+// computed by one full warp in the fixed order (the deterministic nrm2 the
+// FP64 form shares with the oracle): lane l accumulates fma(x_i, x_i, s) over
+// column-major element indices i = l, l+32, ...; then s_l += s_{l+o} for
+// o = 16..1; lane 0 returns sqrt(s_0).
+//
+// The lane's chain s_l (the first half of the definition):
 __device__ __forceinline__ double warp_norm_chain(const double *__restrict__ p, int rs, int cs, size_t ld) {
     const int lane = threadIdx.x & 31;
     double acc = 0.0;
