@@ -153,11 +153,51 @@ def occ_sample_input(sysm, V, n_p):
     return np.asfortranarray(out)
 
 
+def screen_report(api, X, V, C, keys, B, sysm, bs, thr, d3, docc, ctx):
+    """Screening of the two forms, each through the whole pipeline on its own
+    3c->2c output, product by product: surviving block triples of both forms,
+    flips (a triple kept by one form and dropped by the other) with the
+    smallest and largest margin |est - thr| / thr among them, the smallest
+    margin of any live triple, and block-level mask differences of mui_P,
+    ij_P and ijs_P.  The 3c->2c and the mui = U C screens use norms of their
+    inputs (X, V^{-1/2}; U_P = the 3c->2c output, C)."""
+    from strassen_gb300 import screen
+
+    n_bf, n_aux, n_occ = sysm.n_bf, sysm.n_aux, sysm.n_occ
+    out = {}
+    tr = {}
+    for tag, form, nd3, ndo in (("mixed", api.FORM_OZAKI, d3, docc), ("fp64", api.FORM_FP64, 0, 0)):
+        _, n3 = api.transform_3c2c(X, V, bs, thr, form=form, n_digits=nd3, out=B, ctx=ctx, stats=True)
+        _, st, tr[tag] = api.rik_occ_step(B, keys, C, n_bf, n_aux, n_occ, bs, thr, n_part=1, form=form, n_digits=ndo,
+                                          ctx=ctx, trace=True)
+        out[tag] = {"3c2c": n3, "mui": st[0], "ij": st[1], "K": st[2]}
+    cmp = screen.compare(tr["fp64"], tr["mixed"])
+    rep = {}
+    for prod in ("3c2c", "mui", "ij", "K"):
+        r = {"surviving_fp64": out["fp64"][prod], "surviving_mixed": out["mixed"][prod]}
+        if prod in cmp:
+            r.update(flips=cmp[prod]["flips"], flip_margin_min=cmp[prod]["flip_margin_min"],
+                     flip_margin_max=cmp[prod]["flip_margin_max"], margin_min_all_triples=cmp[prod]["margin_min_all"])
+        rep[prod] = r
+    rep["blocks"] = cmp["blocks"]
+    rep["what"] = ("whole pipeline, each form on its own 3c->2c output; ij and K triples recounted on the host from "
+                   "both forms' per-P block norms (margin = |norm product - thr| / thr, thr = tau bs^3)")
+    return rep
+
+
+def cpu_sample_sizes(cores):
+    """Bounded sample that keeps every host core busy: 3c->2c on 16 rows of
+    the port's 512-element super-blocks per core (16 x 22 block rows of 24
+    integral rows; the super-block loop is the port's parallel loop), and the
+    occ-RI-K step on 16 aux functions per core (one P partition per core)."""
+    return 16 * 22 * CFG["bs"], 16 * cores
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    n_rows, n_p = 48, 48
+    n_rows, n_p = cpu_sample_sizes(os.cpu_count() or 1)
     sysm = make_system()
     V = sysm.v_m12()
     C = sysm.c_occ()
@@ -172,12 +212,14 @@ def run_reference(args):
         flops = f
     t = statistics.median(times)
     v = flops / t / 1e12
-    sample = f"3c->2c on {n_rows} of {sysm.n_vec2} integral rows + occ-RI-K on {n_p} of {sysm.n_aux} aux functions"
+    sample = (f"3c->2c on {n_rows} of {sysm.n_vec2} integral rows + occ-RI-K on {n_p} of {sysm.n_aux} aux functions "
+              "(OpenMP over super-blocks and P partitions, dgemm via OpenBLAS), throughput extrapolated to the step")
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "TFLOP/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": WORKLOAD, "sample": sample},
-            "cpu_baseline": {"value": v, "unit": "TFLOP/s", "cores": cores, "kind": "port", "sample": sample},
+            "cpu_baseline": {"value": v, "unit": "TFLOP/s", "cores": cores, "kind": "port", "sample": sample,
+                             "extrapolated": True},
             "e2e": {"value": v, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -307,6 +349,8 @@ def run_ours(args):
                             "rel_err_vs_fp64": float(np.linalg.norm(Kmn_oz - Kmn_64) / np.linalg.norm(Kmn_64)),
                             "block_products": st[api.FORM_FP64][5], "mixed_block_products": st[api.FORM_OZAKI][5],
                             "kmn_product_flops_bound": 2.0 * mprod}
+    if form != api.FORM_FP64 and not args.skip_fp64 and not args.skip_screen:
+        extra["screen"] = screen_report(api, X, V, C, keys, B, sysm, bs, thr, d3, docc, ctx)
     if args.no_e2e:
         print(json.dumps({"metric": METRIC, "value": flops_total(n_bf, n_aux, n_occ, n_vec2) / (ms * 1e-3) / 1e12,
                           "unit": "TFLOP/s", "ms_per_step": ms, "note": "profiling run (no e2e / baselines)",
@@ -351,11 +395,14 @@ def run_ours(args):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         Vn = np.asfortranarray(V.T.cpu().numpy().T)
         Cn = np.asfortranarray(C.T.cpu().numpy().T)
-        Bs = np.asfortranarray(B[:, :48].cpu().numpy())
-        f, t, cores = cpu_sample(sysm, sysm.ints_3c_rows(0, 48), Bs, Vn, Cn)
+        n_rows, n_p = cpu_sample_sizes(os.cpu_count() or 1)
+        Bs = np.asfortranarray(B[:, :n_p].cpu().numpy())
+        f, t, cores = cpu_sample(sysm, sysm.ints_3c_rows(0, n_rows), Bs, Vn, Cn)
         line["cpu_baseline"] = {"value": f / t / 1e12, "unit": "TFLOP/s", "cores": cores, "kind": "port",
-                                "sample": f"3c->2c on 48 of {n_vec2} integral rows + occ-RI-K on 48 of {n_aux} aux "
-                                          "functions (OpenMP over P partitions, dgemm via OpenBLAS)"}
+                                "sample": f"3c->2c on {n_rows} of {n_vec2} integral rows + occ-RI-K on {n_p} of "
+                                          f"{n_aux} aux functions (OpenMP over super-blocks and P partitions, dgemm "
+                                          "via OpenBLAS), throughput extrapolated to the step",
+                                "extrapolated": True}
     if rank == 0:
         print(json.dumps(line))
     if world > 1:
@@ -527,6 +574,111 @@ def run_batched(args):
     print(json.dumps(line))
 
 
+STRASSEN_SHAPES = {
+    # the Strassen benchmark's shape: n 2048, block 64, exp(-|I-J|/6), tau 1e-10, one Winograd level
+    "n2048": dict(n=2048, bs=64, L=6.0, core=0, seed=1, thresh=1e-10, depths=(0, 1)),
+    # the large shape: n 16384, block 64, dense core of the first 4096 rows and columns, exp(-|I-J|/10)
+    # tails, tau 1e-9, Strassen depth 0..3
+    "n16384": dict(n=16384, bs=64, L=10.0, core=4096, seed=4, thresh=1e-9, depths=(0, 1, 2, 3)),
+}
+
+
+def run_strassen(args):
+    """Screened block GEMM and the hybrid Strassen-Winograd / sparse
+    recursion (blocksparsematrix.hpp:293-414, strassen.hpp:687-753) at the
+    Strassen benchmark's shapes.  Inputs are generated on the device (seeded,
+    bit-identical to the host generator) and stored at threshold 0 as
+    main.cpp stores them.  Per shape: the FP64 screened matmult, then
+    matmult_strassen_sparse at each Strassen depth (min_size_for_strassen =
+    n / 2^depth) in the FP64 and the mixed form (bf16 digits on the tensor
+    cores; 4 digits at block 64), each timed after one warm-up call, with
+    the relative error against the FP64 screened product.  TFLOP/s are
+    dense-equivalent (2 n^3, as main.cpp:50 prints) and surviving-pair
+    (2 bs^3 per surviving block triple).  A measurement case, not the bench
+    line."""
+    import torch
+
+    from strassen_gb300 import api
+    from strassen_gb300 import synth as S
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    ctx = api.Context(0)
+    shapes = [args.shape] if args.shape else list(STRASSEN_SHAPES)
+
+    def timed(fn, reps=1):
+        fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            r = fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) / reps, r
+
+    results = []
+    for name in shapes:
+        c = STRASSEN_SHAPES[name]
+        n, bs, thr = c["n"], c["bs"], c["thresh"]
+        a = S.decay_matrix_torch(c["seed"], 1, n, n, bs, c["L"], core=c["core"], device=dev)
+        b = S.decay_matrix_torch(c["seed"], 2, n, n, bs, c["L"], core=c["core"], device=dev)
+        A = api.BlockSparseMatrix.from_dense(a.T, bs, bs, 0.0, ctx=ctx)
+        B = api.BlockSparseMatrix.from_dense(b.T, bs, bs, 0.0, ctx=ctx)
+        del a, b
+        dense_flops = 2.0 * n ** 3
+        C64 = api.BlockSparseMatrix(n, n, bs, bs, 0.0, ctx=ctx)
+        t_mm, nsig = timed(lambda: api.matmult(C64, A, 0, B, 0, thr, 1.0, 0.0))
+        surv_flops = 2.0 * nsig * bs ** 3
+        R = C64.to_matrix()
+        rn = np.linalg.norm(R)
+        row = {"shape": name, "n": n, "bs": bs, "thresh": thr, "L": c["L"], "core": c["core"],
+               "surviving_block_triples": nsig, "surviving_fraction": nsig / (n // bs) ** 3,
+               "fp64_matmult_s": t_mm, "fp64_matmult_tflops_dense_equiv": dense_flops / t_mm / 1e12,
+               "fp64_matmult_tflops_surviving": surv_flops / t_mm / 1e12, "strassen": []}
+        Cz = api.BlockSparseMatrix(n, n, bs, bs, 0.0, ctx=ctx)
+        t_mz, _ = timed(lambda: api.matmult(Cz, A, 0, B, 0, thr, 1.0, 0.0, form=api.FORM_OZAKI, n_digits=0))
+        row["mixed_matmult_s"] = t_mz
+        row["mixed_matmult_rel_err"] = float(np.linalg.norm(Cz.to_matrix() - R) / rn)
+        del Cz
+        for d in c["depths"]:
+            ms = n >> d
+            ent = {"depth": d, "min_size_for_strassen": ms}
+            for form, tag in ((api.FORM_FP64, "fp64"), (api.FORM_OZAKI, "mixed")):
+                CS = api.BlockSparseMatrix(n, n, bs, bs, 0.0, ctx=ctx)
+
+                def go():
+                    CS.fill_with_values(0.0)
+                    api.matmult_strassen_sparse(CS, A, 0, B, 0, thr, 1.0, 0.0, ms, form=form, n_digits=0)
+
+                t, _ = timed(go)
+                ent[tag + "_s"] = t
+                ent[tag + "_tflops_dense_equiv"] = dense_flops / t / 1e12
+                ent[tag + "_rel_err_vs_fp64_matmult"] = float(np.linalg.norm(CS.to_matrix() - R) / rn)
+                del CS
+            row["strassen"].append(ent)
+        if name == "n2048" and not args.no_cpu_baseline:
+            # the reference's CPU path (oracle port, dgemm through OpenBLAS) on the host cores
+            from oracle import oracle as O
+
+            ah = S.decay_matrix(c["seed"], 1, n, n, bs, c["L"], core=c["core"])
+            bh = S.decay_matrix(c["seed"], 2, n, n, bs, c["L"], core=c["core"])
+            oA, oB = O.OBsm(n, n, bs, bs, 0.0, ah), O.OBsm(n, n, bs, bs, 0.0, bh)
+            O.enable_fast_gemm(True)
+            oC = O.OBsm(n, n, bs, bs, 0.0)
+            t0 = time.perf_counter()
+            O.matmult(oC, oA, 0, oB, 0, thr)
+            t_cpu = time.perf_counter() - t0
+            O.enable_fast_gemm(False)
+            row["cpu_baseline"] = {"kind": "port", "cores": os.cpu_count(), "matmult_s": t_cpu,
+                                   "tflops_dense_equiv": dense_flops / t_cpu / 1e12,
+                                   "what": "oracle port of the screened matmult, OpenMP over super-blocks, "
+                                           "dgemm through OpenBLAS"}
+        del A, B, C64
+        torch.cuda.empty_cache()
+        results.append(row)
+    print(json.dumps({"metric": "screened block GEMM and hybrid Strassen-Winograd recursion, FP64 and mixed form",
+                      "unit": "s", "data": "synthetic (seeded, generated on device)", "results": results}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -539,10 +691,13 @@ def main():
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--skip-kmn", action="store_true", help="leave out the symmetric K_mn measurement")
+    ap.add_argument("--skip-screen", action="store_true", help="leave out the per-product screening comparison")
     ap.add_argument("--no-e2e", action="store_true", help="profiling runs: timed device step only")
     ap.add_argument("--atoms", type=int, default=0, help="smaller system for profiler captures")
-    ap.add_argument("--workload", default="rik", choices=["rik", "batched", "rik-large"],
-                    help="rik: the RI-K step (default); batched: the batched-GEMM configuration")
+    ap.add_argument("--workload", default="rik", choices=["rik", "batched", "rik-large", "strassen"],
+                    help="rik: the RI-K step (default); batched: the batched-GEMM configuration; strassen: the "
+                         "screened GEMM and Strassen shapes")
+    ap.add_argument("--shape", default="", choices=["", "n2048", "n16384"], help="strassen workload: one shape")
     ap.add_argument("--count", type=int, default=512, help="products of the batched workload")
     args = ap.parse_args()
     if args.workload == "batched":
@@ -550,6 +705,9 @@ def main():
         return
     if args.workload == "rik-large":
         run_rik_large(args)
+        return
+    if args.workload == "strassen":
+        run_strassen(args)
         return
     if args.impl == "reference":
         run_reference(args)

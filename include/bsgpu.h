@@ -74,8 +74,10 @@ bsg_status bsg_ctx_gemm_timing(bsg_ctx ctx, uint64_t *launches, double *ms, doub
  * operand stages, [1] MMA issuer waiting for a drained accumulator, [2] MMA
  * issuer lifetime, [3] producer waiting for a free stage, [4] epilogue
  * waiting for a finished chain, [5] epilogue draining TMEM, [6] epilogue
- * writing output blocks, [7] operand stages consumed. */
-bsg_status bsg_ctx_gemm_stalls(bsg_ctx ctx, uint64_t out[8]);
+ * writing output blocks, [7] operand stages consumed, [8] MMA instructions
+ * issued, [9] k steps copied, [10] (live slot, live N-side block) pairs in
+ * those steps, [11] slots x N-side blocks of those steps (the capacity). */
+bsg_status bsg_ctx_gemm_stalls(bsg_ctx ctx, uint64_t out[12]);
 
 /* ---- block pool: BlockMemoryPool<double> (blockallocator.h:8-25,
  *      blockallocator.hpp:7-56).  Device slabs grow geometrically from 16 MB
@@ -132,7 +134,12 @@ bsg_status bsg_dot(bsg_bsm a, bsg_bsm b, double thresh, double *out);
 bsg_status bsg_matmult(bsg_bsm C, bsg_bsm A, int tA, bsg_bsm B, int tB, double thresh, double alpha, double beta,
                        uint64_t *nsig_out);
 /* the same product in a chosen arithmetic form (BSG_FORM_OZAKI: n_digits
- * bf16 slices per operand, 2..5; screening stays FP64 so masks are exact) */
+ * bf16 slices per operand, 2..8, 0 = 5 where two pipeline stages fit shared
+ * memory, else 4).  Screening uses the operands' cached FP64 norms in both
+ * forms, so this product's mask and surviving pairs equal the FP64 form's for
+ * the same operands.  A later screen on norms of a result computed in the
+ * mixed form (RI-K's mui_P and ijs_P) can differ from the FP64 form's for
+ * blocks whose norm product lies within the result's error of the threshold. */
 bsg_status bsg_matmult_form(bsg_bsm C, bsg_bsm A, int tA, bsg_bsm B, int tB, double thresh, double alpha,
                             double beta, int form, int n_digits, uint64_t *nsig_out);
 
@@ -244,6 +251,26 @@ typedef struct bsg_rik_args {
 bsg_status bsg_rik_occ_step(bsg_ctx ctx, const bsg_rik_args *args, double *K_out, int out_where,
                             uint64_t stats_out[5]);
 
+/* Screening state of every aux function P after an occ-RI-K step, for mask
+ * parity between the arithmetic forms (host arrays, column-major blocks):
+ * mui_P = U_P C block norms and presence (nb x nob per P, nb = ceil(n_bf/bs),
+ * nob = ceil(n_occ/bs); a norm is meaningful where its flag is set),
+ * ij_P = C^T mui_P presence, ijs_P = ij_P + ij_P^T block norms and presence
+ * (nob x nob per P; the norm of a block without a transpose partner stays 0,
+ * as blocksparsematrix.hpp:224-248 leaves it), and the block norms of C. */
+typedef struct {
+    double *mui_norm;  /* n_aux * nb * nob, index P*nb*nob + a + jb*nb */
+    uint8_t *mui_flag;
+    uint8_t *ij_flag;  /* n_aux * nob * nob, index P*nob*nob + ib + jb*nob */
+    double *ijs_norm;
+    uint8_t *ijs_flag;
+    double *c_norm;    /* nb * nob, index a + jb*nb */
+} bsg_rik_screen_trace;
+/* bsg_rik_occ_step that also fills *trace (the screens of occ_ri_k_step.cpp:
+ * 107-116: mui_P.calc_frobenius_norms() :108, ijs.add_transpose :113) */
+bsg_status bsg_rik_occ_step_trace(bsg_ctx ctx, const bsg_rik_args *args, double *K_out, int out_where,
+                                  uint64_t stats_out[5], const bsg_rik_screen_trace *trace);
+
 /* Symmetric exchange matrix K_mn = sum_{P,i} mui_P(m,i) mui_P(n,i), with
  * mui_P = (mu i|P) the screened product U_P C the occ step builds
  * (occ_ri_k_step.cpp:102-108).  No counterpart in the reference, whose driver
@@ -268,7 +295,13 @@ bsg_status bsg_rik_kmn_step(bsg_ctx ctx, const bsg_rik_args *args, double *Kmn_o
  * until exit; problems whose per-aux-function workspace exceeds it are
  * rejected with BSG_ERR_ARG.  The first call on a device looks up that
  * array's address (make it before any stream capture); calls share the array,
- * so calls that overlap on the GPU race -- serialize them.  Results equal
+ * so calls that overlap on the GPU race -- serialize them.  The current device
+ * must own cuda_stream, K_dev and the inputs (buffers on another device are
+ * rejected with BSG_ERR_ARG).  With stats_out NULL the call only enqueues its
+ * kernels and does not wait for the stream; integral keys are then checked on
+ * the device: a key outside the N_bf x N_bf matrix is skipped and K_dev is
+ * filled with NaN.  With stats_out the call waits for its stream once, and
+ * returns BSG_ERR_ARG for such a key as well.  Results equal
  * bsg_rik_occ_step's bit for bit. */
 bsg_status bsg_rik_occ_step_noalloc(const bsg_rik_args *args, double *K_dev, void *cuda_stream,
                                     uint64_t stats_out[5]);
@@ -278,10 +311,11 @@ bsg_status bsg_rik_occ_step_noalloc(const bsg_rik_args *args, double *K_dev, voi
 bsg_status bsg_3c2c_transform(bsg_ctx ctx, size_t n_vec2, size_t n_aux, const double *ints_3c,
                               const double *v_m12, int where, size_t bs, double thresh, int form, int n_digits,
                               double *out, int out_where);
-
-/* ---- measurement helpers ---- */
-/* device FP64 FMA throughput probe (GFLOP/s) for the roofline denominator */
-bsg_status bsg_probe_fp64_peak(bsg_ctx ctx, double *gflops_out);
+/* the same, with the number of surviving block products in *nsig_out (the
+ * screen uses the FP64 block norms of X and V^{-1/2} in both forms) */
+bsg_status bsg_3c2c_transform_nsig(bsg_ctx ctx, size_t n_vec2, size_t n_aux, const double *ints_3c,
+                                   const double *v_m12, int where, size_t bs, double thresh, int form, int n_digits,
+                                   double *out, int out_where, uint64_t *nsig_out);
 
 #ifdef __cplusplus
 }

@@ -10,13 +10,14 @@
 #                            the reference's own live driver (all of its .cpp
 #                            files, as its Makefile links them) on the shim.
 #
-# The reference part is built only when REF_DIR holds the reference sources;
+# The reference part is built only when REF_DIR (default: a checkout named
+# "reference" beside this repository) holds the reference sources;
 # outputs go to oracle/_ref/ (git-ignored).  Parity flags: -O2
 # -ffp-contract=off (the reference's -Ofast would let the compiler reorder
 # and fuse the Winograd sums; no -march=native so it builds on any host).
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
-REF_DIR="${REF_DIR:-/root/reference}"
+REF_DIR="${REF_DIR:-$HERE/../../reference}"
 CC="${CC:-gcc}"
 CXX="${CXX:-g++}"
 FLAGS="-O2 -ffp-contract=off -fPIC -fopenmp"

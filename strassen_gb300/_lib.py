@@ -40,6 +40,11 @@ class RikArgs(C.Structure):
                 ("n_part", c_int), ("form", c_int), ("n_digits", c_int), ("p_chunk", c_size)]
 
 
+class ScreenTrace(C.Structure):
+    _fields_ = [("mui_norm", c_vp), ("mui_flag", c_vp), ("ij_flag", c_vp), ("ijs_norm", c_vp), ("ijs_flag", c_vp),
+                ("c_norm", c_vp)]
+
+
 def _sig(name, args, res=c_int):
     f = getattr(lib, name)
     f.argtypes = args
@@ -91,9 +96,11 @@ _sig("bsg_matmult_strassen_sparse_form", [c_vp, c_vp, c_vp, c_dbl, c_size, c_int
 _sig("bsg_tensormult_contract", [c_vp, c_vp, c_int, c_vp, c_int, c_size, c_dbl, c_dbl, c_dbl])
 _sig("bsg_tensormult_batched", [c_vp, c_vp, c_int, c_vp, c_int, c_size, c_dbl, c_dbl, c_dbl])
 _sig("bsg_rik_occ_step", [c_vp, C.POINTER(RikArgs), c_vp, c_int, c_u64p])
+_sig("bsg_rik_occ_step_trace", [c_vp, C.POINTER(RikArgs), c_vp, c_int, c_u64p, C.POINTER(ScreenTrace)])
 _sig("bsg_rik_kmn_step", [c_vp, C.POINTER(RikArgs), c_vp, c_vp, c_int, c_u64p])
 _sig("bsg_3c2c_transform", [c_vp, c_size, c_size, c_vp, c_vp, c_int, c_size, c_dbl, c_int, c_int, c_vp, c_int])
-_sig("bsg_probe_fp64_peak", [c_vp, C.POINTER(c_dbl)])
+_sig("bsg_3c2c_transform_nsig", [c_vp, c_size, c_size, c_vp, c_vp, c_int, c_size, c_dbl, c_int, c_int, c_vp, c_int,
+                                 c_u64p])
 c_flt = C.c_float
 _sig("bsg_sched_create", [c_vp, C.POINTER(c_vp)])
 _sig("bsg_sched_destroy", [c_vp])

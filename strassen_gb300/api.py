@@ -22,7 +22,7 @@ import ctypes as C
 
 import numpy as np
 
-from ._lib import BSG_DEVICE, BSG_HOST, FORM_FP64, FORM_OZAKI, BsgError, RikArgs, check, lib  # noqa: F401
+from ._lib import BSG_DEVICE, BSG_HOST, FORM_FP64, FORM_OZAKI, BsgError, RikArgs, ScreenTrace, check, lib  # noqa: F401
 from ._lib import SCHED_COST, SCHED_FEATURES, SCHED_MLP, SCHED_NONE, SCHED_ROOT  # noqa: F401
 
 _DEFAULT_CTX = None
@@ -96,11 +96,12 @@ class Context:
         return {tuple(int(x) for x in r[:4]): (int(r[4]), int(r[5])) for r in e}
 
     STALL_KEYS = ("mma_wait_operands", "mma_wait_accumulator", "mma_total", "producer_wait_stage",
-                  "epilogue_wait_chain", "epilogue_drain", "epilogue_store", "steps")
+                  "epilogue_wait_chain", "epilogue_drain", "epilogue_store", "steps", "mmas", "copied_steps",
+                  "live_pairs", "pair_capacity")
 
     def gemm_stalls(self):
         """stall breakdown of the timed tensor-core GEMM launches (SM cycles summed over CTAs)"""
-        out = (C.c_uint64 * 8)()
+        out = (C.c_uint64 * 12)()
         check(lib.bsg_ctx_gemm_stalls(self.h, out))
         return dict(zip(self.STALL_KEYS, list(out)))
 
@@ -434,11 +435,40 @@ def tensormult_batched(Cs, A, tA, Bs, tB, thresh, alpha=1.0, beta=0.0):
 
 
 def rik_occ_step(ints, keys, c_occ, n_bf, n_aux, n_occ, bs, thresh, n_part=1, form=FORM_FP64, n_digits=4,
-                 p_chunk=0, out=None, ctx=None, stats=False):
+                 p_chunk=0, out=None, ctx=None, stats=False, trace=False):
     """K_{mu j} = sum_{P,i} (mu i|P)[(ij|P)+(ji|P)] (occ_ri_k_step.cpp:83-130).
 
     ints: n_vec2 x n_aux, keys: n_vec2 uint64, c_occ: n_bf x n_occ; numpy
-    (host) or torch CUDA tensors (device, all three alike)."""
+    (host) or torch CUDA tensors (device, all three alike).  trace=True also
+    returns the screening state of every aux function (a dict of numpy
+    arrays, see bsg_rik_screen_trace): (K, stats, trace)."""
+    if trace:
+        ctx = ctx or default_context()
+        pi, w1, k1 = _buf(ints)
+        pk, w2, k2 = _buf(keys, np.uint64)
+        pc, w3, k3 = _buf(c_occ)
+        if not (w1 == w2 == w3):
+            raise BsgError(1, "ints, keys and c_occ must all be host or all device arrays")
+        a = RikArgs(n_bf, n_aux, n_occ, ints.shape[0], pi, pk, pc, w1, bs, float(thresh), n_part, form, n_digits,
+                    p_chunk)
+        if out is None:
+            out = np.zeros((n_bf, n_occ), dtype=np.float64, order="F")
+        po, wo, ko = _buf(out)
+        nb, nob = -(-n_bf // bs), -(-n_occ // bs)
+        tr = {"mui_norm": np.zeros((n_aux, nob, nb)), "mui_flag": np.zeros((n_aux, nob, nb), np.uint8),
+              "ij_flag": np.zeros((n_aux, nob, nob), np.uint8), "ijs_norm": np.zeros((n_aux, nob, nob)),
+              "ijs_flag": np.zeros((n_aux, nob, nob), np.uint8), "c_norm": np.zeros((nob, nb))}
+        t = ScreenTrace(*[C.c_void_p(tr[k].ctypes.data) for k in
+                          ("mui_norm", "mui_flag", "ij_flag", "ijs_norm", "ijs_flag", "c_norm")])
+        st = (C.c_uint64 * 5)()
+        check(lib.bsg_rik_occ_step_trace(ctx.h, C.byref(a), po, wo, st, C.byref(t)))
+        if wo == BSG_HOST and ko is not out:
+            out[...] = ko
+        del k1, k2, k3
+        # [P][jb][a] storage order -> arrays indexed [P, a, jb] (mui) and [P, ib, jb] (ij, ijs), C [a, jb]
+        tr = {k: (np.swapaxes(v, -1, -2) if v.ndim >= 2 else v) for k, v in tr.items()}
+        tr.update(n_bf=n_bf, n_occ=n_occ, bs=bs, thresh=float(thresh))
+        return out, list(st), tr
     ctx = ctx or default_context()
     pi, w1, k1 = _buf(ints)
     pk, w2, k2 = _buf(keys, np.uint64)
@@ -499,8 +529,9 @@ def rik_kmn_step(ints, keys, c_occ, n_bf, n_aux, n_occ, bs, thresh, n_part=1, fo
     return res[0] if len(res) == 1 else res
 
 
-def transform_3c2c(ints_3c, v_m12, bs, thresh, form=FORM_FP64, n_digits=4, out=None, ctx=None):
-    """(mu nu|P)' = sum_Q (mu nu|Q)(Q|P)^{-1/2} (3c_2c_transform.cpp:44-57)"""
+def transform_3c2c(ints_3c, v_m12, bs, thresh, form=FORM_FP64, n_digits=4, out=None, ctx=None, stats=False):
+    """(mu nu|P)' = sum_Q (mu nu|Q)(Q|P)^{-1/2} (3c_2c_transform.cpp:44-57);
+    stats=True: (out, surviving block products)"""
     ctx = ctx or default_context()
     px, w1, k1 = _buf(ints_3c)
     pv, w2, k2 = _buf(v_m12)
@@ -510,15 +541,11 @@ def transform_3c2c(ints_3c, v_m12, bs, thresh, form=FORM_FP64, n_digits=4, out=N
     if out is None:
         out = np.zeros((n_vec2, n_aux), dtype=np.float64, order="F")
     po, wo, ko = _buf(out)
-    check(lib.bsg_3c2c_transform(ctx.h, n_vec2, n_aux, px, pv, w1, bs, float(thresh), form, n_digits, po, wo))
+    nsig = C.c_uint64()
+    check(lib.bsg_3c2c_transform_nsig(ctx.h, n_vec2, n_aux, px, pv, w1, bs, float(thresh), form, n_digits, po, wo,
+                                      C.byref(nsig)))
     if wo == BSG_HOST and ko is not out:
         out[...] = ko
     del k1, k2
-    return out
+    return (out, nsig.value) if stats else out
 
-
-def probe_fp64_peak(ctx=None):
-    ctx = ctx or default_context()
-    v = C.c_double()
-    check(lib.bsg_probe_fp64_peak(ctx.h, C.byref(v)))
-    return v.value

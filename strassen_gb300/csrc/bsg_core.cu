@@ -173,10 +173,10 @@ extern "C" bsg_status bsg_ctx_gemm_timing(bsg_ctx ctx, uint64_t *launches, doubl
     });
 }
 
-extern "C" bsg_status bsg_ctx_gemm_stalls(bsg_ctx ctx, uint64_t out[8]) {
+extern "C" bsg_status bsg_ctx_gemm_stalls(bsg_ctx ctx, uint64_t out[12]) {
     return guard([&] {
         BSG_REQUIRE(ctx && out, BSG_ERR_ARG, "NULL argument");
-        for (int i = 0; i < 8; ++i) out[i] = ctx->oz_stall[i];
+        for (int i = 0; i < 12; ++i) out[i] = ctx->oz_stall[i];
     });
 }
 

@@ -95,7 +95,7 @@ struct bsg_ctx_s {
     double oz_ms = 0.0;
     uint64_t oz_launches = 0;
     double oz_useful_macs = 0.0;  // unpadded block-product multiply-adds (FP64-equivalent)
-    uint64_t oz_stall[8] = {};    // pipeline stall counters of the GEMM kernel (SM cycles over CTAs)
+    uint64_t oz_stall[12] = {};    // pipeline stall counters of the GEMM kernel (SM cycles over CTAs)
     // timeout flag of the tensor-core GEMM launches: set on the device, read
     // once per public call (gemm_check) instead of after every launch
     int *d_gemm_err = nullptr;

@@ -39,6 +39,7 @@ static void *oz_zero_image() {
     static void *addr[64] = {};
     int dev = 0;
     BSG_CUDA(cudaGetDevice(&dev));
+    BSG_REQUIRE(dev >= 0 && dev < 64, BSG_ERR_UNSUPPORTED, "device index out of range");
     std::lock_guard<std::mutex> lk(mu);
     if (!addr[dev]) BSG_CUDA(cudaGetSymbolAddress(&addr[dev], g_oz_zero));
     return addr[dev];
@@ -109,8 +110,13 @@ enum OzProf {
     kProfEpiDrain,       // epilogue reading TMEM and accumulating
     kProfEpiStore,       // epilogue scaling and writing output blocks
     kProfSteps,          // operand stages consumed by the MMA issuer
+    kProfMmas,           // tcgen05.mma instructions issued
+    kProfCopiedSteps,    // k steps copied by the producer (a pair stage holds two)
+    kProfLivePairs,      // (live slot, live N-side sub-block) pairs over those steps
+    kProfPairCapacity,   // slots x sub-blocks over those steps
     kOzProf
 };
+static_assert(kOzProf == 12, "the context keeps 12 GEMM counters");
 
 constexpr int kOzThreads = 320;  // producer, MMA issuer, 8 epilogue warps
 
@@ -211,12 +217,18 @@ __global__ void __launch_bounds__(kOzThreads, 1)
         uint32_t stage = 0, ph = 0;  // ring position of stage `it`
         const uint32_t jfull = (1u << P.J) - 1u;
         // one step's A slots and B digit stack into the half-stage at sA / sB
+        unsigned long long n_copied = 0, n_live = 0;
         auto copy_step = [&](const OzStep &st, uint8_t *sA, uint8_t *sB, uint64_t *bar) {
             // slots whose images are consecutive in a_img (or all zero) go
             // in one copy: a fully live step is one A copy and one B copy
             const uint32_t ai = lane < P.R ? st.a[lane] : kOzNone;
             const uint32_t prev = __shfl_up_sync(0xffffffffu, ai, 1);
             const bool live = ai != kOzNone;
+            if (prof) {
+                ++n_copied;
+                n_live += (unsigned long long)__popc(__ballot_sync(0xffffffffu, live)) *
+                          (unsigned long long)__popc(st.bmask & jfull);
+            }
             const bool joins = lane > 0 && (live ? (prev != kOzNone && prev + 1u == ai) : prev == kOzNone);
             const uint32_t starts = __ballot_sync(0xffffffffu, lane < P.R && !joins) | (1u << P.R);
             if (lane < P.R && !joins) {
@@ -282,14 +294,19 @@ __global__ void __launch_bounds__(kOzThreads, 1)
         if (lane == 0) {
             const uint32_t first = it > (uint32_t)P.S ? it - P.S : 0;
             for (uint32_t j = first; j < it; ++j) tc::mbar_wait(&full[j % P.S], (j / P.S) & 1u, abort);
-            if (prof) atomicAdd(&P.prof[kProfProdWaitEmpty], w_empty);
+            if (prof) {
+                atomicAdd(&P.prof[kProfProdWaitEmpty], w_empty);
+                atomicAdd(&P.prof[kProfCopiedSteps], n_copied);
+                atomicAdd(&P.prof[kProfLivePairs], n_live);
+                atomicAdd(&P.prof[kProfPairCapacity], n_copied * (unsigned long long)(P.R * P.J));
+            }
         }
         __syncwarp();
     } else if (warp == 1) {
         // ---------------- MMA issuer ----------------
         if (lane == 0) {
             const long long t_start = prof ? clock64() : 0;
-            unsigned long long w_full = 0, w_tmem = 0;
+            unsigned long long w_full = 0, w_tmem = 0, n_mma = 0;
             uint32_t it = 0, ch = 0, stage = 0, ph = 0;
             // MMA plan of one k16 slice, computed once: per A digit i, D_i x
             // [E_j0 .. E_j1) stacked along N (N <= 256, rounded up to 16: the
@@ -398,6 +415,7 @@ __global__ void __launch_bounds__(kOzThreads, 1)
                                 tc::mma_bf16(dt, aqs[q] + pa[e], bqs[q] + pb[e], pi[e], ac);
                             }
                         }
+                        if (prof) n_mma += (unsigned long long)n_plan * nq;
                         tc::mma_commit(&empty[stage]);
                         if (++stage == (uint32_t)P.S) {
                             stage = 0;
@@ -413,6 +431,7 @@ __global__ void __launch_bounds__(kOzThreads, 1)
                 atomicAdd(&P.prof[kProfMmaWaitTmem], w_tmem);
                 atomicAdd(&P.prof[kProfMmaTotal], (unsigned long long)(clock64() - t_start));
                 atomicAdd(&P.prof[kProfSteps], (unsigned long long)it);
+                atomicAdd(&P.prof[kProfMmas], n_mma);
             }
         }
         __syncwarp();
@@ -660,7 +679,7 @@ void oz_run(bsg_ctx ctx, const OzShape &sh, const OzTile *d_tiles, size_t n_tile
     ctx->oz_ms += ms;
     ctx->oz_launches += 1;
     ctx->oz_useful_macs += (double)macs;
-    for (int i = 0; i < kOzProf && i < 8; ++i) ctx->oz_stall[i] += st[i];
+    for (int i = 0; i < kOzProf; ++i) ctx->oz_stall[i] += st[i];
     ctx->gemm_check();
 }
 

@@ -318,6 +318,18 @@ static unsigned threads_for(int rows, int cols) {
     return (unsigned)std::max<size_t>(32, ((ceil_div(e, kREPT) + 31) / 32) * 32);
 }
 
+void rik_trace_chunk(const RikDev &d, size_t P0, size_t np, const double *mnorm, const uint8_t *mflag,
+                     const uint8_t *ijflag, const double *snorm, const uint8_t *sflag, cudaStream_t s) {
+    if (!d.tr_mui_norm) return;
+    const size_t nb = ceil_div(d.n_bf, d.bs), nob = ceil_div(d.n_occ, d.bs);
+    const size_t m = nb * nob, o = nob * nob;
+    BSG_CUDA(cudaMemcpyAsync(d.tr_mui_norm + P0 * m, mnorm, np * m * 8, cudaMemcpyDeviceToDevice, s));
+    BSG_CUDA(cudaMemcpyAsync(d.tr_mui_flag + P0 * m, mflag, np * m, cudaMemcpyDeviceToDevice, s));
+    BSG_CUDA(cudaMemcpyAsync(d.tr_ij_flag + P0 * o, ijflag, np * o, cudaMemcpyDeviceToDevice, s));
+    BSG_CUDA(cudaMemcpyAsync(d.tr_ijs_norm + P0 * o, snorm, np * o * 8, cudaMemcpyDeviceToDevice, s));
+    BSG_CUDA(cudaMemcpyAsync(d.tr_ijs_flag + P0 * o, sflag, np * o, cudaMemcpyDeviceToDevice, s));
+}
+
 void rik_fp64(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uint64_t stats[6]) {
     cudaStream_t s = ctx->stream;
     const size_t n_bf = d.n_bf, n_occ = d.n_occ, bs = d.bs, n_aux = d.n_aux;
@@ -351,6 +363,7 @@ void rik_fp64(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uint
     const int wpb = 8;
     k_cnorms<<<(unsigned)ceil_div(nb * nob, wpb), wpb * 32, 0, s>>>(d.c_occ, n_bf, n_occ, bs, nb, nob, dcn.as<double>());
     ctx->note_launch();
+    if (d.tr_c_norm) BSG_CUDA(cudaMemcpyAsync(d.tr_c_norm, dcn.p, nb * nob * 8, cudaMemcpyDeviceToDevice, s));
     const double tpb_u = 1e-20 * (double)(bs * bs);     // U_bsm threshold 1e-20 (:93)
     const double tpb = d.thresh * (double)(bs * bs * bs);  // matmult per-block threshold
     std::vector<uint32_t> plo(T), phi(T);
@@ -376,6 +389,8 @@ void rik_fp64(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uint
             k_ijs<<<(unsigned)(np * nob * nob), 128, 0, s>>>(dij.as<double>(), dijf.as<uint8_t>(), n_occ, bs, nob,
                                                               dijs.as<double>(), dsn.as<double>(), dsf.as<uint8_t>());
             ctx->note_launch(2);
+            rik_trace_chunk(d, P0, np, dmn.as<double>(), dmf.as<uint8_t>(), dijf.as<uint8_t>(), dsn.as<double>(),
+                            dsf.as<uint8_t>(), s);
         }
         for (int t = 0; t < T; ++t) {
             const size_t lo = std::max<size_t>(plo_all[t], P0), hi = std::min<size_t>(phi_all[t], P0 + np);
@@ -441,7 +456,7 @@ namespace {
 
 // shared body of the two RI-K entry points: either output may be NULL
 bsg_status rik_entry(bsg_ctx ctx, const bsg_rik_args *a, double *K_out, double *Kmn_out, int out_where,
-                     uint64_t *stats_out, int n_stats) {
+                     uint64_t *stats_out, int n_stats, const bsg_rik_screen_trace *trace = nullptr) {
     return guard([&] {
         BSG_REQUIRE(ctx && a && (K_out || Kmn_out), BSG_ERR_ARG, "NULL argument");
         BSG_REQUIRE(a->bs > 0 && a->n_part >= 1, BSG_ERR_ARG, "block size and partition count must be positive");
@@ -490,6 +505,30 @@ bsg_status rik_entry(bsg_ctx ctx, const bsg_rik_args *a, double *K_out, double *
                 Kmnd = dkmn.as<double>();
             }
         }
+        // screen trace: device copies of the per-P screening state, read back at the end
+        const size_t nb = ceil_div(a->n_bf, a->bs), nob = ceil_div(a->n_occ, a->bs);
+        const size_t tm = a->n_aux * nb * nob, to = a->n_aux * nob * nob;
+        DevBuf tmn, tmf, tif, tsn, tsf, tcn;
+        if (trace) {
+            BSG_REQUIRE(K_out && trace->mui_norm && trace->mui_flag && trace->ij_flag && trace->ijs_norm &&
+                            trace->ijs_flag && trace->c_norm,
+                        BSG_ERR_ARG, "screen trace: every array is required");
+            tmn = DevBuf(tm * 8, s);
+            tmf = DevBuf(tm, s);
+            tif = DevBuf(to, s);
+            tsn = DevBuf(to * 8, s);
+            tsf = DevBuf(to, s);
+            tcn = DevBuf(nb * nob * 8, s);
+            BSG_CUDA(cudaMemsetAsync(tmf.p, 0, tm, s));
+            BSG_CUDA(cudaMemsetAsync(tif.p, 0, to, s));
+            BSG_CUDA(cudaMemsetAsync(tsf.p, 0, to, s));
+            d.tr_mui_norm = tmn.as<double>();
+            d.tr_mui_flag = tmf.as<uint8_t>();
+            d.tr_ij_flag = tif.as<uint8_t>();
+            d.tr_ijs_norm = tsn.as<double>();
+            d.tr_ijs_flag = tsf.as<uint8_t>();
+            d.tr_c_norm = tcn.as<double>();
+        }
         uint64_t st[6] = {0, 0, 0, 0, 0, 0};
         if (d.n_aux == 0) {
             if (Kd) BSG_CUDA(cudaMemsetAsync(Kd, 0, nk * 8, s));
@@ -502,6 +541,14 @@ bsg_status rik_entry(bsg_ctx ctx, const bsg_rik_args *a, double *K_out, double *
         if (out_where == BSG_HOST) {
             if (K_out) BSG_CUDA(cudaMemcpyAsync(K_out, Kd, nk * 8, cudaMemcpyDeviceToHost, s));
             if (Kmn_out) BSG_CUDA(cudaMemcpyAsync(Kmn_out, Kmnd, nkmn * 8, cudaMemcpyDeviceToHost, s));
+        }
+        if (trace && d.n_aux) {
+            BSG_CUDA(cudaMemcpyAsync(trace->mui_norm, tmn.p, tm * 8, cudaMemcpyDeviceToHost, s));
+            BSG_CUDA(cudaMemcpyAsync(trace->mui_flag, tmf.p, tm, cudaMemcpyDeviceToHost, s));
+            BSG_CUDA(cudaMemcpyAsync(trace->ij_flag, tif.p, to, cudaMemcpyDeviceToHost, s));
+            BSG_CUDA(cudaMemcpyAsync(trace->ijs_norm, tsn.p, to * 8, cudaMemcpyDeviceToHost, s));
+            BSG_CUDA(cudaMemcpyAsync(trace->ijs_flag, tsf.p, to, cudaMemcpyDeviceToHost, s));
+            BSG_CUDA(cudaMemcpyAsync(trace->c_norm, tcn.p, nb * nob * 8, cudaMemcpyDeviceToHost, s));
         }
         BSG_CUDA(cudaStreamSynchronize(s));
         if (stats_out)
@@ -517,6 +564,12 @@ extern "C" bsg_status bsg_rik_occ_step(bsg_ctx ctx, const bsg_rik_args *a, doubl
     return rik_entry(ctx, a, K_out, nullptr, out_where, stats_out, 5);
 }
 
+extern "C" bsg_status bsg_rik_occ_step_trace(bsg_ctx ctx, const bsg_rik_args *a, double *K_out, int out_where,
+                                             uint64_t stats_out[5], const bsg_rik_screen_trace *trace) {
+    if (!K_out || !trace) return guard([] { BSG_REQUIRE(false, BSG_ERR_ARG, "NULL argument"); });
+    return rik_entry(ctx, a, K_out, nullptr, out_where, stats_out, 5, trace);
+}
+
 extern "C" bsg_status bsg_rik_kmn_step(bsg_ctx ctx, const bsg_rik_args *a, double *Kmn_out, double *K_out,
                                        int out_where, uint64_t stats_out[6]) {
     if (!Kmn_out) return guard([] { BSG_REQUIRE(false, BSG_ERR_ARG, "NULL argument"); });
@@ -526,6 +579,13 @@ extern "C" bsg_status bsg_rik_kmn_step(bsg_ctx ctx, const bsg_rik_args *a, doubl
 extern "C" bsg_status bsg_3c2c_transform(bsg_ctx ctx, size_t n_vec2, size_t n_aux, const double *ints_3c,
                                          const double *v_m12, int where, size_t bs, double thresh, int form,
                                          int n_digits, double *out, int out_where) {
+    return bsg_3c2c_transform_nsig(ctx, n_vec2, n_aux, ints_3c, v_m12, where, bs, thresh, form, n_digits, out,
+                                   out_where, nullptr);
+}
+
+extern "C" bsg_status bsg_3c2c_transform_nsig(bsg_ctx ctx, size_t n_vec2, size_t n_aux, const double *ints_3c,
+                                              const double *v_m12, int where, size_t bs, double thresh, int form,
+                                              int n_digits, double *out, int out_where, uint64_t *nsig_out) {
     return guard([&] {
         BSG_REQUIRE(ctx && ints_3c && v_m12 && out, BSG_ERR_ARG, "NULL argument");
         BSG_REQUIRE(bs > 0, BSG_ERR_ARG, "block size must be positive");
@@ -546,9 +606,9 @@ extern "C" bsg_status bsg_3c2c_transform(bsg_ctx ctx, size_t n_vec2, size_t n_au
                 o = dout.as<double>();
             }
             if (where == BSG_HOST)  // the integrals stream in by row ranges, overlapping the transform
-                transform_3c2c_ozaki_upload(ctx, n_vec2, n_aux, ints_3c, v, bs, thresh, n_digits, o, nullptr);
+                transform_3c2c_ozaki_upload(ctx, n_vec2, n_aux, ints_3c, v, bs, thresh, n_digits, o, nsig_out);
             else
-                transform_3c2c_ozaki(ctx, n_vec2, n_aux, ints_3c, v, bs, thresh, n_digits, o, nullptr);
+                transform_3c2c_ozaki(ctx, n_vec2, n_aux, ints_3c, v, bs, thresh, n_digits, o, nsig_out);
             if (out_where == BSG_HOST)
                 BSG_CUDA(cudaMemcpyAsync(out, o, n_vec2 * n_aux * 8, cudaMemcpyDeviceToHost, s));
             BSG_CUDA(cudaStreamSynchronize(s));
@@ -571,7 +631,8 @@ extern "C" bsg_status bsg_3c2c_transform(bsg_ctx ctx, size_t n_vec2, size_t n_au
             if (st) throw Error{st, bsg_last_error()};
             st = bsg_bsm_fill(O, 0.0);  // :54
             if (st) throw Error{st, bsg_last_error()};
-            screened_product(ctx, {O}, {X}, 0, {V}, 0, {{0, 1}}, thresh, 1.0, 1.0, form, n_digits);  // :56
+            const uint64_t n = screened_product(ctx, {O}, {X}, 0, {V}, 0, {{0, 1}}, thresh, 1.0, 1.0, form, n_digits);  // :56
+            if (nsig_out) *nsig_out = n;
             st = bsg_bsm_to_dense(O, out, out_where);
             if (st) throw Error{st, bsg_last_error()};
         } catch (...) {
@@ -596,7 +657,13 @@ extern "C" bsg_status bsg_3c2c_transform(bsg_ctx ctx, size_t n_vec2, size_t n_au
 // device looks up the array's device address (cudaGetSymbolAddress) with
 // that device current; make that first call before any stream capture.
 // Every call reuses the same array, so calls that overlap on the GPU (other
-// streams, other host threads) race on it: serialize them.
+// streams, other host threads) race on it: serialize them.  The kernels go to
+// the caller's stream and use the current device's copy of the array, so the
+// current device must own the stream and every buffer (checked for the
+// buffers).  Without stats_out the call only enqueues work and does not wait
+// for the stream: integral keys are checked on the device, a key outside the
+// N_bf x N_bf matrix is skipped and K is set to NaN; with stats_out the call
+// waits for its stream once and also returns BSG_ERR_ARG for such a key.
 // ---------------------------------------------------------------------------
 
 namespace bsg {
@@ -634,6 +701,38 @@ __global__ void k_part_table(uint32_t *plo, uint32_t *phi, int T, size_t n_aux, 
     phi[t] = lo < hi ? (uint32_t)(hi - P0) : 0;
 }
 
+// decompress_integrals without a host-side key check: a key outside the
+// N_bf x N_bf matrix is skipped (never written) and raises *bad
+__global__ void k_scatter_guarded(const double *__restrict__ ints, const uint64_t *__restrict__ keys, size_t n_vec2,
+                                  size_t P0, size_t u_stride, double *__restrict__ U, int *__restrict__ bad) {
+    const size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t p = blockIdx.y;
+    if (v >= n_vec2) return;
+    const uint64_t key = keys[v];
+    if (key >= (uint64_t)u_stride) {
+        if (p == 0) atomicExch(bad, 1);
+        return;
+    }
+    U[p * u_stride + key] = ints[v + (P0 + p) * n_vec2];
+}
+
+// K = NaN everywhere when a key was bad, so the error shows in the output of
+// a call that does not wait for its stream
+__global__ void k_poison_if_bad(double *__restrict__ K, size_t n, const int *__restrict__ bad) {
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < n && *bad) K[e] = __longlong_as_double(0x7FF8000000000000ll);
+}
+
+// the device that owns a pointer (-1: host memory or unknown)
+static int owner_device(const void *p) {
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return -1;
+    }
+    return (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) ? at.device : -1;
+}
+
 struct ScratchLayout {
     size_t off = 0;
     size_t take(size_t bytes) {
@@ -655,6 +754,16 @@ extern "C" bsg_status bsg_rik_occ_step_noalloc(const bsg_rik_args *a, double *K_
         BSG_REQUIRE(a->n_vec2 == 0 || (a->ints && a->keys), BSG_ERR_ARG, "integrals or keys missing");
         BSG_REQUIRE(a->c_occ, BSG_ERR_ARG, "occupied coefficients missing");
         BSG_REQUIRE((size_t)a->bs * a->bs <= (size_t)kREPT * 256, BSG_ERR_UNSUPPORTED, "bs <= 64 required");
+        int cur = 0;
+        BSG_CUDA(cudaGetDevice(&cur));
+        // the kernels use the current device's copy of the scratch array, so the
+        // buffers (and with them the stream's work) must live on that device
+        for (const void *ptr : {(const void *)K_dev, (const void *)a->c_occ, (const void *)a->ints})
+            if (ptr) {
+                const int od = owner_device(ptr);
+                BSG_REQUIRE(od < 0 || od == cur, BSG_ERR_ARG,
+                            "allocation-free RI-K step: a device buffer belongs to another device than the current one");
+            }
         cudaStream_t s = (cudaStream_t)cuda_stream;
         const size_t n_bf = a->n_bf, n_occ = a->n_occ, bs = a->bs, n_aux = a->n_aux, n_vec2 = a->n_vec2;
         const size_t nb = ceil_div(n_bf, bs), nob = ceil_div(n_occ, bs);
@@ -709,13 +818,8 @@ extern "C" bsg_status bsg_rik_occ_step_noalloc(const bsg_rik_args *a, double *K_
         BSG_CUDA(cudaMemsetAsync(dK, 0, (size_t)T * n_bf * n_occ * 8, s));
         BSG_CUDA(cudaMemsetAsync(cnt, 0, 5 * 8, s));
         BSG_CUDA(cudaMemsetAsync(bad, 0, 4, s));
-        if (n_vec2) {
-            k_check_keys<<<(unsigned)ceil_div(n_vec2, 256), 256, 0, s>>>(a->keys, n_vec2, (uint64_t)(n_bf * n_bf), bad);
-            int h = 0;
-            BSG_CUDA(cudaMemcpyAsync(&h, bad, 4, cudaMemcpyDeviceToHost, s));
-            BSG_CUDA(cudaStreamSynchronize(s));
-            BSG_REQUIRE(!h, BSG_ERR_ARG, "v2m key outside the N_bf x N_bf matrix");
-        }
+        // keys are checked on the device (no wait for the stream here): a key
+        // outside the N_bf x N_bf matrix is never written, and K becomes NaN
         const int wpb = 8;
         k_cnorms<<<(unsigned)ceil_div(nb * nob, wpb), wpb * 32, 0, s>>>(a->c_occ, n_bf, n_occ, bs, nb, nob, dcn);
         const double tpb_u = 1e-20 * (double)(bs * bs);
@@ -725,7 +829,7 @@ extern "C" bsg_status bsg_rik_occ_step_noalloc(const bsg_rik_args *a, double *K_
             BSG_CUDA(cudaMemsetAsync(dU, 0, np * n_bf * n_bf * 8, s));
             if (n_vec2) {
                 dim3 g((unsigned)ceil_div(n_vec2, 256), (unsigned)np);
-                k_scatter<<<g, 256, 0, s>>>(a->ints, a->keys, n_vec2, P0, n_bf * n_bf, dU);
+                k_scatter_guarded<<<g, 256, 0, s>>>(a->ints, a->keys, n_vec2, P0, n_bf * n_bf, dU, bad);
             }
             k_unorms<<<(unsigned)ceil_div(np * nb * nb, wpb), wpb * 32, 0, s>>>(dU, n_bf, bs, nb, np, tpb_u, dun, duf);
             k_mui<<<(unsigned)(np * nb * nob), threads_for((int)bs, (int)bs), 0, s>>>(
@@ -743,12 +847,18 @@ extern "C" bsg_status bsg_rik_occ_step_noalloc(const bsg_rik_args *a, double *K_
             k_kreduce<<<(unsigned)ceil_div(n_bf * n_occ, 256), 256, 0, s>>>(dK, n_bf * n_occ, T, K_dev);
         else
             BSG_CUDA(cudaMemsetAsync(K_dev, 0, n_bf * n_occ * 8, s));
+        if (n_vec2 && n_aux)
+            k_poison_if_bad<<<(unsigned)ceil_div(n_bf * n_occ, 256), 256, 0, s>>>(K_dev, n_bf * n_occ, bad);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) throw Error{BSG_ERR_CUDA, std::string("rik (no-alloc) reduce: ") + cudaGetErrorString(e)};
         if (stats_out) {
+            // the one wait of the call: counters and the key check's verdict
             unsigned long long h[5];
+            int hb = 0;
             BSG_CUDA(cudaMemcpyAsync(h, cnt, 5 * 8, cudaMemcpyDeviceToHost, s));
+            BSG_CUDA(cudaMemcpyAsync(&hb, bad, 4, cudaMemcpyDeviceToHost, s));
             BSG_CUDA(cudaStreamSynchronize(s));
+            BSG_REQUIRE(!hb, BSG_ERR_ARG, "v2m key outside the N_bf x N_bf matrix (K set to NaN)");
             for (int i = 0; i < 5; ++i) stats_out[i] = h[i];
         }
     });

@@ -13,7 +13,21 @@ struct RikDev {
     double thresh = 0.0;
     int n_part = 1;
     int n_digits = 4;
+    // optional screen trace (device arrays of every aux function P, NULL =
+    // off), written per chunk: mui_P block norms and flags (nb x nob, index
+    // P*nb*nob + a + jb*nb), ij_P flags, ijs_P block norms and flags (nob x
+    // nob, index P*nob*nob + ib + jb*nob), and the C block norms (nb x nob)
+    double *tr_mui_norm = nullptr;
+    uint8_t *tr_mui_flag = nullptr;
+    uint8_t *tr_ij_flag = nullptr;
+    double *tr_ijs_norm = nullptr;
+    uint8_t *tr_ijs_flag = nullptr;
+    double *tr_c_norm = nullptr;
 };
+
+// copies one chunk's screening state (aux functions P0 .. P0+np) into the trace
+void rik_trace_chunk(const RikDev &d, size_t P0, size_t np, const double *mnorm, const uint8_t *mflag,
+                     const uint8_t *ijflag, const double *snorm, const uint8_t *sflag, cudaStream_t s);
 
 // K_dev (n_bf x n_occ) and Kmn_dev (n_bf x n_bf) may each be NULL (that
 // output is skipped); stats: the five occ-step counters and the K_mn products

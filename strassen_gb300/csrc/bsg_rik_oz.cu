@@ -925,6 +925,7 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
     // call-constant operands: C norms, C column exponents, C^T images
     const int wpb = 8;
     k_cnorms<<<(unsigned)ceil_div(nb * nob, wpb), wpb * 32, 0, s>>>(d.c_occ, n_bf, n_occ, bs, nb, nob, dcn.as<double>());
+    if (d.tr_c_norm) BSG_CUDA(cudaMemcpyAsync(d.tr_c_norm, dcn.p, nb * nob * 8, cudaMemcpyDeviceToDevice, s));
     k_cexp_C<<<(unsigned)nob, tb, 0, s>>>(d.c_occ, n_bf, n_occ, bs, dcexpC.as<int>());
     k_img_Ct_A<<<oz_img_grid(nob * nb), 32 * kOzImgWarps, 0, s>>>(d.c_occ, dcexpC.as<int>(), D, dimgCtA.as<bf16>());
     // inverse key map of the compressed integrals (replaces the per-P dense rebuild)
@@ -1049,6 +1050,8 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
         // ijs = ij + ij^T (FP64, with the reference's norm bookkeeping)
         k_ijs<<<(unsigned)(np * nob * nob), 128, 0, s>>>(dij.as<double>(), dijf.as<uint8_t>(), n_occ, bs, nob,
                                                           dijs.as<double>(), dsn.as<double>(), dsf.as<uint8_t>());
+        rik_trace_chunk(d, P0, np, dmn.as<double>(), dmf.as<uint8_t>(), dijf.as<uint8_t>(), dsn.as<double>(),
+                        dsf.as<uint8_t>(), s);
         // K += mui ijs
         k_colmax_ijs_sub<<<oz_img_grid(np * nob * nob), 32 * kOzImgWarps, 0, s>>>(
             dijs.as<double>(), dsf.as<uint8_t>(), n_occ, bs, nob, Q, np * nob * nob, bitsSs);

@@ -93,6 +93,33 @@ def decay_matrix(seed, stream, n, m, bs, L, core=0, core_val=1.0):
     return np.asfortranarray(env * gauss_matrix(seed, stream, n, m))
 
 
+def decay_matrix_torch(seed, stream, n, m, bs, L, core=0, core_val=1.0, device="cuda", cols_per_chunk=2048):
+    """decay_matrix generated on a torch device, bit-identical to it (the same
+    envelope table, the same deviates, one double multiply per element).
+    Returns an (m, n) row-major tensor, i.e. the n x m column-major matrix:
+    pass ``.T`` where a column-major n x m operand is expected."""
+    import torch
+
+    nbI, nbJ = -(-n // bs), -(-m // bs)
+    benv = np.exp(-np.abs(np.arange(nbI)[:, None] - np.arange(nbJ)[None, :]) / L)
+    key = stream_key(seed, stream)
+    out = torch.empty((m, n), dtype=torch.float64, device=device)
+    rb = torch.arange(n, device=device) // bs
+    r = torch.arange(n, dtype=torch.int64, device=device)
+    for c0 in range(0, m, cols_per_chunk):
+        c1 = min(m, c0 + cols_per_chunk)
+        c = torch.arange(c0, c1, dtype=torch.int64, device=device)
+        idx = r[None, :] + c[:, None] * n  # [c, r] = r + c n
+        env_c = torch.from_numpy(np.ascontiguousarray(benv[:, np.arange(c0, c1) // bs].T)).to(device)  # [c, I]
+        env = env_c[:, rb]
+        if core:
+            cc = min(core, c1) - c0
+            if cc > 0:
+                env[:cc, :core] = core_val
+        out[c0:c1] = env * gauss_torch(key, idx)
+    return out
+
+
 def block_mask_matrix(seed, stream, n, m, bs, density):
     """Block-Bernoulli(density) pattern with unit deviates inside kept blocks."""
     nbI, nbJ = -(-n // bs), -(-m // bs)

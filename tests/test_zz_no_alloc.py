@@ -21,7 +21,10 @@ from tests.conftest import same_bits
 pytestmark = pytest.mark.gpu
 
 
-def _noalloc(api, ints, keys, c_occ, n_bf, n_aux, n_occ, bs, thresh, n_part, p_chunk=0):
+def _noalloc(api, ints, keys, c_occ, n_bf, n_aux, n_occ, bs, thresh, n_part, p_chunk=0, stream=None, stats=True):
+    """one call through the C ABI; stream: a torch.cuda.Stream (None: the
+    legacy default stream); stats False passes stats_out = NULL, with which
+    the call only enqueues its kernels"""
     import torch
 
     K = torch.zeros((n_occ, n_bf), dtype=torch.float64, device="cuda").T  # column-major n_bf x n_occ
@@ -32,7 +35,10 @@ def _noalloc(api, ints, keys, c_occ, n_bf, n_aux, n_occ, bs, thresh, n_part, p_c
     fn.restype = C.c_int
     torch.cuda.synchronize()
     st = (C.c_uint64 * 5)()
-    rc = fn(C.byref(a), C.c_void_p(K.data_ptr()), None, st)
+    h = C.c_void_p(stream.cuda_stream) if stream is not None else None
+    rc = fn(C.byref(a), C.c_void_p(K.data_ptr()), h, st if stats else None)
+    if stream is not None:
+        stream.synchronize()
     torch.cuda.synchronize()
     return rc, K.cpu().numpy(), list(st)
 
@@ -80,3 +86,34 @@ def test_noalloc_rejects_oversize(api):
     c = torch.zeros((n_occ, n_bf), dtype=torch.float64, device="cuda").T
     rc, _, _ = _noalloc(api, ints, keys, c, n_bf, 1, n_occ, 32, 1e-10, 1)
     assert rc == 1 and b"32 MiB" in api.lib.bsg_last_error()
+
+
+def test_noalloc_on_a_stream_without_stats(api, ctx, h2o):
+    """on a non-default stream, stats_out NULL (the call only enqueues work):
+    the same bits, twice in a row"""
+    import torch
+
+    d = h2o
+    di, dk, dc = _dev(d["ints"]), _dev(d["keys"].view(np.int64)), _dev(d["c"])
+    K_ref = np.asarray(api.rik_occ_step(di, dk, dc, d["n_bf"], d["n_aux"], d["n_occ"], 3, 1e-20, n_part=2, ctx=ctx))
+    st = torch.cuda.Stream()
+    for _ in range(2):
+        rc, K, _ = _noalloc(api, di, dk, dc, d["n_bf"], d["n_aux"], d["n_occ"], 3, 1e-20, 2, stream=st, stats=False)
+        assert rc == 0, api.lib.bsg_last_error()
+        assert same_bits(K, K_ref)
+
+
+def test_noalloc_bad_key(api, ctx, h2o):
+    """a key outside the N_bf x N_bf matrix is never written: K is NaN, and a
+    call with stats_out also returns BSG_ERR_ARG; the next good call is exact"""
+    d = h2o
+    keys = d["keys"].copy()
+    keys[7] = d["n_bf"] * d["n_bf"]  # one past the matrix
+    di, dc = _dev(d["ints"]), _dev(d["c"])
+    rc, K, _ = _noalloc(api, di, _dev(keys.view(np.int64)), dc, d["n_bf"], d["n_aux"], d["n_occ"], 3, 1e-20, 1,
+                        stats=False)
+    assert rc == 0 and np.isnan(K).all()
+    rc, K, _ = _noalloc(api, di, _dev(keys.view(np.int64)), dc, d["n_bf"], d["n_aux"], d["n_occ"], 3, 1e-20, 1)
+    assert rc == 1 and b"v2m key" in api.lib.bsg_last_error()
+    assert np.isnan(K).all()
+    _case(api, ctx, d["ints"], d["keys"], d["c"], d["n_bf"], d["n_aux"], d["n_occ"], 3, 1e-20, 1)
