@@ -131,6 +131,27 @@ __device__ __forceinline__ double oz_i64_to_f64(long long x) {
     const unsigned long long m = (a << (52 - msb)) & 0xFFFFFFFFFFFFFull;
     return __longlong_as_double((long long)(sgn | ((unsigned long long)(msb + 1023) << 52) | m));
 }
+// int64 to double rounded to nearest even, with integer operations
+__device__ __forceinline__ double oz_i64_to_f64_rn(long long x) {
+    if (x == 0) return 0.0;
+    const unsigned long long sgn = x < 0 ? (1ull << 63) : 0ull;
+    const unsigned long long a = x < 0 ? 0ull - (unsigned long long)x : (unsigned long long)x;
+    int msb = 63 - __clzll((long long)a);
+    unsigned long long m;
+    if (msb <= 52) {
+        m = a << (52 - msb);
+    } else {
+        const int sh = msb - 52;
+        const unsigned long long rem = a & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+        m = a >> sh;
+        if (rem > half || (rem == half && (m & 1ull))) ++m;
+        if (m >> 53) {  // rounded up to the next power of two
+            m >>= 1;
+            ++msb;
+        }
+    }
+    return __longlong_as_double((long long)(sgn | ((unsigned long long)(msb + 1023) << 52) | (m & 0xFFFFFFFFFFFFFull)));
+}
 // an FP32 value as a double (exact; zero and subnormal inputs take the
 // hardware conversion)
 __device__ __forceinline__ double oz_f32_to_f64(float f) {
@@ -344,87 +365,126 @@ __global__ void __launch_bounds__(kOzThreads, 1)
                 }
             const uint32_t kstep = P.pair ? 2u : 1u;
             bool ok = true;
-            for (uint32_t t = oz_first_tile(P.chunk); t < n_tiles && ok; t = oz_next_tile(t, P.chunk)) {
-                const uint32_t ns = tiles[t].ns;
-                const uint32_t nch = (ns + P.F - 1) / P.F;
-                for (uint32_t c = 0; c < nch && ok; ++c, ++ch) {
-                    const uint32_t buf = P.nbuf == 2 ? (ch & 1u) : 0u, use = P.nbuf == 2 ? ch >> 1 : ch;
-                    long long c0 = prof ? clock64() : 0;
-                    if (!tc::mbar_wait(&tempty[buf], (use & 1u) ^ 1u, abort)) {
-                        ok = false;
-                        break;
-                    }
-                    if (prof) w_tmem += clock64() - c0;
-                    tc::tc_fence_after();
-                    const uint32_t dbase = tmem + buf * P.tmem_cols;
-                    const uint32_t kend = min(ns, (c + 1) * (uint32_t)P.F);
-                    for (uint32_t k = c * P.F; k < kend; k += kstep, ++it) {
-                        c0 = prof ? clock64() : 0;
-                        if (!tc::mbar_wait(&full[stage], ph, abort)) {
+            // the tile / chain / stage walk; issue(soff, k, ns, first, dbase)
+            // issues one stage's MMAs
+            auto mma_loop = [&](auto &&issue) {
+                for (uint32_t t = oz_first_tile(P.chunk); t < n_tiles && ok; t = oz_next_tile(t, P.chunk)) {
+                    const uint32_t ns = tiles[t].ns;
+                    const uint32_t nch = (ns + P.F - 1) / P.F;
+                    for (uint32_t c = 0; c < nch && ok; ++c, ++ch) {
+                        const uint32_t buf = P.nbuf == 2 ? (ch & 1u) : 0u, use = P.nbuf == 2 ? ch >> 1 : ch;
+                        long long c0 = prof ? clock64() : 0;
+                        if (!tc::mbar_wait(&tempty[buf], (use & 1u) ^ 1u, abort)) {
                             ok = false;
                             break;
                         }
-                        if (prof) w_full += clock64() - c0;
+                        if (prof) w_tmem += clock64() - c0;
                         tc::tc_fence_after();
-                        const uint32_t soff = stage * (stage_bytes >> 4);
-                        // k16 slices of this stage: kp / 16 of one step, or, for a
-                        // pair, the ncol (odd) slices over both halves' 2 ncol core
-                        // columns -- of a lone last step only those touching its half
-                        const uint32_t nq = !P.pair ? (uint32_t)P.kp / 16u : (k + 1 < ns ? ncol : (ncol + 1u) / 2u);
-                        // the first MMA of a chain (digit 0, which spans every TMEM
-                        // region) overwrites the accumulator
-                        uint32_t first = (k == c * P.F) ? 1u : 0u;
-                        // slice descriptors of this stage
-                        uint64_t aqs[8], bqs[8];
-#pragma unroll
-                        for (uint32_t q = 0; q < 8; ++q) {
-                            uint64_t aq = 0, bq = 0;
-                            if (q < nq) {
-                                if (!P.pair) {
-                                    aq = a_desc0 + soff + q * 16u;
-                                    bq = b_desc0 + soff + q * 16u;
-                                } else {
-                                    const uint32_t g = 2u * q;  // first core column of the slice
-                                    if (g + 1u < ncol) {        // both in the first half
-                                        aq = a_desc0 + soff + g * 8u;
-                                        bq = b_desc0 + soff + g * 8u;
-                                    } else if (g + 1u == ncol) {  // straddles the halves
-                                        aq = a_descx + soff + g * 8u;
-                                        bq = b_descx + soff + g * 8u;
-                                    } else {  // both in the second half
-                                        aq = a_desc0 + soff + ((half_bytes + (g - ncol) * 128u) >> 4);
-                                        bq = b_desc0 + soff + ((half_bytes + (g - ncol) * 128u) >> 4);
-                                    }
-                                }
+                        const uint32_t dbase = tmem + buf * P.tmem_cols;
+                        const uint32_t kend = min(ns, (c + 1) * (uint32_t)P.F);
+                        for (uint32_t k = c * P.F; k < kend; k += kstep, ++it) {
+                            c0 = prof ? clock64() : 0;
+                            if (!tc::mbar_wait(&full[stage], ph, abort)) {
+                                ok = false;
+                                break;
                             }
-                            aqs[q] = aq;
-                            bqs[q] = bq;
-                        }
-                        // digit by digit, each over the stage's k16 slices: consecutive
-                        // MMAs accumulate into the same TMEM columns (a k chain), and
-                        // the first MMA of a chain (digit 0, which spans every region)
-                        // overwrites the accumulator
-#pragma unroll
-                        for (int e = 0; e < kMaxPlan; ++e) {
-                            if (e >= n_plan) break;
-                            const uint32_t dt = dbase + (pd[e] & 0xFFFFu);
-#pragma unroll
-                            for (uint32_t q = 0; q < 8; ++q) {
-                                if (q >= nq) break;
-                                const uint32_t ac = (first && q == 0 && (pd[e] >> 16)) ? 0u : 1u;
-                                tc::mma_bf16(dt, aqs[q] + pa[e], bqs[q] + pb[e], pi[e], ac);
+                            if (prof) w_full += clock64() - c0;
+                            tc::tc_fence_after();
+                            const uint32_t soff = stage * (stage_bytes >> 4);
+                            // the first MMA of a chain (digit 0, which spans every TMEM
+                            // region) overwrites the accumulator
+                            issue(soff, k, ns, (k == c * P.F) ? 1u : 0u, dbase);
+                            tc::mma_commit(&empty[stage]);
+                            if (++stage == (uint32_t)P.S) {
+                                stage = 0;
+                                ph ^= 1u;
                             }
                         }
-                        if (prof) n_mma += (unsigned long long)n_plan * nq;
-                        tc::mma_commit(&empty[stage]);
-                        if (++stage == (uint32_t)P.S) {
-                            stage = 0;
-                            ph ^= 1u;
+                        if (!ok) break;
+                        tc::mma_commit(&tfull[buf]);
+                    }
+                }
+            };
+            // any shape: the plan computed above, slices per stage at run time
+            auto issue_generic = [&](uint32_t soff, uint32_t k, uint32_t ns, uint32_t first, uint32_t dbase) {
+                // k16 slices of this stage: kp / 16 of one step, or, for a
+                // pair, the ncol (odd) slices over both halves' 2 ncol core
+                // columns -- of a lone last step only those touching its half
+                const uint32_t nq = !P.pair ? (uint32_t)P.kp / 16u : (k + 1 < ns ? ncol : (ncol + 1u) / 2u);
+                // slice descriptors of this stage
+                uint64_t aqs[8], bqs[8];
+#pragma unroll
+                for (uint32_t q = 0; q < 8; ++q) {
+                    uint64_t aq = 0, bq = 0;
+                    if (q < nq) {
+                        if (!P.pair) {
+                            aq = a_desc0 + soff + q * 16u;
+                            bq = b_desc0 + soff + q * 16u;
+                        } else {
+                            const uint32_t g = 2u * q;  // first core column of the slice
+                            if (g + 1u < ncol) {        // both in the first half
+                                aq = a_desc0 + soff + g * 8u;
+                                bq = b_desc0 + soff + g * 8u;
+                            } else if (g + 1u == ncol) {  // straddles the halves
+                                aq = a_descx + soff + g * 8u;
+                                bq = b_descx + soff + g * 8u;
+                            } else {  // both in the second half
+                                aq = a_desc0 + soff + ((half_bytes + (g - ncol) * 128u) >> 4);
+                                bq = b_desc0 + soff + ((half_bytes + (g - ncol) * 128u) >> 4);
+                            }
                         }
                     }
-                    if (!ok) break;
-                    tc::mma_commit(&tfull[buf]);
+                    aqs[q] = aq;
+                    bqs[q] = bq;
                 }
+                // digit by digit, each over the stage's k16 slices: consecutive
+                // MMAs accumulate into the same TMEM columns (a k chain), and
+                // the first MMA of a chain (digit 0, which spans every region)
+                // overwrites the accumulator
+#pragma unroll
+                for (int e = 0; e < kMaxPlan; ++e) {
+                    if (e >= n_plan) break;
+                    const uint32_t dt = dbase + (pd[e] & 0xFFFFu);
+#pragma unroll
+                    for (uint32_t q = 0; q < 8; ++q) {
+                        if (q >= nq) break;
+                        const uint32_t ac = (first && q == 0 && (pd[e] >> 16)) ? 0u : 1u;
+                        tc::mma_bf16(dt, aqs[q] + pa[e], bqs[q] + pb[e], pi[e], ac);
+                    }
+                }
+                if (prof) n_mma += (unsigned long long)n_plan * nq;
+            };
+            // blocks of 24 in step pairs, 5 digits, two N-side blocks (every
+            // product of the RI-K step on 24-wide blocks): each descriptor is a
+            // fixed offset from the stage's three A and three B slice
+            // descriptors (only their low words depend on the stage) and the
+            // MMA sequence is unrolled at compile time -- the single issuing
+            // thread's instruction latency otherwise paces the tensor core
+            auto issue_fixed = [&](uint32_t soff, uint32_t k, uint32_t ns, uint32_t first, uint32_t dbase) {
+                constexpr uint32_t KP = 24, ND = 5;
+                const uint32_t a_hi = (uint32_t)(a_desc0 >> 32), b_hi = (uint32_t)(b_desc0 >> 32);
+                const uint32_t h2 = (half_bytes + 128u) >> 4;  // the second half's core column 1
+                const uint32_t a0 = (uint32_t)a_desc0 + soff, ax = (uint32_t)a_descx + soff + 16u, a2 = a0 + h2;
+                const uint32_t b0 = (uint32_t)b_desc0 + soff, bx = (uint32_t)b_descx + soff + 16u, b2 = b0 + h2;
+                const bool three = k + 1 < ns;  // a lone last step: the first two slices
+                auto d64 = [](uint32_t lo, uint32_t hi) { return ((uint64_t)hi << 32) | lo; };
+#pragma unroll
+                for (uint32_t i = 0; i < ND; ++i) {
+                    const uint32_t dt = dbase + i * (uint32_t)NP, pa = i * KP;
+                    const uint32_t id = tc::idesc_bf16_f32(128u, ((ND - i) * (uint32_t)NP + 15u) & ~15u);
+                    tc::mma_bf16(dt, d64(a0 + pa, a_hi), d64(b0, b_hi), id, (first && i == 0) ? 0u : 1u);
+                    tc::mma_bf16(dt, d64(ax + pa, a_hi), d64(bx, b_hi), id, 1u);
+                    if (three) tc::mma_bf16(dt, d64(a2 + pa, a_hi), d64(b2, b_hi), id, 1u);
+                }
+                if (prof) n_mma += three ? 3u * ND : 2u * ND;
+            };
+            if constexpr (NP == 48) {
+                if (P.nd == 5 && P.pair && P.kp == 24 && n_plan == 5)
+                    mma_loop(issue_fixed);
+                else
+                    mma_loop(issue_generic);
+            } else {
+                mma_loop(issue_generic);
             }
             if (prof) {
                 atomicAdd(&P.prof[kProfMmaWaitFull], w_full);
@@ -531,38 +591,55 @@ __global__ void __launch_bounds__(kOzThreads, 1)
                     }
                     cex[j] = (c < tcols && (!subm || cc < tsub)) ? tcexp[subm ? js * tcexp_sub + cc : c] : 0;
                 }
-                // column j of this group: output address (null = not stored) and value
-                auto col_out = [&](int j, double *&dst) -> double {
-                    const int c = cbase + j;
-                    int cc = c, js = 0;
-                    if (subm) {
-                        js = c >= (js0 + 1) * npj ? js0 + 1 : js0;
-                        cc = c - js * npj;
+                // every output of the group, its value from total(j) scaled by
+                // 2^(er + de + cex): one loop per way of forming the total, so
+                // that no element pays for both
+                auto store_all = [&](auto &&total, int de) {
+                    // column j of this group: output address (null = not stored) and value
+                    auto col_out = [&](int j, double *&dst) -> double {
+                        const int c = cbase + j;
+                        int cc = c, js = 0;
+                        if (subm) {
+                            js = c >= (js0 + 1) * npj ? js0 + 1 : js0;
+                            cc = c - js * npj;
+                        }
+                        dst = nullptr;
+                        if (!(c < tcols && (!subm || cc < tsub))) return 0.0;
+                        double out = oz_scale_pow2(total(j), er + de + cex[j]);
+                        if (!unit) out = __dmul_rn(P.alpha, out);
+                        double *base = subm ? cp + js * tsub_stride : cp;
+                        dst = ttrans ? base + cc + (size_t)r * ldc : base + r + (size_t)cc * ldc;
+                        return out;
+                    };
+#pragma unroll
+                    for (int j = 0; j < NPH; j += 2) {
+                        double *d0, *d1;
+                        const double o0 = col_out(j, d0), o1 = col_out(j + 1, d1);
+                        // a transposed tile's row is contiguous in the output: pairs of
+                        // columns go as one 16-byte store when adjacent and aligned
+                        if (fresh && d0 && d1 == d0 + 1 && ((reinterpret_cast<uintptr_t>(d0) & 15u) == 0u)) {
+                            *reinterpret_cast<double2 *>(d0) = make_double2(o0, o1);
+                        } else {
+                            if (d0) *d0 = fresh ? o0 : __dadd_rn(*d0, o0);
+                            if (d1) *d1 = fresh ? o1 : __dadd_rn(*d1, o1);
+                        }
                     }
-                    dst = nullptr;
-                    if (!(c < tcols && (!subm || cc < tsub))) return 0.0;
+                };
+                if (P.nd <= 5 && nch < 256) {
+                    // up to 5 digits lo holds weights 3 and 4, multiples of 2^-32,
+                    // so lo 2^32 is an integer (below 2^34) and hi 2^16 + lo 2^32
+                    // the exact sum in units of 2^-32 (hi < 2^39 per chain of <= 512
+                    // k, so below 2^63 for < 256 chains): one rounding to double, the
+                    // same as the FP64 add below makes, without the FP64 pipe
+                    store_all([&](int j) {
+                        return oz_i64_to_f64_rn(hi[j] * 65536ll + __float2ll_rn(lo[j] * 4294967296.f));
+                    }, -16);
+                } else {
                     // both terms are exact doubles built with integer operations
                     // (|hi| < 2^53, lo 2^16 an FP32 value): one FP64 add rounds,
                     // and the power of two goes into the exponent field
-                    const double tot = __dadd_rn(oz_i64_to_f64(hi[j]), oz_f32_to_f64(lo[j] * 65536.f));
-                    double out = oz_scale_pow2(tot, er + cex[j]);
-                    if (!unit) out = __dmul_rn(P.alpha, out);
-                    double *base = subm ? cp + js * tsub_stride : cp;
-                    dst = ttrans ? base + cc + (size_t)r * ldc : base + r + (size_t)cc * ldc;
-                    return out;
-                };
-#pragma unroll
-                for (int j = 0; j < NPH; j += 2) {
-                    double *d0, *d1;
-                    const double o0 = col_out(j, d0), o1 = col_out(j + 1, d1);
-                    // a transposed tile's row is contiguous in the output: pairs of
-                    // columns go as one 16-byte store when adjacent and aligned
-                    if (fresh && d0 && d1 == d0 + 1 && ((reinterpret_cast<uintptr_t>(d0) & 15u) == 0u)) {
-                        *reinterpret_cast<double2 *>(d0) = make_double2(o0, o1);
-                    } else {
-                        if (d0) *d0 = fresh ? o0 : __dadd_rn(*d0, o0);
-                        if (d1) *d1 = fresh ? o1 : __dadd_rn(*d1, o1);
-                    }
+                    store_all([&](int j) { return __dadd_rn(oz_i64_to_f64(hi[j]), oz_f32_to_f64(lo[j] * 65536.f)); },
+                              0);
                 }
                 if (fresh && r == 0 && grp == 0 && T.cnorm[s]) *T.cnorm[s] = 0.0;
             }
