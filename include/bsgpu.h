@@ -187,18 +187,28 @@ bsg_status bsg_ctx_autotune_entries(bsg_ctx ctx, int *entries, int cap, int *n);
 /* ---- learned Strassen scheduling (no counterpart in the reference, whose
  *      choice is the cost model of matmult_strassen_dryrun,
  *      strassen.hpp:602-640) ----
- * Policies for the per-node Strassen-or-sparse choice:
- *   BSG_SCHED_COST  the reference's cost model (what bsg_matmult_strassen_sparse does)
- *   BSG_SCHED_NONE  no Strassen node: screened sparse recursion only
- *   BSG_SCHED_ROOT  Strassen at the root node only (block count a power of two)
- *   BSG_SCHED_MLP   a trained bsg_sched: Strassen where the network predicts
- *                   log(t_strassen / t_sparse) < 0 on nodes whose blocks are all
- *                   present; levels with more than 65536 nodes keep the cost model
- * A bsg_sched is a 2 x 64 MLP (25 node features: level, flop counts, block
- * densities, log-norm histograms) trained on the device by the library's own
- * forward / backward / Adam kernels. */
-enum { BSG_SCHED_COST = 0, BSG_SCHED_NONE = 1, BSG_SCHED_ROOT = 2, BSG_SCHED_MLP = 3 };
-#define BSG_SCHED_FEATURES 25
+ * Policies for the per-node choice (a node is a quadrant product of the
+ * hybrid recursion, strassen.hpp:418-508):
+ *   BSG_SCHED_COST   the reference's cost model (what bsg_matmult_strassen_sparse does)
+ *   BSG_SCHED_NONE   no Strassen node: screened sparse recursion only
+ *   BSG_SCHED_ROOT   Strassen at the root node only (block count a power of two),
+ *                    recursing to min_size_for_strassen
+ *   BSG_SCHED_DENSE  the root node's product as one dense tile (every block
+ *                    product, unscreened)
+ *   BSG_SCHED_MLP    a trained bsg_sched: per node whose blocks are all present,
+ *                    the option with the smallest predicted log(t_option /
+ *                    t_sparse) among Strassen-Winograd of depth 1, 2 or 3 at the
+ *                    node and a dense tile, where that prediction is < 0; the
+ *                    screened sparse recursion elsewhere; levels with more than
+ *                    65536 nodes keep the cost model
+ * A bsg_sched is a 2 x 64 MLP on BSG_SCHED_FEATURES inputs: 25 node features
+ * (level, flop counts, block densities, log-norm histograms) and the option
+ * one-hot (depth 1, 2, 3, dense tile), trained on the device by the library's
+ * own forward / backward / Adam kernels. */
+enum { BSG_SCHED_COST = 0, BSG_SCHED_NONE = 1, BSG_SCHED_ROOT = 2, BSG_SCHED_MLP = 3, BSG_SCHED_DENSE = 4 };
+#define BSG_SCHED_NODE_FEATURES 25
+#define BSG_SCHED_OPTIONS 4
+#define BSG_SCHED_FEATURES 29
 bsg_status bsg_sched_create(bsg_ctx ctx, bsg_sched *out);
 bsg_status bsg_sched_destroy(bsg_sched sched);
 bsg_status bsg_sched_param_count(int *out);
@@ -212,11 +222,12 @@ bsg_status bsg_sched_loss_grad(bsg_sched sched, const float *x, const float *t, 
 /* Adam on the mean squared error, minibatches of a seeded shuffle */
 bsg_status bsg_sched_train(bsg_sched sched, const float *x, const float *t, int n, int epochs, int batch, float lr,
                            uint64_t seed, float *final_loss);
-/* features and eligibility of the root node of C = A B's decision tree */
+/* node features (BSG_SCHED_NODE_FEATURES floats) and eligibility of the root
+ * node of C = A B's decision tree */
 bsg_status bsg_strassen_root_features(bsg_bsm C, bsg_bsm A, bsg_bsm B, double thresh, float *features,
                                       int *eligible);
 /* matmult_strassen_sparse with a scheduling policy; n_strassen_nodes (may be
- * NULL) receives the number of Strassen nodes that ran */
+ * NULL) receives the number of nodes that ran Strassen or a dense tile */
 bsg_status bsg_matmult_strassen_sparse_sched(bsg_bsm C, bsg_bsm A, bsg_bsm B, double thresh,
                                              size_t min_size_for_strassen, int form, int n_digits, int policy,
                                              bsg_sched sched, uint64_t *n_strassen_nodes);

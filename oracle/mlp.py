@@ -1,13 +1,13 @@
 """CPU oracle of the Strassen scheduler's MLP (test infrastructure only).
 
-The same parameter layout as strassen_gb300/csrc/bsg_sched.cu -- W1 [64 x 25],
+The same parameter layout as strassen_gb300/csrc/bsg_sched.cu -- W1 [64 x 29],
 b1 [64], W2 [64 x 64], b2 [64], W3 [64], b3 [1], float32 on the device -- and
 the forward pass y = W3 relu(W2 relu(W1 x + b1) + b2) + b3 with the mean
 squared error loss and its gradient, here in float64 numpy.
 """
 import numpy as np
 
-IN, H = 25, 64
+IN, H = 29, 64  # 25 node features + 4 option one-hot inputs
 N_PARAMS = H * IN + H + H * H + H + H + 1
 
 

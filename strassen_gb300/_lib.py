@@ -121,8 +121,9 @@ _sig("bsg_batched_plan_destroy", [c_vp])
 _sig("bsg_ctx_set_autotune", [c_vp, c_int])
 _sig("bsg_ctx_autotune_entries", [c_vp, c_vp, c_int, C.POINTER(c_int)])
 
-SCHED_COST, SCHED_NONE, SCHED_ROOT, SCHED_MLP = 0, 1, 2, 3
-SCHED_FEATURES = 25
+SCHED_COST, SCHED_NONE, SCHED_ROOT, SCHED_MLP, SCHED_DENSE = 0, 1, 2, 3, 4
+SCHED_NODE_FEATURES, SCHED_OPTIONS = 25, 4
+SCHED_FEATURES = SCHED_NODE_FEATURES + SCHED_OPTIONS
 
 
 def check(status):

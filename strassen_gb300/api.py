@@ -23,7 +23,8 @@ import ctypes as C
 import numpy as np
 
 from ._lib import BSG_DEVICE, BSG_HOST, FORM_FP64, FORM_OZAKI, BsgError, RikArgs, ScreenTrace, check, lib  # noqa: F401
-from ._lib import SCHED_COST, SCHED_FEATURES, SCHED_MLP, SCHED_NONE, SCHED_ROOT  # noqa: F401
+from ._lib import (SCHED_COST, SCHED_DENSE, SCHED_FEATURES, SCHED_MLP, SCHED_NODE_FEATURES, SCHED_NONE,  # noqa: F401
+                   SCHED_OPTIONS, SCHED_ROOT)
 
 _DEFAULT_CTX = None
 
@@ -340,8 +341,9 @@ class BatchPlan:
 
 
 class StrassenScheduler:
-    """The learned Strassen-or-sparse node scheduler (a 2 x 64 MLP on the
-    device; forward, backward and Adam are the library's own kernels)."""
+    """The learned node scheduler of the hybrid recursion (a 2 x 64 MLP on the
+    device scoring Strassen depths and the dense tile against the sparse
+    recursion; forward, backward and Adam are the library's own kernels)."""
 
     def __init__(self, ctx=None, seed=None):
         self.ctx = ctx or default_context()
@@ -396,18 +398,31 @@ class StrassenScheduler:
 
 
 def strassen_root_features(C_, A, B, thresh):
-    """features of the root node of C = A B's Strassen decision tree and
-    whether it may run Strassen (all blocks present, not an edge node)"""
-    f = np.empty(SCHED_FEATURES, np.float32)
+    """node features of the root node of C = A B's Strassen decision tree and
+    whether it may run Strassen or a dense tile (all blocks present, not an
+    edge node)"""
+    f = np.empty(SCHED_NODE_FEATURES, np.float32)
     ok = C.c_int()
     check(lib.bsg_strassen_root_features(C_.h, A.h, B.h, float(thresh), f.ctypes.data, C.byref(ok)))
     return f, bool(ok.value)
 
 
+def option_rows(features, options=None):
+    """network inputs: node features followed by the one-hot of an option
+    (0..2 Strassen depth 1..3, 3 dense tile); one row per (node, option)"""
+    F = np.asarray(features, np.float32).reshape(-1, SCHED_NODE_FEATURES)
+    opts = np.asarray(range(SCHED_OPTIONS) if options is None else options, np.int64)
+    X = np.zeros((len(F) * len(opts), SCHED_FEATURES), np.float32)
+    X[:, :SCHED_NODE_FEATURES] = np.repeat(F, len(opts), axis=0)
+    X[np.arange(len(X)), SCHED_NODE_FEATURES + np.tile(opts, len(F))] = 1.0
+    return X
+
+
 def matmult_strassen_sparse_sched(C_, A, B, thresh, min_size_for_strassen, policy=SCHED_COST, sched=None,
                                   form=FORM_FP64, n_digits=4):
-    """matmult_strassen_sparse with a Strassen scheduling policy; returns the
-    number of Strassen nodes that ran"""
+    """matmult_strassen_sparse with a scheduling policy (SCHED_COST, _NONE,
+    _ROOT, _DENSE, _MLP); returns the number of nodes that ran Strassen or a
+    dense tile"""
     n = C.c_uint64()
     check(lib.bsg_matmult_strassen_sparse_sched(C_.h, A.h, B.h, float(thresh), int(min_size_for_strassen), form,
                                                 int(n_digits), int(policy), sched.h if sched is not None else None,

@@ -182,7 +182,7 @@ __global__ void k_node_features(double *const *__restrict__ A, const double *__r
         }
         const double nfl = (double)nf[node], cst = (double)cost;
         const double dense = 2.0 * (double)bs * bs * bs * (double)((ib1 - ib0) * (jb1 - jb0) * (kb1 - kb0));
-        float *f = F + node * kSchedIn;
+        float *f = F + node * kSchedNodeIn;
         f[0] = (float)level / 8.f;
         f[1] = (float)log2((double)sb) / 8.f;
         f[2] = (float)(log2(1.0 + nfl) / 64.0);
@@ -200,16 +200,46 @@ __global__ void k_node_features(double *const *__restrict__ A, const double *__r
     }
 }
 
-// tree[i] = ok[i] && y[i] < 0 (the network predicts Strassen to be faster)
-__global__ void k_sched_decide(const uint8_t *__restrict__ ok, const float *__restrict__ y, size_t n,
-                               uint8_t *__restrict__ tree) {
-    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) tree[i] = ok[i] && y[i] < 0.f;
+// option rows: node features, then the option's one-hot
+__global__ void k_option_rows(const float *__restrict__ F, size_t n, float *__restrict__ X) {
+    const size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n * kSchedOpts) return;
+    const size_t i = r / kSchedOpts;
+    const int o = (int)(r % kSchedOpts);
+    float *x = X + r * kSchedIn;
+    for (int j = 0; j < kSchedNodeIn; ++j) x[j] = F[i * kSchedNodeIn + j];
+    for (int j = 0; j < kSchedOpts; ++j) x[kSchedNodeIn + j] = j == o ? 1.f : 0.f;
 }
 
-void launch_sched_decide(bsg_ctx ctx, const uint8_t *ok, const float *y, size_t n, uint8_t *tree) {
+void launch_option_rows(bsg_ctx ctx, const float *F, size_t n, float *X) {
     if (!n) return;
-    k_sched_decide<<<(unsigned)ceil_div(n, (size_t)256), 256, 0, ctx->stream>>>(ok, y, n, tree);
+    k_option_rows<<<(unsigned)ceil_div(n * kSchedOpts, (size_t)256), 256, 0, ctx->stream>>>(F, n, X);
+    ctx->note_launch();
+    ctx->check_launch("scheduler option rows");
+}
+
+// per node the option the network predicts fastest, where it beats the
+// sparse recursion (options in order, ties to the first)
+__global__ void k_sched_decide(const uint8_t *__restrict__ ok, const float *__restrict__ y, size_t n, int level,
+                               uint8_t *__restrict__ tree) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int best = -1;
+    float yb = 0.f;
+    for (int o = 0; o < kSchedOpts; ++o) {
+        const bool valid = o == kSchedOpts - 1 || o <= level;  // depth o + 1 needs 2^o | 2^level
+        const float v = y[i * kSchedOpts + o];
+        if (valid && v < yb) {
+            yb = v;
+            best = o;
+        }
+    }
+    tree[i] = (ok[i] && best >= 0) ? (uint8_t)(kNodeDepth1 + best) : kNodeSparse;
+}
+
+void launch_sched_decide(bsg_ctx ctx, const uint8_t *ok, const float *y, size_t n, int level, uint8_t *tree) {
+    if (!n) return;
+    k_sched_decide<<<(unsigned)ceil_div(n, (size_t)256), 256, 0, ctx->stream>>>(ok, y, n, level, tree);
     ctx->note_launch();
     ctx->check_launch("scheduler decisions");
 }

@@ -4,18 +4,36 @@
 
 namespace bsg {
 
-constexpr int kSchedIn = 25;  // node features
+constexpr int kSchedNodeIn = 25;  // node features
+// options the network scores per node (one-hot after the node features):
+// Strassen-Winograd of depth 1, 2, 3 at the node, or the node's product as
+// one dense tile (every block product, unscreened)
+constexpr int kSchedOpts = 4;
+constexpr int kSchedIn = kSchedNodeIn + kSchedOpts;  // network input
 constexpr int kSchedH = 64;   // hidden width (two hidden layers)
+
+// Decision-tree byte of a node: 0 screened sparse recursion, 1 Strassen with
+// the call's min_size_for_strassen, 2..4 Strassen of depth 1..3 at the node,
+// 5 dense tile
+constexpr uint8_t kNodeSparse = 0, kNodeStrassen = 1, kNodeDepth1 = 2, kNodeDense = 5;
 constexpr int kSchedParams = kSchedH * kSchedIn + kSchedH + kSchedH * kSchedH + kSchedH + kSchedH + 1;
 
-// features (kSchedIn floats per node, row-major) and eligibility of every node
-// of one level of the Strassen decision tree; nf / edge / cost from the dry run
+// features (kSchedNodeIn floats per node, row-major) and eligibility of every
+// node of one level of the Strassen decision tree; nf / edge / cost from the
+// dry run
 void launch_node_features(bsg_bsm A, bsg_bsm B, bsg_bsm C, int level, size_t nsi, size_t nsj, size_t nsk,
                           const unsigned long long *nf, const uint8_t *edge, unsigned long long cost, float *F,
                           uint8_t *ok);
 
-// tree[i] = ok[i] && y[i] < 0
-void launch_sched_decide(bsg_ctx ctx, const uint8_t *ok, const float *y, size_t n, uint8_t *tree);
+// network inputs X (n * kSchedOpts rows of kSchedIn: node i's features with
+// option o one-hot at row i * kSchedOpts + o) from the node features F
+void launch_option_rows(bsg_ctx ctx, const float *F, size_t n, float *X);
+
+// tree[i]: the option with the smallest predicted log(t_option / t_sparse)
+// among those valid at the level (depth t needs 2^(t-1) to divide the half
+// side 2^level), kNodeDepth1 + o, where ok[i] and that prediction is < 0;
+// kNodeSparse otherwise
+void launch_sched_decide(bsg_ctx ctx, const uint8_t *ok, const float *y, size_t n, int level, uint8_t *tree);
 
 }  // namespace bsg
 

@@ -519,20 +519,20 @@ __global__ void __launch_bounds__(256) k_apply(double *const *__restrict__ Cp, d
     if (threadIdx.x == 0 && cnt) atomicAdd(nsig, cnt);
 }
 
-// Features (host copy, kSchedIn floats per node) and eligibility of the nodes
-// of one dry-run level.
+// Features (host copy, kSchedNodeIn floats per node) and eligibility of the
+// nodes of one dry-run level.
 static void level_features(bsg_bsm C, bsg_bsm A, bsg_bsm B, const DryResult &R, int L, std::vector<float> &F,
                            std::vector<uint8_t> &ok, DevBuf *dF_keep = nullptr) {
     cudaStream_t s = A->ctx->stream;
     const size_t sb = (size_t)1 << (L + 1);
     const size_t nsi = ceil_div(A->nrb, sb), nsj = ceil_div(B->ncb, sb), nsk = ceil_div(A->ncb, sb);
     const size_t n = nsi * nsj * nsk;
-    DevBuf dF(n * kSchedIn * 4, s), dok(n, s);
+    DevBuf dF(n * kSchedNodeIn * 4, s), dok(n, s);
     launch_node_features(A, B, C, L, nsi, nsj, nsk, R.nf[L].as<unsigned long long>(), R.edge[L].as<uint8_t>(),
                          R.cost[L], dF.as<float>(), dok.as<uint8_t>());
-    F.resize(n * kSchedIn);
+    F.resize(n * kSchedNodeIn);
     ok.resize(n);
-    BSG_CUDA(cudaMemcpyAsync(F.data(), dF.p, n * kSchedIn * 4, cudaMemcpyDeviceToHost, s));
+    BSG_CUDA(cudaMemcpyAsync(F.data(), dF.p, n * kSchedNodeIn * 4, cudaMemcpyDeviceToHost, s));
     BSG_CUDA(cudaMemcpyAsync(ok.data(), dok.p, n, cudaMemcpyDeviceToHost, s));
     BSG_CUDA(cudaStreamSynchronize(s));
     if (dF_keep) *dF_keep = std::move(dF);
@@ -549,13 +549,13 @@ static void apply_policy(bsg_bsm C, bsg_bsm A, bsg_bsm B, DryResult &R, int poli
         for (auto &t : R.tree) std::fill(t.begin(), t.end(), 0);
         return;
     }
-    if (policy == BSG_SCHED_ROOT) {
+    if (policy == BSG_SCHED_ROOT || policy == BSG_SCHED_DENSE) {
         for (auto &t : R.tree) std::fill(t.begin(), t.end(), 0);
         if (NL == 0 || R.tree[NL - 1].size() != 1) return;  // no single root node
         std::vector<float> F;
         std::vector<uint8_t> ok;
         level_features(C, A, B, R, NL - 1, F, ok);
-        R.tree[NL - 1][0] = ok[0];
+        R.tree[NL - 1][0] = ok[0] ? (policy == BSG_SCHED_ROOT ? kNodeStrassen : kNodeDense) : kNodeSparse;
         return;
     }
     BSG_REQUIRE(policy == BSG_SCHED_MLP && sched, BSG_ERR_ARG, "BSG_SCHED_MLP needs a scheduler");
@@ -567,16 +567,20 @@ static void apply_policy(bsg_bsm C, bsg_bsm A, bsg_bsm B, DryResult &R, int poli
     std::vector<int> levels;
     for (int L = 0; L < NL; ++L) {
         const size_t n = R.tree[L].size();
-        if (n > kSchedMaxNodes || !n) continue;  // cost model
+        if (n > kSchedMaxNodes || !n) continue;  // cost model (its Strassen nodes use the call's min_size)
         const size_t sb = (size_t)1 << (L + 1);
-        DevBuf dF(n * kSchedIn * 4, s), dok(n, s), dY(n * 4, s), dT(n, s);
+        DevBuf dF(n * kSchedNodeIn * 4, s), dX(n * kSchedOpts * kSchedIn * 4, s), dok(n, s),
+            dY(n * kSchedOpts * 4, s), dT(n, s);
         launch_node_features(A, B, C, L, ceil_div(A->nrb, sb), ceil_div(B->ncb, sb), ceil_div(A->ncb, sb),
                              R.nf[L].as<unsigned long long>(), R.edge[L].as<uint8_t>(), R.cost[L], dF.as<float>(),
                              dok.as<uint8_t>());
-        sched->predict_dev(dF.as<float>(), (int)n, dY.as<float>());  // predicted log(t_strassen / t_sparse)
-        launch_sched_decide(A->ctx, dok.as<uint8_t>(), dY.as<float>(), n, dT.as<uint8_t>());
+        launch_option_rows(A->ctx, dF.as<float>(), n, dX.as<float>());
+        // predicted log(t_option / t_sparse) of every (node, option)
+        sched->predict_dev(dX.as<float>(), (int)(n * kSchedOpts), dY.as<float>());
+        launch_sched_decide(A->ctx, dok.as<uint8_t>(), dY.as<float>(), n, L, dT.as<uint8_t>());
         BSG_CUDA(cudaMemcpyAsync(R.tree[L].data(), dT.p, n, cudaMemcpyDeviceToHost, s));
         keep.push_back(std::move(dF));
+        keep.push_back(std::move(dX));
         keep.push_back(std::move(dok));
         keep.push_back(std::move(dY));
         keep.push_back(std::move(dT));
@@ -612,6 +616,7 @@ static void strassen_sparse(bsg_bsm C, bsg_bsm A, bsg_bsm B, double thresh, size
     struct Node {
         int L;
         size_t si, sj, sk;
+        uint8_t opt;  // decision-tree byte: Strassen (the call's min_size or a depth) or dense tile
     };
     std::vector<Node> nodes;
     std::vector<std::vector<uint8_t>> cov(NL);
@@ -631,7 +636,7 @@ static void strassen_sparse(bsg_bsm C, bsg_bsm A, bsg_bsm B, double thresh, size
                     cov[L][idx] = above || t;
                     if (t && !above) {
                         node_of[lvl_off[L] + idx] = (int)nodes.size();
-                        nodes.push_back(Node{L, si, sj, sk});
+                        nodes.push_back(Node{L, si, sj, sk, R.tree[L][idx]});
                     }
                 }
     }
@@ -647,47 +652,76 @@ static void strassen_sparse(bsg_bsm C, bsg_bsm A, bsg_bsm B, double thresh, size
                             "strassen: C must be fully allocated (fill_with_values) on Strassen nodes");
             }
     }
-    // Winograd recursion per node size
+    // Winograd recursion per node size and depth; dense tiles per node size
     std::vector<DevBuf> sbufs;
     std::vector<double *> node_S(std::max<size_t>(nodes.size(), 1), nullptr);
     for (int L = 0; L < NL; ++L) {
-        std::vector<Frame> roots;
-        std::vector<int> ids;
-        const size_t sb = (size_t)1 << (L + 1), h = sb / 2;
-        for (size_t i = 0; i < nodes.size(); ++i) {
-            if (nodes[i].L != L) continue;
-            const Node &nd = nodes[i];
-            const size_t ib0 = nd.si * sb, jb0 = nd.sj * sb, kb0 = nd.sk * sb;
-            DevBuf sbuf(4 * h * h * bs * bs * 8, s);
-            BSG_CUDA(cudaMemsetAsync(sbuf.p, 0, sbuf.bytes, s));  // S00..S11 start at 0.0 (:468-471)
-            node_S[i] = sbuf.as<double>();
-            Frame f;
-            for (int q = 0; q < 4; ++q) {
-                f.out[q].n = h;
-                f.out[q].blk.resize(h * h);
-                for (size_t e = 0; e < h * h; ++e) f.out[q].blk[e] = sbuf.as<double>() + (q * h * h + e) * bs * bs;
+        for (uint8_t opt = kNodeStrassen; opt <= kNodeDense; ++opt) {
+            std::vector<Frame> roots;
+            std::vector<int> ids;
+            const size_t sb = (size_t)1 << (L + 1), h = sb / 2;
+            // a node of depth t recurses while the grid side exceeds h / 2^(t-1)
+            const size_t ms = opt == kNodeStrassen ? min_size
+                                                   : std::max<size_t>(1, h >> (opt - kNodeDepth1)) * bs;
+            std::vector<std::tuple<const Grid *, const Grid *, const Grid *>> dense;
+            std::vector<Grid> dgrids;
+            dgrids.reserve(3 * nodes.size());
+            for (size_t i = 0; i < nodes.size(); ++i) {
+                if (nodes[i].L != L || nodes[i].opt != opt) continue;
+                const Node &nd = nodes[i];
+                const size_t ib0 = nd.si * sb, jb0 = nd.sj * sb, kb0 = nd.sk * sb;
+                DevBuf sbuf(4 * h * h * bs * bs * 8, s);
+                BSG_CUDA(cudaMemsetAsync(sbuf.p, 0, sbuf.bytes, s));  // S00..S11 start at 0.0 (:468-471)
+                node_S[i] = sbuf.as<double>();
+                auto view = [&](bsg_bsm M, size_t r0, size_t c0, size_t side) {
+                    Grid g;
+                    g.n = side;
+                    g.blk.resize(side * side);
+                    for (size_t c = 0; c < side; ++c)
+                        for (size_t r = 0; r < side; ++r) g.blk[r + c * side] = M->hptr[(r0 + r) + (c0 + c) * M->nrb];
+                    return g;
+                };
+                if (opt == kNodeDense) {
+                    // the node's product as one dense tile: S (the node's quadrants
+                    // S00, S01, S10, S11, as k_apply reads them) += A_node B_node over
+                    // every block product, unscreened
+                    Grid X;
+                    X.n = sb;
+                    X.blk.resize(sb * sb);
+                    for (size_t c = 0; c < sb; ++c)
+                        for (size_t r = 0; r < sb; ++r) {
+                            const size_t q = (r >= h ? 2 : 0) + (c >= h ? 1 : 0);
+                            X.blk[r + c * sb] = sbuf.as<double>() + (q * h * h + (r % h) + (c % h) * h) * bs * bs;
+                        }
+                    dgrids.push_back(std::move(X));
+                    dgrids.push_back(view(A, ib0, kb0, sb));
+                    dgrids.push_back(view(B, kb0, jb0, sb));
+                    const size_t k = dgrids.size();
+                    dense.emplace_back(&dgrids[k - 3], &dgrids[k - 2], &dgrids[k - 1]);
+                    sbufs.push_back(std::move(sbuf));
+                    continue;
+                }
+                Frame f;
+                for (int q = 0; q < 4; ++q) {
+                    f.out[q].n = h;
+                    f.out[q].blk.resize(h * h);
+                    for (size_t e = 0; e < h * h; ++e) f.out[q].blk[e] = sbuf.as<double>() + (q * h * h + e) * bs * bs;
+                }
+                f.a = view(A, ib0, kb0, h);
+                f.b = view(A, ib0, kb0 + h, h);
+                f.c = view(A, ib0 + h, kb0, h);
+                f.d = view(A, ib0 + h, kb0 + h, h);
+                f.A = view(B, kb0, jb0, h);
+                f.C = view(B, kb0, jb0 + h, h);
+                f.B = view(B, kb0 + h, jb0, h);
+                f.D = view(B, kb0 + h, jb0 + h, h);
+                roots.push_back(std::move(f));
+                ids.push_back((int)i);
+                sbufs.push_back(std::move(sbuf));
             }
-            auto view = [&](bsg_bsm M, size_t r0, size_t c0) {
-                Grid g;
-                g.n = h;
-                g.blk.resize(h * h);
-                for (size_t c = 0; c < h; ++c)
-                    for (size_t r = 0; r < h; ++r) g.blk[r + c * h] = M->hptr[(r0 + r) + (c0 + c) * M->nrb];
-                return g;
-            };
-            f.a = view(A, ib0, kb0);
-            f.b = view(A, ib0, kb0 + h);
-            f.c = view(A, ib0 + h, kb0);
-            f.d = view(A, ib0 + h, kb0 + h);
-            f.A = view(B, kb0, jb0);
-            f.C = view(B, kb0, jb0 + h);
-            f.B = view(B, kb0 + h, jb0);
-            f.D = view(B, kb0 + h, jb0 + h);
-            roots.push_back(std::move(f));
-            ids.push_back((int)i);
-            sbufs.push_back(std::move(sbuf));
+            if (!roots.empty()) winograd(ctx, roots, h, bs, ms, form, n_digits, s);
+            if (!dense.empty()) leaf_products(ctx, dense, (int)bs, form, n_digits, s);
         }
-        if (!roots.empty()) winograd(ctx, roots, h, bs, min_size, form, n_digits, s);
     }
     // ordered application
     std::vector<uint8_t> tree_flat(std::max<size_t>(tot, 1), 0);
@@ -762,7 +796,7 @@ extern "C" bsg_status bsg_matmult_strassen_sparse_sched(bsg_bsm C, bsg_bsm A, bs
                                                         uint64_t *n_strassen_nodes) {
     return guard([&] {
         BSG_REQUIRE(form == BSG_FORM_FP64 || form == BSG_FORM_OZAKI, BSG_ERR_ARG, "unknown form");
-        BSG_REQUIRE(policy >= BSG_SCHED_COST && policy <= BSG_SCHED_MLP, BSG_ERR_ARG, "unknown policy");
+        BSG_REQUIRE(policy >= BSG_SCHED_COST && policy <= BSG_SCHED_DENSE, BSG_ERR_ARG, "unknown policy");
         strassen_sparse(C, A, B, thresh, min_size, form, n_digits, policy, sched, n_strassen_nodes);
     });
 }
@@ -780,7 +814,7 @@ extern "C" bsg_status bsg_strassen_root_features(bsg_bsm C, bsg_bsm A, bsg_bsm B
         std::vector<float> F;
         std::vector<uint8_t> ok;
         level_features(C, A, B, R, R.n_levels - 1, F, ok);
-        std::copy(F.begin(), F.begin() + kSchedIn, features);
+        std::copy(F.begin(), F.begin() + kSchedNodeIn, features);
         *eligible = ok[0];
     });
 }
