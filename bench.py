@@ -417,10 +417,12 @@ def run_rik_large(args):
     against the FP64 form on a sixteenth of the work: the 3c->2c output on the
     first rows of X, and K of the whole pipeline over the first aux functions
     (the full FP64 step does not fit the time budget: about 35 x the mixed
-    one).  A measurement case, not the bench line."""
+    one), with the screen comparison of that part (flips per product and
+    their margins).  A measurement case, not the bench line."""
     import torch
 
     from strassen_gb300 import api
+    from strassen_gb300 import screen
     from strassen_gb300 import synth as S
 
     dev = torch.device("cuda", 0)
@@ -475,15 +477,21 @@ def run_rik_large(args):
         B64 = torch.empty((p_sub, n_vec2), dtype=torch.float64, device=dev).T
         Cb.to_matrix(out=B64)
         del Cb
-        k_64 = api.rik_occ_step(B64, keys, C, n_bf, p_sub, n_occ, bs, thr, ctx=ctx,
-                                out=torch.empty((n_occ, n_bf), dtype=torch.float64, device=dev).T).cpu().numpy()
+        # with the screen trace: per-product flips between the two pipelines
+        k_64, st64, tr64 = api.rik_occ_step(B64, keys, C, n_bf, p_sub, n_occ, bs, thr, ctx=ctx, trace=True,
+                                            out=torch.empty((n_occ, n_bf), dtype=torch.float64, device=dev).T)
+        k_64 = k_64.cpu().numpy()
         del B64
-        k_oz = api.rik_occ_step(B[:, :p_sub], keys, C, n_bf, p_sub, n_occ, bs, thr, form=api.FORM_OZAKI,
-                                n_digits=args.digits_occ, ctx=ctx,
-                                out=torch.empty((n_occ, n_bf), dtype=torch.float64, device=dev).T).cpu().numpy()
+        k_oz, stoz, troz = api.rik_occ_step(B[:, :p_sub], keys, C, n_bf, p_sub, n_occ, bs, thr, form=api.FORM_OZAKI,
+                                            n_digits=args.digits_occ, ctx=ctx, trace=True,
+                                            out=torch.empty((n_occ, n_bf), dtype=torch.float64, device=dev).T)
+        k_oz = k_oz.cpu().numpy()
+        cmp = screen.compare(tr64, troz, chunk=32)
         rel = lambda a, b: float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
         res.append({"tau": thr, "ms_per_step": ms, "tflops_dense_equiv": (f3c + focc) / (ms * 1e-3) / 1e12,
-                    "rel_err_3c2c_rows_1_16": rel(b_oz, b_64), "rel_err_K_aux_1_16": rel(k_oz, k_64)})
+                    "rel_err_3c2c_rows_1_16": rel(b_oz, b_64), "rel_err_K_aux_1_16": rel(k_oz, k_64),
+                    "screen_aux_1_16": {"mui_surviving": [st64[0], stoz[0]],
+                                        "ij": cmp["ij"], "K": cmp["K"], "blocks": cmp["blocks"]}})
         del b_oz, b_64
     print(json.dumps({"metric": "large RI-K step, mixed form, per tau", "unit": "ms",
                       "config": {"workload": f"125 atoms in a 20 A box, n_bf {n_bf}, n_aux {n_aux}, n_occ {n_occ}, "
@@ -580,6 +588,8 @@ STRASSEN_SHAPES = {
     # the large shape: n 16384, block 64, dense core of the first 4096 rows and columns, exp(-|I-J|/10)
     # tails, tau 1e-9, Strassen depth 0..3
     "n16384": dict(n=16384, bs=64, L=10.0, core=4096, seed=4, thresh=1e-9, depths=(0, 1, 2, 3)),
+    # a quarter of it (inputs still larger than L2), for profiler captures of the FP64 kernels
+    "n8192": dict(n=8192, bs=64, L=10.0, core=2048, seed=4, thresh=1e-9, depths=(0, 1)),
 }
 
 
@@ -604,7 +614,8 @@ def run_strassen(args):
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
     ctx = api.Context(0)
-    shapes = [args.shape] if args.shape else list(STRASSEN_SHAPES)
+    shapes = [args.shape] if args.shape else ["n2048", "n16384"]
+    forms = ((api.FORM_FP64, "fp64"),) if args.fp64_only else ((api.FORM_FP64, "fp64"), (api.FORM_OZAKI, "mixed"))
 
     def timed(fn, reps=1):
         fn()
@@ -634,26 +645,35 @@ def run_strassen(args):
                "surviving_block_triples": nsig, "surviving_fraction": nsig / (n // bs) ** 3,
                "fp64_matmult_s": t_mm, "fp64_matmult_tflops_dense_equiv": dense_flops / t_mm / 1e12,
                "fp64_matmult_tflops_surviving": surv_flops / t_mm / 1e12, "strassen": []}
-        Cz = api.BlockSparseMatrix(n, n, bs, bs, 0.0, ctx=ctx)
-        t_mz, _ = timed(lambda: api.matmult(Cz, A, 0, B, 0, thr, 1.0, 0.0, form=api.FORM_OZAKI, n_digits=0))
-        row["mixed_matmult_s"] = t_mz
-        row["mixed_matmult_rel_err"] = float(np.linalg.norm(Cz.to_matrix() - R) / rn)
-        del Cz
+        if not args.fp64_only:
+            Cz = api.BlockSparseMatrix(n, n, bs, bs, 0.0, ctx=ctx)
+            t_mz, _ = timed(lambda: api.matmult(Cz, A, 0, B, 0, thr, 1.0, 0.0, form=api.FORM_OZAKI, n_digits=0))
+            row["mixed_matmult_s"] = t_mz
+            row["mixed_matmult_rel_err"] = float(np.linalg.norm(Cz.to_matrix() - R) / rn)
+            del Cz
         for d in c["depths"]:
             ms = n >> d
             ent = {"depth": d, "min_size_for_strassen": ms}
-            for form, tag in ((api.FORM_FP64, "fp64"), (api.FORM_OZAKI, "mixed")):
-                CS = api.BlockSparseMatrix(n, n, bs, bs, 0.0, ctx=ctx)
+            # the reference's decision tree (cost model), then Strassen forced at
+            # the root (the scheduler's ROOT policy) with the same depth below it
+            for policy, ptag in ((api.SCHED_COST, ""), (api.SCHED_ROOT, "root_")):
+                if policy == api.SCHED_ROOT and d == 0:
+                    continue
+                for form, tag in forms:
+                    CS = api.BlockSparseMatrix(n, n, bs, bs, 0.0, ctx=ctx)
+                    nodes = [0]
 
-                def go():
-                    CS.fill_with_values(0.0)
-                    api.matmult_strassen_sparse(CS, A, 0, B, 0, thr, 1.0, 0.0, ms, form=form, n_digits=0)
+                    def go():
+                        CS.fill_with_values(0.0)
+                        nodes[0] = api.matmult_strassen_sparse_sched(CS, A, B, thr, ms, policy, None, form, 0)
 
-                t, _ = timed(go)
-                ent[tag + "_s"] = t
-                ent[tag + "_tflops_dense_equiv"] = dense_flops / t / 1e12
-                ent[tag + "_rel_err_vs_fp64_matmult"] = float(np.linalg.norm(CS.to_matrix() - R) / rn)
-                del CS
+                    t, _ = timed(go)
+                    key = ptag + tag
+                    ent[key + "_s"] = t
+                    ent[key + "_strassen_nodes"] = nodes[0]
+                    ent[key + "_tflops_dense_equiv"] = dense_flops / t / 1e12
+                    ent[key + "_rel_err_vs_fp64_matmult"] = float(np.linalg.norm(CS.to_matrix() - R) / rn)
+                    del CS
             row["strassen"].append(ent)
         if name == "n2048" and not args.no_cpu_baseline:
             # the reference's CPU path (oracle port, dgemm through OpenBLAS) on the host cores
@@ -697,7 +717,9 @@ def main():
     ap.add_argument("--workload", default="rik", choices=["rik", "batched", "rik-large", "strassen"],
                     help="rik: the RI-K step (default); batched: the batched-GEMM configuration; strassen: the "
                          "screened GEMM and Strassen shapes")
-    ap.add_argument("--shape", default="", choices=["", "n2048", "n16384"], help="strassen workload: one shape")
+    ap.add_argument("--shape", default="", choices=["", "n2048", "n16384", "n8192"],
+                    help="strassen workload: one shape (default: n2048 and n16384)")
+    ap.add_argument("--fp64-only", action="store_true", help="strassen workload: the FP64 form only")
     ap.add_argument("--count", type=int, default=512, help="products of the batched workload")
     args = ap.parse_args()
     if args.workload == "batched":
