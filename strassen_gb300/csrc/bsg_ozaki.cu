@@ -1,20 +1,21 @@
 // Ozaki-scheme split-precision block products on tcgen05 tensor cores
 // (see bsg_ozaki.cuh for the arithmetic).
 //
-// k_ozgemm: persistent, one CTA per SM, 6 warps.
+// k_ozgemm: persistent, one CTA per SM.
 //   warp 0     producer: per step, bulk-copies the digit images of up to R
 //              A blocks (one per row slot; a zero image where the screen
 //              drops the pair) and of the shared B block into a stage of the
 //              shared-memory ring (cp.async.bulk, mbarrier transaction count).
 //   warp 1     MMA issuer (one thread): per k16 step and A digit i, one
-//              tcgen05.mma D_i x [E_1..E_{nd+1-i}] into TMEM region i; a chain
+//              tcgen05.mma D_i x [E_0..E_{nd-1-i}] into TMEM region i; a chain
 //              of <= 512 k is committed to the epilogue.
-//   warps 2-9  epilogue, two groups of four (one TMEM lane quadrant per
-//              warp, half of the columns per group): per chain, the exact
-//              regions R0 (integers), R1 (multiples of 2^-8) and R2
-//              (multiples of 2^-16) are added as integers into an int64
-//              accumulator, the lower-weight regions in FP32; FP64 is used once per tile to combine, scale by
-//              2^(e_row + f_col - 14) and write the output blocks (GB300's
+//   warps 2-   epilogue, G groups of four warps (one TMEM lane quadrant per
+//              warp, NP / G columns per group; G = 3 at 24 and 48 columns,
+//              else 2): per chain, the exact regions R0 (integers), R1 (multiples
+//              of 2^-8) and R2 (multiples of 2^-16) are added as integers into
+//              an int64 accumulator, the lower-weight regions in FP32; once per
+//              tile the two are combined (in integers up to 5 digits), scaled
+//              by 2^(e_row + f_col - 14) and the output blocks written (GB300's
 //              FP64 rate is far below its integer / FP32 rates).
 // Every mbarrier wait is bounded (2 s); a timeout raises a flag that ends
 // all roles and is returned as BSG_ERR_TIMEOUT.
@@ -118,7 +119,21 @@ enum OzProf {
 };
 static_assert(kOzProf == 12, "the context keeps 12 GEMM counters");
 
-constexpr int kOzThreads = 320;  // producer, MMA issuer, 8 epilogue warps
+// Warps: producer, MMA issuer, then the epilogue: four TMEM lane quadrants x
+// G column groups.  Its per-element conversions and stores are integer
+// instructions on the four schedulers, so where the columns split into three
+// groups of whole 8-column loads (24 and 48 columns: the RI-K shapes) the
+// epilogue has 12 warps, three per scheduler.  Registers: each of the SM's
+// four partitions holds 16384, and a CTA's warps are spread over them
+// round-robin, so the busiest partition's ceil(warps / 4) warps set the
+// per-thread cap (14 warps: 128; 10 warps: 168).
+template <int NP>
+struct OzEpi {
+    static constexpr int G = (NP == 24 || NP == 48) ? 3 : 2;
+    static constexpr int warps = 2 + 4 * G;
+    static constexpr int threads = 32 * warps;
+    static constexpr int max_regs = (16384 / (32 * ((warps + 3) / 4))) / 8 * 8;
+};
 
 // Conversions for the epilogue with integer operations instead of the FP64
 // pipe (GB300 runs FP64 at a small fraction of its integer rate).
@@ -184,8 +199,19 @@ __device__ __forceinline__ uint32_t oz_next_tile(uint32_t t, uint32_t chunk) {
     return (t % chunk) ? t : t + (gridDim.x - 1) * chunk;
 }
 
+// digits whose accumulator regions (nd x NP columns, + 8 for a rounded-up N)
+// fit the 512 TMEM columns, and MMAs per k16 slice at that many digits
+__host__ __device__ constexpr int oz_max_digits(int np) {
+    return (512 - 8) / np < kOzMaxDigits ? (512 - 8) / np : kOzMaxDigits;
+}
+__host__ __device__ constexpr int oz_plan_entries(int nd, int planes) {
+    int n = 0;
+    for (int i = 0; i < nd; ++i) n += (nd - i + planes - 1) / planes;
+    return n;
+}
+
 template <int NP>
-__global__ void __launch_bounds__(kOzThreads, 1)
+__global__ void __launch_bounds__(OzEpi<NP>::threads) __maxnreg__(OzEpi<NP>::max_regs)
     k_ozgemm(const OzTile *__restrict__ tiles, uint32_t n_tiles, const OzStep *__restrict__ steps,
              const bf16 *__restrict__ a_img, const bf16 *__restrict__ b_img, OzKParams P, int *__restrict__ err) {
     extern __shared__ __align__(1024) uint8_t smem[];
@@ -213,7 +239,7 @@ __global__ void __launch_bounds__(kOzThreads, 1)
         }
         for (int b = 0; b < 2; ++b) {
             tc::mbar_init(&tfull[b], 1);
-            tc::mbar_init(&tempty[b], 8);
+            tc::mbar_init(&tempty[b], 4 * OzEpi<NP>::G);
         }
         *abort = 0;
         tc::fence_barrier_init();
@@ -345,7 +371,7 @@ __global__ void __launch_bounds__(kOzThreads, 1)
             const uint64_t a_descx = tc::smem_desc(tc::smem_u32(smem), lbo_x, (uint32_t)P.nd * P.kp * 16u);
             const uint64_t b_descx = tc::smem_desc(tc::smem_u32(smem + a_stage), lbo_x, (uint32_t)P.kp * 16u);
             constexpr int kMaxPlanes = 256 / NP;  // B planes one MMA can take
-            constexpr int kMaxPlan = kOzMaxDigits * ((kOzMaxDigits + kMaxPlanes - 1) / kMaxPlanes);
+            constexpr int kMaxPlan = oz_plan_entries(oz_max_digits(NP), kMaxPlanes);
             uint32_t pd[kMaxPlan], pa[kMaxPlan], pb[kMaxPlan], pi[kMaxPlan];  // kept in registers (unrolled)
             int n_plan = 0;
 #pragma unroll
@@ -497,8 +523,9 @@ __global__ void __launch_bounds__(kOzThreads, 1)
         __syncwarp();
     } else {
         // ---------------- epilogue ----------------
-        constexpr int NPH = NP / 2;                   // columns per epilogue group
-        constexpr int CH = (NPH % 8 == 0) ? 8 : 4;  // TMEM columns per load
+        constexpr int NPH = NP / OzEpi<NP>::G;                           // columns per epilogue group
+        constexpr int CH = (NPH % 8 == 0) ? 8 : 4;                       // TMEM columns per load
+        static_assert(NPH % CH == 0, "a group's columns are whole TMEM loads");
         const int q = warp & 3;
         const int grp = (warp - 2) >> 2;
         const int cbase = grp * NPH;
@@ -571,8 +598,8 @@ __global__ void __launch_bounds__(kOzThreads, 1)
                 const int ldc = T.ldc[s];
                 const bool fresh = (T.fresh_mask >> s) & 1u;
                 const bool unit = P.alpha == 1.0;
-                // sub-blocks stored apart (J <= 2, so a group's NP/2 columns cross at
-                // most one sub-block boundary)
+                // sub-blocks stored apart (J <= 2 and G >= 2, so a group's NP / G
+                // columns cross at most one sub-block boundary)
                 const int tcols = T.cols, tsub = T.sub_cols, tcexp_sub = T.cexp_sub, ttrans = T.trans;
                 const long long tsub_stride = T.sub_stride;
                 const int *tcexp = T.cexp;
@@ -697,7 +724,7 @@ static void launch_oz(bsg_ctx ctx, const OzShape &sh, const OzTile *tiles, size_
     }
     const unsigned grid = (unsigned)std::min<size_t>(ceil_div(n_tiles, (size_t)chunk), (size_t)ctx->sm_count);
     BSG_REQUIRE(n_tiles + (size_t)grid * chunk < 0xffffffffull, BSG_ERR_UNSUPPORTED, "too many Ozaki tiles");
-    k_ozgemm<NP><<<grid, kOzThreads, smem, s>>>(tiles, (uint32_t)n_tiles, steps, a_img, b_img, P, err);
+    k_ozgemm<NP><<<grid, OzEpi<NP>::threads, smem, s>>>(tiles, (uint32_t)n_tiles, steps, a_img, b_img, P, err);
     ctx->note_launch();
     ctx->check_launch("ozaki gemm");
 }
