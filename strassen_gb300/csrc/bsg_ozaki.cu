@@ -146,8 +146,21 @@ __device__ __forceinline__ double oz_i64_to_f64(long long x) {
     const unsigned long long m = (a << (52 - msb)) & 0xFFFFFFFFFFFFFull;
     return __longlong_as_double((long long)(sgn | ((unsigned long long)(msb + 1023) << 52) | m));
 }
-// int64 to double rounded to nearest even, with integer operations
-__device__ __forceinline__ double oz_i64_to_f64_rn(long long x) {
+// v 2^e outside the fast paths (zero, subnormal or out-of-range results): an
+// ordinary multiplication by the power of two, as volatile inline PTX so that
+// the compiler branches around it instead of if-converting it (a warp's FP64
+// multiply holds GB300's FP64 pipe for tens of clocks; an if-converted copy
+// would run for every element)
+__device__ __forceinline__ double oz_scale_pow2_slow(double v, int e) {
+    const double sc = (e >= -1022 && e <= 1023) ? __longlong_as_double((long long)(e + 1023) << 52) : ldexp(1.0, e);
+    double r;
+    asm volatile("mul.rn.f64 %0, %1, %2;" : "=d"(r) : "d"(v), "d"(sc));
+    return r;
+}
+// round(x) 2^e (x an int64, rounded to nearest even) with integer operations:
+// the power of two goes straight into the exponent field when the result is
+// a normal number
+__device__ __forceinline__ double oz_i64_to_f64_rn_pow2(long long x, int e) {
     if (x == 0) return 0.0;
     const unsigned long long sgn = x < 0 ? (1ull << 63) : 0ull;
     const unsigned long long a = x < 0 ? 0ull - (unsigned long long)x : (unsigned long long)x;
@@ -165,28 +178,44 @@ __device__ __forceinline__ double oz_i64_to_f64_rn(long long x) {
             ++msb;
         }
     }
-    return __longlong_as_double((long long)(sgn | ((unsigned long long)(msb + 1023) << 52) | (m & 0xFFFFFFFFFFFFFull)));
+    const int field = msb + 1023 + e;
+    if (field > 0 && field < 0x7FF)
+        return __longlong_as_double((long long)(sgn | ((unsigned long long)field << 52) | (m & 0xFFFFFFFFFFFFFull)));
+    return oz_scale_pow2_slow(
+        __longlong_as_double((long long)(sgn | ((unsigned long long)(msb + 1023) << 52) | (m & 0xFFFFFFFFFFFFFull))), e);
+}
+// an integer-valued FP32 value (|f| < 2^62) as an int64, exactly, with
+// integer operations (the hardware conversion to 64 bits runs on the FP64 pipe)
+__device__ __forceinline__ long long oz_f32_int_to_i64(float f) {
+    const uint32_t u = __float_as_uint(f);
+    const int ex = (int)((u >> 23) & 0xFFu);
+    const long long mant = (long long)((u & 0x7FFFFFu) | 0x800000u);
+    const int sh = ex - 150;
+    long long v = sh >= 0 ? mant << sh : mant >> min(-sh, 63);
+    v = ex < 127 ? 0 : v;  // |f| < 1: zero, the only integer there
+    return (u >> 31) ? -v : v;
 }
 // an FP32 value as a double (exact; zero and subnormal inputs take the
 // hardware conversion)
 __device__ __forceinline__ double oz_f32_to_f64(float f) {
     const uint32_t u = __float_as_uint(f);
     const uint32_t ex = (u >> 23) & 0xFFu;
-    if (ex == 0u || ex == 0xFFu) return (double)f;
+    if (ex == 0u || ex == 0xFFu) {  // rare: kept out of the common path (see oz_scale_pow2_slow)
+        double r;
+        asm volatile("cvt.f64.f32 %0, %1;" : "=d"(r) : "f"(f));
+        return r;
+    }
     return __longlong_as_double((long long)(((unsigned long long)(u >> 31) << 63) |
                                             ((unsigned long long)(ex - 127u + 1023u) << 52) |
                                             ((unsigned long long)(u & 0x7FFFFFu) << 29)));
 }
-// v 2^e: the exponent field moves when the result stays a normal number;
-// otherwise (and for zero) an ordinary multiplication by the power of two
+// v 2^e: the exponent field moves when the result stays a normal number
 __device__ __forceinline__ double oz_scale_pow2(double v, int e) {
     const long long b = __double_as_longlong(v);
     const int ev = (int)((b >> 52) & 0x7FF);
     const int en = ev + e;
-    if (ev != 0 && ev != 0x7FF && en > 0 && en < 0x7FF)
-        return __longlong_as_double(b + ((long long)e << 52));
-    const double sc = (e >= -1022 && e <= 1023) ? __longlong_as_double((long long)(e + 1023) << 52) : ldexp(1.0, e);
-    return __dmul_rn(v, sc);
+    if (ev != 0 && ev != 0x7FF && en > 0 && en < 0x7FF) return __longlong_as_double(b + ((long long)e << 52));
+    return oz_scale_pow2_slow(v, e);
 }
 
 // Tile sequence of a CTA: chunks of `chunk` consecutive tiles, chunk
@@ -621,7 +650,7 @@ __global__ void __launch_bounds__(OzEpi<NP>::threads) __maxnreg__(OzEpi<NP>::max
                 // every output of the group, its value from total(j) scaled by
                 // 2^(er + de + cex): one loop per way of forming the total, so
                 // that no element pays for both
-                auto store_all = [&](auto &&total, int de) {
+                auto store_all = [&](auto &&value, int de) {
                     // column j of this group: output address (null = not stored) and value
                     auto col_out = [&](int j, double *&dst) -> double {
                         const int c = cbase + j;
@@ -632,8 +661,7 @@ __global__ void __launch_bounds__(OzEpi<NP>::threads) __maxnreg__(OzEpi<NP>::max
                         }
                         dst = nullptr;
                         if (!(c < tcols && (!subm || cc < tsub))) return 0.0;
-                        double out = oz_scale_pow2(total(j), er + de + cex[j]);
-                        if (!unit) out = __dmul_rn(P.alpha, out);
+                        const double out = value(j, er + de + cex[j]);
                         double *base = subm ? cp + js * tsub_stride : cp;
                         dst = ttrans ? base + cc + (size_t)r * ldc : base + r + (size_t)cc * ldc;
                         return out;
@@ -652,21 +680,31 @@ __global__ void __launch_bounds__(OzEpi<NP>::threads) __maxnreg__(OzEpi<NP>::max
                         }
                     }
                 };
+                // alpha (1 on every RI-K product) multiplies in a loop of its own,
+                // so that the common case carries no FP64 multiply
+                auto store_scaled = [&](auto &&value, int de) {
+                    if (unit)
+                        store_all(value, de);
+                    else
+                        store_all([&](int j, int e) { return __dmul_rn(P.alpha, value(j, e)); }, de);
+                };
                 if (P.nd <= 5 && nch < 256) {
                     // up to 5 digits lo holds weights 3 and 4, multiples of 2^-32,
                     // so lo 2^32 is an integer (below 2^34) and hi 2^16 + lo 2^32
                     // the exact sum in units of 2^-32 (hi < 2^39 per chain of <= 512
                     // k, so below 2^63 for < 256 chains): one rounding to double, the
-                    // same as the FP64 add below makes, without the FP64 pipe
-                    store_all([&](int j) {
-                        return oz_i64_to_f64_rn(hi[j] * 65536ll + __float2ll_rn(lo[j] * 4294967296.f));
+                    // same as the FP64 add below makes, without the FP64 pipe, with
+                    // the power of two put into the rounded value's exponent
+                    store_scaled([&](int j, int e) {
+                        return oz_i64_to_f64_rn_pow2(hi[j] * 65536ll + oz_f32_int_to_i64(lo[j] * 4294967296.f), e);
                     }, -16);
                 } else {
                     // both terms are exact doubles built with integer operations
                     // (|hi| < 2^53, lo 2^16 an FP32 value): one FP64 add rounds,
                     // and the power of two goes into the exponent field
-                    store_all([&](int j) { return __dadd_rn(oz_i64_to_f64(hi[j]), oz_f32_to_f64(lo[j] * 65536.f)); },
-                              0);
+                    store_scaled([&](int j, int e) {
+                        return oz_scale_pow2(__dadd_rn(oz_i64_to_f64(hi[j]), oz_f32_to_f64(lo[j] * 65536.f)), e);
+                    }, 0);
                 }
                 if (fresh && r == 0 && grp == 0 && T.cnorm[s]) *T.cnorm[s] = 0.0;
             }
