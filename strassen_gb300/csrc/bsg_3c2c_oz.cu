@@ -99,8 +99,10 @@ struct Dense3c {
 // insignificant X blocks of its other rows as zero images.
 
 // N-side images of X: J consecutive block rows stacked along N, one image
-// per (group ibp, kb), index ibp + kb*nibp; block ib = J*ibp + j fills rows
-// j*bs.. of its group's image (rows of missing blocks are never read).
+// per (group ibp, kb), index ibp*nkb + kb (a group's k steps back to back, so
+// that the two steps of a stage pair are one copy); block ib = J*ibp + j
+// fills rows j*bs.. of its group's image (rows of missing blocks are never
+// read).
 // kImgXBlocks consecutive blocks x = ib + kb*nib per warp.
 constexpr int kImgXBlocks = 4;
 __global__ void k_img_X(const double *__restrict__ X, const int *__restrict__ rexp, Dense3c D, bf16 *__restrict__ img) {
@@ -117,7 +119,7 @@ __global__ void k_img_X(const double *__restrict__ X, const int *__restrict__ re
             J.rows = ext3(ib, D.bs, D.n_vec2);
             J.k = ext3(kb, D.bs, D.n_aux);
             J.exps = rexp + ib * D.bs;
-            J.dst = img + (ibp + kb * D.nibp) * D.nd * (size_t)D.np * D.kp + j * D.bs * (size_t)D.kp;
+            J.dst = img + (ibp * D.nkb + kb) * D.nd * (size_t)D.np * D.kp + j * D.bs * (size_t)D.kp;
             J.m_side = false;
             J.plane_rows = D.np;
             return true;
@@ -126,13 +128,15 @@ __global__ void k_img_X(const double *__restrict__ X, const int *__restrict__ re
 }
 
 // M-side images of V^T blocks (jb, kb): image row = output column, index
-// jb + kb*njb (a tile's slots are consecutive images)
+// (jg*nkb + kb)*R + s for jb = jg*R + s (a tile's slots are consecutive
+// images, and so are the slots of consecutive k steps)
 __global__ void k_img_V(const double *__restrict__ V, const int *__restrict__ cexp, Dense3c D, bf16 *__restrict__ img) {
     const size_t x = oz_warp_id();
     if (x >= D.nkb * D.njb) return;
     const size_t jb = x % D.njb, kb = x / D.njb;
+    const size_t idx = ((jb / D.R) * D.nkb + kb) * D.R + jb % D.R;
     oz_block_image(V + kb * D.bs + jb * D.bs * D.n_aux, D.n_aux, true, ext3(jb, D.bs, D.n_aux), ext3(kb, D.bs, D.n_aux),
-                   cexp + jb * D.bs, D.mp, D.kp, D.nd, img + x * D.nd * (size_t)D.mp * D.kp, true);
+                   cexp + jb * D.bs, D.mp, D.kp, D.nd, img + idx * D.nd * (size_t)D.mp * D.kp, true);
 }
 
 // tiles and their steps; tile t covers output block rows J*ibp .. J*ibp+J-1
@@ -202,9 +206,9 @@ __global__ void k_tiles_3c(size_t n_tiles, size_t n_jg, size_t Gj, const double 
                 }
             }
             uint32_t a_idx[kOzMaxSlots];
-            for (int s = 0; s < kOzMaxSlots; ++s) a_idx[s] = (uint32_t)(jg * D.R + s + kb * D.njb);
+            for (int s = 0; s < kOzMaxSlots; ++s) a_idx[s] = (uint32_t)((jg * D.nkb + kb) * D.R + s);
             // exact rectangles (the slot sets of a norm-product screen are nested)
-            c = emit_rect_steps(live, D.J, 0u, (uint32_t)(ibp + kb * D.nibp), a_idx, mine);
+            c = emit_rect_steps(live, D.J, 0u, (uint32_t)(ibp * D.nkb + kb), a_idx, mine);
         }
         warp_append_steps(mine, c, steps + T.s0, n);
     }
@@ -264,7 +268,7 @@ void oz3c_prepare_v(bsg_ctx ctx, const double *V, const Dense3c &D, Oz3cV &v) {
     const size_t n_aux = D.n_aux, a_img = (size_t)D.nd * D.mp * D.kp;
     v.vn = DevBuf(D.nkb * D.njb * 8, s);
     v.cexp = DevBuf(n_aux * 4, s);
-    v.ai = DevBuf(D.nkb * D.njb * a_img * 2, s);
+    v.ai = DevBuf(ceil_div(D.njb, (size_t)D.R) * D.R * D.nkb * a_img * 2, s);  // whole slot groups
     const int wpb = 8;
     k_dense_norms<<<(unsigned)ceil_div(D.nkb * D.njb, wpb), wpb * 32, 0, s>>>(V, n_aux, n_aux, n_aux, D.bs, D.nkb,
                                                                               D.nkb * D.njb, v.vn.as<double>());

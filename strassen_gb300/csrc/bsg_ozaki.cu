@@ -32,8 +32,9 @@ namespace bsg {
 
 using bf16 = __nv_bfloat16;
 
-// zeros for masked slots: the largest A stage (8 digits x 128 rows x 64 k)
-static __device__ __align__(128) bf16 g_oz_zero[8 * 128 * 64];
+// zeros for masked slots: the A images of a pair of the largest steps
+// (2 x 8 digits x 128 rows x 64 k; a run of masked slots may span both)
+static __device__ __align__(128) bf16 g_oz_zero[2 * 8 * 128 * 64];
 
 static void *oz_zero_image() {
     static std::mutex mu;
@@ -251,6 +252,15 @@ __global__ void __launch_bounds__(OzEpi<NP>::threads) __maxnreg__(OzEpi<NP>::max
     const uint32_t half_bytes = a_stage + b_stage;  // one step's operands; a pair stage holds two
     const uint32_t stage_bytes = P.pair ? 2u * half_bytes : half_bytes;
     const uint32_t slot_bytes = (uint32_t)P.nd * P.mp * P.kp * 2u;  // one slot's full digit image
+    // Stage layout.  One step: [A: 128 rows | B].  A pair: [A0 | A1 | B0 | B1]
+    // with each A holding only its R slots (a_pack bytes), so that the two
+    // steps' slot images sit back to back as they do in a_img when the
+    // image indices continue from one step to the next (one copy instead of
+    // two; a bulk copy's cost is mostly per copy).  The MMA still reads 128
+    // rows of each A: rows past the R slots fall in the next region of the
+    // same stage (finite digits), and their accumulator rows are never stored.
+    const uint32_t a_pack = P.pair ? (uint32_t)P.R * slot_bytes : a_stage;  // A bytes of one step
+    const uint32_t b_off = P.pair ? 2u * a_pack : a_stage;                  // offset of B0 in the stage
     const size_t slot_elems = (size_t)P.nd * P.mp * P.kp, b_img_elems = (size_t)P.nd * NP * P.kp;
     OzStep *sstep = reinterpret_cast<OzStep *>(smem + (size_t)P.S * stage_bytes);  // 32 prefetched steps
     uint64_t *full = reinterpret_cast<uint64_t *>(sstep + 32);
@@ -292,26 +302,28 @@ __global__ void __launch_bounds__(OzEpi<NP>::threads) __maxnreg__(OzEpi<NP>::max
         unsigned long long w_empty = 0;
         uint32_t stage = 0, ph = 0;  // ring position of stage `it`
         const uint32_t jfull = (1u << P.J) - 1u;
-        // one step's A slots and B digit stack into the half-stage at sA / sB
         unsigned long long n_copied = 0, n_live = 0;
-        auto copy_step = [&](const OzStep &st, uint8_t *sA, uint8_t *sB, uint64_t *bar) {
-            // slots whose images are consecutive in a_img (or all zero) go
-            // in one copy: a fully live step is one A copy and one B copy
-            const uint32_t ai = lane < P.R ? st.a[lane] : kOzNone;
+        // the A slots of a stage: lane l < nA takes slot l % R of step l / R,
+        // at sA + l * slot_bytes (a pair's second step follows the first).
+        // Runs of consecutive images (or of zeros) go in one copy: a fully
+        // live step is one A copy, and so is a fully live pair whose image
+        // indices continue from the first step to the second
+        auto copy_a = [&](const OzStep &st0, const OzStep &st1, bool two, uint8_t *sA, uint64_t *bar) {
+            const uint32_t nA = two ? 2u * (uint32_t)P.R : (uint32_t)P.R;
+            const uint32_t ai =
+                lane < P.R ? st0.a[lane] : ((uint32_t)lane < nA ? st1.a[lane - P.R] : kOzNone);
             const uint32_t prev = __shfl_up_sync(0xffffffffu, ai, 1);
             const bool live = ai != kOzNone;
-            if (prof) {
-                ++n_copied;
-                n_live += (unsigned long long)__popc(__ballot_sync(0xffffffffu, live)) *
-                          (unsigned long long)__popc(st.bmask & jfull);
-            }
             const bool joins = lane > 0 && (live ? (prev != kOzNone && prev + 1u == ai) : prev == kOzNone);
-            const uint32_t starts = __ballot_sync(0xffffffffu, lane < P.R && !joins) | (1u << P.R);
-            if (lane < P.R && !joins) {
+            const uint32_t starts = __ballot_sync(0xffffffffu, (uint32_t)lane < nA && !joins) | (1u << nA);
+            if ((uint32_t)lane < nA && !joins) {
                 const int len = __ffs(starts & ~((2u << lane) - 1u)) - 1 - lane;
                 const bf16 *src = live ? a_img + (size_t)ai * slot_elems : P.zero;
                 tc::bulk_g2s(sA + lane * slot_bytes, src, (uint32_t)len * slot_bytes, bar);
             }
+        };
+        // one step's B digit stack into sB
+        auto copy_b = [&](const OzStep &st, uint8_t *sB, uint64_t *bar) {
             if ((st.bmask & jfull) == jfull) {
                 if (lane == 31) tc::bulk_g2s(sB, b_img + (size_t)st.b * b_img_elems, b_copy, bar);
             } else {
@@ -325,6 +337,12 @@ __global__ void __launch_bounds__(OzEpi<NP>::threads) __maxnreg__(OzEpi<NP>::max
                     tc::bulk_g2s(sB + off * 2, src, (uint32_t)npj * P.kp * 2u, bar);
                 }
             }
+        };
+        auto count_step = [&](const OzStep &st) {
+            const bool live = lane < P.R && st.a[lane] != kOzNone;
+            ++n_copied;
+            n_live += (unsigned long long)__popc(__ballot_sync(0xffffffffu, live)) *
+                      (unsigned long long)__popc(st.bmask & jfull);
         };
         const uint32_t kstep = P.pair ? 2u : 1u;
         for (uint32_t t = oz_first_tile(P.chunk); t < n_tiles && !*abort; t = oz_next_tile(t, P.chunk)) {
@@ -346,7 +364,7 @@ __global__ void __launch_bounds__(OzEpi<NP>::threads) __maxnreg__(OzEpi<NP>::max
                 }
                 if (!__shfl_sync(0xffffffffu, okw, 0)) break;
                 uint8_t *sA = smem + (size_t)stage * stage_bytes;
-                uint8_t *sB = sA + a_stage;
+                uint8_t *sB = sA + b_off;
                 const bool two = P.pair && k + 1 < ns;
                 // a lone last step of a pair stage gets a zero B in the second
                 // half: the k16 slice that straddles into it then adds nothing
@@ -354,11 +372,22 @@ __global__ void __launch_bounds__(OzEpi<NP>::threads) __maxnreg__(OzEpi<NP>::max
                 const uint32_t tx = two ? 2u * P.tx_bytes : (P.pair ? P.tx_bytes + b_copy : P.tx_bytes);
                 if (lane == 0) tc::mbar_arrive_expect_tx(&full[stage], tx);
                 __syncwarp();
-                copy_step(sstep[k & 31u], sA, sB, &full[stage]);
-                if (two) {
-                    copy_step(sstep[(k + 1) & 31u], sA + half_bytes, sB + half_bytes, &full[stage]);
-                } else if (P.pair && lane == 31) {
-                    tc::bulk_g2s(sB + half_bytes, P.zero, b_copy, &full[stage]);
+                const OzStep &st0 = sstep[k & 31u], &st1 = sstep[(k + 1) & 31u];
+                if (prof) {
+                    count_step(st0);
+                    if (two) count_step(st1);
+                }
+                copy_a(st0, st1, two, sA, &full[stage]);
+                if (two && b_stage == b_copy && (st0.bmask & jfull) == jfull && (st1.bmask & jfull) == jfull &&
+                    st1.b == st0.b + 1u) {
+                    // both steps' full B stacks, consecutive in b_img: one copy
+                    if (lane == 31) tc::bulk_g2s(sB, b_img + (size_t)st0.b * b_img_elems, 2u * b_copy, &full[stage]);
+                } else {
+                    copy_b(st0, sB, &full[stage]);
+                    if (two)
+                        copy_b(st1, sB + b_stage, &full[stage]);
+                    else if (P.pair && lane == 31)
+                        tc::bulk_g2s(sB + b_stage, P.zero, b_copy, &full[stage]);
                 }
                 if (++stage == (uint32_t)P.S) {
                     stage = 0;
@@ -391,14 +420,15 @@ __global__ void __launch_bounds__(OzEpi<NP>::threads) __maxnreg__(OzEpi<NP>::max
             // address offsets (16-byte units), w = instruction descriptor.
             // 8-row groups: nd*kp*16 bytes apart on the M side (digits interleaved), kp*16 on the N side
             const uint64_t a_desc0 = tc::smem_desc(tc::smem_u32(smem), 128u, (uint32_t)P.nd * P.kp * 16u);
-            const uint64_t b_desc0 = tc::smem_desc(tc::smem_u32(smem + a_stage), 128u, (uint32_t)P.kp * 16u);
-            // pair mode: the slice that straddles the two halves starts at the
-            // first half's last core column and finds its second one (column 0
-            // of the other half) one leading byte offset further
+            const uint64_t b_desc0 = tc::smem_desc(tc::smem_u32(smem + b_off), 128u, (uint32_t)P.kp * 16u);
+            // pair mode: the slice that straddles the two steps starts at the
+            // first step's last core column and finds its second one (column 0
+            // of the second step, a_pack / b_stage further on) one leading byte
+            // offset further
             const uint32_t ncol = (uint32_t)P.kp / 8u;  // core columns per step
-            const uint32_t lbo_x = half_bytes - (ncol - 1u) * 128u;
-            const uint64_t a_descx = tc::smem_desc(tc::smem_u32(smem), lbo_x, (uint32_t)P.nd * P.kp * 16u);
-            const uint64_t b_descx = tc::smem_desc(tc::smem_u32(smem + a_stage), lbo_x, (uint32_t)P.kp * 16u);
+            const uint32_t lbo_xa = a_pack - (ncol - 1u) * 128u, lbo_xb = b_stage - (ncol - 1u) * 128u;
+            const uint64_t a_descx = tc::smem_desc(tc::smem_u32(smem), lbo_xa, (uint32_t)P.nd * P.kp * 16u);
+            const uint64_t b_descx = tc::smem_desc(tc::smem_u32(smem + b_off), lbo_xb, (uint32_t)P.kp * 16u);
             constexpr int kMaxPlanes = 256 / NP;  // B planes one MMA can take
             constexpr int kMaxPlan = oz_plan_entries(oz_max_digits(NP), kMaxPlanes);
             uint32_t pd[kMaxPlan], pa[kMaxPlan], pb[kMaxPlan], pi[kMaxPlan];  // kept in registers (unrolled)
@@ -483,9 +513,9 @@ __global__ void __launch_bounds__(OzEpi<NP>::threads) __maxnreg__(OzEpi<NP>::max
                             } else if (g + 1u == ncol) {  // straddles the halves
                                 aq = a_descx + soff + g * 8u;
                                 bq = b_descx + soff + g * 8u;
-                            } else {  // both in the second half
-                                aq = a_desc0 + soff + ((half_bytes + (g - ncol) * 128u) >> 4);
-                                bq = b_desc0 + soff + ((half_bytes + (g - ncol) * 128u) >> 4);
+                            } else {  // both in the second step
+                                aq = a_desc0 + soff + ((a_pack + (g - ncol) * 128u) >> 4);
+                                bq = b_desc0 + soff + ((b_stage + (g - ncol) * 128u) >> 4);
                             }
                         }
                     }
@@ -518,9 +548,10 @@ __global__ void __launch_bounds__(OzEpi<NP>::threads) __maxnreg__(OzEpi<NP>::max
             auto issue_fixed = [&](uint32_t soff, uint32_t k, uint32_t ns, uint32_t first, uint32_t dbase) {
                 constexpr uint32_t KP = 24, ND = 5;
                 const uint32_t a_hi = (uint32_t)(a_desc0 >> 32), b_hi = (uint32_t)(b_desc0 >> 32);
-                const uint32_t h2 = (half_bytes + 128u) >> 4;  // the second half's core column 1
-                const uint32_t a0 = (uint32_t)a_desc0 + soff, ax = (uint32_t)a_descx + soff + 16u, a2 = a0 + h2;
-                const uint32_t b0 = (uint32_t)b_desc0 + soff, bx = (uint32_t)b_descx + soff + 16u, b2 = b0 + h2;
+                // the second step's core column 1
+                const uint32_t ha2 = (a_pack + 128u) >> 4, hb2 = (b_stage + 128u) >> 4;
+                const uint32_t a0 = (uint32_t)a_desc0 + soff, ax = (uint32_t)a_descx + soff + 16u, a2 = a0 + ha2;
+                const uint32_t b0 = (uint32_t)b_desc0 + soff, bx = (uint32_t)b_descx + soff + 16u, b2 = b0 + hb2;
                 const bool three = k + 1 < ns;  // a lone last step: the first two slices
                 auto d64 = [](uint32_t lo, uint32_t hi) { return ((uint64_t)hi << 32) | lo; };
 #pragma unroll
