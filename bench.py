@@ -302,7 +302,7 @@ def run_ours(args):
             ctx.set_timing(False)
     # e2e through the C ABI with pinned host buffers (timed before the FP64 comparison, whose
     # allocations would otherwise be released and mapped again inside the timed region)
-    e2e_ms = h2d = d2h = None
+    e2e_ms = h2d = d2h = e2e_parts = None
     if not args.no_e2e:
         Xh = torch.empty((n_aux, n_vec2), dtype=torch.float64, pin_memory=True)
         Xh.copy_(Xt)
@@ -313,14 +313,24 @@ def run_ours(args):
         keys_d = torch.empty_like(keys)
         C_d = torch.empty((n_occ, n_bf), dtype=torch.float64, device=dev)
 
+        parts = {"3c2c_host_X": [], "occ_host_K": []}
+
         def step_e2e():
+            # both calls return once their results are in place (host clock per part)
+            t0 = time.perf_counter()
             api.transform_3c2c(Xh.T.numpy(), Vh.T.numpy(), bs, thr, form=form, n_digits=d3, out=B, ctx=ctx)
+            t1 = time.perf_counter()
             keys_d.copy_(kh, non_blocking=True)
             C_d.copy_(Ch, non_blocking=True)
             api.rik_occ_step(B, keys_d, C_d.T, n_bf, n_aux, n_occ, bs, thr, n_part=1, form=form, n_digits=docc,
                              out=Kh.T.numpy(), ctx=ctx)
+            parts["3c2c_host_X"].append(1e3 * (t1 - t0))
+            parts["occ_host_K"].append(1e3 * (time.perf_counter() - t1))
 
-        e2e_ms, _, _ = timed(step_e2e, max(1, args.steps), 1)
+        e2e_steps = max(1, args.steps)
+        e2e_ms, _, _ = timed(step_e2e, e2e_steps, 1)
+        e2e_parts = {k: float(np.median(v[-e2e_steps:])) for k, v in parts.items()}
+        print("e2e parts per step (ms):", json.dumps(parts), file=sys.stderr)
         h2d = (Xh.numel() + Vh.numel() + Ch.numel() + kh.numel()) * 8
         d2h = Kh.numel() * 8
     extra = {}
@@ -367,7 +377,7 @@ def run_ours(args):
                        "digits": {"3c2c": d3, "occ": docc} if form == api.FORM_OZAKI else None,
                        "l2": "inputs larger than L2 (X is %.1f GB)" % (n_vec2 * n_aux * 8 / 1e9)},
             "e2e": {"value": world * flops / (e2e_ms * 1e-3) / 1e12, "unit": "TFLOP/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
+                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms, "parts_ms": e2e_parts},
             "gpu_launches": int(round(launches)), "clocks": clocks,
             "flops_split": {"3c2c": f3c, "occ": focc}}
     line.update(extra)
