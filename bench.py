@@ -452,7 +452,9 @@ def run_rik_large(args):
     ctx = api.Context(0)
     f3c, focc = step_flops(n_bf, n_aux, n_occ, n_vec2)
     rows = n_vec2 // 16
-    p_sub = n_aux // 16
+    # whole aux blocks: a ragged last block of V[:, :p_sub] would have another
+    # block norm than the same columns inside the full V, and so another screen
+    p_sub = (n_aux // 16) // bs * bs
     Xs = np.asfortranarray(X[:rows].cpu().numpy())
     Vn = np.asfortranarray(V.cpu().numpy())
     res = []
