@@ -302,7 +302,7 @@ def run_ours(args):
             ctx.set_timing(False)
     # e2e through the C ABI with pinned host buffers (timed before the FP64 comparison, whose
     # allocations would otherwise be released and mapped again inside the timed region)
-    e2e_ms = h2d = d2h = e2e_parts = None
+    e2e_ms = h2d = d2h = e2e_parts = e2e_each = None
     if not args.no_e2e:
         Xh = torch.empty((n_aux, n_vec2), dtype=torch.float64, pin_memory=True)
         Xh.copy_(Xt)
@@ -327,8 +327,26 @@ def run_ours(args):
             parts["3c2c_host_X"].append(1e3 * (t1 - t0))
             parts["occ_host_K"].append(1e3 * (time.perf_counter() - t1))
 
-        e2e_steps = max(1, args.steps)
-        e2e_ms, _, _ = timed(step_e2e, e2e_steps, 1)
+        # each step timed on its own (CUDA events on the context's stream), the
+        # median reported: the host link is shared with the other GPUs' jobs,
+        # and single steps of an otherwise steady run take 2-5x as long
+        e2e_steps = max(5, args.steps)
+        step_e2e()  # warm-up
+        torch.cuda.synchronize(dev)
+        if world > 1:
+            torch.distributed.barrier()
+        e2e_each = []
+        with torch.cuda.stream(stream):
+            for _ in range(e2e_steps):
+                a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a0.record(stream)
+                step_e2e()
+                a1.record(stream)
+                torch.cuda.synchronize(dev)
+                e2e_each.append(a0.elapsed_time(a1))
+        if world > 1:
+            torch.distributed.barrier()
+        e2e_ms = float(np.median(e2e_each))
         e2e_parts = {k: float(np.median(v[-e2e_steps:])) for k, v in parts.items()}
         print("e2e parts per step (ms):", json.dumps(parts), file=sys.stderr)
         h2d = (Xh.numel() + Vh.numel() + Ch.numel() + kh.numel()) * 8
@@ -377,7 +395,8 @@ def run_ours(args):
                        "digits": {"3c2c": d3, "occ": docc} if form == api.FORM_OZAKI else None,
                        "l2": "inputs larger than L2 (X is %.1f GB)" % (n_vec2 * n_aux * 8 / 1e9)},
             "e2e": {"value": world * flops / (e2e_ms * 1e-3) / 1e12, "unit": "TFLOP/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms, "parts_ms": e2e_parts},
+                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms, "parts_ms": e2e_parts,
+                    "timing": "median of per-step CUDA-event times", "ms_each": e2e_each},
             "gpu_launches": int(round(launches)), "clocks": clocks,
             "flops_split": {"3c2c": f3c, "occ": focc}}
     line.update(extra)
@@ -425,10 +444,11 @@ def run_rik_large(args):
     sizes 8-32 are not modelled), tau swept over 1e-6 .. 1e-12.  Per tau: one
     timed mixed-form step on device-resident inputs (X is 45 GB), and errors
     against the FP64 form on a sixteenth of the work: the 3c->2c output on the
-    first rows of X, and K of the whole pipeline over the first aux functions
-    (the full FP64 step does not fit the time budget: about 35 x the mixed
-    one), with the screen comparison of that part (flips per product and
-    their margins).  A measurement case, not the bench line."""
+    first rows of X, and K of the whole pipeline over the first aux functions,
+    with the screen comparison of that part (flips per product and their
+    margins).  At tau 1e-10 the whole FP64 step is also timed once (about a
+    minute) and the mixed step's whole K compared with its K.  A measurement
+    case, not the bench line."""
     import torch
 
     from strassen_gb300 import api
@@ -458,6 +478,8 @@ def run_rik_large(args):
     Xs = np.asfortranarray(X[:rows].cpu().numpy())
     Vn = np.asfortranarray(V.cpu().numpy())
     res = []
+    FULL_TAU = 1e-10  # the tau of the whole-step FP64 comparison
+    K_mixed = None
     for thr in (1e-6, 1e-8, 1e-10, 1e-12):
         def step():
             api.transform_3c2c(X, V, bs, thr, form=api.FORM_OZAKI, n_digits=args.digits_3c2c, out=B, ctx=ctx)
@@ -472,6 +494,8 @@ def run_rik_large(args):
         e1.record()
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
+        if thr == FULL_TAU:
+            K_mixed = K.cpu().numpy().copy()
         # errors against the FP64 form: the 3c->2c output on the first sixteenth of
         # the rows, and K of the whole pipeline (both forms from the same X) over
         # the first sixteenth of the aux functions, which needs only those
@@ -505,7 +529,24 @@ def run_rik_large(args):
                     "screen_aux_1_16": {"mui_surviving": [st64[0], stoz[0]],
                                         "ij": cmp["ij"], "K": cmp["K"], "blocks": cmp["blocks"]}})
         del b_oz, b_64
-    print(json.dumps({"metric": "large RI-K step, mixed form, per tau", "unit": "ms",
+    full = None
+    if not args.skip_fp64:
+        # the plain GPU FP64 form, whole step once at one tau (about a minute),
+        # and the error of the mixed step's whole K against it
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        api.transform_3c2c(X, V, bs, FULL_TAU, out=B, ctx=ctx)
+        api.rik_occ_step(B, keys, C, n_bf, n_aux, n_occ, bs, FULL_TAU, out=K, ctx=ctx)
+        e1.record()
+        torch.cuda.synchronize()
+        fp64_ms = e0.elapsed_time(e1)
+        K64 = K.cpu().numpy()
+        mixed_ms = next(r["ms_per_step"] for r in res if r["tau"] == FULL_TAU)
+        full = {"tau": FULL_TAU, "fp64_ms_per_step": fp64_ms, "mixed_ms_per_step": mixed_ms,
+                "speedup_vs_fp64": fp64_ms / mixed_ms,
+                "rel_err_K_vs_fp64": float(np.linalg.norm(K_mixed - K64) / np.linalg.norm(K64))}
+    print(json.dumps({"metric": "large RI-K step, mixed form, per tau", "unit": "ms", "full_step_fp64": full,
                       "config": {"workload": f"125 atoms in a 20 A box, n_bf {n_bf}, n_aux {n_aux}, n_occ {n_occ}, "
                                              f"n_vec2 {n_vec2}, bs {bs} (uniform)",
                                  "digits": {"3c2c": args.digits_3c2c, "occ": args.digits_occ},
@@ -518,8 +559,9 @@ def run_batched(args):
     independent products C_i = A_i B_i, sizes uniform in [256, 4096] (rounded
     to the block size), block sizes from {16, 32, 48, 64}, block densities
     uniform in [0.05, 0.6], tau 1e-10; seeded inputs generated on the device.
-    Mixed form: one persistent tensor-core launch per block-size group
-    (autotuned), also replayed as a CUDA graph plan; FP64 form for reference.
+    Mixed form: one persistent tensor-core launch over every block-size group
+    (slots per tile autotuned per group), also replayed as a CUDA graph plan;
+    FP64 form for reference.
     Metric: useful (FP64-equivalent) TFLOP/s of the surviving block products."""
     import torch
 
@@ -575,7 +617,7 @@ def run_batched(args):
     # useful flops: the unpadded multiply-adds of the surviving block triples
     ctx.set_timing(True)
     api.matmult_batched(Cs, As, Bs, thr, 1.0, 0.0, form=api.FORM_OZAKI)
-    _, gemm_ms, macs = ctx.gemm_timing()
+    gemm_launches, gemm_ms, macs = ctx.gemm_timing()
     ctx.set_timing(False)
     useful = 2.0 * macs
     errs = []
@@ -589,7 +631,8 @@ def run_batched(args):
                        "surviving_block_triples": nsig, "useful_flops": useful},
             "mixed_ms": t_mx * 1e3, "plan_replay_ms": t_plan * 1e3, "plan_tflops": useful / t_plan / 1e12,
             "fp64_ms": t_64 * 1e3, "fp64_tflops": useful / t_64 / 1e12, "speedup_vs_fp64": t_64 / t_mx,
-            "tensor_gemm_ms": gemm_ms, "max_rel_err_first32": float(max(errs)),
+            "tensor_gemm_ms": gemm_ms, "tensor_gemm_launches": gemm_launches,
+            "max_rel_err_first32": float(max(errs)),
             "autotune": {str(k): v for k, v in ctx.autotune_entries().items()}, "dtype": "bf16 digits (auto 4-5) + f64"}
     print(json.dumps(line))
 

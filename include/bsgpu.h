@@ -162,9 +162,10 @@ bsg_status bsg_matmult_strassen_sparse_form(bsg_bsm C, bsg_bsm A, bsg_bsm B, dou
  *      matmult once per product) ----
  * C_i = alpha A_i B_i + beta C_i for i < n, each with matmult's semantics
  * (no transposes), any sizes and block sizes.  Mixed form: products are
- * grouped by block sizes and each group runs as ONE persistent tensor-core
- * launch; the tile height and pipeline depth per group shape come from an
- * autotuner (timed on first use, cached in the context).  nsig_total (may be
+ * grouped by block sizes, and ONE persistent tensor-core launch runs the
+ * tiles of every group (up to 8 groups per launch), each tile in its group's
+ * geometry; the tile height per group shape comes from an autotuner (timed
+ * on first use, group by group, cached in the context).  nsig_total (may be
  * NULL) receives the surviving block triples of all products. */
 bsg_status bsg_matmult_batched(size_t n, const bsg_bsm *C, const bsg_bsm *A, const bsg_bsm *B, double thresh,
                                double alpha, double beta, int form, int n_digits, uint64_t *nsig_total);

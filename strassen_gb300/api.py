@@ -34,10 +34,19 @@ def _is_device(a):
 
 
 def _buf(a, dtype=np.float64):
-    """(pointer, where, keepalive) for a host numpy array or a CUDA tensor."""
+    """(pointer, where, keepalive) for a host numpy array or a CUDA tensor.
+
+    A context's stream does not wait for torch's streams, so the work torch
+    has queued on the current stream (the kernels that produce the tensor)
+    is finished first: otherwise the library could read a tensor that is
+    still being written.  Where the context runs on torch's current stream
+    the stream is already in order and the wait returns at once."""
     if a is None:
         return None, BSG_HOST, None
     if _is_device(a):
+        import torch
+
+        torch.cuda.current_stream(a.device).synchronize()
         return C.c_void_p(a.data_ptr()), BSG_DEVICE, a
     if hasattr(a, "data_ptr"):  # CPU torch tensor
         a = a.numpy()
@@ -310,8 +319,9 @@ def matmult_strassen_sparse(C_, A, tA, B, tB, thresh, alpha, beta, min_size_for_
 
 def matmult_batched(Cs, As, Bs, thresh, alpha=1.0, beta=0.0, form=FORM_FP64, n_digits=0):
     """C_i = alpha A_i B_i + beta C_i for every i (matmult semantics, no
-    transposes); the mixed form runs each block-size group as one persistent
-    tensor-core launch.  Returns the surviving block triples of all products."""
+    transposes); the mixed form runs the tiles of every block-size group in
+    one persistent tensor-core launch (up to 8 groups per launch).  Returns
+    the surviving block triples of all products."""
     assert len(Cs) == len(As) == len(Bs)
     n = C.c_uint64()
     check(lib.bsg_matmult_batched(len(Cs), _handles(Cs), _handles(As), _handles(Bs), float(thresh), float(alpha),

@@ -3,13 +3,14 @@
 // sizes and block sizes.
 //
 // Mixed form: the products are grouped by (block rows, block k, block cols);
-// each group's digit images, exponents and step lists go into shared buffers
-// (per-product index bases) and ONE persistent k_ozgemm launch runs every
-// tile of every product of the group.  The tile height (slots per tile) and
-// the pipeline depth are picked per group shape by an autotuner that times
-// the candidates on the group's own tiles (writing scratch blocks) and caches
-// the winner in the context.  A plan captures the device work of a batch in a
-// CUDA graph for replay.
+// each group's digit images and exponents go into shared buffers (per-product
+// index bases), the tiles of every group into one list (group after group),
+// and ONE persistent k_ozgemm launch runs every tile of every product of the
+// batch, each tile in its group's geometry (up to 8 groups per launch).  The
+// tile height (slots per tile) of each group is picked by an autotuner that
+// times the candidates on the group's own tiles in a launch of their own
+// (writing scratch blocks) and caches the winner in the context.  A plan
+// captures the device work of a batch in a CUDA graph for replay.
 //
 // FP64 form: one grouped FP64 launch per product (the reference's order).
 #include <algorithm>
@@ -79,10 +80,10 @@ static void class_images(bsg_ctx ctx, std::vector<BatchProd> &P, const std::vect
 
 // tiles of every member (scratch: trial runs write scratch blocks)
 static void class_tiles(bsg_ctx ctx, std::vector<BatchProd> &P, ClassRun &cr, const ClassImages &im, bool all_fresh,
-                        double *scratch) {
+                        double *scratch, uint64_t step_base = 0) {
     cr.tp = OzTilePlan();
     cr.tile0.clear();
-    uint64_t steps = 0;
+    uint64_t steps = step_base;
     size_t scratch_items = 0;
     for (size_t q = 0; q < cr.prods.size(); ++q) {
         BatchProd &p = P[cr.prods[q]];
@@ -145,6 +146,74 @@ static void class_launch(bsg_ctx ctx, std::vector<BatchProd> &P, const ClassRun 
     }
     oz_run(ctx, cr.sh, dtl, nt, dst.as<OzStep>(), im.aimg.as<bf16>(), im.bimg.as<bf16>(), alpha, s,
            dmacs.as<unsigned long long>());
+}
+
+// The tiles of groups [c0, c1) of a batch in one list, group after group
+// (step indices continue from group to group), uploaded once.
+struct BatchLists {
+    DevBuf tiles, tib, tjb;
+    size_t c0 = 0, c1 = 0;
+    std::vector<size_t> tile0;  // first tile of each group, then the total
+    uint64_t steps = 0;
+};
+constexpr size_t kGroupsPerLaunch = 8;  // tile geometries one launch can hold
+
+static void batch_tiles(bsg_ctx ctx, std::vector<BatchProd> &P, std::vector<ClassRun> &classes,
+                        const std::vector<ClassImages> &ims, size_t c0, size_t c1, bool all_fresh, BatchLists &L) {
+    cudaStream_t s = ctx->stream;
+    L.c0 = c0;
+    L.c1 = c1;
+    L.tile0.clear();
+    L.steps = 0;
+    std::vector<OzTile> tiles;
+    std::vector<uint32_t> tib, tjb;
+    for (size_t c = c0; c < c1; ++c) {
+        ClassRun &cr = classes[c];
+        class_tiles(ctx, P, cr, ims[c], all_fresh, nullptr, L.steps);
+        L.tile0.push_back(tiles.size());
+        tiles.insert(tiles.end(), cr.tp.tiles.begin(), cr.tp.tiles.end());
+        tib.insert(tib.end(), cr.tp.tib.begin(), cr.tp.tib.end());
+        tjb.insert(tjb.end(), cr.tp.tjb.begin(), cr.tp.tjb.end());
+        L.steps += class_steps(P, cr);
+        BSG_REQUIRE(L.steps < 0xffffffffull, BSG_ERR_UNSUPPORTED, "too many Ozaki steps in one batch launch");
+    }
+    L.tile0.push_back(tiles.size());
+    const size_t nt = tiles.size();
+    L.tiles = DevBuf(std::max<size_t>(nt, 1) * sizeof(OzTile), s);
+    L.tib = DevBuf(std::max<size_t>(tib.size(), 1) * 4, s);
+    L.tjb = DevBuf(std::max<size_t>(nt, 1) * 4, s);
+    if (!nt) return;
+    BSG_CUDA(cudaMemcpyAsync(L.tiles.p, tiles.data(), nt * sizeof(OzTile), cudaMemcpyHostToDevice, s));
+    BSG_CUDA(cudaMemcpyAsync(L.tib.p, tib.data(), tib.size() * 4, cudaMemcpyHostToDevice, s));
+    BSG_CUDA(cudaMemcpyAsync(L.tjb.p, tjb.data(), nt * 4, cudaMemcpyHostToDevice, s));
+    // the host vectors are released on return: they must be copied first
+    BSG_CUDA(cudaStreamSynchronize(s));
+}
+
+// steps of every tile of the list, then one persistent launch over all of
+// them (no synchronization)
+static void batch_launch(bsg_ctx ctx, std::vector<BatchProd> &P, const std::vector<ClassRun> &classes,
+                         const std::vector<ClassImages> &ims, const BatchLists &L, double alpha) {
+    cudaStream_t s = ctx->stream;
+    const size_t nt = L.tile0.back();
+    if (!nt) return;
+    DevBuf dst(std::max<uint64_t>(L.steps, 1) * sizeof(OzStep), s), dmacs(8, s);
+    BSG_CUDA(cudaMemsetAsync(dmacs.p, 0, 8, s));
+    OzTile *dtl = const_cast<OzTile *>(L.tiles.as<OzTile>());
+    const uint32_t *dib = L.tib.as<uint32_t>(), *djb = L.tjb.as<uint32_t>();
+    std::vector<OzRun> runs;
+    for (size_t c = L.c0; c < L.c1; ++c) {
+        const ClassRun &cr = classes[c];
+        const size_t T0 = L.tile0[c - L.c0];
+        for (size_t q = 0; q < cr.prods.size(); ++q) {
+            BatchProd &p = P[cr.prods[q]];
+            const size_t t0 = T0 + cr.tile0[q], t1 = T0 + cr.tile0[q + 1];
+            oz_launch_steps(ctx, dtl + t0, t1 - t0, dib + t0 * kOzMaxSlots, djb + t0, p.A, p.B, p.si.g, cr.sh.R,
+                            dst.as<OzStep>(), dmacs.as<unsigned long long>(), ims[c].abase[q], ims[c].bbase[q]);
+        }
+        runs.push_back(OzRun{cr.sh, ims[c].aimg.as<bf16>(), ims[c].bimg.as<bf16>(), L.tile0[c - L.c0 + 1]});
+    }
+    oz_run_groups(ctx, runs, dtl, nt, dst.as<OzStep>(), alpha, s, dmacs.as<unsigned long long>());
 }
 
 // picks (slots per tile, stages) for the group's shape: cached, or timed on
@@ -264,20 +333,23 @@ extern "C" bsg_status bsg_matmult_batched(size_t n, const bsg_bsm *C, const bsg_
         if (P.empty()) return;
         bsg_ctx ctx = A[0]->ctx;
         std::vector<ClassRun> classes = make_classes(P, n_digits);
-        for (auto &cr : classes) {
-            ClassImages im;
-            class_images(ctx, P, cr.prods, cr.sh, im);
-            class_tune(ctx, P, cr, im, alpha);
-            class_tiles(ctx, P, cr, im, false, nullptr);
-            class_launch(ctx, P, cr, im, alpha);
+        std::vector<ClassImages> ims(classes.size());
+        for (size_t c = 0; c < classes.size(); ++c) {
+            class_images(ctx, P, classes[c].prods, classes[c].sh, ims[c]);
+            class_tune(ctx, P, classes[c], ims[c], alpha);
+        }
+        for (size_t c0 = 0; c0 < classes.size(); c0 += kGroupsPerLaunch) {
+            BatchLists L;
+            batch_tiles(ctx, P, classes, ims, c0, std::min(classes.size(), c0 + kGroupsPerLaunch), false, L);
+            batch_launch(ctx, P, classes, ims, L, alpha);
         }
         ctx->gemm_check();
     });
 }
 
 // A captured batch: the device work (exponents, digit images, step lists,
-// one persistent launch per block-size group) of C_i = alpha A_i B_i as a
-// CUDA graph.  The C block structure is fixed when the plan is made (beta 0:
+// one persistent launch over every block-size group) of C_i = alpha A_i B_i
+// as a CUDA graph.  The C block structure is fixed when the plan is made (beta 0:
 // every output block is overwritten); a replay recomputes everything from the
 // operands' current values and cached norms.
 struct bsg_batch_plan_s {
@@ -285,7 +357,7 @@ struct bsg_batch_plan_s {
     std::vector<BatchProd> prods;
     std::vector<ClassRun> classes;
     std::vector<ClassImages> images;  // exponents and digit images the tiles point into
-    std::vector<ClassLists> lists;    // device tile lists the graph reads
+    std::vector<BatchLists> lists;    // device tile lists the graph reads (up to 8 groups each)
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     uint64_t nsig = 0;
@@ -308,16 +380,18 @@ extern "C" bsg_status bsg_batched_plan_create(size_t n, const bsg_bsm *C, const 
         plan->classes = make_classes(plan->prods, n_digits);
         // buffers the plan owns; tune and run once outside the capture
         // (first-use initialisation, and the plan's own first result)
-        plan->images.resize(plan->classes.size());
-        plan->lists.resize(plan->classes.size());
-        for (size_t c = 0; c < plan->classes.size(); ++c) {
+        const size_t nc = plan->classes.size();
+        plan->images.resize(nc);
+        for (size_t c = 0; c < nc; ++c) {
             ClassRun &cr = plan->classes[c];
-            ClassImages &im = plan->images[c];
-            class_images(ctx, plan->prods, cr.prods, cr.sh, im);
-            class_tune(ctx, plan->prods, cr, im, alpha);
-            class_tiles(ctx, plan->prods, cr, im, true, nullptr);
-            class_upload(ctx, cr, plan->lists[c]);
-            class_launch(ctx, plan->prods, cr, im, alpha, &plan->lists[c]);
+            class_images(ctx, plan->prods, cr.prods, cr.sh, plan->images[c]);
+            class_tune(ctx, plan->prods, cr, plan->images[c], alpha);
+        }
+        plan->lists.resize((nc + kGroupsPerLaunch - 1) / kGroupsPerLaunch);
+        for (size_t k = 0; k < plan->lists.size(); ++k) {
+            batch_tiles(ctx, plan->prods, plan->classes, plan->images, k * kGroupsPerLaunch,
+                        std::min(nc, (k + 1) * kGroupsPerLaunch), true, plan->lists[k]);
+            batch_launch(ctx, plan->prods, plan->classes, plan->images, plan->lists[k], alpha);
         }
         ctx->gemm_check();
         ctx->gemm_err_flag();  // allocated and armed before the capture
@@ -325,11 +399,12 @@ extern "C" bsg_status bsg_batched_plan_create(size_t n, const bsg_bsm *C, const 
         BSG_CUDA(cudaStreamSynchronize(s));
         BSG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
         try {
-            for (size_t c = 0; c < plan->classes.size(); ++c) {
+            for (size_t c = 0; c < nc; ++c) {
                 ClassRun &cr = plan->classes[c];
                 class_images_compute(ctx, plan->prods, cr.prods, cr.sh, plan->images[c]);
-                class_launch(ctx, plan->prods, cr, plan->images[c], alpha, &plan->lists[c]);
             }
+            for (const BatchLists &L : plan->lists)
+                batch_launch(ctx, plan->prods, plan->classes, plan->images, L, alpha);
         } catch (...) {
             cudaGraph_t g = nullptr;
             cudaStreamEndCapture(s, &g);

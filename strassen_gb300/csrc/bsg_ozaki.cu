@@ -53,12 +53,21 @@ static int round_up(int x, int m) { return (x + m - 1) / m * m; }
 // N granularity of 16 (an MMA over an odd number of 8-row planes reads 8
 // zero rows past the stack)
 static uint32_t oz_b_rows(int nd, int np) { return (uint32_t)round_up(nd * np, 16); }
-// bytes of one step's A and B operands in shared memory
-static uint32_t oz_half_bytes(const OzShape &sh) {
-    return (uint32_t)sh.nd * 128u * sh.kp * 2u + oz_b_rows(sh.nd, sh.np) * sh.kp * 2u;
+// bytes of one stage in shared memory: one step's A (128 rows) and B, or a
+// pair's [A0 A1 B0 B1] with each A holding its R slots only.  The MMA reads
+// 128 rows of A1 (a_stage bytes from its start), which run on into B0 and
+// B1; where the slots hold fewer rows than B0 and B1 cover (8-row blocks: 64
+// rows of slots) the stage is extended so that the read stays inside it.
+static uint32_t oz_stage_bytes(const OzShape &sh) {
+    const uint32_t b = oz_b_rows(sh.nd, sh.np) * sh.kp * 2u, a_stage = (uint32_t)sh.nd * 128u * sh.kp * 2u;
+    if (!sh.pair) return a_stage + b;
+    const uint32_t a_pack = (uint32_t)sh.R * sh.nd * sh.mp * sh.kp * 2u;
+    return std::max(2u * a_pack + 2u * b, a_pack + a_stage);
 }
-static uint32_t oz_stage_bytes(const OzShape &sh) { return (sh.pair ? 2u : 1u) * oz_half_bytes(sh); }
 constexpr uint32_t kOzSmemBudget = 200u * 1024u;
+// room for the pipeline stages themselves: up to 224 KB of the 227 KB a CTA
+// can have (the step prefetch and the barriers take the rest)
+constexpr uint32_t kOzSmemStages = 224u * 1024u;
 
 OzShape oz_shape(int bs_rows, int bs_k, int bs_cols, int nd) {
     OzShape s;
@@ -89,18 +98,71 @@ int oz_default_digits(int requested, int bs_rows, int bs_k, int bs_cols) {
     return kOzSmemBudget / oz_stage_bytes(s5) >= 2 ? 5 : 4;
 }
 
+// Geometry of a run of tiles: an OzShape with its operand images.  A launch
+// holds one; a launch over a batch of products of several block sizes holds
+// one per block-size group, its tiles in group order: tiles below
+// geo[0].tile_end have geometry 0, the next ones up to geo[1].tile_end
+// geometry 1, and so on.
+struct OzGeo {
+    int mp, kp, np, R, nd, F;
+    int pair;           // two steps per stage (OzShape::pair)
+    int J;              // N-side sub-blocks of a B image (np / J rows each)
+    uint32_t tx_bytes;  // bytes of one step's copies
+    int S;                // pipeline stages of this geometry's tiles
+    uint32_t stage_bytes; // their stride in the shared-memory ring
+    uint32_t tile_end;
+    const bf16 *a_img, *b_img;
+};
+constexpr int kOzMaxGeo = 8;
+
 struct OzKParams {
-    int mp, kp, R, nd, S, F;
-    int pair;            // two steps per stage (OzShape::pair)
-    int J;               // N-side sub-blocks of a B image (NP / J rows each)
-    uint32_t chunk;      // consecutive tiles per CTA turn
-    int nbuf;            // TMEM accumulator sets (2: the MMA fills one while the epilogue drains the other)
-    uint32_t tmem_cols;  // columns of one accumulator set
-    uint32_t tx_bytes;
+    OzGeo geo[kOzMaxGeo];
+    int n_geo;
+    int S;                 // stage barriers: the most stages of any geometry
+    uint32_t ring_bytes;   // the shared-memory ring: the largest S x stage_bytes of any geometry
+    uint32_t chunk;        // consecutive tiles per CTA turn
+    int nbuf;              // TMEM accumulator sets (2: the MMA fills one while the epilogue drains the other)
+    uint32_t tmem_cols;    // columns of one accumulator set
     const bf16 *zero;
     double alpha;
     unsigned long long *prof;  // optional stall counters (kOzProf entries), null when not timing
 };
+
+// Shared-memory layout of one stage for a geometry (np = the tile's output
+// columns).  One step: [A: 128 rows | B].  A pair: [A0 | A1 | B0 | B1] with
+// each A holding only its R slots (a_pack bytes), so that the two steps'
+// slot images sit back to back as they do in the A images when the image
+// indices continue from one step to the next (one copy instead of two; a
+// bulk copy's cost is mostly per copy).  The MMA still reads 128 rows of each
+// A: rows past the R slots fall in the next region of the same stage (finite
+// digits), and their accumulator rows are never stored.
+struct OzLay {
+    uint32_t a_stage;     // A: 128 rows x nd digits (M-side layout)
+    uint32_t b_copy;      // bytes of one B digit stack
+    uint32_t b_stage;     // its room in the stage (N rounded to 16)
+    uint32_t slot_bytes;  // one slot's full digit image
+    uint32_t a_pack;      // A bytes of one step
+    uint32_t b_off;       // offset of B0 in the stage
+    size_t slot_elems, b_img_elems;
+};
+__device__ __forceinline__ OzLay oz_lay(const OzGeo &g, int np) {
+    OzLay L;
+    L.a_stage = (uint32_t)g.nd * 128u * g.kp * 2u;
+    L.b_copy = (uint32_t)g.nd * np * g.kp * 2u;
+    L.b_stage = (uint32_t)((g.nd * np + 15) & ~15) * g.kp * 2u;
+    L.slot_bytes = (uint32_t)g.nd * g.mp * g.kp * 2u;
+    L.a_pack = g.pair ? (uint32_t)g.R * L.slot_bytes : L.a_stage;
+    L.b_off = g.pair ? 2u * L.a_pack : L.a_stage;
+    L.slot_elems = (size_t)g.nd * g.mp * g.kp;
+    L.b_img_elems = (size_t)g.nd * np * g.kp;
+    return L;
+}
+// geometry index of tile t
+__device__ __forceinline__ int oz_geo_index(const OzGeo *geo, int n_geo, uint32_t t) {
+    int i = 0;
+    while (i + 1 < n_geo && t >= geo[i].tile_end) ++i;
+    return i;
+}
 
 // stall counters (SM clock cycles summed over CTAs), read through bsg_ctx_gemm_stalls
 enum OzProf {
@@ -240,36 +302,39 @@ __host__ __device__ constexpr int oz_plan_entries(int nd, int planes) {
     return n;
 }
 
-template <int NP>
+// MULTI: the launch holds several tile geometries (OzKParams::geo), each
+// tile takes its own; NP is then the largest tile width.  Otherwise every
+// tile has geometry 0, of width NP.
+template <int NP, bool MULTI>
 __global__ void __launch_bounds__(OzEpi<NP>::threads) __maxnreg__(OzEpi<NP>::max_regs)
     k_ozgemm(const OzTile *__restrict__ tiles, uint32_t n_tiles, const OzStep *__restrict__ steps,
-             const bf16 *__restrict__ a_img, const bf16 *__restrict__ b_img, OzKParams P, int *__restrict__ err) {
+             const __grid_constant__ OzKParams P, int *__restrict__ err) {
     extern __shared__ __align__(1024) uint8_t smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t a_stage = (uint32_t)P.nd * 128u * P.kp * 2u;  // A: 128 rows x nd digits (M-side layout)
-    const uint32_t b_copy = (uint32_t)P.nd * NP * P.kp * 2u;           // bytes of one B digit stack
-    const uint32_t b_stage = (uint32_t)((P.nd * NP + 15) & ~15) * P.kp * 2u;  // stage room (N rounded to 16)
-    const uint32_t half_bytes = a_stage + b_stage;  // one step's operands; a pair stage holds two
-    const uint32_t stage_bytes = P.pair ? 2u * half_bytes : half_bytes;
-    const uint32_t slot_bytes = (uint32_t)P.nd * P.mp * P.kp * 2u;  // one slot's full digit image
-    // Stage layout.  One step: [A: 128 rows | B].  A pair: [A0 | A1 | B0 | B1]
-    // with each A holding only its R slots (a_pack bytes), so that the two
-    // steps' slot images sit back to back as they do in a_img when the
-    // image indices continue from one step to the next (one copy instead of
-    // two; a bulk copy's cost is mostly per copy).  The MMA still reads 128
-    // rows of each A: rows past the R slots fall in the next region of the
-    // same stage (finite digits), and their accumulator rows are never stored.
-    const uint32_t a_pack = P.pair ? (uint32_t)P.R * slot_bytes : a_stage;  // A bytes of one step
-    const uint32_t b_off = P.pair ? 2u * a_pack : a_stage;                  // offset of B0 in the stage
-    const size_t slot_elems = (size_t)P.nd * P.mp * P.kp, b_img_elems = (size_t)P.nd * NP * P.kp;
-    OzStep *sstep = reinterpret_cast<OzStep *>(smem + (size_t)P.S * stage_bytes);  // 32 prefetched steps
+    // The ring holds S stages of a geometry, each oz_stage_bytes of it (every
+    // byte the MMAs read from a stage, also A1's 128 rows in pair mode).  A
+    // multi-geometry launch changes S and the stride at a change of geometry
+    // (the producer first waits for every stage to be released); a stage's
+    // barriers keep their own phase across the change (bit s of phb).
+    const OzLay L0 = oz_lay(P.geo[0], NP);  // the stage layout of a one-geometry launch
+    OzStep *sstep = reinterpret_cast<OzStep *>(smem + (size_t)P.ring_bytes);  // 32 prefetched steps
     uint64_t *full = reinterpret_cast<uint64_t *>(sstep + 32);
     uint64_t *empty = full + P.S;
     uint64_t *tfull = empty + P.S;  // [2]
     uint64_t *tempty = tfull + 2;   // [2]
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(tempty + 2);
     volatile int *abort = reinterpret_cast<volatile int *>(tmem_slot + 1);
+    OzGeo *sgeo = reinterpret_cast<OzGeo *>(tmem_slot + 4);  // MULTI: the geometry table
     const bool prof = P.prof != nullptr;
+    // geometry of tile t and its stage layout
+    auto geo_at = [&](uint32_t t) -> const OzGeo & {
+        if constexpr (MULTI) return sgeo[oz_geo_index(sgeo, P.n_geo, t)];
+        else return P.geo[0];
+    };
+    auto lay_of = [&](const OzGeo &g) -> OzLay {
+        if constexpr (MULTI) return oz_lay(g, g.np);
+        else return L0;
+    };
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < P.S; ++s) {
@@ -283,8 +348,11 @@ __global__ void __launch_bounds__(OzEpi<NP>::threads) __maxnreg__(OzEpi<NP>::max
         *abort = 0;
         tc::fence_barrier_init();
     }
+    if constexpr (MULTI) {
+        if (threadIdx.x < (unsigned)P.n_geo) sgeo[threadIdx.x] = P.geo[threadIdx.x];
+    }
     // rows past the last slot are never copied: keep them zero
-    for (uint32_t i = threadIdx.x; i < (uint32_t)P.S * stage_bytes / 16u; i += blockDim.x)
+    for (uint32_t i = threadIdx.x; i < P.ring_bytes / 16u; i += blockDim.x)
         reinterpret_cast<uint4 *>(smem)[i] = make_uint4(0, 0, 0, 0);
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     if (warp == 1) {
@@ -300,52 +368,78 @@ __global__ void __launch_bounds__(OzEpi<NP>::threads) __maxnreg__(OzEpi<NP>::max
         // ---------------- producer ----------------
         uint32_t it = 0;  // stages filled
         unsigned long long w_empty = 0;
-        uint32_t stage = 0, ph = 0;  // ring position of stage `it`
-        const uint32_t jfull = (1u << P.J) - 1u;
-        unsigned long long n_copied = 0, n_live = 0;
+        // ring position; a one-geometry launch flips ph at every wrap, a
+        // multi-geometry one keeps each stage's phase (bit s of phb) and the
+        // stages ever filled
+        uint32_t stage = 0, ph = 0, phb = 0, filled = 0;
+        int cur_geo = -1;
+        uint32_t n_stages = (uint32_t)P.geo[0].S, sbytes = P.geo[0].stage_bytes;
+        unsigned long long n_copied = 0, n_live = 0, n_cap = 0;
         // the A slots of a stage: lane l < nA takes slot l % R of step l / R,
         // at sA + l * slot_bytes (a pair's second step follows the first).
         // Runs of consecutive images (or of zeros) go in one copy: a fully
         // live step is one A copy, and so is a fully live pair whose image
         // indices continue from the first step to the second
-        auto copy_a = [&](const OzStep &st0, const OzStep &st1, bool two, uint8_t *sA, uint64_t *bar) {
-            const uint32_t nA = two ? 2u * (uint32_t)P.R : (uint32_t)P.R;
+        auto copy_a = [&](const OzGeo &g, const OzLay &L, const OzStep &st0, const OzStep &st1, bool two, uint8_t *sA,
+                          uint64_t *bar) {
+            const uint32_t nA = two ? 2u * (uint32_t)g.R : (uint32_t)g.R;
             const uint32_t ai =
-                lane < P.R ? st0.a[lane] : ((uint32_t)lane < nA ? st1.a[lane - P.R] : kOzNone);
+                lane < g.R ? st0.a[lane] : ((uint32_t)lane < nA ? st1.a[lane - g.R] : kOzNone);
             const uint32_t prev = __shfl_up_sync(0xffffffffu, ai, 1);
             const bool live = ai != kOzNone;
             const bool joins = lane > 0 && (live ? (prev != kOzNone && prev + 1u == ai) : prev == kOzNone);
             const uint32_t starts = __ballot_sync(0xffffffffu, (uint32_t)lane < nA && !joins) | (1u << nA);
             if ((uint32_t)lane < nA && !joins) {
                 const int len = __ffs(starts & ~((2u << lane) - 1u)) - 1 - lane;
-                const bf16 *src = live ? a_img + (size_t)ai * slot_elems : P.zero;
-                tc::bulk_g2s(sA + lane * slot_bytes, src, (uint32_t)len * slot_bytes, bar);
+                const bf16 *src = live ? g.a_img + (size_t)ai * L.slot_elems : P.zero;
+                tc::bulk_g2s(sA + lane * L.slot_bytes, src, (uint32_t)len * L.slot_bytes, bar);
             }
         };
         // one step's B digit stack into sB
-        auto copy_b = [&](const OzStep &st, uint8_t *sB, uint64_t *bar) {
+        auto copy_b = [&](const OzGeo &g, const OzLay &L, const OzStep &st, uint8_t *sB, uint64_t *bar) {
+            const uint32_t jfull = (1u << g.J) - 1u;
             if ((st.bmask & jfull) == jfull) {
-                if (lane == 31) tc::bulk_g2s(sB, b_img + (size_t)st.b * b_img_elems, b_copy, bar);
+                if (lane == 31) tc::bulk_g2s(sB, g.b_img + (size_t)st.b * L.b_img_elems, L.b_copy, bar);
             } else {
                 // some N-side sub-blocks are screened out for this step: per
                 // (sub-block, digit) chunk, the image's rows or zeros
-                const int npj = NP / P.J, c = lane - 16;
-                if (c >= 0 && c < P.J * P.nd) {
-                    const int j = c / P.nd, i = c % P.nd;
-                    const size_t off = ((size_t)i * NP + (size_t)j * npj) * P.kp;
-                    const bf16 *src = ((st.bmask >> j) & 1u) ? b_img + (size_t)st.b * b_img_elems + off : P.zero;
-                    tc::bulk_g2s(sB + off * 2, src, (uint32_t)npj * P.kp * 2u, bar);
+                const int np = MULTI ? g.np : NP;
+                const int npj = np / g.J, c = lane - 16;
+                if (c >= 0 && c < g.J * g.nd) {
+                    const int j = c / g.nd, i = c % g.nd;
+                    const size_t off = ((size_t)i * np + (size_t)j * npj) * g.kp;
+                    const bf16 *src =
+                        ((st.bmask >> j) & 1u) ? g.b_img + (size_t)st.b * L.b_img_elems + off : P.zero;
+                    tc::bulk_g2s(sB + off * 2, src, (uint32_t)npj * g.kp * 2u, bar);
                 }
             }
         };
-        auto count_step = [&](const OzStep &st) {
-            const bool live = lane < P.R && st.a[lane] != kOzNone;
+        auto count_step = [&](const OzGeo &g, const OzStep &st) {
+            const bool live = lane < g.R && st.a[lane] != kOzNone;
             ++n_copied;
+            n_cap += (unsigned long long)(g.R * g.J);
             n_live += (unsigned long long)__popc(__ballot_sync(0xffffffffu, live)) *
-                      (unsigned long long)__popc(st.bmask & jfull);
+                      (unsigned long long)__popc(st.bmask & ((1u << g.J) - 1u));
         };
-        const uint32_t kstep = P.pair ? 2u : 1u;
-        for (uint32_t t = oz_first_tile(P.chunk); t < n_tiles && !*abort; t = oz_next_tile(t, P.chunk)) {
+        bool pok = true;
+        for (uint32_t t = oz_first_tile(P.chunk); t < n_tiles && pok && !*abort; t = oz_next_tile(t, P.chunk)) {
+            const OzGeo &g = geo_at(t);
+            const OzLay L = lay_of(g);
+            const int gi = MULTI ? oz_geo_index(sgeo, P.n_geo, t) : 0;
+            if (MULTI && gi != cur_geo) {
+                // a new geometry: every filled stage released before the ring is laid out anew
+                if (cur_geo >= 0 && lane == 0) {
+                    for (int s2 = 0; s2 < P.S && pok; ++s2)
+                        if ((filled >> s2) & 1u) pok = tc::mbar_wait_sleep(&empty[s2], ((phb >> s2) & 1u) ^ 1u, abort);
+                }
+                pok = __shfl_sync(0xffffffffu, pok ? 1 : 0, 0) != 0;
+                if (!pok) break;
+                cur_geo = gi;
+                stage = 0;
+                n_stages = (uint32_t)g.S;
+                sbytes = g.stage_bytes;
+            }
+            const uint32_t jfull = (1u << g.J) - 1u, kstep = g.pair ? 2u : 1u;
             const uint32_t s0 = tiles[t].s0, ns = tiles[t].ns;
             for (uint32_t k = 0; k < ns; k += kstep, ++it) {
                 if ((k & 31u) == 0) {
@@ -359,51 +453,63 @@ __global__ void __launch_bounds__(OzEpi<NP>::threads) __maxnreg__(OzEpi<NP>::max
                 int okw = 1;
                 if (lane == 0) {
                     const long long c0 = prof ? clock64() : 0;
-                    okw = tc::mbar_wait_sleep(&empty[stage], ph ^ 1u, abort) ? 1 : 0;
+                    const uint32_t par = MULTI ? ((phb >> stage) & 1u) ^ 1u : ph ^ 1u;
+                    okw = tc::mbar_wait_sleep(&empty[stage], par, abort) ? 1 : 0;
                     if (prof) w_empty += clock64() - c0;
                 }
                 if (!__shfl_sync(0xffffffffu, okw, 0)) break;
-                uint8_t *sA = smem + (size_t)stage * stage_bytes;
-                uint8_t *sB = sA + b_off;
-                const bool two = P.pair && k + 1 < ns;
+                uint8_t *sA = smem + (size_t)stage * sbytes;
+                uint8_t *sB = sA + L.b_off;
+                const bool two = g.pair && k + 1 < ns;
                 // a lone last step of a pair stage gets a zero B in the second
                 // half: the k16 slice that straddles into it then adds nothing
                 // (its A half holds earlier digits or zeros, always finite)
-                const uint32_t tx = two ? 2u * P.tx_bytes : (P.pair ? P.tx_bytes + b_copy : P.tx_bytes);
+                const uint32_t tx = two ? 2u * g.tx_bytes : (g.pair ? g.tx_bytes + L.b_copy : g.tx_bytes);
                 if (lane == 0) tc::mbar_arrive_expect_tx(&full[stage], tx);
                 __syncwarp();
                 const OzStep &st0 = sstep[k & 31u], &st1 = sstep[(k + 1) & 31u];
                 if (prof) {
-                    count_step(st0);
-                    if (two) count_step(st1);
+                    count_step(g, st0);
+                    if (two) count_step(g, st1);
                 }
-                copy_a(st0, st1, two, sA, &full[stage]);
-                if (two && b_stage == b_copy && (st0.bmask & jfull) == jfull && (st1.bmask & jfull) == jfull &&
+                copy_a(g, L, st0, st1, two, sA, &full[stage]);
+                if (two && L.b_stage == L.b_copy && (st0.bmask & jfull) == jfull && (st1.bmask & jfull) == jfull &&
                     st1.b == st0.b + 1u) {
-                    // both steps' full B stacks, consecutive in b_img: one copy
-                    if (lane == 31) tc::bulk_g2s(sB, b_img + (size_t)st0.b * b_img_elems, 2u * b_copy, &full[stage]);
+                    // both steps' full B stacks, consecutive in the B images: one copy
+                    if (lane == 31)
+                        tc::bulk_g2s(sB, g.b_img + (size_t)st0.b * L.b_img_elems, 2u * L.b_copy, &full[stage]);
                 } else {
-                    copy_b(st0, sB, &full[stage]);
+                    copy_b(g, L, st0, sB, &full[stage]);
                     if (two)
-                        copy_b(st1, sB + b_stage, &full[stage]);
-                    else if (P.pair && lane == 31)
-                        tc::bulk_g2s(sB + b_stage, P.zero, b_copy, &full[stage]);
+                        copy_b(g, L, st1, sB + L.b_stage, &full[stage]);
+                    else if (g.pair && lane == 31)
+                        tc::bulk_g2s(sB + L.b_stage, P.zero, L.b_copy, &full[stage]);
                 }
-                if (++stage == (uint32_t)P.S) {
+                if constexpr (MULTI) {
+                    phb ^= 1u << stage;
+                    filled |= 1u << stage;
+                    if (++stage == n_stages) stage = 0;
+                } else if (++stage == (uint32_t)P.S) {
                     stage = 0;
                     ph ^= 1u;
                 }
             }
         }
-        // let the copies in flight land before the CTA can exit
+        // let the copies in flight land before the CTA can exit: the last
+        // fill of every stage
         if (lane == 0) {
-            const uint32_t first = it > (uint32_t)P.S ? it - P.S : 0;
-            for (uint32_t j = first; j < it; ++j) tc::mbar_wait(&full[j % P.S], (j / P.S) & 1u, abort);
+            if constexpr (MULTI) {
+                for (int s2 = 0; s2 < P.S; ++s2)
+                    if ((filled >> s2) & 1u) tc::mbar_wait(&full[s2], ((phb >> s2) & 1u) ^ 1u, abort);
+            } else {
+                const uint32_t first = it > (uint32_t)P.S ? it - P.S : 0;
+                for (uint32_t j = first; j < it; ++j) tc::mbar_wait(&full[j % P.S], (j / P.S) & 1u, abort);
+            }
             if (prof) {
                 atomicAdd(&P.prof[kProfProdWaitEmpty], w_empty);
                 atomicAdd(&P.prof[kProfCopiedSteps], n_copied);
                 atomicAdd(&P.prof[kProfLivePairs], n_live);
-                atomicAdd(&P.prof[kProfPairCapacity], n_copied * (unsigned long long)(P.R * P.J));
+                atomicAdd(&P.prof[kProfPairCapacity], n_cap);
             }
         }
         __syncwarp();
@@ -412,50 +518,78 @@ __global__ void __launch_bounds__(OzEpi<NP>::threads) __maxnreg__(OzEpi<NP>::max
         if (lane == 0) {
             const long long t_start = prof ? clock64() : 0;
             unsigned long long w_full = 0, w_tmem = 0, n_mma = 0;
-            uint32_t it = 0, ch = 0, stage = 0, ph = 0;
-            // MMA plan of one k16 slice, computed once: per A digit i, D_i x
+            uint32_t it = 0, ch = 0, stage = 0, ph = 0, phb = 0;  // phb: per-stage phases (multi-geometry)
+            // MMA plan of one k16 slice for a geometry: per A digit i, D_i x
             // [E_j0 .. E_j1) stacked along N (N <= 256, rounded up to 16: the
-            // extra 8 columns land past the last region) into TMEM region i + j0.
+            // extra columns land past the last region) into TMEM region i + j0.
             // Entry: x = TMEM column | (i == 0) << 16, y / z = A / B descriptor
-            // address offsets (16-byte units), w = instruction descriptor.
-            // 8-row groups: nd*kp*16 bytes apart on the M side (digits interleaved), kp*16 on the N side
-            const uint64_t a_desc0 = tc::smem_desc(tc::smem_u32(smem), 128u, (uint32_t)P.nd * P.kp * 16u);
-            const uint64_t b_desc0 = tc::smem_desc(tc::smem_u32(smem + b_off), 128u, (uint32_t)P.kp * 16u);
-            // pair mode: the slice that straddles the two steps starts at the
-            // first step's last core column and finds its second one (column 0
-            // of the second step, a_pack / b_stage further on) one leading byte
-            // offset further
-            const uint32_t ncol = (uint32_t)P.kp / 8u;  // core columns per step
-            const uint32_t lbo_xa = a_pack - (ncol - 1u) * 128u, lbo_xb = b_stage - (ncol - 1u) * 128u;
-            const uint64_t a_descx = tc::smem_desc(tc::smem_u32(smem), lbo_xa, (uint32_t)P.nd * P.kp * 16u);
-            const uint64_t b_descx = tc::smem_desc(tc::smem_u32(smem + b_off), lbo_xb, (uint32_t)P.kp * 16u);
-            constexpr int kMaxPlanes = 256 / NP;  // B planes one MMA can take
+            // address offsets (16-byte units), w = instruction descriptor.  The
+            // plan is held in registers (the loops below are unrolled); a
+            // multi-geometry launch rebuilds it when the geometry changes.
+            constexpr int kMaxPlanes = 256 / NP;  // B planes one MMA can take at width NP
             constexpr int kMaxPlan = oz_plan_entries(oz_max_digits(NP), kMaxPlanes);
-            uint32_t pd[kMaxPlan], pa[kMaxPlan], pb[kMaxPlan], pi[kMaxPlan];  // kept in registers (unrolled)
+            uint32_t pd[kMaxPlan], pa[kMaxPlan], pb[kMaxPlan], pi[kMaxPlan];
             int n_plan = 0;
+            uint64_t a_desc0 = 0, b_desc0 = 0, a_descx = 0, b_descx = 0;
+            uint32_t ncol = 0, cF = 1, ckstep = 1, ca_pack = 0, cb_stage = 0;
+            int cpair = 0, ckp = 0;
+            auto setup = [&](const OzGeo &g, const OzLay &L) {
+                const int np = MULTI ? g.np : NP;
+                const int planes = MULTI ? 256 / np : kMaxPlanes;
+                // 8-row groups: nd*kp*16 bytes apart on the M side (digits interleaved), kp*16 on the N side
+                a_desc0 = tc::smem_desc(tc::smem_u32(smem), 128u, (uint32_t)g.nd * g.kp * 16u);
+                b_desc0 = tc::smem_desc(tc::smem_u32(smem + L.b_off), 128u, (uint32_t)g.kp * 16u);
+                // pair mode: the slice that straddles the two steps starts at the
+                // first step's last core column and finds its second one (column 0
+                // of the second step, a_pack / b_stage further on) one leading byte
+                // offset further
+                ncol = (uint32_t)g.kp / 8u;  // core columns per step
+                const uint32_t lbo_xa = L.a_pack - (ncol - 1u) * 128u, lbo_xb = L.b_stage - (ncol - 1u) * 128u;
+                a_descx = tc::smem_desc(tc::smem_u32(smem), lbo_xa, (uint32_t)g.nd * g.kp * 16u);
+                b_descx = tc::smem_desc(tc::smem_u32(smem + L.b_off), lbo_xb, (uint32_t)g.kp * 16u);
+                cF = (uint32_t)g.F;
+                cpair = g.pair;
+                ckp = g.kp;
+                ckstep = g.pair ? 2u : 1u;
+                ca_pack = L.a_pack;
+                cb_stage = L.b_stage;
+                n_plan = 0;
 #pragma unroll
-            for (int e = 0; e < kMaxPlan; ++e) pd[e] = pa[e] = pb[e] = pi[e] = 0;
-            for (int i = 0; i < P.nd; ++i)
-                for (int j0 = 0; j0 < P.nd - i; j0 += kMaxPlanes) {
-                    const int j1 = min(P.nd - i, j0 + kMaxPlanes);
+                for (int e = 0; e < kMaxPlan; ++e) pd[e] = pa[e] = pb[e] = pi[e] = 0;
+                for (int i = 0; i < g.nd; ++i)
+                    for (int j0 = 0; j0 < g.nd - i; j0 += planes) {
+                        const int j1 = min(g.nd - i, j0 + planes);
 #pragma unroll
-                    for (int e = 0; e < kMaxPlan; ++e)
-                        if (e == n_plan) {
-                            pd[e] = (uint32_t)((i + j0) * NP) | (i == 0 ? 1u << 16 : 0u);
-                            pa[e] = ((uint32_t)i * P.kp * 16u) >> 4;
-                            pb[e] = ((uint32_t)j0 * NP * P.kp * 2u) >> 4;
-                            pi[e] = tc::idesc_bf16_f32(128u, (uint32_t)(((j1 - j0) * NP + 15) & ~15));
-                        }
-                    ++n_plan;
-                }
-            const uint32_t kstep = P.pair ? 2u : 1u;
+                        for (int e = 0; e < kMaxPlan; ++e)
+                            if (e == n_plan) {
+                                pd[e] = (uint32_t)((i + j0) * np) | (i == 0 ? 1u << 16 : 0u);
+                                pa[e] = ((uint32_t)i * g.kp * 16u) >> 4;
+                                pb[e] = ((uint32_t)j0 * np * g.kp * 2u) >> 4;
+                                pi[e] = tc::idesc_bf16_f32(128u, (uint32_t)(((j1 - j0) * np + 15) & ~15));
+                            }
+                        ++n_plan;
+                    }
+            };
+            setup(P.geo[0], L0);
+            int cur_geo = 0;
+            uint32_t n_stages = (uint32_t)P.geo[0].S, sbytes16 = P.geo[0].stage_bytes >> 4;
             bool ok = true;
             // the tile / chain / stage walk; issue(soff, k, ns, first, dbase)
             // issues one stage's MMAs
             auto mma_loop = [&](auto &&issue) {
                 for (uint32_t t = oz_first_tile(P.chunk); t < n_tiles && ok; t = oz_next_tile(t, P.chunk)) {
+                    if constexpr (MULTI) {
+                        const int gi = oz_geo_index(sgeo, P.n_geo, t);
+                        if (gi != cur_geo) {
+                            cur_geo = gi;
+                            setup(sgeo[gi], oz_lay(sgeo[gi], sgeo[gi].np));
+                            stage = 0;  // the producer lays the ring out anew
+                            n_stages = (uint32_t)sgeo[gi].S;
+                            sbytes16 = sgeo[gi].stage_bytes >> 4;
+                        }
+                    }
                     const uint32_t ns = tiles[t].ns;
-                    const uint32_t nch = (ns + P.F - 1) / P.F;
+                    const uint32_t nch = (ns + cF - 1) / cF;
                     for (uint32_t c = 0; c < nch && ok; ++c, ++ch) {
                         const uint32_t buf = P.nbuf == 2 ? (ch & 1u) : 0u, use = P.nbuf == 2 ? ch >> 1 : ch;
                         long long c0 = prof ? clock64() : 0;
@@ -466,21 +600,24 @@ __global__ void __launch_bounds__(OzEpi<NP>::threads) __maxnreg__(OzEpi<NP>::max
                         if (prof) w_tmem += clock64() - c0;
                         tc::tc_fence_after();
                         const uint32_t dbase = tmem + buf * P.tmem_cols;
-                        const uint32_t kend = min(ns, (c + 1) * (uint32_t)P.F);
-                        for (uint32_t k = c * P.F; k < kend; k += kstep, ++it) {
+                        const uint32_t kend = min(ns, (c + 1) * cF);
+                        for (uint32_t k = c * cF; k < kend; k += ckstep, ++it) {
                             c0 = prof ? clock64() : 0;
-                            if (!tc::mbar_wait(&full[stage], ph, abort)) {
+                            if (!tc::mbar_wait(&full[stage], MULTI ? (phb >> stage) & 1u : ph, abort)) {
                                 ok = false;
                                 break;
                             }
                             if (prof) w_full += clock64() - c0;
                             tc::tc_fence_after();
-                            const uint32_t soff = stage * (stage_bytes >> 4);
+                            const uint32_t soff = stage * (MULTI ? sbytes16 : P.geo[0].stage_bytes >> 4);
                             // the first MMA of a chain (digit 0, which spans every TMEM
                             // region) overwrites the accumulator
-                            issue(soff, k, ns, (k == c * P.F) ? 1u : 0u, dbase);
+                            issue(soff, k, ns, (k == c * cF) ? 1u : 0u, dbase);
                             tc::mma_commit(&empty[stage]);
-                            if (++stage == (uint32_t)P.S) {
+                            if constexpr (MULTI) {
+                                phb ^= 1u << stage;
+                                if (++stage == n_stages) stage = 0;
+                            } else if (++stage == (uint32_t)P.S) {
                                 stage = 0;
                                 ph ^= 1u;
                             }
@@ -495,14 +632,14 @@ __global__ void __launch_bounds__(OzEpi<NP>::threads) __maxnreg__(OzEpi<NP>::max
                 // k16 slices of this stage: kp / 16 of one step, or, for a
                 // pair, the ncol (odd) slices over both halves' 2 ncol core
                 // columns -- of a lone last step only those touching its half
-                const uint32_t nq = !P.pair ? (uint32_t)P.kp / 16u : (k + 1 < ns ? ncol : (ncol + 1u) / 2u);
+                const uint32_t nq = !cpair ? (uint32_t)ckp / 16u : (k + 1 < ns ? ncol : (ncol + 1u) / 2u);
                 // slice descriptors of this stage
                 uint64_t aqs[8], bqs[8];
 #pragma unroll
                 for (uint32_t q = 0; q < 8; ++q) {
                     uint64_t aq = 0, bq = 0;
                     if (q < nq) {
-                        if (!P.pair) {
+                        if (!cpair) {
                             aq = a_desc0 + soff + q * 16u;
                             bq = b_desc0 + soff + q * 16u;
                         } else {
@@ -514,8 +651,8 @@ __global__ void __launch_bounds__(OzEpi<NP>::threads) __maxnreg__(OzEpi<NP>::max
                                 aq = a_descx + soff + g * 8u;
                                 bq = b_descx + soff + g * 8u;
                             } else {  // both in the second step
-                                aq = a_desc0 + soff + ((a_pack + (g - ncol) * 128u) >> 4);
-                                bq = b_desc0 + soff + ((b_stage + (g - ncol) * 128u) >> 4);
+                                aq = a_desc0 + soff + ((ca_pack + (g - ncol) * 128u) >> 4);
+                                bq = b_desc0 + soff + ((cb_stage + (g - ncol) * 128u) >> 4);
                             }
                         }
                     }
@@ -549,7 +686,7 @@ __global__ void __launch_bounds__(OzEpi<NP>::threads) __maxnreg__(OzEpi<NP>::max
                 constexpr uint32_t KP = 24, ND = 5;
                 const uint32_t a_hi = (uint32_t)(a_desc0 >> 32), b_hi = (uint32_t)(b_desc0 >> 32);
                 // the second step's core column 1
-                const uint32_t ha2 = (a_pack + 128u) >> 4, hb2 = (b_stage + 128u) >> 4;
+                const uint32_t ha2 = (L0.a_pack + 128u) >> 4, hb2 = (L0.b_stage + 128u) >> 4;
                 const uint32_t a0 = (uint32_t)a_desc0 + soff, ax = (uint32_t)a_descx + soff + 16u, a2 = a0 + ha2;
                 const uint32_t b0 = (uint32_t)b_desc0 + soff, bx = (uint32_t)b_descx + soff + 16u, b2 = b0 + hb2;
                 const bool three = k + 1 < ns;  // a lone last step: the first two slices
@@ -564,8 +701,8 @@ __global__ void __launch_bounds__(OzEpi<NP>::threads) __maxnreg__(OzEpi<NP>::max
                 }
                 if (prof) n_mma += three ? 3u * ND : 2u * ND;
             };
-            if constexpr (NP == 48) {
-                if (P.nd == 5 && P.pair && P.kp == 24 && n_plan == 5)
+            if constexpr (NP == 48 && !MULTI) {
+                if (P.geo[0].nd == 5 && P.geo[0].pair && P.geo[0].kp == 24 && n_plan == 5)
                     mma_loop(issue_fixed);
                 else
                     mma_loop(issue_generic);
@@ -588,16 +725,21 @@ __global__ void __launch_bounds__(OzEpi<NP>::threads) __maxnreg__(OzEpi<NP>::max
         static_assert(NPH % CH == 0, "a group's columns are whole TMEM loads");
         const int q = warp & 3;
         const int grp = (warp - 2) >> 2;
-        const int cbase = grp * NPH;
         const int m = q * 32 + lane;
         const uint32_t lane_off = (uint32_t)(q * 32) << 16;
         unsigned long long w_full = 0, t_drain = 0, t_store = 0;
         uint32_t ch = 0;
         bool ok = true;
         for (uint32_t t = oz_first_tile(P.chunk); t < n_tiles && ok; t = oz_next_tile(t, P.chunk)) {
+            const OzGeo &g = geo_at(t);
+            const int np = MULTI ? g.np : NP;  // TMEM columns per weight region
+            // this group's columns: NP / G, or (a narrower geometry of a
+            // multi-geometry launch) its width's share in whole TMEM loads
+            const int npg = MULTI ? (np / OzEpi<NP>::G + CH - 1) / CH * CH : NPH;
+            const int cbase = grp * npg;
             const OzTile &T = tiles[t];
             const uint32_t ns = T.ns;
-            const uint32_t nch = (ns + P.F - 1) / P.F;
+            const uint32_t nch = (ns + g.F - 1) / g.F;
             long long hi[NPH];  // R0 + R1 + R2 in units of 2^-16
             float lo[NPH];      // R3 + R4 + ...
 #pragma unroll
@@ -618,10 +760,11 @@ __global__ void __launch_bounds__(OzEpi<NP>::threads) __maxnreg__(OzEpi<NP>::max
                 const uint32_t lane_addr = tmem + buf * P.tmem_cols + lane_off;
 #pragma unroll
                 for (int c0 = 0; c0 < NPH; c0 += CH) {
+                    if (MULTI && c0 >= npg) break;
                     float v0[CH], v1[CH], v2[CH];
                     tc::tmem_ldn<CH>(lane_addr + (uint32_t)(cbase + c0), v0);
-                    tc::tmem_ldn<CH>(lane_addr + (uint32_t)(NP + cbase + c0), v1);
-                    if (P.nd > 2) tc::tmem_ldn<CH>(lane_addr + (uint32_t)(2 * NP + cbase + c0), v2);
+                    tc::tmem_ldn<CH>(lane_addr + (uint32_t)(np + cbase + c0), v1);
+                    if (g.nd > 2) tc::tmem_ldn<CH>(lane_addr + (uint32_t)(2 * np + cbase + c0), v2);
                     tc::tmem_wait_ld();
                     // R0 is an integer < 2^24 and R1 a multiple of 2^-8 below 2^16: both
                     // exact in the FP32 accumulator.  R2 is a multiple of 2^-16 and exact
@@ -630,12 +773,12 @@ __global__ void __launch_bounds__(OzEpi<NP>::threads) __maxnreg__(OzEpi<NP>::max
                     for (int j = 0; j < CH; ++j) {
                         long long h = ((long long)__float2int_rn(v0[j]) << 16) +
                                       ((long long)__float2int_rn(v1[j] * 256.f) << 8);
-                        if (P.nd > 2) h += (long long)__float2int_rn(v2[j] * 65536.f);
+                        if (g.nd > 2) h += (long long)__float2int_rn(v2[j] * 65536.f);
                         hi[c0 + j] += h;
                     }
-                    for (int w = 3; w < P.nd; ++w) {
+                    for (int w = 3; w < g.nd; ++w) {
                         float v[CH];
-                        tc::tmem_ldn<CH>(lane_addr + (uint32_t)(w * NP + cbase + c0), v);
+                        tc::tmem_ldn<CH>(lane_addr + (uint32_t)(w * np + cbase + c0), v);
                         tc::tmem_wait_ld();
 #pragma unroll
                         for (int j = 0; j < CH; ++j) lo[c0 + j] += v[j];
@@ -648,8 +791,8 @@ __global__ void __launch_bounds__(OzEpi<NP>::threads) __maxnreg__(OzEpi<NP>::max
             }
             if (!ok) break;
             const long long c2 = prof ? clock64() : 0;
-            const int s = m / P.mp, r = m % P.mp;
-            if (s < P.R && T.c[s] != nullptr && r < T.rows[s]) {
+            const int s = m / g.mp, r = m % g.mp;
+            if (s < g.R && T.c[s] != nullptr && r < T.rows[s]) {
                 // value = alpha * (hi 2^-16 + lo) 2^(e_row + f_col - 14), formed as
                 // (hi + lo 2^16) 2^(e_row + f_col - 30): the same rounding (scaling
                 // by powers of two is exact), the power of two built from its bits
@@ -664,7 +807,7 @@ __global__ void __launch_bounds__(OzEpi<NP>::threads) __maxnreg__(OzEpi<NP>::max
                 const long long tsub_stride = T.sub_stride;
                 const int *tcexp = T.cexp;
                 const bool subm = tsub != 0;
-                const int npj = NP / P.J, js0 = cbase / npj;
+                const int npj = np / g.J, js0 = cbase / npj;
                 // every column's exponent loaded before the first store (the stores
                 // could alias the exponent array, which would serialize the loads)
                 int cex[NPH];
@@ -699,6 +842,7 @@ __global__ void __launch_bounds__(OzEpi<NP>::threads) __maxnreg__(OzEpi<NP>::max
                     };
 #pragma unroll
                     for (int j = 0; j < NPH; j += 2) {
+                        if (MULTI && j >= npg) break;
                         double *d0, *d1;
                         const double o0 = col_out(j, d0), o1 = col_out(j + 1, d1);
                         // a transposed tile's row is contiguous in the output: pairs of
@@ -719,7 +863,7 @@ __global__ void __launch_bounds__(OzEpi<NP>::threads) __maxnreg__(OzEpi<NP>::max
                     else
                         store_all([&](int j, int e) { return __dmul_rn(P.alpha, value(j, e)); }, de);
                 };
-                if (P.nd <= 5 && nch < 256) {
+                if (g.nd <= 5 && nch < 256) {
                     // up to 5 digits lo holds weights 3 and 4, multiples of 2^-32,
                     // so lo 2^32 is an integer (below 2^34) and hi 2^16 + lo 2^32
                     // the exact sum in units of 2^-32 (hi < 2^39 per chain of <= 512
@@ -753,75 +897,136 @@ __global__ void __launch_bounds__(OzEpi<NP>::threads) __maxnreg__(OzEpi<NP>::max
     if (threadIdx.x == 0 && *abort) atomicExch(err, 1);
 }
 
-template <int NP>
-static void launch_oz(bsg_ctx ctx, const OzShape &sh, const OzTile *tiles, size_t n_tiles, const OzStep *steps,
-                      const bf16 *a_img, const bf16 *b_img, double alpha, int *err, unsigned long long *prof,
-                      uint32_t chunk, cudaStream_t s) {
+// TMEM columns the MMA plan of a geometry writes (per A digit i, planes
+// j0..j1 stacked from column (i + j0) np, N rounded up to 16), with the
+// MMA's planes per instruction for tile width np_max
+static uint32_t oz_tmem_extent(int nd, int np, int np_max) {
+    const int planes = 256 / np_max;
+    uint32_t ext = 0;
+    for (int i = 0; i < nd; ++i)
+        for (int j0 = 0; j0 < nd - i; j0 += planes) {
+            const int j1 = std::min(nd - i, j0 + planes);
+            ext = std::max(ext, (uint32_t)((i + j0) * np + (((j1 - j0) * np + 15) & ~15)));
+        }
+    return ext;
+}
+
+// One launch over the tiles of one or several geometries (MULTI: each run of
+// tiles has its own shape and images; the kernel is instantiated for the
+// largest width NP, and a narrower geometry's MMAs take 256 / np planes).
+template <int NP, bool MULTI>
+static void launch_oz(bsg_ctx ctx, const std::vector<OzRun> &runs, const OzTile *tiles, size_t n_tiles,
+                      const OzStep *steps, double alpha, int *err, unsigned long long *prof, uint32_t chunk,
+                      cudaStream_t s) {
+    BSG_REQUIRE(!runs.empty() && runs.size() <= (size_t)kOzMaxGeo && (MULTI || runs.size() == 1), BSG_ERR_UNSUPPORTED,
+                "Ozaki launch: tile geometries");
     OzKParams P;
     P.chunk = chunk;
-    P.J = sh.J;
-    BSG_REQUIRE(sh.J >= 1 && sh.J * sh.nd <= 16 && NP % sh.J == 0 && (NP / sh.J) % 8 == 0, BSG_ERR_UNSUPPORTED,
-                "Ozaki tile: N-side sub-blocks");
-    P.mp = sh.mp;
-    P.kp = sh.kp;
-    P.R = sh.R;
-    P.nd = sh.nd;
-    P.F = sh.F;
-    P.pair = sh.pair;
-    BSG_REQUIRE(!sh.pair || (sh.F % 2 == 0 && sh.kp % 16 == 8), BSG_ERR_UNSUPPORTED, "Ozaki tile: step pairs");
+    P.n_geo = (int)runs.size();
     P.alpha = alpha;
     P.prof = prof;
     P.zero = static_cast<const bf16 *>(oz_zero_image());
-    const uint32_t stage_bytes = oz_stage_bytes(sh);
-    P.S = (int)std::min<uint32_t>(sh.S > 0 ? (uint32_t)sh.S : 4u, kOzSmemBudget / stage_bytes);
-    BSG_REQUIRE(P.S >= 2, BSG_ERR_UNSUPPORTED, "Ozaki tile does not fit shared memory");
-    uint32_t cols = 32;  // regions plus the <= 8 overrun columns of a rounded-up N
-    while (cols < (uint32_t)sh.nd * NP + 8u) cols <<= 1;
-    P.tmem_cols = cols;
-    P.nbuf = cols <= 256 ? 2 : 1;
-    P.tx_bytes = (uint32_t)sh.R * sh.nd * sh.mp * sh.kp * 2u + (uint32_t)sh.nd * NP * sh.kp * 2u;
-    BSG_REQUIRE(cols <= 512, BSG_ERR_UNSUPPORTED, "Ozaki form: digits x padded block columns exceed TMEM");
-    const size_t smem = (size_t)P.S * stage_bytes + 32 * sizeof(OzStep) + (2 * P.S + 4) * 8 + 16;
+    uint32_t ring = 0, cols = 0;
+    int S = 0;
+    constexpr int kMaxPlan = oz_plan_entries(oz_max_digits(NP), 256 / NP);
+    for (size_t i = 0; i < runs.size(); ++i) {
+        const OzShape &sh = runs[i].sh;
+        const int np = MULTI ? sh.np : NP;
+        BSG_REQUIRE(np == sh.np && np <= NP, BSG_ERR_UNSUPPORTED, "Ozaki launch: tile width");
+        BSG_REQUIRE(sh.J >= 1 && sh.J * sh.nd <= 16 && np % sh.J == 0 && (np / sh.J) % 8 == 0, BSG_ERR_UNSUPPORTED,
+                    "Ozaki tile: N-side sub-blocks");
+        BSG_REQUIRE(!sh.pair || (sh.F % 2 == 0 && sh.kp % 16 == 8), BSG_ERR_UNSUPPORTED, "Ozaki tile: step pairs");
+        BSG_REQUIRE(oz_plan_entries(sh.nd, 256 / np) <= kMaxPlan, BSG_ERR_UNSUPPORTED, "Ozaki tile: MMA plan");
+        BSG_REQUIRE(i == 0 || runs[i].tile_end >= runs[i - 1].tile_end, BSG_ERR_ARG, "Ozaki launch: tile runs");
+        OzGeo &g = P.geo[i];
+        g.mp = sh.mp;
+        g.kp = sh.kp;
+        g.np = np;
+        g.R = sh.R;
+        g.nd = sh.nd;
+        g.F = sh.F;
+        g.pair = sh.pair;
+        g.J = sh.J;
+        g.tx_bytes = (uint32_t)sh.R * sh.nd * sh.mp * sh.kp * 2u + (uint32_t)sh.nd * np * sh.kp * 2u;
+        g.tile_end = (uint32_t)runs[i].tile_end;
+        g.a_img = runs[i].a_img;
+        g.b_img = runs[i].b_img;
+        {  // every byte an MMA reads lies inside the stage: A0/A1 128 rows each, B0/B1
+            const uint32_t a_stage = (uint32_t)sh.nd * 128u * sh.kp * 2u, b_st = oz_b_rows(sh.nd, np) * sh.kp * 2u;
+            const uint32_t a_pack = sh.pair ? (uint32_t)sh.R * sh.nd * sh.mp * sh.kp * 2u : a_stage;
+            const uint32_t b_off = sh.pair ? 2u * a_pack : a_stage;
+            const uint32_t reach = std::max((sh.pair ? a_pack : 0u) + a_stage, b_off + (sh.pair ? 2u : 1u) * b_st);
+            BSG_REQUIRE(reach <= oz_stage_bytes(sh), BSG_ERR_UNSUPPORTED, "Ozaki tile: stage layout");
+        }
+        g.stage_bytes = oz_stage_bytes(sh);
+        g.S = (int)std::min<uint32_t>(sh.S > 0 ? (uint32_t)sh.S : 4u, kOzSmemStages / g.stage_bytes);
+        BSG_REQUIRE(g.S >= 2, BSG_ERR_UNSUPPORTED, "Ozaki tile does not fit shared memory");
+        ring = std::max(ring, (uint32_t)g.S * g.stage_bytes);
+        S = std::max(S, g.S);
+        // the columns the MMAs write; the epilogue reads NP / G columns past
+        // each region's start
+        cols = std::max(cols, oz_tmem_extent(sh.nd, np, np));
+        if (MULTI) cols = std::max(cols, (uint32_t)((sh.nd - 1) * np + NP));
+    }
+    BSG_REQUIRE(runs.back().tile_end == n_tiles, BSG_ERR_ARG, "Ozaki launch: tile runs");
+    P.ring_bytes = ring;
+    P.S = S;
+    uint32_t tcols = 32;
+    while (tcols < cols) tcols <<= 1;
+    P.tmem_cols = tcols;
+    P.nbuf = tcols <= 256 ? 2 : 1;
+    BSG_REQUIRE(tcols <= 512, BSG_ERR_UNSUPPORTED, "Ozaki form: digits x padded block columns exceed TMEM");
+    const size_t smem = (size_t)ring + 32 * sizeof(OzStep) + (2 * P.S + 4) * 8 + 16 +
+                        (MULTI ? kOzMaxGeo * sizeof(OzGeo) : 0);
     {  // raise the shared-memory limit only when needed (never inside a graph capture)
         static std::atomic<int> set_to[64];
         int dev = 0;
         BSG_CUDA(cudaGetDevice(&dev));
         if (dev < 0 || dev >= 64 || (int)smem > set_to[dev].load()) {
-            BSG_CUDA(cudaFuncSetAttribute(k_ozgemm<NP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            BSG_CUDA(cudaFuncSetAttribute(k_ozgemm<NP, MULTI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
             if (dev >= 0 && dev < 64) set_to[dev].store((int)smem);
         }
     }
     const unsigned grid = (unsigned)std::min<size_t>(ceil_div(n_tiles, (size_t)chunk), (size_t)ctx->sm_count);
     BSG_REQUIRE(n_tiles + (size_t)grid * chunk < 0xffffffffull, BSG_ERR_UNSUPPORTED, "too many Ozaki tiles");
-    k_ozgemm<NP><<<grid, OzEpi<NP>::threads, smem, s>>>(tiles, (uint32_t)n_tiles, steps, a_img, b_img, P, err);
+    k_ozgemm<NP, MULTI><<<grid, OzEpi<NP>::threads, smem, s>>>(tiles, (uint32_t)n_tiles, steps, P, err);
     ctx->note_launch();
     ctx->check_launch("ozaki gemm");
 }
 
-void oz_run(bsg_ctx ctx, const OzShape &sh, const OzTile *d_tiles, size_t n_tiles, const OzStep *d_steps,
-            const bf16 *a_img, const bf16 *b_img, double alpha, cudaStream_t s, const unsigned long long *d_macs,
-            uint32_t chunk) {
-    if (!n_tiles) return;
+// one launch of the given runs; in timing mode with CUDA events around it,
+// the kernel's stall counters and the useful multiply-adds (d_macs) read back
+static void oz_launch_timed(bsg_ctx ctx, const std::vector<OzRun> &runs, const OzTile *d_tiles, size_t n_tiles,
+                            const OzStep *d_steps, double alpha, cudaStream_t s, const unsigned long long *d_macs,
+                            uint32_t chunk) {
     BSG_REQUIRE(chunk >= 1, BSG_ERR_ARG, "tile chunk");
-    BSG_REQUIRE(sh.nd >= 2 && sh.nd <= kOzMaxDigits && sh.nd * sh.np + 8 <= 512, BSG_ERR_UNSUPPORTED,
-                "Ozaki form: 2..8 digits, digits x padded block columns < 512");
+    for (const OzRun &r : runs)
+        BSG_REQUIRE(r.sh.nd >= 2 && r.sh.nd <= kOzMaxDigits && r.sh.nd * r.sh.np + 8 <= 512, BSG_ERR_UNSUPPORTED,
+                    "Ozaki form: 2..8 digits, digits x padded block columns < 512");
     int *err = ctx->gemm_err_flag();
-    if (!ctx->timing) {
-        // no synchronization: the flag is read once at the end of the public call
-        switch (sh.np) {
-            case 8: launch_oz<8>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, nullptr, chunk, s); break;
-            case 16: launch_oz<16>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, nullptr, chunk, s); break;
-            case 24: launch_oz<24>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, nullptr, chunk, s); break;
-            case 32: launch_oz<32>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, nullptr, chunk, s); break;
-            case 40: launch_oz<40>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, nullptr, chunk, s); break;
-            case 48: launch_oz<48>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, nullptr, chunk, s); break;
-            case 56: launch_oz<56>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, nullptr, chunk, s); break;
-            case 64: launch_oz<64>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, nullptr, chunk, s); break;
+    auto launch = [&](unsigned long long *prof) {
+        if (runs.size() > 1) {
+            // every width up to 64 runs in the widest instantiation
+            launch_oz<64, true>(ctx, runs, d_tiles, n_tiles, d_steps, alpha, err, prof, chunk, s);
+            return;
+        }
+        switch (runs[0].sh.np) {
+            case 8: launch_oz<8, false>(ctx, runs, d_tiles, n_tiles, d_steps, alpha, err, prof, chunk, s); break;
+            case 16: launch_oz<16, false>(ctx, runs, d_tiles, n_tiles, d_steps, alpha, err, prof, chunk, s); break;
+            case 24: launch_oz<24, false>(ctx, runs, d_tiles, n_tiles, d_steps, alpha, err, prof, chunk, s); break;
+            case 32: launch_oz<32, false>(ctx, runs, d_tiles, n_tiles, d_steps, alpha, err, prof, chunk, s); break;
+            case 40: launch_oz<40, false>(ctx, runs, d_tiles, n_tiles, d_steps, alpha, err, prof, chunk, s); break;
+            case 48: launch_oz<48, false>(ctx, runs, d_tiles, n_tiles, d_steps, alpha, err, prof, chunk, s); break;
+            case 56: launch_oz<56, false>(ctx, runs, d_tiles, n_tiles, d_steps, alpha, err, prof, chunk, s); break;
+            case 64: launch_oz<64, false>(ctx, runs, d_tiles, n_tiles, d_steps, alpha, err, prof, chunk, s); break;
             default: throw Error{BSG_ERR_UNSUPPORTED, "Ozaki form supports block sizes up to 64"};
         }
+    };
+    if (!ctx->timing) {
+        // no synchronization: the flag is read once at the end of the public call
+        launch(nullptr);
         return;
     }
-    // timing mode: CUDA events around the launch, stall counters, read back at once
     DevBuf profbuf(8 * kOzProf, s);
     BSG_CUDA(cudaMemsetAsync(profbuf.p, 0, 8 * kOzProf, s));
     auto *prof = profbuf.as<unsigned long long>();
@@ -829,17 +1034,7 @@ void oz_run(bsg_ctx ctx, const OzShape &sh, const OzTile *d_tiles, size_t n_tile
     BSG_CUDA(cudaEventCreate(&e0));
     BSG_CUDA(cudaEventCreate(&e1));
     BSG_CUDA(cudaEventRecord(e0, s));
-    switch (sh.np) {
-        case 8: launch_oz<8>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, prof, chunk, s); break;
-        case 16: launch_oz<16>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, prof, chunk, s); break;
-        case 24: launch_oz<24>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, prof, chunk, s); break;
-        case 32: launch_oz<32>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, prof, chunk, s); break;
-        case 40: launch_oz<40>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, prof, chunk, s); break;
-        case 48: launch_oz<48>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, prof, chunk, s); break;
-        case 56: launch_oz<56>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, prof, chunk, s); break;
-        case 64: launch_oz<64>(ctx, sh, d_tiles, n_tiles, d_steps, a_img, b_img, alpha, err, prof, chunk, s); break;
-        default: throw Error{BSG_ERR_UNSUPPORTED, "Ozaki form supports block sizes up to 64"};
-    }
+    launch(prof);
     BSG_CUDA(cudaEventRecord(e1, s));
     unsigned long long macs = 0, st[kOzProf] = {};
     if (d_macs) BSG_CUDA(cudaMemcpyAsync(&macs, d_macs, 8, cudaMemcpyDeviceToHost, s));
@@ -854,6 +1049,22 @@ void oz_run(bsg_ctx ctx, const OzShape &sh, const OzTile *d_tiles, size_t n_tile
     ctx->oz_useful_macs += (double)macs;
     for (int i = 0; i < kOzProf; ++i) ctx->oz_stall[i] += st[i];
     ctx->gemm_check();
+}
+
+void oz_run(bsg_ctx ctx, const OzShape &sh, const OzTile *d_tiles, size_t n_tiles, const OzStep *d_steps,
+            const bf16 *a_img, const bf16 *b_img, double alpha, cudaStream_t s, const unsigned long long *d_macs,
+            uint32_t chunk) {
+    if (!n_tiles) return;
+    oz_launch_timed(ctx, {OzRun{sh, a_img, b_img, n_tiles}}, d_tiles, n_tiles, d_steps, alpha, s, d_macs, chunk);
+}
+
+void oz_run_groups(bsg_ctx ctx, const std::vector<OzRun> &runs, const OzTile *d_tiles, size_t n_tiles,
+                   const OzStep *d_steps, double alpha, cudaStream_t s, const unsigned long long *d_macs) {
+    if (!n_tiles) return;
+    std::vector<OzRun> live;  // runs with tiles (an empty run would only cost a table entry)
+    for (const OzRun &r : runs)
+        if (r.tile_end > (live.empty() ? 0 : live.back().tile_end)) live.push_back(r);
+    oz_launch_timed(ctx, live, d_tiles, n_tiles, d_steps, alpha, s, d_macs, 1);
 }
 
 // ---------------------------------------------------------------------------

@@ -83,6 +83,21 @@ void oz_run(bsg_ctx ctx, const OzShape &sh, const OzTile *d_tiles, size_t n_tile
             const __nv_bfloat16 *a_img, const __nv_bfloat16 *b_img, double alpha, cudaStream_t s,
             const unsigned long long *d_macs = nullptr, uint32_t chunk = 1);
 
+// A run of tiles of one geometry inside a larger tile list: tiles below
+// tile_end (and at or above the previous run's tile_end) have shape sh and
+// take their operands from a_img / b_img.
+struct OzRun {
+    OzShape sh;
+    const __nv_bfloat16 *a_img, *b_img;
+    size_t tile_end;
+};
+// One persistent launch over the tiles of several geometries (at most 8
+// runs, block widths up to 64): the tiles of a batch of products of
+// different block sizes, in run order.  Step indices are absolute; each
+// step's image indices refer to its run's images.
+void oz_run_groups(bsg_ctx ctx, const std::vector<OzRun> &runs, const OzTile *d_tiles, size_t n_tiles,
+                   const OzStep *d_steps, double alpha, cudaStream_t s, const unsigned long long *d_macs = nullptr);
+
 // ---- building blocks of a mixed-form screened product ----
 // row exponents of op(A), column exponents of op(B) and their digit images
 // (one image per stored block, at the block's table index)

@@ -1,5 +1,6 @@
-"""Batched screened products (one persistent tensor-core launch per block-size
-group, autotuned, CUDA-graph plans) against the per-product FP64 matmult."""
+"""Batched screened products (one persistent tensor-core launch over every
+block-size group, per-group autotuning, CUDA-graph plans) against the
+per-product FP64 matmult."""
 import numpy as np
 import pytest
 
@@ -45,6 +46,36 @@ def test_batched_mixed_matches_fp64(api, ctx):
     assert len(tuned) >= 1  # one entry per block-size group shape
     for (mp, kp, np_, nd), (R, S_) in tuned.items():
         assert 1 <= R <= 128 // mp and S_ in (0, 2)
+
+
+def test_batched_one_launch_over_block_sizes(api, ctx):
+    """A batch of four block sizes runs as ONE persistent tensor-core launch,
+    each tile in its group's geometry (once the autotuner has cached its
+    choices: its trial launches run group by group), and every product stays
+    within the form's bound of the per-product FP64 matmult with its mask."""
+    batch = _batch(api, ctx, 11, 12)
+    assert len({b[0] for b in batch}) >= 3
+    As = [b[3] for b in batch]
+    Bs = [b[4] for b in batch]
+    C64, Cmx = _outs(api, ctx, batch), _outs(api, ctx, batch)
+    thr = 1e-9
+    n64 = sum(api.matmult(c, a, 0, b, 0, thr, 1.0, 0.0) for c, a, b in zip(C64, As, Bs))
+    api.matmult_batched(Cmx, As, Bs, thr, 1.0, 0.0, form=api.FORM_OZAKI)  # tunes the group shapes
+    for c in Cmx:
+        c.scale(0.0)
+    ctx.set_timing(True)
+    try:
+        nmx = api.matmult_batched(Cmx, As, Bs, thr, 1.0, 0.0, form=api.FORM_OZAKI)
+        launches = ctx.gemm_timing()[0]
+    finally:
+        ctx.set_timing(False)
+    assert launches == 1
+    assert n64 == nmx
+    for (bs, *_), c64, cmx in zip(batch, C64, Cmx):
+        assert np.array_equal(c64.mask(), cmx.mask())
+        r64, rmx = c64.to_matrix(), cmx.to_matrix()
+        err = np.linalg.norm(rmx - r64) / max(np.linalg.norm(r64), 1e-300)
+        assert err < (1e-7 if bs == 64 else 1e-9), (bs, err)
 
 
 def test_batched_fp64_is_bit_exact(api, ctx):
