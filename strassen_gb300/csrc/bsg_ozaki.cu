@@ -570,7 +570,7 @@ __global__ void __launch_bounds__(OzEpi<NP>::threads) __maxnreg__(OzEpi<NP>::max
                         ++n_plan;
                     }
             };
-            setup(P.geo[0], L0);
+            setup(P.geo[0], MULTI ? oz_lay(P.geo[0], P.geo[0].np) : L0);  // L0 is laid out for width NP
             int cur_geo = 0;
             uint32_t n_stages = (uint32_t)P.geo[0].S, sbytes16 = P.geo[0].stage_bytes >> 4;
             bool ok = true;

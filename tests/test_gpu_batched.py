@@ -9,11 +9,12 @@ from strassen_gb300 import synth as S
 pytestmark = pytest.mark.gpu
 
 
-def _batch(api, ctx, seed, n, sizes=(96, 128, 192, 256, 320), bss=(16, 32, 48, 64)):
+def _batch(api, ctx, seed, n, sizes=(96, 128, 192, 256, 320), bss=(16, 32, 48, 64), cycle=False):
+    """n seeded products; block sizes drawn from bss (cycle: bss in turn)"""
     rng = np.random.default_rng(seed)
     out = []
     for i in range(n):
-        bs = int(rng.choice(bss))
+        bs = int(bss[i % len(bss)]) if cycle else int(rng.choice(bss))
         m, k, nn = (int(rng.choice(sizes)) // bs * bs or bs for _ in range(3))
         dens = float(rng.uniform(0.05, 0.6))
         a = S.block_mask_matrix(seed * 100 + i, 1, m, k, bs, dens)
@@ -76,6 +77,37 @@ def test_batched_one_launch_over_block_sizes(api, ctx):
         r64, rmx = c64.to_matrix(), cmx.to_matrix()
         err = np.linalg.norm(rmx - r64) / max(np.linalg.norm(r64), 1e-300)
         assert err < (1e-7 if bs == 64 else 1e-9), (bs, err)
+
+
+@pytest.mark.parametrize("bss", [(8, 24, 40, 56), (8, 12, 16, 20, 24, 28, 32, 40, 48)])
+def test_batched_geometries_in_one_launch(api, ctx, bss):
+    """Geometries that differ in more than the tile width share a launch:
+    step pairs (block sizes 8, 24 and 40: k = 8 mod 16), 8-row blocks whose
+    slots hold only 64 of the MMA's 128 rows, 56-wide blocks at 4 digits next
+    to 5-digit ones; more than eight block-size groups take one launch per
+    eight groups.  Every product keeps the FP64 form's mask and bound."""
+    batch = _batch(api, ctx, 13, 3 * len(bss), sizes=(96, 160, 224), bss=bss, cycle=True)
+    As = [b[3] for b in batch]
+    Bs = [b[4] for b in batch]
+    C64, Cmx = _outs(api, ctx, batch), _outs(api, ctx, batch)
+    thr = 1e-9
+    n64 = sum(api.matmult(c, a, 0, b, 0, thr, 1.0, 0.0) for c, a, b in zip(C64, As, Bs))
+    api.matmult_batched(Cmx, As, Bs, thr, 1.0, 0.0, form=api.FORM_OZAKI)  # tunes the group shapes
+    groups = len({b[0] for b in batch})
+    assert groups == len(bss)
+    ctx.set_timing(True)
+    try:
+        nmx = api.matmult_batched(Cmx, As, Bs, thr, 1.0, 0.0, form=api.FORM_OZAKI)
+        launches = ctx.gemm_timing()[0]
+    finally:
+        ctx.set_timing(False)
+    assert launches == -(-groups // 8)
+    assert n64 == nmx
+    for (bs, *_), c64, cmx in zip(batch, C64, Cmx):
+        assert np.array_equal(c64.mask(), cmx.mask())
+        r64, rmx = c64.to_matrix(), cmx.to_matrix()
+        err = np.linalg.norm(rmx - r64) / max(np.linalg.norm(r64), 1e-300)
+        assert err < (1e-7 if bs >= 56 else 1e-9), (bs, err)
 
 
 def test_batched_fp64_is_bit_exact(api, ctx):
