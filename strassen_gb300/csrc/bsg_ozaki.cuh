@@ -18,6 +18,7 @@
 #pragma once
 #include <cuda_bf16.h>
 
+#include "bsg_digits.h"
 #include "bsg_gemm64.cuh"
 
 namespace bsg {
@@ -167,22 +168,9 @@ __device__ __forceinline__ size_t oz_plane_stride(bool m_side, int mpad, int kp)
 }
 
 // Fixed-point value of v with row/column exponent e, integer arithmetic only:
-// N = round(v 2^(K - e)) with ties to even (|N| <= 2^K).  With q = M >> s
-// the rounded quotient is (M + 2^(s-1) - 1 + (q & 1)) >> s, one add chain
-// instead of compares; s is capped at 63 (any s >= 54 rounds to 0 either way).
+// N = round(v 2^(K - e)) with ties to even (|N| <= 2^K); see bsg_digits.h.
 __device__ __forceinline__ long long oz_fixed(double v, int e, int K) {
-    const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
-    const int E = (int)((bits >> 52) & 0x7FF);
-    const unsigned long long M = (bits & 0xFFFFFFFFFFFFFull) | (E ? (1ull << 52) : 0ull);
-    const int sh = (E ? E : 1) - 1075 + K - e;  // N = M * 2^sh
-    unsigned long long N;
-    if (sh >= 0) {
-        N = M << sh;
-    } else {
-        const int s = -sh < 63 ? -sh : 63;
-        N = (M + ((1ull << (s - 1)) - 1ull) + ((M >> s) & 1ull)) >> s;
-    }
-    return (bits >> 63) ? -(long long)N : (long long)N;
+    return oz_fixed_bits((unsigned long long)__double_as_longlong(v), e, K);
 }
 
 // Split into nd balanced base-256 digits: N = d_0 256^(nd-1) + ... + d_{nd-1}
