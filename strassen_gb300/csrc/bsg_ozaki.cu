@@ -198,17 +198,10 @@ struct OzEpi {
     static constexpr int max_regs = (16384 / (32 * ((warps + 3) / 4))) / 8 * 8;
 };
 
-// Conversions for the epilogue with integer operations instead of the FP64
-// pipe (GB300 runs FP64 at a small fraction of its integer rate).
-// x exactly as a double, for |x| < 2^53
-__device__ __forceinline__ double oz_i64_to_f64(long long x) {
-    if (x == 0) return 0.0;
-    const unsigned long long sgn = x < 0 ? (1ull << 63) : 0ull;
-    const unsigned long long a = x < 0 ? 0ull - (unsigned long long)x : (unsigned long long)x;
-    const int msb = 63 - __clzll((long long)a);
-    const unsigned long long m = (a << (52 - msb)) & 0xFFFFFFFFFFFFFull;
-    return __longlong_as_double((long long)(sgn | ((unsigned long long)(msb + 1023) << 52) | m));
-}
+// Helpers of the epilogue's conversions.  FP64 arithmetic stays off its
+// common path (GB300 runs FP64 at a small fraction of its integer rate); the
+// float -> int64 and int64 -> double conversions are the hardware ones, one
+// instruction each, where integer restatements are long dependent chains.
 // v 2^e outside the fast paths (zero, subnormal or out-of-range results): an
 // ordinary multiplication by the power of two, as volatile inline PTX so that
 // the compiler branches around it instead of if-converting it (a warp's FP64
@@ -219,44 +212,6 @@ __device__ __forceinline__ double oz_scale_pow2_slow(double v, int e) {
     double r;
     asm volatile("mul.rn.f64 %0, %1, %2;" : "=d"(r) : "d"(v), "d"(sc));
     return r;
-}
-// round(x) 2^e (x an int64, rounded to nearest even) with integer operations:
-// the power of two goes straight into the exponent field when the result is
-// a normal number
-__device__ __forceinline__ double oz_i64_to_f64_rn_pow2(long long x, int e) {
-    if (x == 0) return 0.0;
-    const unsigned long long sgn = x < 0 ? (1ull << 63) : 0ull;
-    const unsigned long long a = x < 0 ? 0ull - (unsigned long long)x : (unsigned long long)x;
-    int msb = 63 - __clzll((long long)a);
-    unsigned long long m;
-    if (msb <= 52) {
-        m = a << (52 - msb);
-    } else {
-        const int sh = msb - 52;
-        const unsigned long long rem = a & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
-        m = a >> sh;
-        if (rem > half || (rem == half && (m & 1ull))) ++m;
-        if (m >> 53) {  // rounded up to the next power of two
-            m >>= 1;
-            ++msb;
-        }
-    }
-    const int field = msb + 1023 + e;
-    if (field > 0 && field < 0x7FF)
-        return __longlong_as_double((long long)(sgn | ((unsigned long long)field << 52) | (m & 0xFFFFFFFFFFFFFull)));
-    return oz_scale_pow2_slow(
-        __longlong_as_double((long long)(sgn | ((unsigned long long)(msb + 1023) << 52) | (m & 0xFFFFFFFFFFFFFull))), e);
-}
-// an integer-valued FP32 value (|f| < 2^62) as an int64, exactly, with
-// integer operations (the hardware conversion to 64 bits runs on the FP64 pipe)
-__device__ __forceinline__ long long oz_f32_int_to_i64(float f) {
-    const uint32_t u = __float_as_uint(f);
-    const int ex = (int)((u >> 23) & 0xFFu);
-    const long long mant = (long long)((u & 0x7FFFFFu) | 0x800000u);
-    const int sh = ex - 150;
-    long long v = sh >= 0 ? mant << sh : mant >> min(-sh, 63);
-    v = ex < 127 ? 0 : v;  // |f| < 1: zero, the only integer there
-    return (u >> 31) ? -v : v;
 }
 // an FP32 value as a double (exact; zero and subnormal inputs take the
 // hardware conversion)
@@ -867,18 +822,22 @@ __global__ void __launch_bounds__(OzEpi<NP>::threads) __maxnreg__(OzEpi<NP>::max
                     // up to 5 digits lo holds weights 3 and 4, multiples of 2^-32,
                     // so lo 2^32 is an integer (below 2^34) and hi 2^16 + lo 2^32
                     // the exact sum in units of 2^-32 (hi < 2^39 per chain of <= 512
-                    // k, so below 2^63 for < 256 chains): one rounding to double, the
-                    // same as the FP64 add below makes, without the FP64 pipe, with
-                    // the power of two put into the rounded value's exponent
+                    // k, so below 2^63 for < 256 chains): one rounding to double (the
+                    // hardware int64 conversion, round to nearest even: the same as the
+                    // FP64 add below makes), then the power of two put into the
+                    // exponent field.  The conversion is one instruction per element;
+                    // the same rounding done with integer operations is a long
+                    // dependent chain that kept the epilogue waiting (occ products
+                    // 18.9 -> 18.2 ms with the conversion)
                     store_scaled([&](int j, int e) {
-                        return oz_i64_to_f64_rn_pow2(hi[j] * 65536ll + oz_f32_int_to_i64(lo[j] * 4294967296.f), e);
+                        return oz_scale_pow2(__ll2double_rn(hi[j] * 65536ll + __float2ll_rn(lo[j] * 4294967296.f)), e);
                     }, -16);
                 } else {
-                    // both terms are exact doubles built with integer operations
-                    // (|hi| < 2^53, lo 2^16 an FP32 value): one FP64 add rounds,
-                    // and the power of two goes into the exponent field
+                    // both terms are exact doubles (|hi| < 2^53, lo 2^16 an FP32
+                    // value): one FP64 add rounds, and the power of two goes into the
+                    // exponent field
                     store_scaled([&](int j, int e) {
-                        return oz_scale_pow2(__dadd_rn(oz_i64_to_f64(hi[j]), oz_f32_to_f64(lo[j] * 65536.f)), e);
+                        return oz_scale_pow2(__dadd_rn(__ll2double_rn(hi[j]), oz_f32_to_f64(lo[j] * 65536.f)), e);
                     }, 0);
                 }
                 if (fresh && r == 0 && grp == 0 && T.cnorm[s]) *T.cnorm[s] = 0.0;
