@@ -98,14 +98,32 @@ struct Dense3c {
 // always all live; with block rows as slots a step would carry the
 // insignificant X blocks of its other rows as zero images.
 
+// The screen ||X_ib,kb|| ||V_kb,jb|| >= tpb keeps no product of block
+// (ib, kb) of X in any tile when it fails for the largest ||V_kb,jb|| of the
+// k step (a correctly rounded product is monotone in each factor), so the
+// test against vmax[kb] decides it for every slot at once.
+__device__ __forceinline__ bool x_block_dead(double xn, double vmax, double tpb) { return !(__dmul_rn(xn, vmax) >= tpb); }
+
+// vmax[kb] = max over jb of ||V_kb,jb|| (vn column-major, nkb rows)
+__global__ void k_vn_rowmax(const double *__restrict__ vn, size_t nkb, size_t njb, double *__restrict__ vmax) {
+    const size_t kb = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (kb >= nkb) return;
+    double m = 0.0;
+    for (size_t jb = 0; jb < njb; ++jb) m = fmax(m, vn[kb + jb * nkb]);
+    vmax[kb] = m;
+}
+
 // N-side images of X: J consecutive block rows stacked along N, one image
 // per (group ibp, kb), index ibp*nkb + kb (a group's k steps back to back, so
 // that the two steps of a stage pair are one copy); block ib = J*ibp + j
 // fills rows j*bs.. of its group's image (rows of missing blocks are never
-// read).
+// read).  A block that the screen drops in every tile gets an all-zero
+// image: a step may then copy its group's whole image (one copy) and the
+// MMA adds exact zeros for it.
 // kImgXBlocks consecutive blocks x = ib + kb*nib per warp.
 constexpr int kImgXBlocks = 4;
-__global__ void k_img_X(const double *__restrict__ X, const int *__restrict__ rexp, Dense3c D, bf16 *__restrict__ img) {
+__global__ void k_img_X(const double *__restrict__ X, const int *__restrict__ rexp, const double *__restrict__ xn,
+                        const double *__restrict__ vmax, double tpb, Dense3c D, bf16 *__restrict__ img) {
     __shared__ OzImgJob sj[kOzImgWarps][kImgXBlocks];
     const size_t x0 = oz_warp_id() * kImgXBlocks, n = D.nib * D.nkb;
     if (x0 >= n) return;
@@ -116,7 +134,7 @@ __global__ void k_img_X(const double *__restrict__ X, const int *__restrict__ re
             if (x >= n) return false;
             const size_t ib = x % D.nib, kb = x / D.nib, ibp = ib / D.J, j = ib % D.J;
             J.get = OzDenseGet{X + ib * D.bs + kb * D.bs * D.ldx, D.ldx, false};
-            J.rows = ext3(ib, D.bs, D.n_vec2);
+            J.rows = x_block_dead(xn[x], vmax[kb], tpb) ? 0 : ext3(ib, D.bs, D.n_vec2);  // 0 rows: zeros
             J.k = ext3(kb, D.bs, D.n_aux);
             J.exps = rexp + ib * D.bs;
             J.dst = img + (ibp * D.nkb + kb) * D.nd * (size_t)D.np * D.kp + j * D.bs * (size_t)D.kp;
@@ -148,7 +166,8 @@ __global__ void k_img_V(const double *__restrict__ V, const int *__restrict__ ce
 // ||X_ib,kb|| ||V_kb,jb|| >= tpb, so for fixed kb the slot sets of the
 // sub-blocks are nested and split into at most J exact rectangles.
 __global__ void k_tiles_3c(size_t n_tiles, size_t n_jg, size_t Gj, const double *__restrict__ xn,
-                           const double *__restrict__ vn, const int *__restrict__ rexp, const int *__restrict__ cexp,
+                           const double *__restrict__ vn, const double *__restrict__ vmax,
+                           const int *__restrict__ rexp, const int *__restrict__ cexp,
                            double *__restrict__ out, Dense3c D, double tpb, OzTile *__restrict__ tiles,
                            OzStep *__restrict__ steps, unsigned long long *__restrict__ nsig,
                            unsigned long long *__restrict__ macs) {
@@ -192,9 +211,12 @@ __global__ void k_tiles_3c(size_t n_tiles, size_t n_jg, size_t Gj, const double 
         OzStep mine[2];
         uint32_t c = 0;
         if (kb < D.nkb) {
-            uint32_t live[2] = {0, 0};
+            uint32_t live[2] = {0, 0}, phantom = 0;
             for (int j = 0; j < nsub; ++j) {
                 const double x = xn[ibp * D.J + j + kb * D.nib];
+                // a block dropped in every tile has a zero image: its
+                // sub-block may ride along in a whole-image copy
+                if (x_block_dead(x, vmax[kb], tpb)) phantom |= 1u << j;
                 for (int s = 0; s < D.R; ++s) {
                     const size_t jb = jg * D.R + s;
                     if (jb >= D.njb) break;
@@ -208,7 +230,7 @@ __global__ void k_tiles_3c(size_t n_tiles, size_t n_jg, size_t Gj, const double 
             uint32_t a_idx[kOzMaxSlots];
             for (int s = 0; s < kOzMaxSlots; ++s) a_idx[s] = (uint32_t)((jg * D.nkb + kb) * D.R + s);
             // exact rectangles (the slot sets of a norm-product screen are nested)
-            c = emit_rect_steps(live, D.J, 0u, (uint32_t)(ibp * D.nkb + kb), a_idx, mine);
+            c = emit_rect_steps(live, D.J, phantom, (uint32_t)(ibp * D.nkb + kb), a_idx, mine);
         }
         warp_append_steps(mine, c, steps + T.s0, n);
     }
@@ -227,7 +249,7 @@ namespace {
 // V-side operands (block norms, column exponents, M-side digit images of
 // V^T), shared by every row range of X
 struct Oz3cV {
-    DevBuf vn, cexp, ai;
+    DevBuf vn, vmax, cexp, ai;
 };
 
 Dense3c oz3c_dims(size_t n_aux, size_t bs, int nd, OzShape &sh) {
@@ -272,9 +294,12 @@ void oz3c_prepare_v(bsg_ctx ctx, const double *V, const Dense3c &D, Oz3cV &v) {
     const int wpb = 8;
     k_dense_norms<<<(unsigned)ceil_div(D.nkb * D.njb, wpb), wpb * 32, 0, s>>>(V, n_aux, n_aux, n_aux, D.bs, D.nkb,
                                                                               D.nkb * D.njb, v.vn.as<double>());
+    v.vmax = DevBuf(D.nkb * 8, s);
+    k_vn_rowmax<<<(unsigned)ceil_div(D.nkb, (size_t)128), 128, 0, s>>>(v.vn.as<double>(), D.nkb, D.njb,
+                                                                      v.vmax.as<double>());
     k_colexp_dense<<<(unsigned)n_aux, 256, 0, s>>>(V, n_aux, v.cexp.as<int>());
     k_img_V<<<oz_img_grid(D.nkb * D.njb), 32 * kOzImgWarps, 0, s>>>(V, v.cexp.as<int>(), D, v.ai.as<bf16>());
-    ctx->note_launch(3);
+    ctx->note_launch(4);
     ctx->check_launch("3c2c ozaki V prep");
 }
 
@@ -297,19 +322,20 @@ void oz3c_rows(bsg_ctx ctx, Dense3c D, const OzShape &sh, const Oz3cV &v, const 
         X, ldx, rows, n_aux, bs, D.nib, D.nib * D.nkb, xn.as<double>(), rbits.as<unsigned long long>());
     k_bits_to_exp<<<(unsigned)ceil_div(rows, (size_t)256), 256, 0, s>>>(rbits.as<unsigned long long>(), rows,
                                                                         rexp.as<int>());
-    k_img_X<<<oz_img_grid(ceil_div(D.nib * D.nkb, (size_t)kImgXBlocks)), 32 * kOzImgWarps, 0, s>>>(X, rexp.as<int>(), D,
-                                                                                              bi.as<bf16>());
+    const double tpb = thresh * (double)(bs * bs * bs);
+    k_img_X<<<oz_img_grid(ceil_div(D.nib * D.nkb, (size_t)kImgXBlocks)), 32 * kOzImgWarps, 0, s>>>(
+        X, rexp.as<int>(), xn.as<double>(), v.vmax.as<double>(), tpb, D, bi.as<bf16>());
     ctx->note_launch(3);
     ctx->check_launch("3c2c ozaki X prep");
     const size_t n_jg = ceil_div(D.njb, (size_t)D.R), n_tiles = D.nibp * n_jg;
     BSG_REQUIRE(n_tiles * D.nkb * D.J < 0xffffffffull, BSG_ERR_UNSUPPORTED, "too many Ozaki steps in one call");
     DevBuf dt(n_tiles * sizeof(OzTile), s), dst(n_tiles * D.nkb * D.J * sizeof(OzStep), s);
-    const double tpb = thresh * (double)(bs * bs * bs);
     // V^T images of one slot group: R * nkb images; keep about 48 MB of them in L2
     const size_t grp_bytes = (size_t)D.R * D.nkb * a_img * 2;
     const size_t Gj = std::max<size_t>(1, std::min<size_t>(n_jg, (48ull << 20) / std::max<size_t>(grp_bytes, 1)));
     k_tiles_3c<<<oz_img_grid(n_tiles), 32 * kOzImgWarps, 0, s>>>(n_tiles, n_jg, Gj, xn.as<double>(), v.vn.as<double>(),
-                                                                rexp.as<int>(), v.cexp.as<int>(), out, D, tpb,
+                                                                v.vmax.as<double>(), rexp.as<int>(),
+                                                                v.cexp.as<int>(), out, D, tpb,
                                                                 dt.as<OzTile>(), dst.as<OzStep>(), cnt, cnt + 1);
     ctx->note_launch();
     ctx->check_launch("3c2c ozaki tiles");

@@ -176,7 +176,8 @@ enum OzProf {
     kProfSteps,          // operand stages consumed by the MMA issuer
     kProfMmas,           // tcgen05.mma instructions issued
     kProfCopiedSteps,    // k steps copied by the producer (a pair stage holds two)
-    kProfLivePairs,      // (live slot, live N-side sub-block) pairs over those steps
+    kProfLivePairs,      // (live slot, copied N-side sub-block) pairs over those steps (a zero-image
+                         // sub-block that rides along in a whole-image copy counts)
     kProfPairCapacity,   // slots x sub-blocks over those steps
     kOzProf
 };
