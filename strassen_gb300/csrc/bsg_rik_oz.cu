@@ -187,6 +187,39 @@ __device__ __forceinline__ int rows_in_group(const OzDims &D) { return D.J == 1 
 
 
 
+// Sub-blocks that the screen drops in every tile.  A product's N-side
+// sub-block survives with slot s when nA_s nB >= tpb; a correctly rounded
+// product is monotone in each factor, so the test against the largest slot
+// norm any tile can hold decides it for every tile at once.  Such a
+// sub-block gets an all-zero image where the other sub-block of its image
+// does survive somewhere, so that the tile builders may count it as present
+// (one whole-image copy per step instead of one per digit plane and
+// sub-block) while the MMA adds exact zeros for it.
+__device__ __forceinline__ bool sub_dead(bool present, double nslot_max, double nb_, double tpb) {
+    return !present || !(__dmul_rn(nslot_max, nb_) >= tpb);
+}
+
+// cmax[x] = max over occupied block columns ib of ||C(x, ib)|| (cnorm: x + ib*nb)
+__global__ void k_cnorm_rowmax(const double *__restrict__ cnorm, size_t nb, size_t nob, double *__restrict__ cmax) {
+    const size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= nb) return;
+    double m = 0.0;
+    for (size_t ib = 0; ib < nob; ++ib) m = fmax(m, cnorm[x + ib * nb]);
+    cmax[x] = m;
+}
+
+// mmax[p*nob + ib] = max over basis blocks a of the present ||mui_p(a, ib)||
+__global__ void k_mnorm_max(const double *__restrict__ mnorm, const uint8_t *__restrict__ mflag, size_t np, size_t nb,
+                            size_t nob, double *__restrict__ mmax) {
+    const size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= np * nob) return;
+    const size_t p = x / nob, ib = x % nob, base = p * nb * nob + ib * nb;
+    double m = 0.0;
+    for (size_t a = 0; a < nb; ++a)
+        if (mflag[base + a]) m = fmax(m, mnorm[base + a]);
+    mmax[x] = m;
+}
+
 // U_p blocks (a, b) as the N side of mui^T = C^T U^T (image rows = the
 // block's rows mu, k = its columns), from the dense copies; kImgUBlocks
 // consecutive occupied blocks w per warp.  The blocks of Jm consecutive aux
@@ -194,7 +227,8 @@ __device__ __forceinline__ int rows_in_group(const OzDims &D) { return D.J == 1 
 // function j at rows j*bs.
 constexpr int kImgUBlocks = 4;
 __global__ void k_img_U(const double *__restrict__ ucomp, const uint32_t *__restrict__ ob_list, size_t n_ob,
-                        size_t n_p, const uint8_t *__restrict__ uflag, const int *__restrict__ rexp, OzDims D,
+                        size_t n_p, const uint8_t *__restrict__ uflag, const double *__restrict__ unorm,
+                        const double *__restrict__ cmax, double tpb, const int *__restrict__ rexp, OzDims D,
                         bf16 *__restrict__ img) {
     __shared__ OzImgJob sj[kOzImgWarps][kImgUBlocks];
     const size_t w0 = oz_warp_id() * kImgUBlocks, nw = n_p * n_ob;
@@ -205,11 +239,18 @@ __global__ void k_img_U(const double *__restrict__ ucomp, const uint32_t *__rest
             const size_t w = w0 + q;
             if (w >= nw) return false;
             const size_t p = w / n_ob, rr = ob_list[w % n_ob], a = rr % D.nb, b = rr / D.nb;
-            if (!uflag[p * D.nb * D.nb + rr]) return false;
             const size_t pp = p / D.Jm, j = p % D.Jm;
+            const size_t u = p * D.nb * D.nb + rr;
+            bool zero = false;
+            if (sub_dead(uflag[u], cmax[b], unorm[u], tpb)) {
+                // zeros where the pair's other aux function survives
+                const size_t q = pp * D.Jm + (1 - j), uq = q * D.nb * D.nb + rr;
+                if (D.Jm != 2 || q >= n_p || sub_dead(uflag[uq], cmax[b], unorm[uq], tpb)) return false;
+                zero = true;
+            }
             const int rows = ext_r(a, D.bs, D.n_bf);
             J.get = OzDenseGet{ucomp + w * D.bs * D.bs, (size_t)rows, false};
-            J.rows = rows;
+            J.rows = zero ? 0 : rows;  // 0 rows: all digits zero
             J.k = ext_r(b, D.bs, D.n_bf);
             J.exps = rexp + p * D.n_bf + a * D.bs;
             J.dst = img + (pp * D.nb * D.nb + rr) * D.nd * (size_t)D.npm * D.kp + j * D.bs * (size_t)D.kp;
@@ -238,6 +279,7 @@ __global__ void k_img_Ct_A(const double *__restrict__ C, const int *__restrict__
 // so the block is read from DRAM once and the second split hits L1.
 constexpr int kImgMBlocks = 2;
 __global__ void k_img_mui_all(const double *__restrict__ mui, const uint8_t *__restrict__ mflag,
+                              const double *__restrict__ mnorm, const double *__restrict__ cmax, double tpb,
                               const int *__restrict__ rexp, size_t Q, const int *__restrict__ cexp, OzDims D, size_t n,
                               bf16 *__restrict__ imgA, bf16 *__restrict__ imgB, bf16 *__restrict__ imgT) {
     __shared__ OzImgJob sj[kOzImgWarps][2 * kImgMBlocks];
@@ -251,12 +293,11 @@ __global__ void k_img_mui_all(const double *__restrict__ mui, const uint8_t *__r
         const size_t a = x % D.nb, jb = (x / D.nb) % nj, p = x / (D.nb * nj);
         const bool real = jb < D.nob;
         const size_t xb = p * D.nb * D.nob + a + jb * D.nb;
-        if (real && !mflag[xb]) return false;
         const size_t jc = real ? jb : 0;
         const double *M = mui + p * D.n_bf * D.n_occ + a * D.bs + jc * D.bs * D.n_bf;
         const int ra = ext_r(a, D.bs, D.n_bf), rj = real ? ext_r(jb, D.bs, D.n_occ) : 0;
         if (jj & 1) {
-            if (!real || !imgA) return false;
+            if (!real || !mflag[xb] || !imgA) return false;
             J.get = OzDenseGet{M, D.n_bf, false};
             J.rows = ra;
             J.k = rj;
@@ -267,8 +308,15 @@ __global__ void k_img_mui_all(const double *__restrict__ mui, const uint8_t *__r
         } else {
             if (!imgB) return false;
             const size_t jbp = jb / D.J, j = jb % D.J;
+            bool zero = false;
+            if (real && sub_dead(mflag[xb], cmax[a], mnorm[xb], tpb)) {
+                // zeros where the group's other block column survives in ij
+                const size_t jq = jbp * D.J + (1 - j), xq = p * D.nb * D.nob + a + jq * D.nb;
+                if (D.J != 2 || jq >= D.nob || sub_dead(mflag[xq], cmax[a], mnorm[xq], tpb)) return false;
+                zero = true;
+            }
             J.get = OzDenseGet{M, D.n_bf, true};
-            J.rows = rj;
+            J.rows = zero ? 0 : rj;  // 0 rows: all digits zero
             J.k = real ? ra : 0;
             J.exps = cexp + p * D.n_occ + jc * D.bs;
             J.dst = imgB + ((p * D.nobp + jbp) * D.nb + a) * D.nd * (size_t)D.npJ * D.kp + j * D.bs * (size_t)D.kp;
@@ -306,6 +354,7 @@ __global__ void k_img_mui_all(const double *__restrict__ mui, const uint8_t *__r
 // kImgSBlocks consecutive blocks per warp
 constexpr int kImgSBlocks = 4;
 __global__ void k_img_ijs_B(const double *__restrict__ ijs, const uint8_t *__restrict__ sflag,
+                            const double *__restrict__ snorm, const double *__restrict__ mmax, double tpb,
                             const int *__restrict__ cexp, size_t Q, OzDims D, size_t n, bf16 *__restrict__ img) {
     __shared__ OzImgJob sj[kOzImgWarps][kImgSBlocks];
     const size_t x0 = oz_warp_id() * kImgSBlocks;
@@ -318,10 +367,17 @@ __global__ void k_img_ijs_B(const double *__restrict__ ijs, const uint8_t *__res
             const size_t nj = D.nobp * D.J, ib = x % D.nob, jb = (x / D.nob) % nj, p = x / (D.nob * nj);
             const size_t jbp = jb / D.J, j = jb % D.J;
             const bool real = jb < D.nob;
-            if (real && !sflag[p * D.nob * D.nob + ib + jb * D.nob]) return false;
+            bool zero = !real;
+            const size_t sb = p * D.nob * D.nob + ib + jb * D.nob;
+            if (real && sub_dead(sflag[sb], mmax[p * D.nob + ib], snorm[sb], tpb)) {
+                // zeros where the group's other block column survives in K
+                const size_t jq = jbp * D.J + (1 - j), sq = p * D.nob * D.nob + ib + jq * D.nob;
+                if (D.J != 2 || jq >= D.nob || sub_dead(sflag[sq], mmax[p * D.nob + ib], snorm[sq], tpb)) return false;
+                zero = true;
+            }
             const size_t jc = real ? jb : 0;
             J.get = OzDenseGet{ijs + p * D.n_occ * D.n_occ + ib * D.bs + jc * D.bs * D.n_occ, D.n_occ, true};
-            J.rows = real ? ext_r(jb, D.bs, D.n_occ) : 0;
+            J.rows = zero ? 0 : ext_r(jb, D.bs, D.n_occ);  // 0 rows: all digits zero
             J.k = real ? ext_r(ib, D.bs, D.n_occ) : 0;
             J.exps = cexp + (p / Q) * D.n_occ + jc * D.bs;
             J.dst = img + ((p * D.nobp + jbp) * D.nob + ib) * D.nd * (size_t)D.npJ * D.kp + j * D.bs * (size_t)D.kp;
@@ -352,7 +408,8 @@ __device__ __forceinline__ void tile_clear(OzTile &T) {
 // same).  t = (pp, a, group g of R block columns j), written transposed; the
 // aux functions' outputs are n_bf*n_occ apart (sub-blocks stored apart).
 __global__ void k_tiles_mui(const uint8_t *__restrict__ uflag, const double *__restrict__ unorm,
-                            const double *__restrict__ cnorm, const int *__restrict__ rexp_U,
+                            const double *__restrict__ cnorm, const double *__restrict__ cmax,
+                            const int *__restrict__ rexp_U,
                             const int *__restrict__ cexp_C, double *__restrict__ mui, OzDims D, size_t np,
                             size_t n_tiles, double tpb, OzTile *__restrict__ tiles, OzStep *__restrict__ steps,
                             uint8_t *__restrict__ mflag, unsigned long long *__restrict__ nsig,
@@ -393,11 +450,13 @@ __global__ void k_tiles_mui(const uint8_t *__restrict__ uflag, const double *__r
         OzStep mine[2];
         uint32_t c = 0;
         if (b < D.nb) {
-            uint32_t live[2] = {0, 0};
+            uint32_t live[2] = {0, 0}, phantom = 0;
             uint32_t a_idx[kOzMaxSlots];
             for (int s = 0; s < kOzMaxSlots; ++s) a_idx[s] = (uint32_t)(g * D.R + s + b * D.nob);
             for (int js = 0; js < nsub; ++js) {
                 const size_t ub = (p0 + js) * D.nb * D.nb + a + b * D.nb;
+                // dropped in every tile: a zero image where the other aux function survives
+                if (D.Jm == 2 && sub_dead(uflag[ub], cmax[b], unorm[ub], tpb)) phantom |= 1u << js;
                 if (!uflag[ub]) continue;
                 for (int s = 0; s < D.R; ++s) {
                     if (!T.c[s]) continue;
@@ -409,7 +468,7 @@ __global__ void k_tiles_mui(const uint8_t *__restrict__ uflag, const double *__r
                 }
             }
             // a missing aux function (odd chunk end) counts as absent: its image rows are never written
-            c = emit_rect_steps(live, D.Jm, 0u, (uint32_t)(pp * D.nb * D.nb + a + b * D.nb), a_idx, mine);
+            c = emit_rect_steps(live, D.Jm, phantom, (uint32_t)(pp * D.nb * D.nb + a + b * D.nb), a_idx, mine);
         }
         warp_append_steps(mine, c, steps + T.s0, n);
     }
@@ -436,7 +495,8 @@ __global__ void k_tiles_mui(const uint8_t *__restrict__ uflag, const double *__r
 // jb = J*jbp + j, steps over a (split into exact rectangles); one warp per
 // tile, lanes over a
 __global__ void k_tiles_ij(const uint8_t *__restrict__ mflag, const double *__restrict__ mnorm,
-                           const double *__restrict__ cnorm, const int *__restrict__ cexp_C,
+                           const double *__restrict__ cnorm, const double *__restrict__ cmax,
+                           const int *__restrict__ cexp_C,
                            const int *__restrict__ cexp_mui, double *__restrict__ ij, OzDims D, size_t n_tiles,
                            double tpb, OzTile *__restrict__ tiles, OzStep *__restrict__ steps,
                            uint8_t *__restrict__ ijflag, unsigned long long *__restrict__ nsig,
@@ -474,13 +534,15 @@ __global__ void k_tiles_ij(const uint8_t *__restrict__ mflag, const double *__re
         OzStep mine[2];
         uint32_t cnt = 0;
         if (a < D.nb) {
-            uint32_t live[2] = {0, 0};
+            uint32_t live[2] = {0, 0}, ph = phantom;
             uint32_t a_idx[kOzMaxSlots];
             for (int s = 0; s < kOzMaxSlots; ++s) a_idx[s] = (uint32_t)(g * D.R + s + a * D.nob);
             for (int j = 0; j < D.J; ++j) {
                 const size_t jb = jbp * D.J + j;
                 if (jb >= D.nob) continue;
                 const size_t mb = p * D.nb * D.nob + a + jb * D.nb;
+                // dropped in every tile: a zero image where the other block column survives
+                if (D.J == 2 && sub_dead(mflag[mb], cmax[a], mnorm[mb], tpb)) ph |= 1u << j;
                 if (!mflag[mb]) continue;
                 for (int s = 0; s < D.R; ++s) {
                     if (!T.c[s]) continue;
@@ -491,7 +553,7 @@ __global__ void k_tiles_ij(const uint8_t *__restrict__ mflag, const double *__re
                     ++seen[s][j];
                 }
             }
-            cnt = emit_rect_steps(live, D.J, phantom, (uint32_t)((p * D.nobp + jbp) * D.nb + a), a_idx, mine);
+            cnt = emit_rect_steps(live, D.J, ph, (uint32_t)((p * D.nobp + jbp) * D.nb + a), a_idx, mine);
         }
         warp_append_steps(mine, cnt, steps + T.s0, n);
     }
@@ -523,6 +585,7 @@ __global__ void k_tiles_ij(const uint8_t *__restrict__ mflag, const double *__re
 // the (p, ib) steps.
 __global__ void k_tiles_K(const uint8_t *__restrict__ mflag, const double *__restrict__ mnorm,
                           const uint8_t *__restrict__ sflag, const double *__restrict__ snorm,
+                          const double *__restrict__ mmax,
                           const int *__restrict__ rexp_sub, const int *__restrict__ cexp_sub, double *__restrict__ Kpart,
                           OzDims D, size_t np, size_t Q, size_t n_tiles, double tpb, OzTile *__restrict__ tiles,
                           OzStep *__restrict__ steps, unsigned long long *__restrict__ nsig,
@@ -563,13 +626,15 @@ __global__ void k_tiles_K(const uint8_t *__restrict__ mflag, const double *__res
         uint32_t cnt = 0;
         if (idx < n_k) {
             const size_t p = p0 + idx / D.nob, ib = idx % D.nob;
-            uint32_t live[2] = {0, 0};
+            uint32_t live[2] = {0, 0}, ph = phantom;
             uint32_t a_idx[kOzMaxSlots];
             for (int s = 0; s < kOzMaxSlots; ++s) a_idx[s] = (uint32_t)(p * D.nb * D.nob + g * D.R + s + ib * D.nb);
             for (int j = 0; j < D.J; ++j) {
                 const size_t jb = jbp * D.J + j;
                 if (jb >= D.nob) continue;
                 const size_t sb = p * D.nob * D.nob + ib + jb * D.nob;
+                // dropped in every tile: a zero image where the other block column survives
+                if (D.J == 2 && sub_dead(sflag[sb], mmax[p * D.nob + ib], snorm[sb], tpb)) ph |= 1u << j;
                 if (!sflag[sb]) continue;
                 for (int s = 0; s < D.R; ++s) {
                     if (!T.c[s]) continue;
@@ -581,7 +646,7 @@ __global__ void k_tiles_K(const uint8_t *__restrict__ mflag, const double *__res
                     ++tot;
                 }
             }
-            cnt = emit_rect_steps(live, D.J, phantom, (uint32_t)((p * D.nobp + jbp) * D.nob + ib), a_idx, mine);
+            cnt = emit_rect_steps(live, D.J, ph, (uint32_t)((p * D.nobp + jbp) * D.nob + ib), a_idx, mine);
         }
         warp_append_steps(mine, cnt, steps + T.s0, n);
     }
@@ -892,6 +957,7 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
     DevBuf dij(pc * n_occ * n_occ * 8, s), dijf(pc * nob * nob, s);
     DevBuf dijs(pc * n_occ * n_occ * 8, s), dsn(pc * nob * nob * 8, s), dsf(pc * nob * nob, s);
     DevBuf dcn(nb * nob * 8, s), dcexpC(nob * bs * 4, s), dimgCtA(nob * nb * a_img * 2, s);
+    DevBuf dcmax(nb * 8, s), dmmax(pc * nob * 8, s);  // largest slot norms of the N-side screens
     DevBuf drexpU[2] = {DevBuf(pc * n_bf * 4, s), DevBuf(pc * n_bf * 4, s)};
     DevBuf dbitsU[2] = {DevBuf(pc * n_bf * 8, s), DevBuf(pc * n_bf * 8, s)};
     const size_t u_img_bytes = ceil_div(pc, (size_t)Jm) * nb * nb * b_imgM * 2;
@@ -926,6 +992,7 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
     const int wpb = 8;
     k_cnorms<<<(unsigned)ceil_div(nb * nob, wpb), wpb * 32, 0, s>>>(d.c_occ, n_bf, n_occ, bs, nb, nob, dcn.as<double>());
     if (d.tr_c_norm) BSG_CUDA(cudaMemcpyAsync(d.tr_c_norm, dcn.p, nb * nob * 8, cudaMemcpyDeviceToDevice, s));
+    k_cnorm_rowmax<<<(unsigned)ceil_div(nb, (size_t)128), 128, 0, s>>>(dcn.as<double>(), nb, nob, dcmax.as<double>());
     k_cexp_C<<<(unsigned)nob, tb, 0, s>>>(d.c_occ, n_bf, n_occ, bs, dcexpC.as<int>());
     k_img_Ct_A<<<oz_img_grid(nob * nb), 32 * kOzImgWarps, 0, s>>>(d.c_occ, dcexpC.as<int>(), D, dimgCtA.as<bf16>());
     // inverse key map of the compressed integrals (replaces the per-P dense rebuild)
@@ -934,7 +1001,7 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
     if (d.n_vec2)
         k_key_inverse<<<(unsigned)ceil_div(d.n_vec2, 256), 256, 0, s>>>(d.keys, d.n_vec2, n_bf, bs, nb, dinv.as<int>(),
                                                                         docc.as<uint8_t>());
-    ctx->note_launch(4);
+    ctx->note_launch(5);
     // the U blocks that hold any integral (the same for every P), in block order
     std::vector<uint8_t> hocc(nb * nb);
     BSG_CUDA(cudaMemcpyAsync(hocc.data(), docc.p, nb * nb, cudaMemcpyDeviceToHost, s));
@@ -974,8 +1041,8 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
                                                                                    drexpU[x].as<int>());
         if (n_ob)
             k_img_U<<<oz_img_grid(ceil_div(np * n_ob, (size_t)kImgUBlocks)), 32 * kOzImgWarps, 0, ss>>>(
-                ducomp[x].as<double>(), dob.as<uint32_t>(), n_ob, np, duf[x].as<uint8_t>(), drexpU[x].as<int>(), D,
-                dimgU[x].as<bf16>());
+                ducomp[x].as<double>(), dob.as<uint32_t>(), n_ob, np, duf[x].as<uint8_t>(), dun[x].as<double>(),
+                dcmax.as<double>(), tpb, drexpU[x].as<int>(), D, dimgU[x].as<bf16>());
         ctx->note_launch(n_ob ? 3 : 1);
         ctx->check_launch("rik ozaki U pass");
         BSG_CUDA(cudaEventRecord(fork.u_ready[x], ss));
@@ -992,7 +1059,8 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
         BSG_CUDA(cudaMemsetAsync(dbits.p, 0, nbits * 8, s));
         const size_t tm = ceil_div(np, (size_t)Jm) * nb * ng_i;
         k_tiles_mui<<<oz_img_grid(tm), 32 * kOzImgWarps, 0, s>>>(
-            duf_.as<uint8_t>(), dun_.as<double>(), dcn.as<double>(), drexpU_.as<int>(), dcexpC.as<int>(),
+            duf_.as<uint8_t>(), dun_.as<double>(), dcn.as<double>(), dcmax.as<double>(), drexpU_.as<int>(),
+            dcexpC.as<int>(),
             dmui.as<double>(), D, np, tm, tpb, dtm.as<OzTile>(), dsm.as<OzStep>(), dmf.as<uint8_t>(), cnt + 0,
             macs + 0);
         ctx->note_launch();
@@ -1020,9 +1088,13 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
                                                                                      dcexpM.as<int>());
         // every digit image of mui in one pass
         k_img_mui_all<<<oz_img_grid(ceil_div(np * nb * nobp * J, (size_t)kImgMBlocks)), 32 * kOzImgWarps, 0, s>>>(
-            dmui.as<double>(), dmf.as<uint8_t>(), drexpMs.as<int>(), Q, dcexpM.as<int>(), D, np * nb * nobp * J,
-            dimgMA.as<bf16>(), want_k ? dimgMB.as<bf16>() : nullptr, want_kmn ? dimgMT.as<bf16>() : nullptr);
-        ctx->note_launch(want_k ? 4 : 3);
+            dmui.as<double>(), dmf.as<uint8_t>(), dmn.as<double>(), dcmax.as<double>(), tpb, drexpMs.as<int>(), Q,
+            dcexpM.as<int>(), D, np * nb * nobp * J, dimgMA.as<bf16>(), want_k ? dimgMB.as<bf16>() : nullptr,
+            want_kmn ? dimgMT.as<bf16>() : nullptr);
+        if (want_k)
+            k_mnorm_max<<<(unsigned)ceil_div(np * nob, (size_t)128), 128, 0, s>>>(dmn.as<double>(), dmf.as<uint8_t>(),
+                                                                                 np, nb, nob, dmmax.as<double>());
+        ctx->note_launch(want_k ? 5 : 3);
         if (want_kmn) {
             // K_mn += mui mui^T
             const size_t tkm = n_sub * n_pairs;
@@ -1041,8 +1113,8 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
         // ij = C^T mui
         const size_t ti = np * nobp * ng_i;
         k_tiles_ij<<<oz_img_grid(ti), 32 * kOzImgWarps, 0, s>>>(
-            dmf.as<uint8_t>(), dmn.as<double>(), dcn.as<double>(), dcexpC.as<int>(), dcexpM.as<int>(),
-            dij.as<double>(), D, ti, tpb, dti.as<OzTile>(), dsi.as<OzStep>(), dijf.as<uint8_t>(), cnt + 1, macs + 1);
+            dmf.as<uint8_t>(), dmn.as<double>(), dcn.as<double>(), dcmax.as<double>(), dcexpC.as<int>(),
+            dcexpM.as<int>(), dij.as<double>(), D, ti, tpb, dti.as<OzTile>(), dsi.as<OzStep>(), dijf.as<uint8_t>(), cnt + 1, macs + 1);
         ctx->note_launch();
         ctx->check_launch("rik ozaki ij prep");
         oz_run(ctx, shJ, dti.as<OzTile>(), ti, dsi.as<OzStep>(), dimgCtA.as<bf16>(), dimgMB.as<bf16>(), 1.0, s,
@@ -1058,11 +1130,12 @@ void rik_ozaki(bsg_ctx ctx, const RikDev &d, double *K_dev, double *Kmn_dev, uin
         k_bits_to_exp<<<(unsigned)ceil_div(n_sub * n_occ, (size_t)256), 256, 0, s>>>(bitsSs, n_sub * n_occ,
                                                                                   dcexpSs.as<int>());
         k_img_ijs_B<<<oz_img_grid(ceil_div(np * nob * nobp * J, (size_t)kImgSBlocks)), 32 * kOzImgWarps, 0, s>>>(
-            dijs.as<double>(), dsf.as<uint8_t>(), dcexpSs.as<int>(), Q, D, np * nob * nobp * J, dimgSB.as<bf16>());
+            dijs.as<double>(), dsf.as<uint8_t>(), dsn.as<double>(), dmmax.as<double>(), tpb, dcexpSs.as<int>(), Q, D,
+            np * nob * nobp * J, dimgSB.as<bf16>());
         const size_t tk = n_sub * nobp * ng_a;
         k_tiles_K<<<oz_img_grid(tk), 32 * kOzImgWarps, 0, s>>>(
-            dmf.as<uint8_t>(), dmn.as<double>(), dsf.as<uint8_t>(), dsn.as<double>(), drexpMs.as<int>(),
-            dcexpSs.as<int>(), dKp.as<double>(), D, np, Q, tk, tpb, dtk.as<OzTile>(), dsk.as<OzStep>(), cnt + 2,
+            dmf.as<uint8_t>(), dmn.as<double>(), dsf.as<uint8_t>(), dsn.as<double>(), dmmax.as<double>(),
+            drexpMs.as<int>(), dcexpSs.as<int>(), dKp.as<double>(), D, np, Q, tk, tpb, dtk.as<OzTile>(), dsk.as<OzStep>(), cnt + 2,
             macs + 2);
         ctx->note_launch(5);
         ctx->check_launch("rik ozaki K prep");
