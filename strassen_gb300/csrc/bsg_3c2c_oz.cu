@@ -118,8 +118,9 @@ __global__ void k_vn_rowmax(const double *__restrict__ vn, size_t nkb, size_t nj
 // that the two steps of a stage pair are one copy); block ib = J*ibp + j
 // fills rows j*bs.. of its group's image (rows of missing blocks are never
 // read).  A block that the screen drops in every tile gets an all-zero
-// image: a step may then copy its group's whole image (one copy) and the
-// MMA adds exact zeros for it.
+// image where the other block row of its group survives: a step may then
+// copy the group's whole image (one copy) and the MMA adds exact zeros for
+// it.  Where neither survives, no step reads the image and it is not written.
 // kImgXBlocks consecutive blocks x = ib + kb*nib per warp.
 constexpr int kImgXBlocks = 4;
 __global__ void k_img_X(const double *__restrict__ X, const int *__restrict__ rexp, const double *__restrict__ xn,
@@ -133,8 +134,15 @@ __global__ void k_img_X(const double *__restrict__ X, const int *__restrict__ re
             const size_t x = x0 + q;
             if (x >= n) return false;
             const size_t ib = x % D.nib, kb = x / D.nib, ibp = ib / D.J, j = ib % D.J;
+            bool zero = false;
+            if (x_block_dead(xn[x], vmax[kb], tpb)) {
+                // zeros where the group's other block row survives (else no step reads the image)
+                const size_t iq = ibp * D.J + (1 - j);
+                if (D.J != 2 || iq >= D.nib || x_block_dead(xn[iq + kb * D.nib], vmax[kb], tpb)) return false;
+                zero = true;
+            }
             J.get = OzDenseGet{X + ib * D.bs + kb * D.bs * D.ldx, D.ldx, false};
-            J.rows = x_block_dead(xn[x], vmax[kb], tpb) ? 0 : ext3(ib, D.bs, D.n_vec2);  // 0 rows: zeros
+            J.rows = zero ? 0 : ext3(ib, D.bs, D.n_vec2);  // 0 rows: all digits zero
             J.k = ext3(kb, D.bs, D.n_aux);
             J.exps = rexp + ib * D.bs;
             J.dst = img + (ibp * D.nkb + kb) * D.nd * (size_t)D.np * D.kp + j * D.bs * (size_t)D.kp;
