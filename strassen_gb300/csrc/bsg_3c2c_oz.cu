@@ -354,6 +354,43 @@ void oz3c_rows(bsg_ctx ctx, Dense3c D, const OzShape &sh, const Oz3cV &v, const 
     oz_run(ctx, sh, dt.as<OzTile>(), n_tiles, dst.as<OzStep>(), v.ai.as<bf16>(), bi.as<bf16>(), 1.0, s, cnt + 1, 1);
 }
 
+// Rows [0, rows) of every column of a column-major host matrix (leading
+// dimension ld, pinned and mapped into the device's address space) into a
+// rows x ncols device buffer, read by the SMs over the host link: one CTA
+// per column at a time, eight 16-byte loads in flight per thread.  The copy
+// engine takes a strided copy one row of the 2D copy at a time, well below
+// the link's rate; a handful of SMs reach it.  vec: every column start on
+// both sides 16-byte aligned and rows even (else 8-byte loads).
+__global__ void __launch_bounds__(1024) k_fetch_host_rows(const double *__restrict__ src, size_t ld, size_t rows,
+                                                          size_t ncols, double *__restrict__ dst, int vec) {
+    for (size_t c = blockIdx.x; c < ncols; c += gridDim.x) {
+        const double *sc = src + c * ld;
+        double *dc = dst + c * rows;
+        if (vec) {
+            const double2 *s2 = reinterpret_cast<const double2 *>(sc);
+            double2 *d2 = reinterpret_cast<double2 *>(dc);
+            const size_t n2 = rows / 2, step = blockDim.x;
+            size_t i = threadIdx.x;
+            for (; i + 7 * step < n2; i += 8 * step) {
+                double2 v[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) v[u] = s2[i + u * step];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) d2[i + u * step] = v[u];
+            }
+            for (; i < n2; i += step) d2[i] = s2[i];
+        } else {
+            for (size_t i = threadIdx.x; i < rows; i += blockDim.x) dc[i] = sc[i];
+        }
+    }
+}
+
+// SMs left to the host fetch beside the GEMM, one CTA of 1024 threads each:
+// a CTA this size does not fit beside a GEMM CTA, and the block scheduler
+// spreads a grid over idle SMs first, so any more CTAs would land on SMs a
+// GEMM CTA needs
+constexpr int kFetchSms = 16;
+
 struct EventPair {
     cudaEvent_t e[2] = {nullptr, nullptr};
     EventPair() {
@@ -397,8 +434,12 @@ void transform_3c2c_ozaki(bsg_ctx ctx, size_t n_vec2, size_t n_aux, const double
 
 // Host X: uploaded in row ranges on the context's upload stream, each range
 // transformed on the compute stream while the next one is in flight (two
-// device range buffers).  The rows of the output are independent, so the
-// result equals transform_3c2c_ozaki's bit for bit.
+// device range buffers).  A range of the column-major X is strided: from
+// pinned host memory that the device can address, k_fetch_host_rows reads it
+// on kFetchSms SMs that the GEMM launches of the call leave free (about 190
+// GB/s on GB300 against about 140 for the copy engine's 2D copy); other
+// host memory goes through cudaMemcpy2DAsync.  The rows of the output are
+// independent, so the result equals transform_3c2c_ozaki's bit for bit.
 void transform_3c2c_ozaki_upload(bsg_ctx ctx, size_t n_vec2, size_t n_aux, const double *X_host, const double *V,
                                  size_t bs, double thresh, int n_digits, double *out, uint64_t *nsig_out) {
     cudaStream_t s = ctx->stream;
@@ -419,10 +460,35 @@ void transform_3c2c_ozaki_upload(bsg_ctx ctx, size_t n_vec2, size_t n_aux, const
     EventPair copied, used, ready;
     BSG_CUDA(cudaEventRecord(ready.e[0], s));  // the range buffers exist (stream-ordered allocation)
     BSG_CUDA(cudaStreamWaitEvent(up, ready.e[0], 0));
+    // pinned host memory the device can address: fetched by SMs
+    const double *X_mapped = nullptr;
+    {
+        cudaPointerAttributes at{};
+        if (cudaPointerGetAttributes(&at, X_host) == cudaSuccess && at.type == cudaMemoryTypeHost && at.devicePointer)
+            X_mapped = static_cast<const double *>(at.devicePointer);
+        else
+            cudaGetLastError();  // not a registered pointer: clear the error, copy with the copy engine
+    }
+    const bool fetch = X_mapped && ctx->sm_count > 4 * kFetchSms;
+    struct Reserve {  // the GEMM launches of this call leave kFetchSms SMs free
+        bsg_ctx c;
+        int prev;
+        ~Reserve() { c->oz_sm_reserve = prev; }
+    } reserve{ctx, ctx->oz_sm_reserve};
+    if (fetch) ctx->oz_sm_reserve = kFetchSms;
     auto upload = [&](size_t c) {
         const size_t r0 = c * rc, rows = std::min(rc, n_vec2 - r0);
-        BSG_CUDA(cudaMemcpy2DAsync(xb[c & 1], rows * 8, X_host + r0, n_vec2 * 8, rows * 8, n_aux,
-                                   cudaMemcpyHostToDevice, up));
+        if (fetch) {
+            const int vec = ((reinterpret_cast<uintptr_t>(X_mapped + r0) | reinterpret_cast<uintptr_t>(xb[c & 1]) |
+                              (n_vec2 * 8) | (rows * 8)) &
+                             15u) == 0;
+            k_fetch_host_rows<<<kFetchSms, 1024, 0, up>>>(X_mapped + r0, n_vec2, rows, n_aux, xb[c & 1], vec);
+            ctx->note_launch();
+            ctx->check_launch("3c2c host fetch");
+        } else {
+            BSG_CUDA(cudaMemcpy2DAsync(xb[c & 1], rows * 8, X_host + r0, n_vec2 * 8, rows * 8, n_aux,
+                                       cudaMemcpyHostToDevice, up));
+        }
         BSG_CUDA(cudaEventRecord(copied.e[c & 1], up));
     };
     upload(0);

@@ -104,6 +104,9 @@ struct bsg_ctx_s {
     // GEMM per (block rows, block k, block cols, digits)
     bool autotune = true;
     std::map<std::array<int, 4>, std::array<int, 2>> oz_tune;
+    // SMs the tensor-core GEMM leaves free for a kernel that runs beside it
+    // (the host-memory fetch of the 3c->2c upload path); 0 otherwise
+    int oz_sm_reserve = 0;
     // second stream for host->device uploads that overlap compute on `stream`
     // (created on first use, released with the context)
     cudaStream_t copy_stream = 0;

@@ -947,7 +947,8 @@ static void launch_oz(bsg_ctx ctx, const std::vector<OzRun> &runs, const OzTile 
             if (dev >= 0 && dev < 64) set_to[dev].store((int)smem);
         }
     }
-    const unsigned grid = (unsigned)std::min<size_t>(ceil_div(n_tiles, (size_t)chunk), (size_t)ctx->sm_count);
+    const int sms = std::max(1, ctx->sm_count - ctx->oz_sm_reserve);
+    const unsigned grid = (unsigned)std::min<size_t>(ceil_div(n_tiles, (size_t)chunk), (size_t)sms);
     BSG_REQUIRE(n_tiles + (size_t)grid * chunk < 0xffffffffull, BSG_ERR_UNSUPPORTED, "too many Ozaki tiles");
     k_ozgemm<NP, MULTI><<<grid, OzEpi<NP>::threads, smem, s>>>(tiles, (uint32_t)n_tiles, steps, P, err);
     ctx->note_launch();

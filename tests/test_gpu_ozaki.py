@@ -147,16 +147,24 @@ def test_ozaki_pipeline(api, ctx):
     assert err < 1e-9
 
 
+@pytest.mark.parametrize("pinned", [False, True])
 @pytest.mark.parametrize("nd,tol", [(6, 1e-10), (5, 1e-7)])
 @pytest.mark.parametrize("n_atoms,bs", [(8, 24), (3, 16), (1, 24)])
-def test_3c2c_host_upload_matches_device(api, ctx, n_atoms, bs, nd, tol):
+def test_3c2c_host_upload_matches_device(api, ctx, n_atoms, bs, nd, tol, pinned):
     """host integrals stream in by row ranges overlapping the transform: the
     output equals the device-input transform bit for bit (ranges of whole
     block rows, a ragged last range, and a single range); at 5 digits the
-    tiles carry two X block rows (split into exact rectangles)"""
+    tiles carry two X block rows (split into exact rectangles).  Pageable
+    host memory goes through the copy engine, pinned memory is read by SMs
+    beside the GEMM launches (one atom: 299 rows, odd, so 8-byte loads)"""
     torch = pytest.importorskip("torch")
     s = S.RikSystem(seed=4, n_atoms=n_atoms, nbf=24, naux=12, n_occ=10, box=5.0)
     X, V = s.ints_3c(), s.v_m12()
+    if n_atoms == 1:
+        X = np.asfortranarray(X[:-1])
+    if pinned:
+        Xp = torch.from_numpy(np.ascontiguousarray(X.T)).pin_memory()
+        X = Xp.numpy().T  # the same column-major matrix in pinned memory
     out_h = api.transform_3c2c(X, V, bs, 1e-10, form=api.FORM_OZAKI, n_digits=nd, ctx=ctx)
     Xd = torch.from_numpy(np.ascontiguousarray(X.T)).cuda().T
     Vd = torch.from_numpy(np.ascontiguousarray(V.T)).cuda().T
