@@ -453,13 +453,15 @@ void transform_3c2c_ozaki_upload(bsg_ctx ctx, size_t n_vec2, size_t n_aux, const
     const size_t n_ch = ceil_div(n_vec2, rc);
     DevBuf cnt(16, s), xb0(rc * n_aux * 8, s), xb1(n_ch > 1 ? rc * n_aux * 8 : 0, s);
     double *xb[2] = {xb0.as<double>(), xb1.as<double>()};
+    cudaStream_t up = ctx->upload_stream();
+    EventPair copied, used, ready;
+    // the range buffers exist (stream-ordered allocation): the first range's
+    // upload may start, beside the V operands' preparation
+    BSG_CUDA(cudaEventRecord(ready.e[0], s));
+    BSG_CUDA(cudaStreamWaitEvent(up, ready.e[0], 0));
     BSG_CUDA(cudaMemsetAsync(cnt.p, 0, 16, s));
     Oz3cV v;
     oz3c_prepare_v(ctx, V, D, v);
-    cudaStream_t up = ctx->upload_stream();
-    EventPair copied, used, ready;
-    BSG_CUDA(cudaEventRecord(ready.e[0], s));  // the range buffers exist (stream-ordered allocation)
-    BSG_CUDA(cudaStreamWaitEvent(up, ready.e[0], 0));
     // pinned host memory the device can address: fetched by SMs
     const double *X_mapped = nullptr;
     {
