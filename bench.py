@@ -411,10 +411,10 @@ def run_ours(args):
         # DRAM bytes (read + write) of the largest launch, the 3c->2c k_ozgemm, per launch like
         # `achieved`: dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture of the full
         # workload's 3c->2c launch (two counters, one pass)
-        traffic = 12.18e9 + 5.25e9 if args.atoms in (0, CFG["n_atoms"]) and d3 == 5 else None
+        traffic = 16.45e9 + 5.33e9 if args.atoms in (0, CFG["n_atoms"]) and d3 == 5 else None
         line["roofline"] = {"kernel": "k_ozgemm (tcgen05 digit-slice GEMM)", "bound": "tensor", "achieved": achieved,
                             "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
-                            "traffic_launch": "3c->2c k_ozgemm launch (28 ms), dram__bytes_read.sum + write.sum (one-pass ncu capture)",
+                            "traffic_launch": "3c->2c k_ozgemm launch (23 ms), dram__bytes_read.sum + write.sum (one-pass ncu capture)",
                             "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained" if peaks else "fallback",
                             "launches_per_step": l3 + lo, "kernel_ms_per_step": kms,
                             "fp64_equivalent_tflops": 2.0 * (m3 + mo) / (kms * 1e-3) / 1e12,
