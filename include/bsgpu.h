@@ -319,7 +319,11 @@ bsg_status bsg_rik_occ_step_noalloc(const bsg_rik_args *args, double *K_dev, voi
                                     uint64_t stats_out[5]);
 
 /* 3c->2c transform (3c_2c_transform.cpp:44-57): out = X * V^{-1/2} through
- * matmult on block-sparse copies (input threshold 0, out pre-filled 0). */
+ * matmult on block-sparse copies (input threshold 0, out pre-filled 0).  In
+ * the mixed form with where == BSG_HOST, X streams in by row ranges beside
+ * the transform: pinned host memory (cudaHostAlloc / cudaHostRegister) is read
+ * by 16 SMs the GEMM launches of the call leave free, other host memory goes
+ * through the copy engine; the result is the same either way. */
 bsg_status bsg_3c2c_transform(bsg_ctx ctx, size_t n_vec2, size_t n_aux, const double *ints_3c,
                               const double *v_m12, int where, size_t bs, double thresh, int form, int n_digits,
                               double *out, int out_where);
