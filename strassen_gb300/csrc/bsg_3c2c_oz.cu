@@ -472,12 +472,11 @@ void transform_3c2c_ozaki_upload(bsg_ctx ctx, size_t n_vec2, size_t n_aux, const
             cudaGetLastError();  // not a registered pointer: clear the error, copy with the copy engine
     }
     const bool fetch = X_mapped && ctx->sm_count > 4 * kFetchSms;
-    struct Reserve {  // the GEMM launches of this call leave kFetchSms SMs free
+    struct Reserve {  // GEMM launches beside a fetch leave kFetchSms SMs free (restored on exit)
         bsg_ctx c;
         int prev;
         ~Reserve() { c->oz_sm_reserve = prev; }
     } reserve{ctx, ctx->oz_sm_reserve};
-    if (fetch) ctx->oz_sm_reserve = kFetchSms;
     auto upload = [&](size_t c) {
         const size_t r0 = c * rc, rows = std::min(rc, n_vec2 - r0);
         if (fetch) {
@@ -501,6 +500,8 @@ void transform_3c2c_ozaki_upload(bsg_ctx ctx, size_t n_vec2, size_t n_aux, const
         }
         BSG_CUDA(cudaStreamWaitEvent(s, copied.e[c & 1], 0));
         const size_t r0 = c * rc, rows = std::min(rc, n_vec2 - r0);
+        // the last range runs with no fetch beside it: its GEMM takes every SM
+        ctx->oz_sm_reserve = (fetch && c + 1 < n_ch) ? kFetchSms : reserve.prev;
         oz3c_rows(ctx, D, sh, v, xb[c & 1], rows, rows, out + r0, n_vec2, thresh, cnt.as<unsigned long long>());
         BSG_CUDA(cudaEventRecord(used.e[c & 1], s));
     }
