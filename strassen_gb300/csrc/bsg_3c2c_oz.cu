@@ -223,8 +223,12 @@ __global__ void k_tiles_3c(size_t n_tiles, size_t n_jg, size_t Gj, const double 
             for (int j = 0; j < nsub; ++j) {
                 const double x = xn[ibp * D.J + j + kb * D.nib];
                 // a block dropped in every tile has a zero image: its
-                // sub-block may ride along in a whole-image copy
-                if (x_block_dead(x, vmax[kb], tpb)) phantom |= 1u << j;
+                // sub-block may ride along in a whole-image copy (and no slot
+                // needs a test)
+                if (x_block_dead(x, vmax[kb], tpb)) {
+                    phantom |= 1u << j;
+                    continue;
+                }
                 for (int s = 0; s < D.R; ++s) {
                     const size_t jb = jg * D.R + s;
                     if (jb >= D.njb) break;

@@ -456,8 +456,11 @@ __global__ void k_tiles_mui(const uint8_t *__restrict__ uflag, const double *__r
             for (int js = 0; js < nsub; ++js) {
                 const size_t ub = (p0 + js) * D.nb * D.nb + a + b * D.nb;
                 // dropped in every tile: a zero image where the other aux function survives
-                if (D.Jm == 2 && sub_dead(uflag[ub], cmax[b], unorm[ub], tpb)) phantom |= 1u << js;
-                if (!uflag[ub]) continue;
+                // (and no slot needs a test)
+                if (sub_dead(uflag[ub], cmax[b], unorm[ub], tpb)) {
+                    if (D.Jm == 2) phantom |= 1u << js;
+                    continue;
+                }
                 for (int s = 0; s < D.R; ++s) {
                     if (!T.c[s]) continue;
                     const size_t j = g * D.R + s;
@@ -542,8 +545,11 @@ __global__ void k_tiles_ij(const uint8_t *__restrict__ mflag, const double *__re
                 if (jb >= D.nob) continue;
                 const size_t mb = p * D.nb * D.nob + a + jb * D.nb;
                 // dropped in every tile: a zero image where the other block column survives
-                if (D.J == 2 && sub_dead(mflag[mb], cmax[a], mnorm[mb], tpb)) ph |= 1u << j;
-                if (!mflag[mb]) continue;
+                // (and no slot needs a test)
+                if (sub_dead(mflag[mb], cmax[a], mnorm[mb], tpb)) {
+                    if (D.J == 2) ph |= 1u << j;
+                    continue;
+                }
                 for (int s = 0; s < D.R; ++s) {
                     if (!T.c[s]) continue;
                     const size_t ib = g * D.R + s;
@@ -634,8 +640,11 @@ __global__ void k_tiles_K(const uint8_t *__restrict__ mflag, const double *__res
                 if (jb >= D.nob) continue;
                 const size_t sb = p * D.nob * D.nob + ib + jb * D.nob;
                 // dropped in every tile: a zero image where the other block column survives
-                if (D.J == 2 && sub_dead(sflag[sb], mmax[p * D.nob + ib], snorm[sb], tpb)) ph |= 1u << j;
-                if (!sflag[sb]) continue;
+                // (and no slot needs a test)
+                if (sub_dead(sflag[sb], mmax[p * D.nob + ib], snorm[sb], tpb)) {
+                    if (D.J == 2) ph |= 1u << j;
+                    continue;
+                }
                 for (int s = 0; s < D.R; ++s) {
                     if (!T.c[s]) continue;
                     const size_t mb = p * D.nb * D.nob + g * D.R + s + ib * D.nb;
