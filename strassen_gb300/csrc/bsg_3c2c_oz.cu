@@ -466,14 +466,21 @@ void transform_3c2c_ozaki_upload(bsg_ctx ctx, size_t n_vec2, size_t n_aux, const
     BSG_CUDA(cudaMemsetAsync(cnt.p, 0, 16, s));
     Oz3cV v;
     oz3c_prepare_v(ctx, V, D, v);
-    // pinned host memory the device can address: fetched by SMs
+    // pinned host memory the device can address, first and last element
+    // alike (so the matrix does not reach past a registered region): fetched
+    // by SMs
     const double *X_mapped = nullptr;
     {
-        cudaPointerAttributes at{};
-        if (cudaPointerGetAttributes(&at, X_host) == cudaSuccess && at.type == cudaMemoryTypeHost && at.devicePointer)
-            X_mapped = static_cast<const double *>(at.devicePointer);
-        else
+        auto mapped = [](const double *h) -> const double * {
+            cudaPointerAttributes at{};
+            if (cudaPointerGetAttributes(&at, h) == cudaSuccess && at.type == cudaMemoryTypeHost && at.devicePointer)
+                return static_cast<const double *>(at.devicePointer);
             cudaGetLastError();  // not a registered pointer: clear the error, copy with the copy engine
+            return nullptr;
+        };
+        const size_t last = n_vec2 * n_aux - 1;
+        const double *first_d = mapped(X_host), *last_d = mapped(X_host + last);
+        if (first_d && last_d == first_d + last) X_mapped = first_d;
     }
     const bool fetch = X_mapped && ctx->sm_count > 4 * kFetchSms;
     struct Reserve {  // GEMM launches beside a fetch leave kFetchSms SMs free (restored on exit)

@@ -147,7 +147,7 @@ def test_ozaki_pipeline(api, ctx):
     assert err < 1e-9
 
 
-@pytest.mark.parametrize("pinned", [False, True])
+@pytest.mark.parametrize("pinned", [False, True, "interior"])
 @pytest.mark.parametrize("nd,tol", [(6, 1e-10), (5, 1e-7)])
 @pytest.mark.parametrize("n_atoms,bs", [(8, 24), (3, 16), (1, 24)])
 def test_3c2c_host_upload_matches_device(api, ctx, n_atoms, bs, nd, tol, pinned):
@@ -162,7 +162,12 @@ def test_3c2c_host_upload_matches_device(api, ctx, n_atoms, bs, nd, tol, pinned)
     X, V = s.ints_3c(), s.v_m12()
     if n_atoms == 1:
         X = np.asfortranarray(X[:-1])
-    if pinned:
+    if pinned == "interior":
+        # the matrix starts one column into a larger pinned allocation
+        Xp = torch.zeros((X.shape[1] + 1, X.shape[0]), dtype=torch.float64).pin_memory()
+        Xp[1:] = torch.from_numpy(np.ascontiguousarray(X.T))
+        X = Xp[1:].numpy().T
+    elif pinned:
         Xp = torch.from_numpy(np.ascontiguousarray(X.T)).pin_memory()
         X = Xp.numpy().T  # the same column-major matrix in pinned memory
     out_h = api.transform_3c2c(X, V, bs, 1e-10, form=api.FORM_OZAKI, n_digits=nd, ctx=ctx)
